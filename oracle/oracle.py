@@ -1,0 +1,206 @@
+"""ctypes loader for the parity oracle.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs
+import this module; the product (``qusim_gb300``) never does.
+
+Two libraries:
+
+* ``liboracle.so`` -- the C restatement of the reference's split-operator
+  algorithm (``qusim_oracle.c``), available wherever gcc is.
+* ``_ref/libqusim_ref.so`` -- the reference's own sources compiled as they lie
+  (``make ref``), available only where the reference tree exists.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libqusim_ref.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_sz = ctypes.c_size_t
+_d = ctypes.c_double
+_i = ctypes.c_int
+_u64 = ctypes.c_uint64
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (and the reference build when ``ref``)."""
+    targets = ["all"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Oracle:
+    """The C restatement (qusim_oracle.c)."""
+
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        lib.orc_fft1d.argtypes = [_sz, _i, _dp, _dp]
+        lib.orc_fft2d.argtypes = [_sz, _sz, _i, _dp, _dp]
+        lib.orc_evolve1d.argtypes = [_sz, _d, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, _u64]
+        lib.orc_evolve2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp, _u64]
+        lib.orc_kinen1d.argtypes = [_sz, _d, _d, _d, _i, _dp]
+        lib.orc_kinen1d.restype = _d
+        lib.orc_kinen2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _dp]
+        lib.orc_kinen2d.restype = _d
+        lib.orc_norm2.argtypes = [_sz, _d, _dp]
+        lib.orc_norm2.restype = _d
+        lib.orc_poten.argtypes = [_sz, _d, _dp, _dp]
+        lib.orc_poten.restype = _d
+        lib.orc_xavg.argtypes = [_sz, _d, _d, _dp]
+        lib.orc_xavg.restype = _d
+        lib.orc_norm2_range.argtypes = [_sz, _d, _d, _d, _d, _dp]
+        lib.orc_norm2_range.restype = _d
+        lib.orc_splitting_constants.argtypes = [_dp, _dp, _dp, _dp]
+        self.lib = lib
+
+    def fft1d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        assert self.lib.orc_fft1d(x.size, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
+
+    def fft2d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        nx, ny = x.shape
+        assert self.lib.orc_fft2d(nx, ny, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
+
+    def evolve1d(self, psi, V, dx, dt, nsteps, order=2, mass=1.0, hbar=1.0,
+                 wall=False, renormalize=False):
+        """One Step() call of ``nsteps`` steps; renormalise once at the end."""
+        psi = _c128(psi).copy()
+        V = _f64(V)
+        dt = complex(dt)
+        rc = self.lib.orc_evolve1d(psi.size, dx, mass, hbar, dt.real, dt.imag, order,
+                                   int(wall), 0, _ptr(psi), _ptr(V), nsteps)
+        assert rc == 0
+        if renormalize:
+            psi /= np.sqrt(self.norm2(psi, dx))
+        return psi
+
+    def evolve2d(self, psi, V, dx, dy, dt, nsteps, order=2, mass=1.0, hbar=1.0,
+                 renormalize=False):
+        psi = _c128(psi).copy()
+        V = _f64(V)
+        dt = complex(dt)
+        nx, ny = psi.shape
+        rc = self.lib.orc_evolve2d(nx, ny, dx, dy, mass, hbar, dt.real, dt.imag, order, 0,
+                                   _ptr(psi), _ptr(V), nsteps)
+        assert rc == 0
+        if renormalize:
+            psi /= np.sqrt(self.norm2(psi, dx * dy))
+        return psi
+
+    def norm2(self, psi, dv):
+        psi = _c128(psi)
+        return self.lib.orc_norm2(psi.size, dv, _ptr(psi))
+
+    def poten(self, psi, V, dv):
+        psi, V = _c128(psi), _f64(V)
+        return self.lib.orc_poten(psi.size, dv, _ptr(psi), _ptr(V))
+
+    def kinen1d(self, psi, dx, mass=1.0, hbar=1.0, wall=False):
+        psi = _c128(psi)
+        return self.lib.orc_kinen1d(psi.size, dx, mass, hbar, int(wall), _ptr(psi))
+
+    def kinen2d(self, psi, dx, dy, mass=1.0, hbar=1.0):
+        psi = _c128(psi)
+        nx, ny = psi.shape
+        return self.lib.orc_kinen2d(nx, ny, dx, dy, mass, hbar, _ptr(psi))
+
+    def xavg(self, psi, x0, dx):
+        psi = _c128(psi)
+        return self.lib.orc_xavg(psi.size, x0, dx, _ptr(psi))
+
+    def norm2_range(self, psi, x0, dx, xa, xb):
+        psi = _c128(psi)
+        return self.lib.orc_norm2_range(psi.size, x0, dx, xa, xb, _ptr(psi))
+
+    def splitting_constants(self):
+        v = [ctypes.c_double() for _ in range(4)]
+        self.lib.orc_splitting_constants(*[ctypes.byref(c) for c in v])
+        return tuple(c.value for c in v)
+
+
+class Reference:
+    """The reference's own SplittingMethod1D/2D (compiled from its sources)."""
+
+    def __init__(self, path: str = REF_SO):
+        lib = ctypes.CDLL(path)
+        lib.ref_evolve1d.argtypes = [_sz, _d, _d, _d, _d, _d, _d, _i, _i, _i, _dp, _dp,
+                                     _u64, _u64, _dp, _dp, _dp]
+        lib.ref_evolve2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _d, _d, _i, _i, _dp,
+                                     _dp, _u64, _u64, _dp, _dp, _dp]
+        lib.ref_fft1d.argtypes = [_sz, _i, _dp, _dp]
+        lib.ref_fft2d.argtypes = [_sz, _sz, _i, _dp, _dp]
+        self.lib = lib
+
+    @staticmethod
+    def available(path: str = REF_SO) -> bool:
+        return os.path.exists(path)
+
+    def fft1d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        assert self.lib.ref_fft1d(x.size, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
+
+    def fft2d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        nx, ny = x.shape
+        assert self.lib.ref_fft2d(nx, ny, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
+
+    def evolve1d(self, psi, V, x0, x1, dt, batch, calls=1, order=2, mass=1.0, hbar=1.0,
+                 wall=False, fnes=False):
+        """Returns (psi, norm2, kin, pot) after ``calls`` Step() calls."""
+        psi = _c128(psi).copy()
+        V = _f64(V)
+        dt = complex(dt)
+        outs = [ctypes.c_double() for _ in range(3)]
+        rc = self.lib.ref_evolve1d(psi.size, x0, x1, mass, hbar, dt.real, dt.imag, order,
+                                   int(wall), int(fnes), _ptr(psi), _ptr(V), batch, calls,
+                                   *[ctypes.pointer(o) for o in outs])
+        assert rc == 0
+        return (psi,) + tuple(o.value for o in outs)
+
+    def evolve2d(self, psi, V, x0, x1, y0, y1, dt, batch, calls=1, order=2, mass=1.0,
+                 hbar=1.0, fnes=False):
+        psi = _c128(psi).copy()
+        V = _f64(V)
+        dt = complex(dt)
+        nx, ny = psi.shape
+        outs = [ctypes.c_double() for _ in range(3)]
+        rc = self.lib.ref_evolve2d(nx, ny, x0, x1, y0, y1, mass, hbar, dt.real, dt.imag,
+                                   order, int(fnes), _ptr(psi), _ptr(V), batch, calls,
+                                   *[ctypes.pointer(o) for o in outs])
+        assert rc == 0
+        return (psi,) + tuple(o.value for o in outs)
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))

@@ -1,0 +1,80 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own SplittingMethod1D/2D and KISS FourierTransform,
+compiled from its sources by ``make -C oracle ref`` (oracle/_ref), on seeded
+inputs and stores inputs + outputs as .npz.  The reference tree is needed
+only here; the committed fixtures travel without it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as orc  # noqa: E402
+from tests.workloads import gauss_packet_1d, gauss_packet_2d, gaussian_bumps_2d  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    print("wrote", os.path.relpath(path, ROOT), os.path.getsize(path), "bytes")
+
+
+def main():
+    orc.build(ref=True)
+    ref = orc.Reference()
+
+    # FFT ramp input x[i] = i (not stored: np.arange), the shapes of applications/QuSimTest/TestFFT.cpp:89-99
+    for n in (1234, 4096):
+        x = np.arange(n, dtype=np.complex128)
+        save(f"fft1d_ramp_{n}", fwd=ref.fft1d(x), inv=ref.fft1d(x, inverse=True))
+    for nx, ny in ((123, 234), (64, 128)):
+        x = np.arange(nx * ny, dtype=np.complex128).reshape(nx, ny)
+        save(f"fft2d_ramp_{nx}x{ny}", fwd=ref.fft2d(x), inv=ref.fft2d(x, inverse=True))
+
+    # 1D evolutions.  (name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes)
+    cases_1d = [
+        # the 1D plain configuration: N=4096 on [-200,200), k0=1, x0=-50, s=10,
+        # V=0.5 exp(-x^2/2), dt=0.05, 2000 O2 steps
+        ("evolve1d_n4096_o2_2000", 4096, -200.0, 200.0, 1.0, -50.0, 10.0, 2, False, 0.05, 2000, 1, False),
+        ("evolve1d_n4096_o4_200", 4096, -200.0, 200.0, 1.0, -50.0, 10.0, 4, False, 0.05, 200, 1, False),
+        ("evolve1d_n256_o2_b7x3_fnes", 256, -30.0, 30.0, 2.0, -5.0, 2.0, 2, False, 0.01, 7, 3, True),
+        ("evolve1d_n1024_o4_imag", 1024, -50.0, 50.0, 1.5, -10.0, 3.0, 4, False, 0.02 - 0.005j, 40, 1, False),
+        ("evolve1d_n512_o2_wall", 512, -40.0, 40.0, 1.0, -10.0, 3.0, 2, True, 0.02, 100, 1, False),
+        ("evolve1d_n1000_o2", 1000, -50.0, 50.0, 1.0, -10.0, 3.0, 2, False, 0.02, 100, 1, False),
+    ]
+    for name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes in cases_1d:
+        psi0, V, dx = gauss_packet_1d(n, x0, x1, k0, xc, s, barrier=0.5)
+        psi, nrm, kin, pot = ref.evolve1d(psi0, V, x0, x1, dt, batch, calls=calls, order=order,
+                                          wall=wall, fnes=fnes)
+        save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
+             params=np.array([n, x0, x1, order, int(wall), batch, calls, int(fnes)], dtype=np.float64),
+             dt=np.complex128(dt))
+
+    # 2D evolutions.  (name, nx, ny, half_x, half_y, order, dt, batch, calls, fnes)
+    cases_2d = [
+        ("evolve2d_64x128_o2_50", 64, 128, 20.0, 40.0, 2, 0.02, 50, 1, False),
+        ("evolve2d_128x128_o4_20", 128, 128, 30.0, 30.0, 4, 0.02, 20, 1, False),
+        ("evolve2d_32x64_o4_b5x2_fnes", 32, 64, 10.0, 20.0, 4, 0.01 - 0.002j, 5, 2, True),
+    ]
+    for name, nx, ny, hx, hy, order, dt, batch, calls, fnes in cases_2d:
+        x0, x1, y0, y1 = -hx, hx, -hy, hy
+        psi0, dx, dy = gauss_packet_2d(nx, ny, x0, x1, y0, y1, kx=1.5, ky=0.0, xc=-0.3 * hx, yc=0.0, s=0.1 * hx)
+        V = gaussian_bumps_2d(nx, ny, x0, x1, y0, y1, nbumps=16, seed=0, spread=0.5 * hx)
+        psi, nrm, kin, pot = ref.evolve2d(psi0, V, x0, x1, y0, y1, dt, batch, calls=calls,
+                                          order=order, fnes=fnes)
+        save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
+             params=np.array([nx, ny, x0, x1, y0, y1, order, batch, calls, int(fnes)], dtype=np.float64),
+             dt=np.complex128(dt))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,106 @@
+"""The oracle (C restatement) against the reference's golden vectors and known answers.
+
+CPU only.  The fixtures in tests/golden/ were produced by the reference's own
+sources compiled as they lie (tests/golden/make_golden.py); the oracle must
+reproduce them to the last bit (same algorithm, same operation order).
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import load_golden
+
+EVOLVE_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
+             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1000_o2"]
+EVOLVE_2D = ["evolve2d_64x128_o2_50", "evolve2d_128x128_o4_20", "evolve2d_32x64_o4_b5x2_fnes"]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.mark.parametrize("n", [1234, 4096])
+def test_fft1d_ramp_matches_reference(oracle, n):
+    g = load_golden(f"fft1d_ramp_{n}")
+    x = np.arange(n, dtype=np.complex128)
+    assert np.array_equal(oracle.fft1d(x), g["fwd"])
+    assert np.array_equal(oracle.fft1d(x, inverse=True), g["inv"])
+    # applications/QuSimTest/TestFFT.cpp:71-81: round trip, sum |a-b|^2 < 1e-8
+    rt = oracle.fft1d(oracle.fft1d(x), inverse=True) / n
+    assert np.sum(np.abs(rt - x) ** 2) < 1e-8
+
+
+@pytest.mark.parametrize("shape", [(123, 234), (64, 128)])
+def test_fft2d_ramp_matches_reference(oracle, shape):
+    nx, ny = shape
+    g = load_golden(f"fft2d_ramp_{nx}x{ny}")
+    x = np.arange(nx * ny, dtype=np.complex128).reshape(nx, ny)
+    assert np.array_equal(oracle.fft2d(x), g["fwd"])
+    assert np.array_equal(oracle.fft2d(x, inverse=True), g["inv"])
+    assert rel_l2(oracle.fft2d(x), np.fft.fft2(x)) < 1e-13
+
+
+@pytest.mark.parametrize("name", EVOLVE_1D)
+def test_evolve1d_matches_reference(oracle, name):
+    g = load_golden(name)
+    n, x0, x1, order, wall, batch, calls, fnes = g["params"]
+    n, order, batch, calls = int(n), int(order), int(batch), int(calls)
+    dx = (x1 - x0) / n
+    psi = g["psi0"]
+    for _ in range(calls):
+        psi = oracle.evolve1d(psi, g["V"], dx, complex(g["dt"]), batch, order=order,
+                              wall=bool(wall), renormalize=bool(fnes))
+    assert rel_l2(psi, g["psi"]) < 1e-14
+    assert abs(oracle.norm2(psi, dx) - g["norm2"]) < 1e-13
+    assert abs(oracle.kinen1d(psi, dx, wall=bool(wall)) - g["kin"]) < 1e-12 * max(1, abs(g["kin"]))
+    assert abs(oracle.poten(psi, g["V"], dx) - g["pot"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", EVOLVE_2D)
+def test_evolve2d_matches_reference(oracle, name):
+    g = load_golden(name)
+    nx, ny, x0, x1, y0, y1, order, batch, calls, fnes = g["params"]
+    nx, ny, order, batch, calls = int(nx), int(ny), int(order), int(batch), int(calls)
+    dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+    psi = g["psi0"]
+    for _ in range(calls):
+        psi = oracle.evolve2d(psi, g["V"], dx, dy, complex(g["dt"]), batch, order=order,
+                              renormalize=bool(fnes))
+    assert rel_l2(psi, g["psi"]) < 1e-14
+    assert abs(oracle.norm2(psi, dx * dy) - g["norm2"]) < 1e-13
+    assert abs(oracle.kinen2d(psi, dx, dy) - g["kin"]) < 1e-12 * max(1, abs(g["kin"]))
+    assert abs(oracle.poten(psi, g["V"], dx * dy) - g["pot"]) < 1e-13
+
+
+def test_splitting_constants(oracle):
+    c1, c2, d1, d2 = oracle.splitting_constants()
+    # SplittingUtils.cpp:3-8; consistency: 2 C1 + 2 C2 = 1, 2 D1 + D2 = 1
+    assert abs(2 * c1 + 2 * c2 - 1) < 1e-15
+    assert abs(2 * d1 + d2 - 1) < 1e-15
+    assert abs(c1 - 0.6756035959798288) < 1e-15
+
+
+def test_tunnelling_known_answer(oracle):
+    """applications/QuEvol1DPrecision/QuSimPrecision.cpp:82,106-120: the
+    transmitted probability of gauss(x,-20,5)*exp(I*x) through exp(-x*x) on
+    [-100,100) at t=64 is 0.15937744085."""
+    ref = (0.1593774409 + 0.1593774408) / 2
+    n, dt = 2048, 0.02
+    x0, x1 = -100.0, 100.0
+    dx = (x1 - x0) / n
+    xs = x0 + dx * np.arange(n)
+    psi = np.exp(-0.5 * ((xs + 20) / 5) ** 2) * np.exp(1j * xs)
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx)
+    p = oracle.evolve1d(psi, np.exp(-xs * xs), dx, dt, 3200, order=4)
+    assert abs(oracle.norm2_range(p, x0, dx, 0.0, x1) - ref) < 1e-9
+
+
+def test_group_velocity(oracle):
+    """QuSimPrecision.cpp:206-218: a free packet gauss(x,0,5)*exp(I*x) moves at 1."""
+    n, dt, x0, x1 = 1024, 0.01, -100.0, 100.0
+    dx = (x1 - x0) / n
+    xs = x0 + dx * np.arange(n)
+    psi = np.exp(-0.5 * (xs / 5) ** 2) * np.exp(1j * xs)
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx)
+    xa = oracle.xavg(psi, x0, dx)
+    p = oracle.evolve1d(psi, np.zeros(n), dx, dt, 11, order=2)
+    assert abs((oracle.xavg(p, x0, dx) - xa) / (11 * dt) - 1) < 1e-10

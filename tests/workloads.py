@@ -1,0 +1,80 @@
+"""Seeded synthetic inputs with the shapes of the benchmark configurations.
+
+Gaussian packets use psi ~ exp(i k.r) exp(-|r - r0|^2 / (4 s^2)), normalised to
+sum |psi|^2 dv = 1; potentials are real.  Grids are x_i = x0 + i dx with
+dx = (x1 - x0) / n and index iy + ix*ny (y contiguous), as QuSim samples them
+(src/EvolverImpl1D.cpp:33-81, src/EvolverImpl2D.cpp:39-98).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def grid(n, x0, x1):
+    dx = (x1 - x0) / n
+    return x0 + dx * np.arange(n), dx
+
+
+def gauss_packet_1d(n, x0, x1, k0, xc, s, barrier=0.5):
+    """Packet plus the barrier V = barrier * exp(-x^2/2)."""
+    xs, dx = grid(n, x0, x1)
+    psi = np.exp(1j * k0 * xs) * np.exp(-((xs - xc) ** 2) / (4 * s * s))
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx)
+    V = barrier * np.exp(-xs * xs / 2)
+    return psi.astype(np.complex128), V.astype(np.float64), dx
+
+
+def gauss_packet_2d(nx, ny, x0, x1, y0, y1, kx, ky, xc, yc, s):
+    xs, dx = grid(nx, x0, x1)
+    ys, dy = grid(ny, y0, y1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    psi = np.exp(1j * (kx * X + ky * Y)) * np.exp(-((X - xc) ** 2 + (Y - yc) ** 2) / (4 * s * s))
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx * dy)
+    return psi.astype(np.complex128), dx, dy
+
+
+def gaussian_bumps_2d(nx, ny, x0, x1, y0, y1, nbumps=16, seed=0, spread=30.0,
+                      hmin=-1.0, hmax=1.0, wmin=1.0, wmax=5.0):
+    """Sum of seeded Gaussian bumps h exp(-|r-c|^2/(2w^2)), c ~ U[-spread, spread]^2."""
+    rng = np.random.default_rng(seed)
+    xs, _ = grid(nx, x0, x1)
+    ys, _ = grid(ny, y0, y1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    V = np.zeros((nx, ny))
+    c = rng.uniform(-spread, spread, size=(nbumps, 2))
+    h = rng.uniform(hmin, hmax, size=nbumps)
+    w = rng.uniform(wmin, wmax, size=nbumps)
+    for i in range(nbumps):
+        V += h[i] * np.exp(-((X - c[i, 0]) ** 2 + (Y - c[i, 1]) ** 2) / (2 * w[i] ** 2))
+    return V
+
+
+def config_1d_plain():
+    """N=4096 on [-200,200), k0=1, x0=-50, s=10, V=0.5 exp(-x^2/2), dt=0.05, O2 x 2000."""
+    psi, V, dx = gauss_packet_1d(4096, -200.0, 200.0, 1.0, -50.0, 10.0, barrier=0.5)
+    return dict(psi=psi, V=V, dx=dx, x0=-200.0, x1=200.0, dt=0.05, steps=2000, order=2)
+
+
+def config_2d_1024():
+    """1024^2 on [-100,100)^2, k=(1.5,0), s=8 at (-40,0); 16 bumps (seed 0); dt=0.02, O4 x 1000."""
+    psi, dx, dy = gauss_packet_2d(1024, 1024, -100, 100, -100, 100, 1.5, 0.0, -40.0, 0.0, 8.0)
+    V = gaussian_bumps_2d(1024, 1024, -100, 100, -100, 100, nbumps=16, seed=0, spread=30.0)
+    return dict(psi=psi, V=V, dx=dx, dy=dy, dt=0.02, steps=1000, order=4)
+
+
+def double_slit_2d(nx=4096, ny=4096, half=200.0, seed=0):
+    """Wall V=10 on |x|<1 with openings of width 2 at y=+-6, plus U[-0.01,0.01] noise."""
+    xs, dx = grid(nx, -half, half)
+    ys, dy = grid(ny, -half, half)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    V = np.where(np.abs(X) < 1.0, 10.0, 0.0)
+    V = np.where((np.abs(X) < 1.0) & ((np.abs(Y - 6.0) < 1.0) | (np.abs(Y + 6.0) < 1.0)), 0.0, V)
+    V = V + np.random.default_rng(seed).uniform(-0.01, 0.01, size=(nx, ny))
+    return V, dx, dy
+
+
+def config_2d_4096():
+    """4096^2 on [-200,200)^2, double slit, k=(2,0), s=10 at (-60,0); dt=0.01, O4 x 2000."""
+    psi, dx, dy = gauss_packet_2d(4096, 4096, -200, 200, -200, 200, 2.0, 0.0, -60.0, 0.0, 10.0)
+    V, _, _ = double_slit_2d()
+    return dict(psi=psi, V=V, dx=dx, dy=dy, dt=0.01, steps=2000, order=4)
