@@ -1,0 +1,431 @@
+"""Benchmark of the split-operator step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload 2d4096|2d1024|1d4096] [--precision mixed|fp64]
+
+Default workload: the large 2D configuration -- 4096x4096 periodic grid on
+[-200,200)^2, double-slit wall (V=10 on |x|<1 except openings of width 2 at
+y=+-6) plus seeded U[-0.01,0.01] noise, Gaussian packet k=(2,0), s=10 at
+(-60,0), dt=0.01, O4, complex64-mixed.  Synthetic seeded inputs; the
+complex128 plain path runs the same steps beside it for the error figures.
+
+A "step" is one O4 time step of the whole grid.  K steps are timed as one
+qsg_step(K) call (launches queued back to back on the context stream),
+bracketed by CUDA events on that stream.  psi (128 MiB) plus its phase tables
+(256 MiB) exceed the 129 MB L2, so no flush is needed between steps.
+
+Multi-GPU: the workload is one grid; the path does not shard (no collective),
+so --gpus N runs N independent replicas ("replicas only"), value = total
+site-steps over the slowest rank's time.
+
+--impl reference times the reference's CPU path (the oracle: the reference
+compiled from its own sources when that build is present, otherwise the C
+restatement of the same algorithm) on this host, one core (the reference's
+CPU path is single-threaded for one grid), on a bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from tests.workloads import double_slit_2d, gauss_packet_1d, gauss_packet_2d, gaussian_bumps_2d  # noqa: E402
+
+WORKLOADS = {
+    "2d4096": dict(desc="2D 4096x4096 double slit, O4, dt=0.01", dim=2, nx=4096, ny=4096, half=200.0,
+                   k=(2.0, 0.0), c=(-60.0, 0.0), s=10.0, dt=0.01, order=4),
+    "2d1024": dict(desc="2D 1024x1024 16 Gaussian bumps (seed 0), O4, dt=0.02", dim=2, nx=1024, ny=1024,
+                   half=100.0, k=(1.5, 0.0), c=(-40.0, 0.0), s=8.0, dt=0.02, order=4),
+    "1d4096": dict(desc="1D N=4096 barrier 0.5 exp(-x^2/2), O2, dt=0.05", dim=1, n=4096, dt=0.05, order=2),
+}
+
+
+def make_inputs(w):
+    if w["dim"] == 1:
+        psi, V, dx = gauss_packet_1d(w["n"], -200.0, 200.0, 1.0, -50.0, 10.0, barrier=0.5)
+        return psi, V, (dx,)
+    h = w["half"]
+    psi, dx, dy = gauss_packet_2d(w["nx"], w["ny"], -h, h, -h, h, w["k"][0], w["k"][1], w["c"][0], w["c"][1],
+                                  w["s"])
+    if w["nx"] == 4096:
+        V, _, _ = double_slit_2d(w["nx"], w["ny"], h, seed=0)
+    else:
+        V = gaussian_bumps_2d(w["nx"], w["ny"], -h, h, -h, h, nbumps=16, seed=0, spread=30.0)
+    return psi, V, (dx, dy)
+
+
+def algorithmic_bytes(w, precision):
+    """Minimal-fused-schedule HBM bytes per site-step (psi in and out per pass,
+    one V table read per real-space pass): 2D O4 = 6 passes x 2 psi + 3 tables,
+    O2 = 2 passes x 2 psi + 1 table; 1D resident = one round trip per call."""
+    sc = 8 if precision == "mixed" else 16
+    if w["dim"] == 2:
+        return (6 * 2 * sc + 3 * sc) if w["order"] == 4 else (2 * 2 * sc + sc)
+    return None
+
+
+def kernel_bytes_per_site(name, precision):
+    sc = 8 if precision == "mixed" else 16
+    return {"row_pass": 3 * sc, "col_pass": 2 * sc}.get(name)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per site of one launch of `kernel` from the committed ncu summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_sample(w, budget_s=15.0):
+    """Time the oracle on a bounded sample of the workload on this host (1 core)."""
+    from oracle import oracle as orc
+    if not os.path.exists(orc.ORACLE_SO):
+        orc.build()
+    o = orc.Oracle()
+    kind = "port"
+    if w["dim"] == 1:
+        psi, V, (dx,) = make_inputs(w)
+        st = orc.Stepper1D(o, psi, V, dx, w["dt"], order=w["order"])
+        st.step(5)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < budget_s:
+            st.step(50)
+            n += 50
+        el = time.perf_counter() - t0
+        st.close()
+        return dict(value=w["n"] * n / el, unit="site-steps/s", cores=1, kind=kind,
+                    sample=f"{n} steps of the N={w['n']} workload, single thread")
+    # 2D: a slab of R full-length rows (row FFT length unchanged) stepped once
+    h = w["half"]
+    nx_full, ny = w["nx"], w["ny"]
+    rows = nx_full
+    est = 9.0 * (nx_full * ny) / (4096 * 4096)  # seconds per O4 step, measured scale
+    while rows > 256 and est * rows / nx_full > budget_s:
+        rows //= 2
+    dy = 2 * h / ny
+    dx = 2 * h / nx_full
+    ys = -h + dy * np.arange(ny)
+    xs = -h + dx * np.arange(rows) + (nx_full - rows) // 2 * dx
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    psi = np.exp(1j * (w["k"][0] * X)) * np.exp(-((X - w["c"][0]) ** 2 + Y ** 2) / (4 * w["s"] ** 2)) + 1e-3
+    V = np.where(np.abs(X) < 1, 10.0, 0.0)
+    st = orc.Stepper2D(o, psi, V, dx, dy, w["dt"], order=w["order"])
+    n, t0 = 0, time.perf_counter()
+    while True:
+        st.step(1)
+        n += 1
+        if time.perf_counter() - t0 > budget_s * 0.5:
+            break
+    el = time.perf_counter() - t0
+    st.close()
+    return dict(value=rows * ny * n / el, unit="site-steps/s", cores=1, kind=kind,
+                sample=f"{n} O4 step(s) of a {rows}x{ny} slab of the workload (full-length rows), single thread")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args, w):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    if not os.path.exists(orc.ORACLE_SO):
+        orc.build()
+    o = orc.Oracle()
+    kind = "port"
+    if w["dim"] == 1:
+        psi, V, (dx,) = make_inputs(w)
+        st = orc.Stepper1D(o, psi, V, dx, w["dt"], order=w["order"])
+        st.step(args.warmup)
+        t0 = time.perf_counter()
+        st.step(args.steps)
+        el = time.perf_counter() - t0
+        sites, sample = w["n"], f"full N={w['n']} grid, K={args.steps} steps"
+    else:
+        # each step: one O4 step of a slab of full-length rows, sized so the run stays within minutes
+        h = w["half"]
+        ny = w["ny"]
+        per_step_budget = 150.0 / max(1, args.steps + args.warmup)
+        rows = w["nx"]
+        while rows > 128 and 9.0 * rows * ny / (4096 * 4096) > per_step_budget:
+            rows //= 2
+        dx, dy = 2 * h / w["nx"], 2 * h / ny
+        xs = -h + dx * np.arange(rows) + (w["nx"] - rows) // 2 * dx
+        ys = -h + dy * np.arange(ny)
+        X, Y = np.meshgrid(xs, ys, indexing="ij")
+        psi = np.exp(1j * (w["k"][0] * X)) * np.exp(-((X - w["c"][0]) ** 2 + Y ** 2) / (4 * w["s"] ** 2)) + 1e-3
+        V = np.where(np.abs(X) < 1, 10.0, 0.0)
+        st = orc.Stepper2D(o, psi, V, dx, dy, w["dt"], order=w["order"])
+        st.step(args.warmup)
+        t0 = time.perf_counter()
+        st.step(args.steps)
+        el = time.perf_counter() - t0
+        sites = rows * ny
+        sample = f"each step: one O4 step of a {rows}x{ny} slab (full-length rows) of the workload"
+    st.close()
+    v = sites * args.steps / el
+    line = {"metric": "site-steps/s", "value": v, "unit": "site-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": w["desc"], "precision": "fp64", "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "site-steps/s", "cores": 1, "kind": kind, "sample": sample},
+            "e2e": {"value": v, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="2d4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the fp64 comparison run")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args, w)
+
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import qusim_gb300 as q
+
+    psi0, V, d = make_inputs(w)
+    sites = psi0.size
+    ctx = q.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def create(precision):
+        if w["dim"] == 1:
+            return q.Instance.create_1d(ctx, psi0, V, d[0], w["dt"], order=w["order"], precision=precision)
+        return q.Instance.create_2d(ctx, psi0, V, d[0], d[1], w["dt"], order=w["order"], precision=precision)
+
+    inst = create(args.precision)
+    inst.step(args.warmup)
+    inst.sync()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    ctx.profile(True)
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        inst.step(args.steps)
+        e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = sites * args.steps * world / (ms / 1e3)
+
+    # dominant kernel and its roofline
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if dom:
+        name, (nl, tot) = dom
+        bps = kernel_bytes_per_site(name, args.precision)
+        avg_ms = tot / nl
+        if bps:
+            ach = bps * sites / (avg_ms / 1e3) / 1e9
+            tr = profile_traffic(f"{name}_{args.precision}")
+            roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "peak_source": peak_kind, "avg_launch_ms": avg_ms,
+                    "algorithmic_bytes_per_launch": bps * sites,
+                    "traffic": (tr * sites) if tr else None,
+                    "share": tot / sum(v[1] for v in prof.values())}
+        else:
+            roof = {"bound": "fp64" if args.precision == "fp64" else "on-chip", "kernel": name,
+                    "avg_launch_ms": avg_ms, "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                    "traffic": None}
+    launches = int(sum(v[0] for v in prof.values()))
+    ab = algorithmic_bytes(w, args.precision)
+    step_roof = {"algorithmic_bytes_per_site_step": ab, "achieved_gbs": ab * value / world / 1e9,
+                 "frac": ab * value / world / 1e9 / peak} if ab else None
+
+    # accuracy against the fp64 path run for the same steps
+    acc = None
+    plain = None
+    if not args.no_plain and args.precision == "mixed":
+        ref = create("fp64")
+        k0, p0 = ref.energies()
+        ref.step(args.warmup)
+        ref.sync()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        psteps = max(1, min(args.steps, 20))
+        with torch.cuda.stream(stream):
+            f0.record(stream)
+            ref.step(psteps)
+            f1.record(stream)
+        f1.synchronize()
+        pms = f0.elapsed_time(f1)
+        plain = {"value": sites * psteps / (pms / 1e3), "unit": "site-steps/s", "steps": psteps,
+                 "dtype": "c128"}
+        if psteps < args.steps:
+            ref.step(args.steps - psteps)
+        a, b = inst.get_psi(), ref.get_psi()
+        km, pm = inst.energies()
+        kr, pr = ref.energies()
+        dv = np.prod(d)
+        acc = {"rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+               "norm_drift": float(inst.norm2() - np.sum(np.abs(psi0) ** 2) * dv),
+               "energy_drift_vs_fp64": float((km + pm) - (kr + pr)),
+               "energy_fp64_start": float(k0 + p0), "steps": args.steps + args.warmup}
+        ref.close()
+
+    # end to end through the public API: H2D of psi0 and V from pinned memory,
+    # K x (step + Norm2 read back), final psi read back
+    import torch as _t
+    pin_psi = _t.from_numpy(psi0.view(np.float64).copy()).pin_memory()
+    pin_V = _t.from_numpy(np.ascontiguousarray(V, dtype=np.float64)).pin_memory()
+    out = _t.empty(psi0.size * 2, dtype=_t.float64).pin_memory()
+    psi_pinned = pin_psi.numpy().view(np.complex128).reshape(psi0.shape)
+    V_pinned = pin_V.numpy().reshape(V.shape)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    if w["dim"] == 1:
+        e2 = q.Instance.create_1d(ctx, psi_pinned, V_pinned, d[0], w["dt"], order=w["order"],
+                                  precision=args.precision)
+    else:
+        e2 = q.Instance.create_2d(ctx, psi_pinned, V_pinned, d[0], d[1], w["dt"], order=w["order"],
+                                  precision=args.precision)
+    for _ in range(args.steps):
+        e2.step(1)
+        e2.norm2()
+    e2.get_psi(out.numpy().view(np.complex128).reshape(psi0.shape))
+    e2.close()
+    el = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([el], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
+    e2e = {"value": sites * args.steps * world / el, "unit": "site-steps/s",
+           "h2d_bytes_per_step": (psi0.nbytes + V.nbytes) / args.steps,
+           "d2h_bytes_per_step": psi0.nbytes / args.steps + 8,
+           "includes": "instance creation (H2D psi0+V, phase tables), K x (step + Norm2 read back), "
+                       "final psi read back"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample(w)
+
+    if rank == 0:
+        line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                           "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
+                "roofline": roof, "step_roofline": step_roof, "accuracy": acc, "plain_fp64": plain,
+                "e2e": e2e, "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]}
+                                                                  for k, v in prof.items()},
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+/*
+ * qsg.h -- C ABI of the GB300 split-operator engine (libqsg.so).
+ *
+ * Plain C, plain pointers and sizes; no exceptions cross it.  Every call
+ * returns a qsg_status (0 = ok); qsg_last_error() gives the message of the
+ * calling thread's last failure.
+ *
+ * It replaces, for the split-operator path of lhprojects/QuSim, what the
+ * reference's evolver implementation does behind include/QuSim.h:
+ *   - QuEvolverImpl / SplittingMethod1D / SplittingMethod2D
+ *     (src/EvolverImpl.h:54-57, src/SplittingMethod1D.h, src/SplittingMethod2D.h)
+ *   - its Device ops and FFT wrappers on the GPU_CUDA device
+ *     (src/CudaDevice.cu:98-302, src/FourierTransform.cpp:84-127, 336-360)
+ * A host evolver (include/qusim_gb300/Evolver.h, or the reference's own
+ * QuEvolverImpl subclass shown in INTEGRATION.md) drives it.
+ *
+ * Layout conventions are the reference's: complex values are interleaved
+ * (re, im) doubles (std::complex<double>), a 2D grid is stored with index
+ * iy + ix*ny (y contiguous; include/QuSim.h:47-52), and grid point i sits at
+ * x0 + i*dx with dx = (x1 - x0)/n (src/EvolverImpl1D.cpp:11).
+ */
+#ifndef QSG_H
+#define QSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    QSG_OK = 0,
+    QSG_ERR_ARG = 1,          /* bad argument (null pointer, size, order ...)        */
+    QSG_ERR_BUDGET = 2,       /* the request does not fit the context's HBM budget  */
+    QSG_ERR_CUDA = 3,         /* a CUDA runtime error (message in qsg_last_error)   */
+    QSG_ERR_TIMEOUT = 4,      /* a bounded device-side wait ran out                 */
+    QSG_ERR_UNSUPPORTED = 5,  /* valid for the reference, not built here (e.g. a
+                                 non-power-of-two grid, InfiniteWall in 2D)         */
+    QSG_ERR_STATE = 6         /* call not valid in the object's current state       */
+} qsg_status;
+
+typedef enum { QSG_FP64 = 0, QSG_MIXED = 1 } qsg_precision;
+typedef enum { QSG_PERIOD = 0, QSG_INFINITE_WALL = 1 } qsg_boundary;
+
+typedef struct qsg_ctx qsg_ctx;
+typedef struct qsg_inst qsg_inst;
+
+/* Library version string. */
+const char *qsg_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *qsg_last_error(void);
+
+/* Open a context on CUDA device `device_ordinal`.  hbm_budget_bytes bounds the
+ * device memory that instances of this context may hold (0 = no bound).
+ * Replaces Device::Create(GPU_CUDA) (src/Device.cpp:24-33). */
+int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out);
+void qsg_ctx_destroy(qsg_ctx *ctx);
+
+/* The cudaStream_t every launch of this context goes to (as void*). */
+void *qsg_ctx_stream(qsg_ctx *ctx);
+
+/* Device bytes currently held by the context's instances and scratch. */
+size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
+
+/* Create a 1D instance.  psi0: n complex (re,im); V: n real (the reference keeps
+ * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
+ * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
+ * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
+ * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
+ * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
+int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
+                  double dt_re, double dt_im, int order, int precision, int boundary,
+                  const double *psi0, const double *V, qsg_inst **out);
+
+/* Create a 2D instance, nx*ny sites, index iy + ix*ny.  Periodic only, as in
+ * the reference (src/SplittingMethod2D.cpp:21-29).
+ * Replaces SplittingMethod2D::InitSystem2D (src/SplittingMethod2D.cpp:5-31). */
+int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
+                  double hbar, double dt_re, double dt_im, int order, int precision,
+                  const double *psi0, const double *V, qsg_inst **out);
+
+/* Advance by nsteps steps (O2: V/2 T V/2; O4: the 7-factor Forest-Ruth
+ * sequence), then, if renormalize, scale psi to Norm2 == 1.  Asynchronous:
+ * returns once the launches are queued.
+ * Replaces QuEvolverImpl::Step (src/EvolverImpl.cpp:56-68) with "batch" =
+ * nsteps and force_normalization_each_step = renormalize, minus its device to
+ * host copy of psi (qsg_get_psi does that on demand). */
+int qsg_step(qsg_inst *inst, uint64_t nsteps, int renormalize);
+
+/* Wait for the instance's queued work. */
+int qsg_sync(qsg_inst *inst);
+
+/* Norm2 = sum |psi|^2 dv (src/EvolverImpl.cpp:51-54). */
+int qsg_norm2(qsg_inst *inst, double *out);
+
+/* Kinetic and potential energy, as QuEvolverImpl::KinEn / PotEn
+ * (src/SplittingMethod1D.cpp:91-107, src/SplittingMethod2D.cpp:123-138,
+ * src/EvolverImpl.cpp:45-49).  Either pointer may be null. */
+int qsg_energies(qsg_inst *inst, double *kin, double *pot);
+
+/* <x> (src/EvolverImpl1D.cpp:83-88) and Norm2 over [xa, xb)
+ * (src/EvolverImpl1D.cpp:90-102); 1D only.  x0 is the grid origin. */
+int qsg_xavg(qsg_inst *inst, double x0, double *out);
+int qsg_norm2_range(qsg_inst *inst, double x0, double xa, double xb, double *out);
+
+/* Copy psi to the host as complex128 (n or nx*ny complex).  Synchronous. */
+int qsg_get_psi(qsg_inst *inst, double *out);
+
+/* Replace psi from a host complex128 array. */
+int qsg_set_psi(qsg_inst *inst, const double *psi);
+
+/* Steps taken so far (Time() = steps * dt, src/EvolverImpl.h:63-66). */
+int qsg_steps_taken(qsg_inst *inst, uint64_t *out);
+
+void qsg_destroy(qsg_inst *inst);
+
+/* Per-kernel timing of this context's launches (CUDA events around every
+ * launch on the context stream), for roofline reporting.  Enabling resets the
+ * counters.  qsg_profile_read fills up to cap entries of name / launches /
+ * total milliseconds and returns the number of kernel kinds seen. */
+int qsg_profile_enable(qsg_ctx *ctx, int on);
+int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launches,
+                     double *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSG_H */

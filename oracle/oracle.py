@@ -71,6 +71,14 @@ class Oracle:
         lib.orc_norm2_range.argtypes = [_sz, _d, _d, _d, _d, _dp]
         lib.orc_norm2_range.restype = _d
         lib.orc_splitting_constants.argtypes = [_dp, _dp, _dp, _dp]
+        lib.orc_ev1d_new.argtypes = [_sz, _d, _d, _d, _d, _d, _i, _i]
+        lib.orc_ev1d_new.restype = ctypes.c_void_p
+        lib.orc_ev1d_step.argtypes = [ctypes.c_void_p, _dp, _dp, _u64]
+        lib.orc_ev1d_free.argtypes = [ctypes.c_void_p]
+        lib.orc_ev2d_new.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _i, _dp]
+        lib.orc_ev2d_new.restype = ctypes.c_void_p
+        lib.orc_ev2d_step.argtypes = [ctypes.c_void_p, _dp, _u64]
+        lib.orc_ev2d_free.argtypes = [ctypes.c_void_p]
         self.lib = lib
 
     def fft1d(self, x, inverse=False):
@@ -141,6 +149,45 @@ class Oracle:
         v = [ctypes.c_double() for _ in range(4)]
         self.lib.orc_splitting_constants(*[ctypes.byref(c) for c in v])
         return tuple(c.value for c in v)
+
+
+class Stepper2D:
+    """A persistent oracle 2D evolver (tables built once), for timing."""
+
+    def __init__(self, orc: "Oracle", psi, V, dx, dy, dt, order=4, mass=1.0, hbar=1.0):
+        self.lib = orc.lib
+        self.V = _f64(V)
+        self.psi = _c128(psi).copy()
+        dt = complex(dt)
+        nx, ny = self.psi.shape
+        self.h = self.lib.orc_ev2d_new(nx, ny, dx, dy, mass, hbar, dt.real, dt.imag, order, _ptr(self.V))
+        assert self.h
+
+    def step(self, n):
+        self.lib.orc_ev2d_step(self.h, _ptr(self.psi), n)
+
+    def close(self):
+        if self.h:
+            self.lib.orc_ev2d_free(self.h)
+            self.h = None
+
+
+class Stepper1D:
+    def __init__(self, orc: "Oracle", psi, V, dx, dt, order=2, mass=1.0, hbar=1.0):
+        self.lib = orc.lib
+        self.V = _f64(V)
+        self.psi = _c128(psi).copy()
+        dt = complex(dt)
+        self.h = self.lib.orc_ev1d_new(self.psi.size, dx, mass, hbar, dt.real, dt.imag, order, 0)
+        assert self.h
+
+    def step(self, n):
+        self.lib.orc_ev1d_step(self.h, _ptr(self.psi), _ptr(self.V), n)
+
+    def close(self):
+        if self.h:
+            self.lib.orc_ev1d_free(self.h)
+            self.h = None
 
 
 class Reference:

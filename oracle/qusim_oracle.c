@@ -601,3 +601,58 @@ double orc_norm2_range(size_t n, double x0, double dx, double xa, double xb, con
     if (i1 >= i2) return 0;
     return norm2_raw((const cplx *)psi + i1, (size_t)(i2 - i1)) * dx;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Persistent evolvers: set up once (plans, tables), step many times.  Used */
+/* to time the CPU path per step, as the reference's Evolver::step() runs.  */
+/* ------------------------------------------------------------------------ */
+
+void *orc_ev1d_new(size_t n, double dx, double mass, double hbar, double dt_re, double dt_im,
+                   int order, int wall)
+{
+    ev1d *e = (ev1d *)malloc(sizeof(ev1d));
+    if (!e) return NULL;
+    if (ev1d_init(e, n, dx, mass, hbar, dt_re, dt_im, order, wall)) {
+        ev1d_free(e);
+        free(e);
+        return NULL;
+    }
+    return e;
+}
+
+void orc_ev1d_step(void *h, double *psi, const double *V, uint64_t nsteps)
+{
+    for (uint64_t s = 0; s < nsteps; ++s) ev1d_step((ev1d *)h, (cplx *)psi, V);
+}
+
+void orc_ev1d_free(void *h)
+{
+    if (!h) return;
+    ev1d_free((ev1d *)h);
+    free(h);
+}
+
+void *orc_ev2d_new(size_t nx, size_t ny, double dx, double dy, double mass, double hbar,
+                   double dt_re, double dt_im, int order, const double *V)
+{
+    ev2d *e = (ev2d *)malloc(sizeof(ev2d));
+    if (!e) return NULL;
+    if (ev2d_init(e, nx, ny, dx, dy, mass, hbar, dt_re, dt_im, order, V)) {
+        ev2d_free(e);
+        free(e);
+        return NULL;
+    }
+    return e;
+}
+
+void orc_ev2d_step(void *h, double *psi, uint64_t nsteps)
+{
+    for (uint64_t s = 0; s < nsteps; ++s) ev2d_step((ev2d *)h, (cplx *)psi);
+}
+
+void orc_ev2d_free(void *h)
+{
+    if (!h) return;
+    ev2d_free((ev2d *)h);
+    free(h);
+}

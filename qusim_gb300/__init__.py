@@ -1,0 +1,10 @@
+"""qusim_gb300 -- GB300 (sm_103a) split-operator time evolution, a drop-in
+GPU_GB300 device for QuSim's SplittingMethod1D/2D (O2, O4).
+
+The engine is libqsg.so (C ABI, include/qsg.h); this package holds its
+sources (csrc/), its build (build.py) and a Python mirror of the reference's
+Evolver/Options API (evolver.py).
+"""
+from ._lib import QsgError, load  # noqa: F401
+from .evolver import (BoundaryCondition, Context, Evolver1D, Evolver2D, Instance,  # noqa: F401
+                      Options, SolverMethod, default_context)

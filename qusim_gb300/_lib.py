@@ -1,0 +1,100 @@
+"""ctypes binding of libqsg.so (include/qsg.h).
+
+The library is the product: there is no fallback.  ``load()`` raises
+``QsgError`` if libqsg.so is missing or cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqsg.so")
+
+QSG_OK = 0
+QSG_ERR_ARG = 1
+QSG_ERR_BUDGET = 2
+QSG_ERR_CUDA = 3
+QSG_ERR_TIMEOUT = 4
+QSG_ERR_UNSUPPORTED = 5
+QSG_ERR_STATE = 6
+QSG_FP64 = 0
+QSG_MIXED = 1
+QSG_PERIOD = 0
+QSG_INFINITE_WALL = 1
+
+STATUS_NAMES = {0: "ok", 1: "bad argument", 2: "out of budget", 3: "cuda error", 4: "timeout",
+                5: "unsupported", 6: "bad state"}
+
+# every symbol include/qsg.h declares
+EXPORTS = [
+    "qsg_version", "qsg_last_error", "qsg_init", "qsg_ctx_destroy", "qsg_ctx_stream",
+    "qsg_ctx_bytes_in_use", "qsg_create_1d", "qsg_create_2d", "qsg_step", "qsg_sync",
+    "qsg_norm2", "qsg_energies", "qsg_xavg", "qsg_norm2_range", "qsg_get_psi", "qsg_set_psi",
+    "qsg_steps_taken", "qsg_destroy", "qsg_profile_enable", "qsg_profile_read",
+]
+
+
+class QsgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{STATUS_NAMES.get(code, code)}] {msg}")
+        self.code = code
+
+
+_lib = None
+_lock = threading.Lock()
+
+_vp = ctypes.c_void_p
+_d = ctypes.c_double
+_dp = ctypes.POINTER(ctypes.c_double)
+_u64 = ctypes.c_uint64
+_i = ctypes.c_int
+_sz = ctypes.c_size_t
+
+
+def _declare(lib):
+    lib.qsg_version.restype = ctypes.c_char_p
+    lib.qsg_last_error.restype = ctypes.c_char_p
+    lib.qsg_init.argtypes = [_i, _sz, ctypes.POINTER(_vp)]
+    lib.qsg_ctx_destroy.argtypes = [_vp]
+    lib.qsg_ctx_destroy.restype = None
+    lib.qsg_ctx_stream.argtypes = [_vp]
+    lib.qsg_ctx_stream.restype = _vp
+    lib.qsg_ctx_bytes_in_use.argtypes = [_vp]
+    lib.qsg_ctx_bytes_in_use.restype = _sz
+    lib.qsg_create_1d.argtypes = [_vp, _u64, _d, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, ctypes.POINTER(_vp)]
+    lib.qsg_create_2d.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp,
+                                  ctypes.POINTER(_vp)]
+    lib.qsg_step.argtypes = [_vp, _u64, _i]
+    lib.qsg_sync.argtypes = [_vp]
+    lib.qsg_norm2.argtypes = [_vp, _dp]
+    lib.qsg_energies.argtypes = [_vp, _dp, _dp]
+    lib.qsg_xavg.argtypes = [_vp, _d, _dp]
+    lib.qsg_norm2_range.argtypes = [_vp, _d, _d, _d, _dp]
+    lib.qsg_get_psi.argtypes = [_vp, _dp]
+    lib.qsg_set_psi.argtypes = [_vp, _dp]
+    lib.qsg_steps_taken.argtypes = [_vp, ctypes.POINTER(_u64)]
+    lib.qsg_destroy.argtypes = [_vp]
+    lib.qsg_destroy.restype = None
+    lib.qsg_profile_enable.argtypes = [_vp, _i]
+    lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
+
+
+def load(path: str = LIB_PATH):
+    """Load libqsg.so (once).  Raises QsgError if it is not there."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise QsgError(QSG_ERR_STATE, f"{path} not built: run `python -m qusim_gb300.build`")
+            lib = ctypes.CDLL(path)
+            _declare(lib)
+            _lib = lib
+        return _lib
+
+
+def check(rc: int):
+    if rc != QSG_OK:
+        raise QsgError(rc, load().qsg_last_error().decode())
+    return rc

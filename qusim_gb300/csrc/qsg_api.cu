@@ -1,0 +1,869 @@
+// qsg_api.cu -- the C ABI (include/qsg.h): contexts, instances, step
+// scheduling, observables.
+//
+// Step schedule (reference: QuUpdatePsi, src/SplittingUtils.h:14-64, with
+// fold_head_tail == false, so every V factor is applied as its own multiply):
+//
+//   1D, n fits one CTA:  one k_evolve1d_resident launch runs all nsteps.
+//   2D:  R(N->S, V)  then per step
+//          O2: C(K1)  R(S->S, V V)            ... last step: R(S->N, V)
+//          O4: C(KD1) R(S->S, VC2) C(KD2) R(S->S, VC2) C(KD1) R(S->S, VC1 VC1)
+//                                              ... last step: R(S->N, VC1)
+//        R = k_row_pass, C = k_col_pass, N = natural real space, S = split-k
+//        space; "V V" multiplies by the same table twice (the reference's two
+//        ExpV calls at the step boundary).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/qsg.h"
+#include "qsg_aux.h"
+#include "qsg_launch.h"
+
+using qsg::Geom2D;
+using cd = std::complex<double>;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define QSG_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ == cudaErrorNotSupported)                                                   \
+            return fail(QSG_ERR_UNSUPPORTED, std::string("unsupported size: ") + #call);   \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(QSG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+const double kPi = 3.141592653589793238462643383279502884197169399375;
+
+// SplittingUtils.cpp:3-8
+struct SplitConsts {
+    double c1, c2, d1, d2;
+    SplitConsts()
+    {
+        const double t = std::pow(2.0, 1.0 / 3.0);
+        c1 = 1 / (2 * (2 - t));
+        c2 = (1 - t) / (2 * (2 - t));
+        d1 = 1 / (2 - t);
+        d2 = -t / (2 - t);
+    }
+};
+
+struct ProfStat {
+    uint64_t launches = 0;
+    double total_ms = 0;
+};
+
+}  // namespace
+
+struct qsg_ctx {
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    size_t budget = 0, in_use = 0;
+    std::mutex mu;
+    std::map<std::tuple<int, int, int>, void *> tw_cache;  // (prec, L, E) -> stage-major twiddles
+    std::map<std::pair<int, int>, void *> circle_cache;    // (prec, n) -> exp(-2 pi i m/n)
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    double *partials = nullptr;  // reduction partials
+    int max_partials = 0;
+    double *sums = nullptr;      // small device result buffer
+    double *host_sums = nullptr; // pinned mirror
+    bool prof = false;
+    std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> prof_pending;
+    std::vector<cudaEvent_t> event_pool;
+    std::map<std::string, ProfStat> prof_stats;
+    std::vector<std::string> prof_names;  // stable storage for returned names
+};
+
+struct qsg_inst {
+    qsg_ctx *ctx = nullptr;
+    int dim = 1;
+    uint64_t n = 0;
+    int nx = 0, ny = 0;
+    double dx = 0, dy = 0, dv = 0, mass = 1, hbar = 1;
+    cd dt;
+    int order = 2, prec = 0, boundary = 0;
+    void *psi = nullptr;
+    double *V = nullptr;
+    void *vtab[2] = {nullptr, nullptr};
+    void *ktab[2] = {nullptr, nullptr};  // 1D kinetic tables, or 2D fp64 full tables
+    void *kx[2] = {nullptr, nullptr}, *ky[2] = {nullptr, nullptr};  // 2D complex64 separable
+    const void *tw = nullptr, *tw_row = nullptr, *tw_col = nullptr, *tw_nx = nullptr;
+    Geom2D geom{};
+    uint64_t steps = 0;
+    std::vector<void *> allocs;
+    size_t bytes = 0;
+};
+
+namespace {
+
+size_t csize(int prec) { return prec == 1 ? 8 : 16; }
+
+// Allocate device memory.  Instance memory, twiddle tables and scratch count
+// against the context's HBM budget; the context's own fixed buffers (budgeted
+// = false) do not.
+int dev_alloc(qsg_ctx *ctx, size_t bytes, void **p, size_t *acct, bool budgeted = true)
+{
+    if (budgeted && ctx->budget && ctx->in_use + bytes > ctx->budget)
+        return fail(QSG_ERR_BUDGET, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
+                                        std::to_string(ctx->budget - ctx->in_use) + " left");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (budgeted) ctx->in_use += bytes;
+    if (acct) *acct += bytes;
+    return QSG_OK;
+}
+
+int inst_alloc(qsg_inst *in, size_t bytes, void **p)
+{
+    int rc = dev_alloc(in->ctx, bytes, p, &in->bytes);
+    if (rc == QSG_OK) in->allocs.push_back(*p);
+    return rc;
+}
+
+int ensure_scratch(qsg_ctx *ctx, size_t bytes)
+{
+    if (ctx->scratch_bytes >= bytes) return QSG_OK;
+    if (ctx->scratch) {
+        cudaStreamSynchronize(ctx->st);
+        cudaFree(ctx->scratch);
+        ctx->in_use -= ctx->scratch_bytes;
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    int rc = dev_alloc(ctx, bytes, &ctx->scratch, nullptr);
+    if (rc == QSG_OK) ctx->scratch_bytes = bytes;
+    return rc;
+}
+
+// twiddle table entry: complex128 {re, im}; complex64 {hi.re, hi.im, lo.re, lo.im}
+// with hi = float(v), lo = float(v - hi)
+size_t twsize(int) { return 16; }
+
+void put_twiddle(int prec, unsigned char *dst, long double re, long double im)
+{
+    if (prec == 1) {
+        const float hr = (float)re, hi = (float)im;
+        float v[4] = {hr, hi, (float)(re - (long double)hr), (float)(im - (long double)hi)};
+        std::memcpy(dst, v, 16);
+    } else {
+        double v[2] = {(double)re, (double)im};
+        std::memcpy(dst, v, 16);
+    }
+}
+
+// stage-major twiddles of qsg::Plan<L, E>, from long double
+int get_twiddles(qsg_ctx *ctx, int prec, int L, int E, const void **out)
+{
+    auto key = std::make_tuple(prec, L, E);
+    auto it = ctx->tw_cache.find(key);
+    if (it != ctx->tw_cache.end()) {
+        *out = it->second;
+        return QSG_OK;
+    }
+    qsg::PlanRT p(L, E);
+    const int size = p.tw_size() > 0 ? p.tw_size() : 1;
+    std::vector<long double> re(size, 1.0L), im(size, 0.0L);
+    int off = 0;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int s = 1; s < p.nst; ++s) {
+        const int R = 1 << p.radix_log(s), P = 1 << p.p_log(s);
+        for (int q = 1; q < R; ++q)
+            for (int k = 0; k < P; ++k) {
+                const long double ang = two_pi * (long double)(q * k) / (long double)(P * R);
+                re[off + (q - 1) * P + k] = cosl(ang);
+                im[off + (q - 1) * P + k] = -sinl(ang);
+            }
+        off += (R - 1) * P;
+    }
+    std::vector<unsigned char> host(size * twsize(prec));
+    for (int i = 0; i < size; ++i) put_twiddle(prec, &host[i * twsize(prec)], re[i], im[i]);
+    void *d = nullptr;
+    int rc = dev_alloc(ctx, host.size(), &d, nullptr);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice));
+    ctx->tw_cache[key] = d;
+    *out = d;
+    return QSG_OK;
+}
+
+// exp(-2 pi i m / n), m < n
+int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
+{
+    auto key = std::make_pair(prec, n);
+    auto it = ctx->circle_cache.find(key);
+    if (it != ctx->circle_cache.end()) {
+        *out = it->second;
+        return QSG_OK;
+    }
+    std::vector<unsigned char> host((size_t)n * twsize(prec));
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int m = 0; m < n; ++m) {
+        const long double ang = two_pi * (long double)m / (long double)n;
+        put_twiddle(prec, &host[(size_t)m * twsize(prec)], cosl(ang), -sinl(ang));
+    }
+    void *d = nullptr;
+    int rc = dev_alloc(ctx, host.size(), &d, nullptr);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice));
+    ctx->circle_cache[key] = d;
+    *out = d;
+    return QSG_OK;
+}
+
+// --- profiling -------------------------------------------------------------
+
+cudaEvent_t take_event(qsg_ctx *ctx)
+{
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct ProfScope {
+    qsg_ctx *ctx;
+    const char *name;
+    cudaEvent_t e0 = nullptr;
+    ProfScope(qsg_ctx *c, const char *n) : ctx(c), name(n)
+    {
+        if (ctx->prof) {
+            e0 = take_event(ctx);
+            cudaEventRecord(e0, ctx->st);
+        }
+    }
+    ~ProfScope()
+    {
+        if (e0) {
+            cudaEvent_t e1 = take_event(ctx);
+            cudaEventRecord(e1, ctx->st);
+            ctx->prof_pending.emplace_back(name, e0, e1);
+        }
+    }
+};
+
+void prof_drain(qsg_ctx *ctx)
+{
+    if (ctx->prof_pending.empty()) return;
+    cudaStreamSynchronize(ctx->st);
+    for (auto &p : ctx->prof_pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, std::get<1>(p), std::get<2>(p));
+        auto &s = ctx->prof_stats[std::get<0>(p)];
+        s.launches += 1;
+        s.total_ms += ms;
+        ctx->event_pool.push_back(std::get<1>(p));
+        ctx->event_pool.push_back(std::get<2>(p));
+    }
+    ctx->prof_pending.clear();
+}
+
+// --- steps -----------------------------------------------------------------
+
+int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
+{
+    qsg::Evolve1DArgs a{};
+    a.psi = in->psi;
+    a.vtab[0] = in->vtab[0];
+    a.vtab[1] = in->vtab[1];
+    a.ktab[0] = in->ktab[0];
+    a.ktab[1] = in->ktab[1];
+    a.tw = in->tw;
+    a.norm_out = nullptr;
+    a.dv = in->dv;
+    a.nsteps = nsteps;
+    a.order = in->order;
+    a.renormalize = renorm;
+    ProfScope ps(in->ctx, "evolve1d_resident");
+    QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, in->ctx->st));
+    return QSG_OK;
+}
+
+int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double *partials,
+             const void *src = nullptr, void *dst = nullptr)
+{
+    qsg::RowPassArgs a{};
+    a.in = src ? src : in->psi;
+    a.out = dst ? dst : in->psi;
+    a.vtab = v;
+    a.vtwice = vtwice ? 1 : 0;
+    a.tw_row = in->tw_row;
+    a.tw_nx = in->tw_nx;
+    a.partials = partials;
+    a.nx = in->nx;
+    a.m = in->geom.m;
+    ProfScope ps(in->ctx, "row_pass");
+    QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, is, os, a, in->ctx->st));
+    return QSG_OK;
+}
+
+int col_pass(qsg_inst *in, int d)
+{
+    qsg::ColPassArgs a{};
+    a.psi = in->psi;
+    a.kx = in->kx[d];
+    a.ky = in->ky[d];
+    a.k2d = in->ktab[d];
+    a.tw_col = in->tw_col;
+    a.nx = in->nx;
+    a.ny = in->ny;
+    a.g = in->geom.g;
+    a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
+    ProfScope ps(in->ctx, "col_pass");
+    QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->ctx->st));
+    return QSG_OK;
+}
+
+int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
+{
+    qsg_ctx *ctx = in->ctx;
+    double *parts = nullptr;
+    if (renorm) {
+        if (in->geom.row_blocks > ctx->max_partials)
+            return fail(QSG_ERR_STATE, "partials buffer too small");
+        parts = ctx->partials;
+    }
+    int rc;
+    const void *V0 = in->vtab[0], *V1 = in->vtab[1];
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        const bool last = s + 1 == nsteps;
+        if (s == 0 && (rc = row_pass(in, false, true, V0, false, nullptr))) return rc;
+        if (in->order == 2) {
+            if ((rc = col_pass(in, 0))) return rc;
+        } else {
+            if ((rc = col_pass(in, 0))) return rc;
+            if ((rc = row_pass(in, true, true, V1, false, nullptr))) return rc;
+            if ((rc = col_pass(in, 1))) return rc;
+            if ((rc = row_pass(in, true, true, V1, false, nullptr))) return rc;
+            if ((rc = col_pass(in, 0))) return rc;
+        }
+        if (last)
+            rc = row_pass(in, true, false, V0, false, parts);
+        else
+            rc = row_pass(in, true, true, V0, true, nullptr);
+        if (rc) return rc;
+    }
+    if (renorm) {
+        ProfScope ps(ctx, "renorm");
+        QSG_CUDA(qsg::launch_finalize(ctx->partials, in->geom.row_blocks, 1, ctx->sums, ctx->st));
+        QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
+    }
+    return QSG_OK;
+}
+
+// sum over psi[lo, hi) with the given reduction mode; synchronous
+int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
+{
+    qsg_ctx *ctx = in->ctx;
+    int np = 0;
+    QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, lo, hi, mode, ctx->partials, ctx->max_partials,
+                                &np, ctx->st));
+    QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    *out = ctx->host_sums[0];
+    return QSG_OK;
+}
+
+int build_tables(qsg_inst *in)
+{
+    qsg_ctx *ctx = in->ctx;
+    const SplitConsts sc;
+    const int ntab = in->order == 2 ? 1 : 2;
+    const double vc[2] = {in->order == 2 ? 0.5 : sc.c1, sc.c2};
+    const double tc[2] = {in->order == 2 ? 1.0 : sc.d1, sc.d2};
+    const size_t cs = csize(in->prec);
+    const cd I(0, 1);
+    int rc;
+    for (int k = 0; k < ntab; ++k) {
+        // ExpV coefficient -i/hbar * dt * c (SplittingMethod1D.cpp:87, SplittingMethod2D.cpp:43-50)
+        const cd f = (-I / in->hbar) * in->dt * vc[k];
+        if ((rc = inst_alloc(in, in->n * cs, &in->vtab[k]))) return rc;
+        QSG_CUDA(qsg::launch_vtable(in->prec, in->vtab[k], in->V, in->n, f.real(), f.imag(), ctx->st));
+    }
+    if (in->dim == 1) {
+        // ExpT periodic: f = -i DT dt t / hbar, DT = (Dk hbar)^2/(2m), Dk = 2 pi/(dx N)
+        // (SplittingMethod1D.cpp:51-53)
+        const double dk = 2 * kPi / (in->dx * in->n);
+        const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
+        for (int k = 0; k < ntab; ++k) {
+            const cd f = -I * DT * in->dt * tc[k] / in->hbar;
+            if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
+            QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
+                                          1.0 / (double)in->n, ctx->st));
+        }
+    } else {
+        // SplittingMethod2D::InitExpT (src/SplittingMethod2D.cpp:56-79)
+        const double dkx = 2 * kPi / (in->dx * in->nx), dky = 2 * kPi / (in->dy * in->ny);
+        const double DTx = (dkx * in->hbar) * (dkx * in->hbar) / (2 * in->mass);
+        const double DTy = (dky * in->hbar) * (dky * in->hbar) / (2 * in->mass);
+        const cd alpha = -I * in->dt / in->hbar;
+        for (int k = 0; k < ntab; ++k) {
+            const cd a = in->order == 2 ? alpha : alpha * tc[k];
+            if (in->prec == 0) {
+                if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
+                QSG_CUDA(qsg::launch_ktable2d(in->ktab[k], in->nx, in->ny, a.real(), a.imag(), DTx, DTy,
+                                              1.0 / ((double)in->nx * in->ny), ctx->st));
+            } else {
+                const cd fx = a * DTx, fy = a * DTy;
+                if ((rc = inst_alloc(in, (size_t)in->nx * cs, &in->kx[k]))) return rc;
+                if ((rc = inst_alloc(in, (size_t)in->ny * cs, &in->ky[k]))) return rc;
+                QSG_CUDA(qsg::launch_ktable1d(1, in->kx[k], in->nx, fx.real(), fx.imag(), 1.0, ctx->st));
+                QSG_CUDA(qsg::launch_ktable1d(1, in->ky[k], in->ny, fy.real(), fy.imag(), 1.0, ctx->st));
+            }
+        }
+    }
+    return QSG_OK;
+}
+
+int upload_psi(qsg_inst *in, const double *psi)
+{
+    qsg_ctx *ctx = in->ctx;
+    if (in->prec == 0) {
+        QSG_CUDA(cudaMemcpyAsync(in->psi, psi, in->n * 16, cudaMemcpyHostToDevice, ctx->st));
+        return QSG_OK;
+    }
+    int rc = ensure_scratch(ctx, in->n * 16);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, psi, in->n * 16, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(qsg::launch_c128_to_c64(in->psi, ctx->scratch, in->n, ctx->st));
+    return QSG_OK;
+}
+
+void free_inst(qsg_inst *in)
+{
+    if (!in) return;
+    if (in->ctx) {
+        cudaStreamSynchronize(in->ctx->st);
+        for (void *p : in->allocs) cudaFree(p);
+        in->ctx->in_use -= in->bytes;
+    }
+    delete in;
+}
+
+int common_create(qsg_inst *in, const double *psi0, const double *V)
+{
+    qsg_ctx *ctx = in->ctx;
+    int rc;
+    if ((rc = inst_alloc(in, in->n * csize(in->prec), &in->psi))) return rc;
+    void *v = nullptr;
+    if ((rc = inst_alloc(in, in->n * 8, &v))) return rc;
+    in->V = (double *)v;
+    QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyHostToDevice, ctx->st));
+    if ((rc = upload_psi(in, psi0))) return rc;
+    if ((rc = build_tables(in))) return rc;
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return QSG_OK;
+}
+
+bool finite_pos(double v) { return std::isfinite(v) && v > 0; }
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+const char *qsg_version(void) { return "qsg 0.1 (sm_103a)"; }
+
+const char *qsg_last_error(void) { return g_last_error.c_str(); }
+
+int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
+{
+    if (!out) return fail(QSG_ERR_ARG, "qsg_init: out is null");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+    if (device_ordinal < 0 || device_ordinal >= ndev)
+        return fail(QSG_ERR_ARG, "qsg_init: no CUDA device " + std::to_string(device_ordinal));
+    QSG_CUDA(cudaSetDevice(device_ordinal));
+    cudaDeviceProp prop;
+    QSG_CUDA(cudaGetDeviceProperties(&prop, device_ordinal));
+    if (prop.major * 10 + prop.minor < 100)
+        return fail(QSG_ERR_UNSUPPORTED, std::string("qsg_init: device ") + prop.name +
+                                             " is not a Blackwell (sm_10x) GPU");
+    qsg_ctx *ctx = new qsg_ctx();
+    ctx->dev = device_ordinal;
+    ctx->budget = hbm_budget_bytes;
+    e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return fail(QSG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    ctx->max_partials = 65536;
+    void *p = nullptr;
+    int rc = dev_alloc(ctx, sizeof(double) * 2 * ctx->max_partials, &p, nullptr, false);
+    if (rc) {
+        qsg_ctx_destroy(ctx);
+        return rc;
+    }
+    ctx->partials = (double *)p;
+    if ((rc = dev_alloc(ctx, sizeof(double) * 8, &p, nullptr, false))) {
+        qsg_ctx_destroy(ctx);
+        return rc;
+    }
+    ctx->sums = (double *)p;
+    e = cudaMallocHost(&p, sizeof(double) * 8);
+    if (e != cudaSuccess) {
+        qsg_ctx_destroy(ctx);
+        return fail(QSG_ERR_CUDA, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    ctx->host_sums = (double *)p;
+    *out = ctx;
+    return QSG_OK;
+}
+
+void qsg_ctx_destroy(qsg_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->dev);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (auto &kv : ctx->tw_cache) cudaFree(kv.second);
+    for (auto &kv : ctx->circle_cache) cudaFree(kv.second);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->partials) cudaFree(ctx->partials);
+    if (ctx->sums) cudaFree(ctx->sums);
+    if (ctx->host_sums) cudaFreeHost(ctx->host_sums);
+    for (auto &p : ctx->prof_pending) {
+        cudaEventDestroy(std::get<1>(p));
+        cudaEventDestroy(std::get<2>(p));
+    }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+void *qsg_ctx_stream(qsg_ctx *ctx) { return ctx ? (void *)ctx->st : nullptr; }
+
+size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx) { return ctx ? ctx->in_use : 0; }
+
+int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
+                  double dt_im, int order, int precision, int boundary, const double *psi0,
+                  const double *V, qsg_inst **out)
+{
+    if (!ctx || !out || !psi0 || !V) return fail(QSG_ERR_ARG, "qsg_create_1d: null argument");
+    *out = nullptr;
+    if (order != 2 && order != 4) return fail(QSG_ERR_ARG, "qsg_create_1d: order must be 2 or 4");
+    if (precision != QSG_FP64 && precision != QSG_MIXED)
+        return fail(QSG_ERR_ARG, "qsg_create_1d: precision must be QSG_FP64 or QSG_MIXED");
+    if (!finite_pos(dx) || !finite_pos(mass) || !finite_pos(hbar) || !std::isfinite(dt_re) ||
+        !std::isfinite(dt_im))
+        return fail(QSG_ERR_ARG, "qsg_create_1d: dx, mass, hbar must be finite and > 0, dt finite");
+    if (boundary == QSG_INFINITE_WALL)
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall boundary is not built");
+    if (boundary != QSG_PERIOD) return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
+    if (!qsg::evolve1d_supported(precision, n))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
+                                             " (supported: powers of two, 64 .. " +
+                                             (precision == 1 ? "8192" : "4096") + ")");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    qsg_inst *in = new qsg_inst();
+    in->ctx = ctx;
+    in->dim = 1;
+    in->n = n;
+    in->nx = (int)n;
+    in->dx = dx;
+    in->dv = dx;
+    in->mass = mass;
+    in->hbar = hbar;
+    in->dt = cd(dt_re, dt_im);
+    in->order = order;
+    in->prec = precision;
+    in->boundary = boundary;
+    int rc = get_twiddles(ctx, precision, (int)n, qsg::elems_per_thread(precision), &in->tw);
+    if (!rc) rc = common_create(in, psi0, V);
+    if (rc) {
+        std::string msg = g_last_error;
+        free_inst(in);
+        return fail(rc, msg);
+    }
+    *out = in;
+    return QSG_OK;
+}
+
+int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
+                  double hbar, double dt_re, double dt_im, int order, int precision,
+                  const double *psi0, const double *V, qsg_inst **out)
+{
+    if (!ctx || !out || !psi0 || !V) return fail(QSG_ERR_ARG, "qsg_create_2d: null argument");
+    *out = nullptr;
+    if (order != 2 && order != 4) return fail(QSG_ERR_ARG, "qsg_create_2d: order must be 2 or 4");
+    if (precision != QSG_FP64 && precision != QSG_MIXED)
+        return fail(QSG_ERR_ARG, "qsg_create_2d: precision must be QSG_FP64 or QSG_MIXED");
+    if (!finite_pos(dx) || !finite_pos(dy) || !finite_pos(mass) || !finite_pos(hbar) ||
+        !std::isfinite(dt_re) || !std::isfinite(dt_im))
+        return fail(QSG_ERR_ARG, "qsg_create_2d: dx, dy, mass, hbar must be finite and > 0, dt finite");
+    Geom2D g{};
+    if (nx > 65536 || ny > 65536 || !qsg::geom2d(precision, (int)nx, (int)ny, &g))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" +
+                                             std::to_string(ny) +
+                                             " (supported: powers of two, 128 .. 4096 per side)");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    qsg_inst *in = new qsg_inst();
+    in->ctx = ctx;
+    in->dim = 2;
+    in->nx = (int)nx;
+    in->ny = (int)ny;
+    in->n = nx * ny;
+    in->dx = dx;
+    in->dy = dy;
+    in->dv = dx * dy;
+    in->mass = mass;
+    in->hbar = hbar;
+    in->dt = cd(dt_re, dt_im);
+    in->order = order;
+    in->prec = precision;
+    in->geom = g;
+    const int E = qsg::elems_per_thread(precision);
+    int rc = get_twiddles(ctx, precision, (int)ny, E, &in->tw_row);
+    if (!rc) rc = get_twiddles(ctx, precision, g.m, E, &in->tw_col);
+    if (!rc) rc = get_circle(ctx, precision, (int)nx, &in->tw_nx);
+    if (!rc) rc = common_create(in, psi0, V);
+    if (rc) {
+        std::string msg = g_last_error;
+        free_inst(in);
+        return fail(rc, msg);
+    }
+    *out = in;
+    return QSG_OK;
+}
+
+int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_step: null instance");
+    if (nsteps == 0 && !renormalize) return QSG_OK;
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    QSG_CUDA(cudaSetDevice(in->ctx->dev));
+    int rc;
+    if (nsteps == 0) {
+        // renormalise only
+        double s = 0;
+        if ((rc = reduce(in, 0, in->n, 0, &s))) return rc;
+        QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, in->ctx->sums, in->dv, in->ctx->st));
+        return QSG_OK;
+    }
+    rc = in->dim == 1 ? step1d(in, nsteps, renormalize) : step2d(in, nsteps, renormalize);
+    if (rc) return rc;
+    in->steps += nsteps;
+    return QSG_OK;
+}
+
+int qsg_sync(qsg_inst *in)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_sync: null instance");
+    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    return QSG_OK;
+}
+
+int qsg_norm2(qsg_inst *in, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    double s = 0;
+    int rc = reduce(in, 0, in->n, 0, &s);
+    if (rc) return rc;
+    *out = s * in->dv;
+    return QSG_OK;
+}
+
+int qsg_energies(qsg_inst *in, double *kin, double *pot)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_energies: null instance");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    qsg_ctx *ctx = in->ctx;
+    int rc;
+    if (pot) {
+        // Abs2Mul(psi, V) dv / Norm2 (src/EvolverImpl.cpp:45-49)
+        double s1 = 0, s0 = 0;
+        if ((rc = reduce(in, 0, in->n, 1, &s1))) return rc;
+        if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
+        *pot = (s1 * in->dv) / (s0 * in->dv);
+    }
+    if (kin) {
+        if (in->dim == 1) {
+            // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102)
+            const double dk = 2 * kPi / (in->dx * in->n);
+            const double DT = dk * dk / (2 * in->mass);
+            QSG_CUDA(qsg::launch_kinetic1d(in->prec, (int)in->n, in->psi, in->tw, DT, ctx->sums, ctx->st));
+            QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                     ctx->st));
+            QSG_CUDA(cudaStreamSynchronize(ctx->st));
+            *kin = ctx->host_sums[0] / ctx->host_sums[1];
+        } else {
+            const double dkx = 2 * kPi / (in->dx * in->nx), dky = 2 * kPi / (in->dy * in->ny);
+            const double DTx = (dkx * in->hbar) * (dkx * in->hbar) / (2 * in->mass);
+            const double DTy = (dky * in->hbar) * (dky * in->hbar) / (2 * in->mass);
+            if ((rc = ensure_scratch(ctx, in->n * csize(in->prec)))) return rc;
+            if ((rc = row_pass(in, false, true, nullptr, false, nullptr, in->psi, ctx->scratch))) return rc;
+            qsg::ColPassArgs a{};
+            a.psi = ctx->scratch;
+            a.tw_col = in->tw_col;
+            a.nx = in->nx;
+            a.ny = in->ny;
+            a.g = in->geom.g;
+            const int nblk = (in->ny / in->geom.col_w) * in->geom.g;
+            if (nblk > ctx->max_partials) return fail(QSG_ERR_STATE, "partials buffer too small");
+            QSG_CUDA(qsg::launch_col_kinetic(in->prec, in->geom, a, DTx, DTy, ctx->partials, ctx->st));
+            QSG_CUDA(qsg::launch_finalize(ctx->partials, nblk, 2, ctx->sums, ctx->st));
+            QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                     ctx->st));
+            QSG_CUDA(cudaStreamSynchronize(ctx->st));
+            *kin = ctx->host_sums[0] / ctx->host_sums[1];
+        }
+    }
+    return QSG_OK;
+}
+
+int qsg_xavg(qsg_inst *in, double x0, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_xavg: null argument");
+    if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_xavg: 1D instances only");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    double s2 = 0, s0 = 0;
+    int rc;
+    if ((rc = reduce(in, 0, in->n, 2, &s2))) return rc;
+    if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
+    *out = x0 + in->dx * (s2 / s0);
+    return QSG_OK;
+}
+
+int qsg_norm2_range(qsg_inst *in, double x0, double xa, double xb, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2_range: null argument");
+    if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_norm2_range: 1D instances only");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    int64_t i1 = (int64_t)((xa - x0) / in->dx), i2 = (int64_t)((xb - x0) / in->dx);
+    if (i1 <= 0) i1 = 0;
+    if (i2 >= (int64_t)in->n) i2 = (int64_t)in->n;
+    if (i1 >= i2) {
+        *out = 0;
+        return QSG_OK;
+    }
+    double s = 0;
+    int rc = reduce(in, (size_t)i1, (size_t)i2, 0, &s);
+    if (rc) return rc;
+    *out = s * in->dx;
+    return QSG_OK;
+}
+
+int qsg_get_psi(qsg_inst *in, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_psi: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    qsg_ctx *ctx = in->ctx;
+    if (in->prec == 0) {
+        QSG_CUDA(cudaMemcpyAsync(out, in->psi, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
+    } else {
+        int rc = ensure_scratch(ctx, in->n * 16);
+        if (rc) return rc;
+        QSG_CUDA(qsg::launch_c64_to_c128(ctx->scratch, in->psi, in->n, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(out, ctx->scratch, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
+    }
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return QSG_OK;
+}
+
+int qsg_set_psi(qsg_inst *in, const double *psi)
+{
+    if (!in || !psi) return fail(QSG_ERR_ARG, "qsg_set_psi: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    int rc = upload_psi(in, psi);
+    if (rc) return rc;
+    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    return QSG_OK;
+}
+
+int qsg_steps_taken(qsg_inst *in, uint64_t *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_steps_taken: null argument");
+    *out = in->steps;
+    return QSG_OK;
+}
+
+void qsg_destroy(qsg_inst *in)
+{
+    if (!in) return;
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    free_inst(in);
+}
+
+int qsg_profile_enable(qsg_ctx *ctx, int on)
+{
+    if (!ctx) return fail(QSG_ERR_ARG, "qsg_profile_enable: null context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    prof_drain(ctx);
+    ctx->prof_stats.clear();
+    ctx->prof = on != 0;
+    return QSG_OK;
+}
+
+int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launches, double *total_ms)
+{
+    if (!ctx) return fail(QSG_ERR_ARG, "qsg_profile_read: null context");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    prof_drain(ctx);
+    ctx->prof_names.clear();
+    for (auto &kv : ctx->prof_stats) ctx->prof_names.push_back(kv.first);
+    int i = 0;
+    for (auto &kv : ctx->prof_stats) {
+        if (i < cap) {
+            if (names) names[i] = ctx->prof_names[i].c_str();
+            if (launches) launches[i] = kv.second.launches;
+            if (total_ms) total_ms[i] = kv.second.total_ms;
+        }
+        ++i;
+    }
+    return i;
+}
+
+}  // extern "C"
+
+namespace qsg {
+
+PlanRT::PlanRT(int L_, int E_) : L(L_), E(E_)
+{
+    auto lg = [](int v) {
+        int r = 0;
+        while ((1 << r) < v) ++r;
+        return r;
+    };
+    const int logl = lg(L), le = lg(E);
+    loge = le;
+    nst = (logl + le - 1) / le;
+    logr0 = logl - (nst - 1) * le;
+}
+
+int PlanRT::tw_size() const
+{
+    int off = 0;
+    for (int s = 1; s < nst; ++s) off += ((1 << radix_log(s)) - 1) * (1 << p_log(s));
+    return off;
+}
+
+}  // namespace qsg

@@ -1,0 +1,398 @@
+// qsg_fft.cuh -- register/shared-memory Stockham FFT building blocks for sm_103a.
+//
+// A "line" is one 1D transform of length L (a power of two).  Each thread of a
+// line owns E elements (E a power of two, E <= L): at entry and exit of a
+// transform, register slot e of thread t holds element t + e*(L/E) of the line
+// (natural order), so an FFT, a pointwise multiply and an inverse FFT chain in
+// registers with no reordering.  Between radix stages the data goes through
+// shared memory once (Stockham autosort: every stage reads element t + e*L/E
+// and writes a permuted position, so no bit reversal pass is ever needed).
+//
+// Transform definitions follow the reference (src/FourierTransform.h:16-20):
+// forward X_k = sum_n x_n exp(-2 pi i k n / L), inverse unnormalised with the
+// + sign.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qsg {
+
+template <class T> struct CplxOf;
+template <> struct CplxOf<float> { using type = float2; };
+template <> struct CplxOf<double> { using type = double2; };
+template <class T> using cplx_t = typename CplxOf<T>::type;
+
+template <class C> struct RealOf;
+template <> struct RealOf<float2> { using type = float; };
+template <> struct RealOf<double2> { using type = double; };
+
+template <class C>
+__device__ __forceinline__ C cmk(typename RealOf<C>::type x, typename RealOf<C>::type y)
+{
+    C r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+template <class C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
+template <class C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+template <class C> __device__ __forceinline__ C cmul(C a, C b)
+{
+    return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <class C> __device__ __forceinline__ C cmulc(C a, C b)  // a * conj(b)
+{
+    return cmk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <class C> __device__ __forceinline__ C cscale(C a, typename RealOf<C>::type s)
+{
+    return cmk<C>(a.x * s, a.y * s);
+}
+// multiply by w or conj(w): forward transforms use the table value w = exp(-i th),
+// inverse transforms its conjugate
+template <bool INV, class C> __device__ __forceinline__ C cmulw(C a, C w)
+{
+    return INV ? cmulc(a, w) : cmul(a, w);
+}
+// a * (1 + m) for m stored as (cos th - 1, sin th): the "phase minus one"
+// representation used by the complex64 tables, which keeps the systematic
+// rounding of a unit-modulus factor proportional to |th| instead of to 1.
+template <class C> __device__ __forceinline__ C cmul1p(C a, C m)
+{
+    return cmk<C>(fma(a.x, m.x, fma(-a.y, m.y, a.x)), fma(a.y, m.x, fma(a.x, m.y, a.y)));
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, class C> __device__ __forceinline__ C crot(C a)
+{
+    return INV ? cmk<C>(-a.y, a.x) : cmk<C>(a.y, -a.x);
+}
+
+// ---------------------------------------------------------------------------
+// Small DFTs on register arrays (natural order in, natural order out).
+// ---------------------------------------------------------------------------
+
+template <bool INV, class C> __device__ __forceinline__ void dft2(C &a0, C &a1)
+{
+    C t = a0;
+    a0 = cadd(t, a1);
+    a1 = csub(t, a1);
+}
+
+template <bool INV, class C> __device__ __forceinline__ void dft4(C &a0, C &a1, C &a2, C &a3)
+{
+    C s02 = cadd(a0, a2), d02 = csub(a0, a2);
+    C s13 = cadd(a1, a3), d13 = crot<INV>(csub(a1, a3));
+    a0 = cadd(s02, s13);
+    a2 = csub(s02, s13);
+    a1 = cadd(d02, d13);
+    a3 = csub(d02, d13);
+}
+
+// ---------------------------------------------------------------------------
+// Multiplication by the fixed roots of unity inside the radix-8/16 butterflies.
+//
+// complex128 uses the constants rounded once.  In complex64 a float rounding
+// of cos(pi/8) or 1/sqrt(2) is off the unit circle by ~3e-8, and since the
+// same constant is applied in every transform of every step, that modulus
+// error compounds coherently (~1e-4 relative error after 2000 O2 steps at
+// N=4096, measured); the complex64 rotations below avoid it (see Roots<float2>),
+// leaving random rounding, which grows like sqrt(steps).
+// ---------------------------------------------------------------------------
+
+template <class C> struct Roots;
+template <> struct Roots<double2> {
+    // a * exp(-+ i th), (c, s) = (cos th, sin th)
+    template <bool INV> static __device__ __forceinline__ double2 cs(double2 a, double c, double s)
+    {
+        return INV ? cmk<double2>(a.x * c - a.y * s, a.y * c + a.x * s)
+                   : cmk<double2>(a.x * c + a.y * s, a.y * c - a.x * s);
+    }
+    static constexpr double C1 = 0.92387953251128675613, S1 = 0.38268343236508977173;
+    static constexpr double H = 0.70710678118654752440;
+    template <bool INV> static __device__ __forceinline__ double2 w16_1(double2 a) { return cs<INV>(a, C1, S1); }
+    template <bool INV> static __device__ __forceinline__ double2 w16_3(double2 a) { return cs<INV>(a, S1, C1); }
+    template <bool INV> static __device__ __forceinline__ double2 w16_9(double2 a) { return cs<INV>(a, -C1, -S1); }
+    // exp(-+ i pi/4), exp(-+ 3 i pi/4)
+    template <bool INV> static __device__ __forceinline__ double2 w8_1(double2 a)
+    {
+        return INV ? cmk<double2>((a.x - a.y) * H, (a.x + a.y) * H) : cmk<double2>((a.x + a.y) * H, (a.y - a.x) * H);
+    }
+    template <bool INV> static __device__ __forceinline__ double2 w8_3(double2 a)
+    {
+        return INV ? cmk<double2>(-(a.x + a.y) * H, (a.x - a.y) * H) : cmk<double2>((a.y - a.x) * H, -(a.x + a.y) * H);
+    }
+};
+template <> struct Roots<float2> {
+    // complex64: each fixed rotation by phi is three shears,
+    //   x += a y;  y += b x;  x += a y,   a = -tan(phi/2), b = sin(phi),
+    // whose matrix has determinant exactly 1 for any rounded a, b, so the
+    // rounding of the constants cannot shrink or grow |psi| coherently (the
+    // modulus error is second order).  3 FMAs instead of the 4 of a complex
+    // product.  Constants for phi = -pi/8, -pi/4, -3pi/8; the inverse uses -a, -b.
+    static constexpr float A1 = 0x1.975f5ep-3f, B1 = -0x1.87de2ap-2f;  // phi = -pi/8
+    static constexpr float A2 = 0x1.a8279ap-2f, B2 = -0x1.6a09e6p-1f;  // phi = -pi/4
+    static constexpr float A3 = 0x1.561b82p-1f, B3 = -0x1.d906bcp-1f;  // phi = -3pi/8
+    template <bool INV> static __device__ __forceinline__ float2 shear(float2 v, float a, float b)
+    {
+        if (INV) {
+            a = -a;
+            b = -b;
+        }
+        float x = fmaf(a, v.y, v.x);
+        const float y = fmaf(b, x, v.y);
+        x = fmaf(a, y, x);
+        return cmk<float2>(x, y);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w16_1(float2 a) { return shear<INV>(a, A1, B1); }
+    template <bool INV> static __device__ __forceinline__ float2 w16_3(float2 a) { return shear<INV>(a, A3, B3); }
+    template <bool INV> static __device__ __forceinline__ float2 w16_9(float2 a)
+    {
+        return shear<INV>(cmk<float2>(-a.x, -a.y), A1, B1);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a) { return shear<INV>(a, A2, B2); }
+    // exp(-+ 3 i pi/4) = exp(-+ i pi/4) * (-+ i)
+    template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a)
+    {
+        return shear<INV>(crot<INV>(a), A2, B2);
+    }
+};
+
+// Table twiddles: complex128 tables hold the factor; complex64 tables hold
+// float4 {hi.x, hi.y, lo.x, lo.y}, the factor as an unevaluated sum of two
+// float pairs (lo = float(w - hi)), multiplied in by both so the product is
+// as accurate as with an exact twiddle (same coherent-modulus reason as above).
+template <class C> struct TwOf;
+template <> struct TwOf<double2> { using type = double2; };
+template <> struct TwOf<float2> { using type = float4; };
+template <class C> using tw_t = typename TwOf<C>::type;
+
+template <bool INV> __device__ __forceinline__ double2 twmul(double2 a, double2 w) { return cmulw<INV>(a, w); }
+template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float4 w)
+{
+    if (INV) {  // a * conj(w)
+        const float lx = fmaf(a.x, w.z, a.y * w.w), ly = fmaf(a.y, w.z, -a.x * w.w);
+        return cmk<float2>(fmaf(a.x, w.x, fmaf(a.y, w.y, lx)), fmaf(a.y, w.x, fmaf(-a.x, w.y, ly)));
+    }
+    const float lx = fmaf(a.x, w.z, -a.y * w.w), ly = fmaf(a.x, w.w, a.y * w.z);
+    return cmk<float2>(fmaf(a.x, w.x, fmaf(-a.y, w.y, lx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ly)));
+}
+
+template <bool INV, class C> __device__ __forceinline__ void dft8(C (&v)[8])
+{
+    // even / odd halves, then combine with w8^k
+    dft4<INV>(v[0], v[2], v[4], v[6]);
+    dft4<INV>(v[1], v[3], v[5], v[7]);
+    C o1 = Roots<C>::template w8_1<INV>(v[3]), o2 = crot<INV>(v[5]), o3 = Roots<C>::template w8_3<INV>(v[7]);
+    C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    v[0] = cadd(e0, v[1]);
+    v[4] = csub(e0, v[1]);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+template <bool INV, class C> __device__ __forceinline__ void dft16(C (&v)[16])
+{
+    using RT = Roots<C>;
+    // n = 4 n1 + n2; first DFT4 over n1 for each n2
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+    // v[4 k1 + n2] now holds z[n2][k1]; twiddle w16^(n2 k1)
+    v[5] = RT::template w16_1<INV>(v[5]);    // n2=1,k1=1: w^1
+    v[6] = RT::template w8_1<INV>(v[6]);     // n2=2,k1=1: w^2
+    v[7] = RT::template w16_3<INV>(v[7]);    // n2=3,k1=1: w^3
+    v[9] = RT::template w8_1<INV>(v[9]);     // n2=1,k1=2: w^2
+    v[10] = crot<INV>(v[10]);                // n2=2,k1=2: w^4
+    v[11] = RT::template w8_3<INV>(v[11]);   // n2=3,k1=2: w^6
+    v[13] = RT::template w16_3<INV>(v[13]);  // n2=1,k1=3: w^3
+    v[14] = RT::template w8_3<INV>(v[14]);   // n2=2,k1=3: w^6
+    v[15] = RT::template w16_9<INV>(v[15]);  // n2=3,k1=3: w^9 = -w^1
+    // second DFT4 over n2 for each k1: output k = k1 + 4 k2
+    C r[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        C a0 = v[4 * k1], a1 = v[4 * k1 + 1], a2 = v[4 * k1 + 2], a3 = v[4 * k1 + 3];
+        dft4<INV>(a0, a1, a2, a3);
+        r[k1] = a0;
+        r[k1 + 4] = a1;
+        r[k1 + 8] = a2;
+        r[k1 + 12] = a3;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = r[i];
+}
+
+template <int R, bool INV, class C> __device__ __forceinline__ void dft(C (&v)[R])
+{
+    if constexpr (R == 2) {
+        dft2<INV>(v[0], v[1]);
+    } else if constexpr (R == 4) {
+        dft4<INV>(v[0], v[1], v[2], v[3]);
+    } else if constexpr (R == 8) {
+        dft8<INV>(v);
+    } else if constexpr (R == 16) {
+        dft16<INV>(v);
+    } else {
+        static_assert(R == 1, "radix must be 1, 2, 4, 8 or 16");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Radix plan for a line of length L with E elements per thread.
+// Stage 0 has radix 2^(log L - (S-1) log E) (the remainder), every later stage
+// radix E.  p_s = product of the radices before stage s.
+// ---------------------------------------------------------------------------
+
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+
+template <int L, int E> struct Plan {
+    static_assert((L & (L - 1)) == 0 && (E & (E - 1)) == 0, "powers of two only");
+    static_assert(E >= 2 && E <= 16 && E <= L, "2 <= E <= 16, E <= L");
+    static constexpr int LOGL = ilog2(L);
+    static constexpr int LOGE = ilog2(E);
+    static constexpr int NST = (LOGL + LOGE - 1) / LOGE;
+    static constexpr int LOGR0 = LOGL - (NST - 1) * LOGE;
+    static constexpr int TL = L / E;  // threads per line
+    __host__ __device__ static constexpr int radix_log(int s) { return s == 0 ? LOGR0 : LOGE; }
+    __host__ __device__ static constexpr int p_log(int s) { return s == 0 ? 0 : LOGR0 + (s - 1) * LOGE; }
+    // offset of stage s in the stage-major twiddle table; stage s holds
+    // (R_s - 1) * p_s entries tw[(q-1)*p_s + k] = exp(-2 pi i q k / (p_s R_s))
+    __host__ __device__ static constexpr int tw_offset(int s)
+    {
+        return s <= 1 ? 0 : tw_offset(s - 1) + ((1 << radix_log(s - 1)) - 1) * (1 << p_log(s - 1));
+    }
+    static constexpr int TW_SIZE = tw_offset(NST);
+};
+
+// One Stockham stage: butterflies on the register slots, twiddles from the
+// stage-major table, then (unless this is the last stage) scatter to shared
+// memory and gather the next stage's inputs.
+//
+//   lay(n)  -> shared-memory element index of line element n (this line)
+//   bar()   -> barrier over every thread that shares the buffer
+template <class C, int L, int E, bool INV, int S, class Lay, class Bar>
+__device__ __forceinline__ void fft_stage(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
+                                          const tw_t<C> *__restrict__ tw)
+{
+    using P = Plan<L, E>;
+    constexpr int RL = P::radix_log(S);
+    constexpr int R = 1 << RL;
+    constexpr int PL = P::p_log(S);
+    constexpr int PP = 1 << PL;
+    constexpr int J = E / R;  // butterflies per thread in this stage
+    constexpr int TL = P::TL;
+    constexpr int TWO = P::tw_offset(S);
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+        C v[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) v[q] = x[j + q * J];
+        if constexpr (PP > 1) {
+            const int k = (t + j * TL) & (PP - 1);
+#pragma unroll
+            for (int q = 1; q < R; ++q) v[q] = twmul<INV>(v[q], __ldg(&tw[TWO + (q - 1) * PP + k]));
+        }
+        dft<R, INV>(v);
+#pragma unroll
+        for (int q = 0; q < R; ++q) x[j + q * J] = v[q];
+    }
+    if constexpr (S + 1 < P::NST) {
+        bar();  // every reader of the previous stage is done with the buffer
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int b = t + j * TL;
+            const int k = b & (PP - 1);
+            const int o = ((b - k) << RL) + k;
+#pragma unroll
+            for (int q = 0; q < R; ++q) sm[lay(o + q * PP)] = x[j + q * J];
+        }
+        bar();
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = sm[lay(t + e * TL)];
+    }
+}
+
+template <class C, int L, int E, bool INV, int S, class Lay, class Bar>
+__device__ __forceinline__ void fft_stages(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
+                                           const tw_t<C> *__restrict__ tw)
+{
+    if constexpr (S < Plan<L, E>::NST) {
+        fft_stage<C, L, E, INV, S>(x, sm, lay, bar, t, tw);
+        fft_stages<C, L, E, INV, S + 1>(x, sm, lay, bar, t, tw);
+    }
+}
+
+// A copy of p the compiler cannot prove equal to p.  A forward and an inverse
+// transform read the same twiddle entries; without this the compiler keeps the
+// first transform's twiddles live in registers for the second (dozens of
+// registers, spills), where reloading them from L1 is nearly free.
+template <class P> __device__ __forceinline__ const P *opaque(const P *p)
+{
+    const P *r;
+    asm volatile("mov.b64 %0, %1;" : "=l"(r) : "l"(p));
+    return r;
+}
+
+// Full transform of one line held in registers (natural order in and out).
+template <class C, int L, int E, bool INV, class Lay, class Bar>
+__device__ __forceinline__ void line_fft(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
+                                         const tw_t<C> *__restrict__ tw)
+{
+    fft_stages<C, L, E, INV, 0>(x, sm, lay, bar, t, opaque(tw));
+}
+
+// Shared-memory index maps.  PADSHIFT adds one element of padding every
+// 2^PADSHIFT elements, which breaks the power-of-two strides of the Stockham
+// scatter across banks.
+template <int PADSHIFT> struct RowLayout {
+    int base;
+    __device__ __forceinline__ int operator()(int n) const { return base + n + (n >> PADSHIFT); }
+};
+// column tile: element n of column c at n*W + c + (n >> SH)*P.  The pad is a
+// function of the row index only, so every address of a thread is a base plus
+// compile-time offsets (no per-element index arithmetic held in registers).
+// (SH, P) per shape come from col_pad(), chosen by a bank-conflict model of
+// the Stockham gather / scatter patterns.
+template <int W, int SH, int P> struct ColLayout {
+    int c;
+    __device__ __forceinline__ int operator()(int n) const { return n * W + c + (n >> SH) * P; }
+};
+struct ColPad {
+    int sh, p;
+};
+__host__ __device__ constexpr ColPad col_pad(int esize, int m, int w)
+{
+    if (esize == 8) {
+        if (w >= 16) return ColPad{0, 1};
+        if (m <= 128) return ColPad{1, 2};
+        if (m >= 1024) return ColPad{1, 4};
+        return ColPad{1, 1};
+    }
+    if (w >= 8) return ColPad{0, 1};
+    if (w == 4) return m <= 128 ? ColPad{1, 4} : m == 256 ? ColPad{1, 2} : m == 512 ? ColPad{1, 1} : ColPad{1, 4};
+    return (m == 256 || m >= 2048) ? ColPad{2, 2} : ColPad{2, 1};
+}
+// elements of shared memory a column tile needs
+__host__ __device__ constexpr int col_tile_elems(int esize, int m, int w)
+{
+    return m * w + (m >> col_pad(esize, m, w).sh) * col_pad(esize, m, w).p;
+}
+
+template <int L, int PADSHIFT> __host__ __device__ constexpr int padded(int n) { return n + (n >> PADSHIFT); }
+
+struct CtaBarrier {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+// named barrier over the NT threads [id*NT, (id+1)*NT) of one line group
+struct NamedBarrier {
+    int id, nthreads;
+    __device__ __forceinline__ void operator()() const
+    {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+    }
+};
+
+}  // namespace qsg

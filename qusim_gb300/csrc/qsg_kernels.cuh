@@ -1,0 +1,502 @@
+// qsg_kernels.cuh -- kernel templates of the split-operator step.
+//
+// Reference path (lhprojects/QuSim): QuUpdatePsi (src/SplittingUtils.h:14-64)
+// drives ExpV / ExpT of SplittingMethod1D (src/SplittingMethod1D.cpp:40-89)
+// and SplittingMethod2D (src/SplittingMethod2D.cpp:81-121), each of which is a
+// separate Device op (src/DeviceTemplate.h:1458-1579) plus FFT calls.  Here
+// one kernel owns several of those ops at once:
+//
+//   k_evolve1d_resident  whole O2/O4 step sequence of a 1D instance that fits
+//                        in one CTA's shared memory, for any number of steps,
+//                        psi kept in registers/shared memory between steps.
+//   k_row_pass           2D real-space pass: [inverse x-split stage, row iFFT]
+//                        -> V phase(s) -> [row FFT, forward x-split stage].
+//   k_col_pass           2D k-space pass: column FFT -> kinetic phase -> column
+//                        iFFT, over one x-split block.
+//
+// The x-split: a column transform of length Nx = G*M is a radix-G
+// decimation-in-frequency stage across the G rows n1 + j*M (done in the row
+// pass, with twiddles exp(-2 pi i n1 q / Nx)) followed by M-point transforms
+// over each block q of M consecutive rows (the column pass).  Output
+// frequency of block q, position k2 is kx = G*k2 + q.  The inverse runs the
+// same stages backwards.
+#pragma once
+#include <type_traits>
+#include "qsg_fft.cuh"
+
+namespace qsg {
+
+// ---------------------------------------------------------------------------
+// shared helpers
+// ---------------------------------------------------------------------------
+
+template <class C> struct PhaseOps;
+// complex128: tables hold the factor itself (the reference's own exp(f V)),
+// multiplied in as a plain complex product.
+template <> struct PhaseOps<double2> {
+    static __device__ __forceinline__ double2 apply(double2 a, double2 m) { return cmul(a, m); }
+};
+// complex64: tables hold factor - 1 (see cmul1p).
+template <> struct PhaseOps<float2> {
+    static __device__ __forceinline__ float2 apply(float2 a, float2 m) { return cmul1p(a, m); }
+};
+
+template <class C> __device__ __forceinline__ C ld_c(const C *p) { return __ldg(p); }
+template <class C> __device__ __forceinline__ C ld_stream(const C *p) { return __ldcs(p); }
+template <class C> __device__ __forceinline__ void st_stream(C *p, C v) { __stcs(p, v); }
+
+template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, -a.y); }
+
+// Every inverse transform here is computed as conj(FFT(conj(x))), which is
+// bit-identical to running the transform with conjugated twiddles and
+// constants (negation is exact), and every kernel runs its transforms in a
+// non-unrolled loop over one forward-transform body: two inlined transform
+// bodies roughly triple the register demand (the scheduler interleaves them).
+// The conjugations fold into the neighbouring phase multiplies.
+
+template <class C> __device__ __forceinline__ double abs2d(C a)
+{
+    return double(a.x) * double(a.x) + double(a.y) * double(a.y);
+}
+
+// block-wide sum of a double; every thread gets the result
+template <int NT> __device__ __forceinline__ double block_sum(double v, double *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (NT + 31) / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) red[0] = s;
+    }
+    __syncthreads();
+    s = red[0];
+    __syncthreads();
+    return s;
+}
+
+// G-point DFT on registers (G = 1, 2, 4)
+template <int G, bool INV, class C> __device__ __forceinline__ void dftg(C (&v)[G])
+{
+    if constexpr (G == 2) dft2<INV>(v[0], v[1]);
+    if constexpr (G == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+}
+
+// ---------------------------------------------------------------------------
+// 1D resident evolution
+// ---------------------------------------------------------------------------
+
+struct Evolve1DArgs {
+    void *psi;              // N complex, natural order, in/out
+    const void *vtab[2];    // V phase tables: O2 {1/2}, O4 {C1, C2}
+    const void *ktab[2];    // kinetic tables with 1/N folded in (complex128) or
+                            // factor - 1 (complex64): O2 {1}, O4 {D1, D2}
+    const void *tw;         // stage-major twiddles for (N, E)
+    double *norm_out;       // if set: sum |psi|^2 after the run (before renormalisation)
+    double dv;              // grid volume element for renormalisation
+    uint64_t nsteps;
+    int order;              // 2 or 4
+    int renormalize;        // scale to Norm2 == 1 after the run
+};
+
+template <class T, int L, int E>
+__global__ void __launch_bounds__(L / E) k_evolve1d_resident(Evolve1DArgs a)
+{
+    using C = cplx_t<T>;
+    using P = Plan<L, E>;
+    constexpr int TL = P::TL;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const int t = threadIdx.x;
+    C *psi = static_cast<C *>(a.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
+    const C *v0 = static_cast<const C *>(a.vtab[0]);
+    const C *v1 = static_cast<const C *>(a.vtab[1]);
+    const C *k0 = static_cast<const C *>(a.ktab[0]);
+    const C *k1 = static_cast<const C *>(a.ktab[1]);
+    const RowLayout<PADS> lay{0};
+    const CtaBarrier bar{};
+    constexpr T inv_n = T(1) / T(L);
+
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = psi[t + e * TL];
+
+    // substep schedule: V(v[0]) T(k[0]) V(v[1]) T(k[1]) ... V(v[nsub])
+    // O2: V1/2 T1 V1/2;  O4: VC1 TD1 VC2 TD2 VC2 TD1 VC1
+    // T(k) = iFFT(k * FFT(x)) = conj(FFT(conj(k * FFT(x)))): each half-substep
+    // is one forward transform followed by a conjugating multiply.
+    const int nsub = a.order == 2 ? 1 : 3;
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], ld_c(v0 + t + e * TL));
+    for (uint64_t s = 0; s < a.nsteps; ++s) {
+#pragma unroll 1
+        for (int h = 0; h < 2 * nsub; ++h) {
+            line_fft<C, L, E, false>(x, sm, lay, bar, t, tw);
+            const int u = h >> 1;
+            if ((h & 1) == 0) {
+                const C *kt = (a.order == 4 && u == 1) ? k1 : k0;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    if constexpr (sizeof(C) == 8) x[e] = cscale(x[e], inv_n);
+                    x[e] = cconj(PhaseOps<C>::apply(x[e], ld_c(kt + t + e * TL)));
+                }
+            } else {
+                // the next V: the step's own closing factor, then (if more
+                // steps follow) the next step's opening factor
+                const bool last = u == nsub - 1;
+                const C *vt = (a.order == 4 && !last) ? v1 : v0;
+                const bool twice = last && s + 1 < a.nsteps;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const C m = ld_c(vt + t + e * TL);
+                    x[e] = PhaseOps<C>::apply(cconj(x[e]), m);
+                    if (twice) x[e] = PhaseOps<C>::apply(x[e], m);
+                }
+            }
+        }
+    }
+
+    if (a.norm_out || a.renormalize) {
+        double s = 0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) s += abs2d(x[e]);
+        s = block_sum<L / E>(s, red);
+        if (t == 0 && a.norm_out) *a.norm_out = s;
+        if (a.renormalize) {
+            const T sc = T(1.0 / sqrt(s * a.dv));
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = cscale(x[e], sc);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) psi[t + e * TL] = x[e];
+}
+
+// ---------------------------------------------------------------------------
+// 2D passes
+// ---------------------------------------------------------------------------
+
+struct RowPassArgs {
+    const void *in;
+    void *out;
+    const void *vtab;       // V phase table (Nx*Ny), or null (plain transform)
+    int vtwice;             // apply it twice (the two ExpV calls at a step boundary)
+    const void *tw_row;     // stage-major twiddles for (Ny, E)
+    const void *tw_nx;      // full circle exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
+    double *partials;       // per-CTA sum |psi|^2 (natural-output passes), or null
+    int nx, m;              // Nx and M = Nx / G
+};
+
+// IN_SPLIT: input is in split-k space (inverse x-split stage + row iFFT first);
+//           otherwise natural real-space rows.
+// OUT_SPLIT: output goes back to split-k space (row FFT + forward x-split
+//           stage); otherwise natural real-space rows (+ norm partials).
+// One CTA handles B row groups; group b has the G rows n1 + j*M, j < G,
+// n1 = blockIdx.x*B + b, i.e. NL = B*G lines of NY.  The NT threads work on
+// NL/RS lines at a time and go over the CTA's lines in RS rounds.
+template <class T, int NY, int E, int G, int B, int RS, bool IN_SPLIT, bool OUT_SPLIT>
+__global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
+{
+    using C = cplx_t<T>;
+    using P = Plan<NY, E>;
+    constexpr int TL = P::TL;
+    constexpr int NL = B * G;
+    constexpr int NT = NL * TL / RS;
+    constexpr int LPR = NL / RS;  // lines per round
+    static_assert(NL % RS == 0, "");
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    constexpr int LINE = padded<NY, PADS>(NY);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+
+    const int tid = threadIdx.x;
+    const int grp = tid / TL;  // line slot within a round
+    const int t = tid - grp * TL;
+    const C *in = static_cast<const C *>(a.in);
+    C *out = static_cast<C *>(a.out);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_row);
+    const tw_t<C> *twx = static_cast<const tw_t<C> *>(a.tw_nx);
+    const C *vt = static_cast<const C *>(a.vtab);
+    const CtaBarrier cbar{};
+    // lines of whole warps synchronise among themselves; otherwise CTA-wide
+    constexpr bool NAMED = (TL % 32 == 0) && (LPR <= 15) && (LPR > 1);
+    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
+    LineBar lbar;
+    if constexpr (NAMED) lbar = NamedBarrier{1 + grp, TL};
+    constexpr bool VIA_SMEM_IN = IN_SPLIT && G > 1;
+    constexpr bool VIA_SMEM_OUT = OUT_SPLIT && G > 1;
+
+    if constexpr (VIA_SMEM_IN) {
+        // inverse x-split stage over every column of every group of this CTA
+#pragma unroll 4
+        for (int u = 0; u < B * NY / NT; ++u) {
+            const int gc = tid + u * NT;
+            const int bb = gc / NY, c = gc - bb * NY;
+            const int nn1 = blockIdx.x * B + bb;
+            C y[G];
+#pragma unroll
+            for (int q = 0; q < G; ++q) {
+                y[q] = ld_stream(in + (size_t)(q * a.m + nn1) * NY + c);
+                if (q > 0) y[q] = twmul<true>(y[q], __ldg(twx + nn1 * q));
+            }
+            dftg<G, true>(y);
+#pragma unroll
+            for (int q = 0; q < G; ++q) sm[(bb * G + q) * LINE + c + (c >> PADS)] = y[q];
+        }
+        cbar();
+    }
+
+    double nsum = 0;
+#pragma unroll 1
+    for (int r = 0; r < RS; ++r) {
+        const int line = r * LPR + grp;
+        const int b = line / G, j = line - b * G;
+        const int row = blockIdx.x * B + b + j * a.m;
+        const RowLayout<PADS> lay{line * LINE};
+        C x[E];
+        if constexpr (VIA_SMEM_IN) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = sm[lay(t + e * TL)];
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = ld_stream(in + (size_t)row * NY + t + e * TL);
+        }
+        // [row iFFT] -> V -> [row FFT], the iFFT as conj(FFT(conj(x)))
+        constexpr int NPASS = (IN_SPLIT ? 1 : 0) + (OUT_SPLIT ? 1 : 0);
+        constexpr int VPOS = IN_SPLIT ? 1 : 0;
+        if constexpr (IN_SPLIT) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+        }
+#pragma unroll 1
+        for (int p = 0; p <= NPASS; ++p) {
+            if (p == VPOS) {
+                if constexpr (IN_SPLIT) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+                }
+                if (vt) {
+                    const C *vr = opaque(vt) + (size_t)row * NY + t;
+#pragma unroll
+                    for (int e = 0; e < E; ++e) {
+                        const C m = ld_stream(vr + e * TL);
+                        x[e] = PhaseOps<C>::apply(x[e], m);
+                        if (a.vtwice) x[e] = PhaseOps<C>::apply(x[e], m);
+                    }
+                }
+            }
+            if (p < NPASS) line_fft<C, NY, E, false>(x, sm, lay, lbar, t, tw);
+        }
+        if constexpr (!OUT_SPLIT) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                st_stream(out + (size_t)row * NY + t + e * TL, x[e]);
+                nsum += abs2d(x[e]);
+            }
+        } else {
+            if constexpr (VIA_SMEM_OUT) {
+                lbar();  // this line's readers of the last exchange are done
+#pragma unroll
+                for (int e = 0; e < E; ++e) sm[lay(t + e * TL)] = x[e];
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; ++e) st_stream(out + (size_t)row * NY + t + e * TL, x[e]);
+            }
+        }
+    }
+
+    if constexpr (VIA_SMEM_OUT) {
+        cbar();
+#pragma unroll 4
+        for (int u = 0; u < B * NY / NT; ++u) {
+            const int gc = tid + u * NT;
+            const int bb = gc / NY, c = gc - bb * NY;
+            const int nn1 = blockIdx.x * B + bb;
+            C y[G];
+#pragma unroll
+            for (int q = 0; q < G; ++q) y[q] = sm[(bb * G + q) * LINE + c + (c >> PADS)];
+            dftg<G, false>(y);
+#pragma unroll
+            for (int q = 0; q < G; ++q) {
+                if (q > 0) y[q] = twmul<false>(y[q], __ldg(twx + nn1 * q));
+                st_stream(out + (size_t)(q * a.m + nn1) * NY + c, y[q]);
+            }
+        }
+    }
+    if constexpr (!OUT_SPLIT) {
+        if (a.partials) {
+            nsum = block_sum<NT>(nsum, red);
+            if (tid == 0) a.partials[blockIdx.x] = nsum;
+        }
+    }
+}
+
+struct ColPassArgs {
+    void *psi;              // in/out, Nx*Ny in split-k layout
+    const void *kx;         // complex64: x kinetic factor - 1, Nx entries
+    const void *ky;         // complex64: y kinetic factor - 1, Ny entries
+    const void *k2d;        // complex128: full table Nx*Ny with 1/(Nx Ny) folded in
+    const void *tw_col;     // stage-major twiddles for (M, E)
+    int nx, ny, g;
+    float inv_n;            // 1/(Nx Ny) (complex64 path)
+};
+
+// One CTA: block q = blockIdx.y, columns [blockIdx.x*W, +W).
+template <class T, int M, int E, int W>
+__global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
+{
+    using C = cplx_t<T>;
+    using P = Plan<M, E>;
+    constexpr int TM = P::TL;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    const int tid = threadIdx.x;
+    const int c = tid % W, t = tid / W;
+    const int q = blockIdx.y;
+    const int col = blockIdx.x * W + c;
+    const int ny = a.ny;
+    C *psi = static_cast<C *>(a.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_col);
+    constexpr ColPad CP = col_pad(sizeof(C), M, W);
+    const ColLayout<W, CP.sh, CP.p> lay{c};
+    const CtaBarrier bar{};
+    const size_t base = ((size_t)q * M + t) * ny + col;
+    const int stride = TM * ny;  // between a thread's elements
+
+    C x[E];
+    {
+        const C *p = psi + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = ld_stream(p + (size_t)e * stride);
+    }
+
+    // FFT -> K -> iFFT, the iFFT as conj(FFT(conj(x)))
+#pragma unroll 1
+    for (int p = 0; p < 2; ++p) {
+        line_fft<C, M, E, false>(x, sm, lay, bar, t, tw);
+        if (p == 1) continue;  // (a break here makes the compiler duplicate the body)
+        if constexpr (sizeof(C) == 8) {
+            const C *kx = opaque(static_cast<const C *>(a.kx));
+            const C ky = ld_c(static_cast<const C *>(a.ky) + col);
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int kxi = a.g * (t + e * TM) + q;
+                C v = cscale(x[e], a.inv_n);
+                v = cmul1p(v, ld_c(kx + kxi));
+                x[e] = cconj(cmul1p(v, ky));
+            }
+        } else {
+            const C *k2 = static_cast<const C *>(a.k2d) + col;
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int kxi = a.g * (t + e * TM) + q;
+                x[e] = cconj(cmul(x[e], ld_stream(k2 + (size_t)kxi * ny)));
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+
+    {
+        // recomputed rather than kept live across both transforms
+        C *p = const_cast<C *>(opaque(psi)) + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) st_stream(p + (size_t)e * stride, x[e]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kinetic energy: forward transform + reductions
+// ---------------------------------------------------------------------------
+
+// 1D: sums[0] = sum |X_i|^2 fold(i)^2 * dtk, sums[1] = sum |X_i|^2
+// (SplittingMethod1D::CalKinEn, src/SplittingMethod1D.cpp:93-107)
+template <class T, int L, int E>
+__global__ void __launch_bounds__(L / E) k_kinetic1d(const void *psi_, const void *tw_, double dtk,
+                                                     double *sums)
+{
+    using C = cplx_t<T>;
+    constexpr int TL = Plan<L, E>::TL;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const int t = threadIdx.x;
+    const C *psi = static_cast<const C *>(psi_);
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = psi[t + e * TL];
+    line_fft<C, L, E, false>(x, sm, RowLayout<PADS>{0}, CtaBarrier{}, t, static_cast<const tw_t<C> *>(tw_));
+    double k = 0, nn = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int i = t + e * TL;
+        const double f = double(i > L / 2 ? L - i : i);
+        const double a2 = abs2d(x[e]);
+        k += a2 * (f * f) * dtk;
+        nn += a2;
+    }
+    k = block_sum<L / E>(k, red);
+    nn = block_sum<L / E>(nn, red);
+    if (t == 0) {
+        sums[0] = k;
+        sums[1] = nn;
+    }
+}
+
+// 2D column transform of one split block + kinetic reductions; partials[2*cta]
+// = sum |X|^2 (fold(kx)^2 DTx + fold(ky)^2 DTy), partials[2*cta+1] = sum |X|^2
+// (SplittingMethod2D::CalKinEn, src/SplittingMethod2D.cpp:123-138)
+template <class T, int M, int E, int W>
+__global__ void __launch_bounds__(W *(M / E)) k_col_kinetic(ColPassArgs a, double dtx, double dty,
+                                                            double *partials)
+{
+    using C = cplx_t<T>;
+    constexpr int TM = Plan<M, E>::TL;
+    constexpr int NT = W * TM;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const int tid = threadIdx.x;
+    const int c = tid % W, t = tid / W;
+    const int q = blockIdx.y;
+    const int col = blockIdx.x * W + c;
+    const int ny = a.ny, nx = a.nx;
+    const C *psi = static_cast<const C *>(a.psi);
+    const size_t base = (size_t)q * M * ny + col;
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = psi[base + (size_t)(t + e * TM) * ny];
+    constexpr ColPad CP = col_pad(sizeof(C), M, W);
+    line_fft<C, M, E, false>(x, sm, ColLayout<W, CP.sh, CP.p>{c}, CtaBarrier{}, t,
+                             static_cast<const tw_t<C> *>(a.tw_col));
+    const double fy = double(col > ny / 2 ? ny - col : col);
+    double k = 0, nn = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const int kxi = a.g * (t + e * TM) + q;
+        const double fx = double(kxi > nx / 2 ? nx - kxi : kxi);
+        const double a2 = abs2d(x[e]);
+        k += a2 * ((fx * fx) * dtx + (fy * fy) * dty);
+        nn += a2;
+    }
+    k = block_sum<NT>(k, red);
+    nn = block_sum<NT>(nn, red);
+    if (tid == 0) {
+        const int cta = blockIdx.y * gridDim.x + blockIdx.x;
+        partials[2 * cta] = k;
+        partials[2 * cta + 1] = nn;
+    }
+}
+
+}  // namespace qsg

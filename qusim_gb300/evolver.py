@@ -1,0 +1,363 @@
+"""Python mirror of QuSim's Evolver / Options API for the GPU_GB300 device.
+
+Same names, argument meaning and error behaviour as include/QuSim.h:
+``Evolver1D.init(psi, force_normalization, dt, force_normalization_each_step,
+v, x0, x1, n, b, solver, mass, hbar, opts)`` (QuSim.h:558-563),
+``Evolver2D.init(..., x0, x1, nx, y0, y1, ny, ...)`` (QuSim.h:583-589), then
+``step() / Norm2() / Time() / PotEn() / KinEn() / GetPsi() / GetV()``.
+psi and v may be callables of x (or x, y), sampled on the host at
+x_i = x0 + i*dx exactly as QuEvolver1DImpl::InitPsi / InitPotential do
+(src/EvolverImpl1D.cpp:33-81, src/EvolverImpl2D.cpp:39-98), or arrays of the
+grid values.
+
+Only the split-operator methods on the "GPU_GB300" device are served here;
+anything else raises, as the reference raises for unsupported solvers
+(src/QuSim.cpp:99).
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+
+import numpy as np
+
+from . import _lib
+from ._lib import QsgError, check
+
+
+class BoundaryCondition(enum.Enum):
+    Period = 0
+    InfiniteWall = 1
+
+
+class SolverMethod(enum.Enum):
+    Unknown = 0
+    SplittingMethodO2 = 1
+    SplittingMethodO4 = 2
+
+
+class Options:
+    """Key/value options (include/QuSim.h:286-458).  Gb300() selects this engine."""
+
+    def __init__(self):
+        self._kv = {}
+
+    def Gb300(self):
+        self._kv["device"] = "GPU_GB300"
+        return self
+
+    def Batch(self, n: int):
+        self._kv["batch"] = int(n)
+        return self
+
+    def Precision(self, p: str):
+        if p not in ("fp64", "mixed"):
+            raise ValueError(f"invalid precision: {p}")
+        self._kv["precision"] = p
+        return self
+
+    def HbmBudget(self, nbytes: int):
+        self._kv["hbm_budget"] = int(nbytes)
+        return self
+
+    def DeviceOrdinal(self, i: int):
+        self._kv["device_ordinal"] = int(i)
+        return self
+
+    def SetInt(self, k, v):
+        self._kv[k] = int(v)
+
+    def SetString(self, k, v):
+        self._kv[k] = str(v)
+
+    def SetReal(self, k, v):
+        self._kv[k] = float(v)
+
+    def SetBool(self, k, v):
+        self._kv[k] = bool(v)
+
+    def get(self, k, default=None):
+        return self._kv.get(k, default)
+
+
+class Context:
+    """One qsg_ctx (a device, a stream, an HBM budget)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(lib.qsg_init(device, hbm_budget, ctypes.byref(h)))
+        self.h = h
+        self.lib = lib
+
+    def close(self):
+        if self.h:
+            self.lib.qsg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return self.lib.qsg_ctx_stream(self.h) or 0
+
+    def bytes_in_use(self) -> int:
+        return self.lib.qsg_ctx_bytes_in_use(self.h)
+
+    def profile(self, on: bool):
+        check(self.lib.qsg_profile_enable(self.h, int(on)))
+
+    def profile_read(self):
+        n = self.lib.qsg_profile_read(self.h, 0, None, None, None)
+        names = (ctypes.c_char_p * max(n, 1))()
+        launches = (ctypes.c_uint64 * max(n, 1))()
+        ms = (ctypes.c_double * max(n, 1))()
+        n = self.lib.qsg_profile_read(self.h, n, names, launches, ms)
+        return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(n)}
+
+
+_default_ctx = {}
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default_ctx:
+        _default_ctx[device] = Context(device)
+    return _default_ctx[device]
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Instance:
+    """One qsg_inst: a wavefunction resident on the device."""
+
+    def __init__(self, ctx: Context, handle, shape, dv):
+        self.ctx = ctx
+        self.h = handle
+        self.shape = shape
+        self.dv = dv
+
+    @classmethod
+    def create_1d(cls, ctx, psi0, V, dx, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
+                  boundary=BoundaryCondition.Period):
+        psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        if psi0.ndim != 1 or V.shape != psi0.shape:
+            raise ValueError("psi0 and V must be 1D arrays of the same length")
+        dt = complex(dt)
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_1d(ctx.h, psi0.size, dx, mass, hbar, dt.real, dt.imag, order,
+                                    _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                    boundary.value, _dptr(psi0.view(np.float64)), _dptr(V),
+                                    ctypes.byref(h)))
+        return cls(ctx, h, psi0.shape, dx)
+
+    @classmethod
+    def create_2d(cls, ctx, psi0, V, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
+        psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        if psi0.ndim != 2 or V.shape != psi0.shape:
+            raise ValueError("psi0 and V must be 2D arrays of the same shape (nx, ny)")
+        dt = complex(dt)
+        nx, ny = psi0.shape
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_2d(ctx.h, nx, ny, dx, dy, mass, hbar, dt.real, dt.imag, order,
+                                    _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                    _dptr(psi0.view(np.float64)), _dptr(V), ctypes.byref(h)))
+        return cls(ctx, h, psi0.shape, dx * dy)
+
+    def step(self, nsteps: int, renormalize: bool = False):
+        check(self.ctx.lib.qsg_step(self.h, nsteps, int(renormalize)))
+
+    def sync(self):
+        check(self.ctx.lib.qsg_sync(self.h))
+
+    def norm2(self) -> float:
+        v = ctypes.c_double()
+        check(self.ctx.lib.qsg_norm2(self.h, ctypes.byref(v)))
+        return v.value
+
+    def energies(self):
+        k, p = ctypes.c_double(), ctypes.c_double()
+        check(self.ctx.lib.qsg_energies(self.h, ctypes.byref(k), ctypes.byref(p)))
+        return k.value, p.value
+
+    def xavg(self, x0: float) -> float:
+        v = ctypes.c_double()
+        check(self.ctx.lib.qsg_xavg(self.h, x0, ctypes.byref(v)))
+        return v.value
+
+    def norm2_range(self, x0, xa, xb) -> float:
+        v = ctypes.c_double()
+        check(self.ctx.lib.qsg_norm2_range(self.h, x0, xa, xb, ctypes.byref(v)))
+        return v.value
+
+    def get_psi(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.shape, dtype=np.complex128)
+        check(self.ctx.lib.qsg_get_psi(self.h, _dptr(out.view(np.float64))))
+        return out
+
+    def set_psi(self, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
+        check(self.ctx.lib.qsg_set_psi(self.h, _dptr(psi.view(np.float64))))
+
+    def steps_taken(self) -> int:
+        v = ctypes.c_uint64()
+        check(self.ctx.lib.qsg_steps_taken(self.h, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.qsg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _check_device(opts: Options):
+    dev = opts.get("device", "CPU_SEQ")
+    if dev != "GPU_GB300":
+        # the reference's GetDeviceType raises std::invalid_argument for unknown
+        # devices (src/DeviceType.h:21); here only GPU_GB300 is served
+        raise ValueError(f"invalid device: {dev} (this package serves device GPU_GB300; "
+                         "select it with Options().Gb300())")
+
+
+class Evolver:
+    def __init__(self):
+        self._inst = None
+        self._fnes = False
+        self._batch = 1
+        self._dt = 0j
+        self._method = SolverMethod.Unknown
+        self._psi_cache = None
+        self._V = None
+
+    def step(self):
+        """Evolver::step (src/QuSim.cpp:39-42 -> EvolverImpl.cpp:56-68): `batch` steps,
+        then renormalise if force_normalization_each_step."""
+        self._inst.step(self._batch, self._fnes)
+        self._psi_cache = None
+
+    def Norm2(self, *args):
+        return self._inst.norm2()
+
+    def Time(self):
+        return (self._inst.steps_taken() * self._dt).real
+
+    def PotEn(self):
+        return self._inst.energies()[1]
+
+    def KinEn(self):
+        return self._inst.energies()[0]
+
+    def GetMethod(self):
+        return self._method
+
+    def _common(self, dt, fnes, solver, opts):
+        _check_device(opts)
+        if solver not in (SolverMethod.SplittingMethodO2, SolverMethod.SplittingMethodO4):
+            raise RuntimeError("unspported solver")
+        self._dt = complex(dt)
+        self._fnes = bool(fnes)
+        self._batch = int(opts.get("batch", 1))
+        self._method = solver
+        order = 2 if solver == SolverMethod.SplittingMethodO2 else 4
+        precision = opts.get("precision", "fp64")
+        ctx = default_context(opts.get("device_ordinal", 0))
+        return ctx, order, precision
+
+
+def _normalise(psi, dv):
+    return psi / np.sqrt(np.sum(np.abs(psi) ** 2) * dv)
+
+
+class Evolver1D(Evolver):
+    def init(self, psi, force_normalization, dt, force_normalization_each_step, v, x0, x1, n,
+             b, solver, mass, hbar, opts):
+        ctx, order, precision = self._common(dt, force_normalization_each_step, solver, opts)
+        n = int(n)
+        dx = (x1 - x0) / n
+        xs = dx * np.arange(n) + x0
+        psi0 = np.asarray([psi(x) for x in xs] if callable(psi) else psi, dtype=np.complex128)
+        V = np.real(np.asarray([v(x) for x in xs] if callable(v) else v)).astype(np.float64)
+        if force_normalization:
+            psi0 = _normalise(psi0, dx)
+        self._x0, self._x1, self._n, self._dx = x0, x1, n, dx
+        self._V = V
+        self._inst = Instance.create_1d(ctx, psi0, V, dx, dt, order, precision, mass, hbar, b)
+
+    def GetPsi(self):
+        if self._psi_cache is None:
+            self._psi_cache = self._inst.get_psi()
+        return self._psi_cache
+
+    def GetV(self):
+        return self._V
+
+    def Xavg(self):
+        return self._inst.xavg(self._x0)
+
+    def GetN(self):
+        return self._n
+
+    def GetX0(self):
+        return self._x0
+
+    def GetX1(self):
+        return self._x1
+
+    def Norm2(self, *args):
+        if len(args) == 2:
+            return self._inst.norm2_range(self._x0, args[0], args[1])
+        return self._inst.norm2()
+
+
+class Evolver2D(Evolver):
+    def init(self, psi, force_normalization, dt, force_normalization_each_step, v, x0, x1, nx,
+             y0, y1, ny, b, solver, mass, hbar, opts):
+        ctx, order, precision = self._common(dt, force_normalization_each_step, solver, opts)
+        if b != BoundaryCondition.Period:
+            raise RuntimeError("unsupported boundary condition!")
+        nx, ny = int(nx), int(ny)
+        dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+        if callable(psi) or callable(v):
+            xs = dx * np.arange(nx) + x0
+            ys = dy * np.arange(ny) + y0
+        psi0 = (np.array([[psi(x, y) for y in ys] for x in xs], dtype=np.complex128)
+                if callable(psi) else np.asarray(psi, dtype=np.complex128))
+        V = (np.real(np.array([[v(x, y) for y in ys] for x in xs]))
+             if callable(v) else np.real(np.asarray(v))).astype(np.float64)
+        if force_normalization:
+            psi0 = _normalise(psi0, dx * dy)
+        self._nx, self._ny = nx, ny
+        self._V = V
+        self._inst = Instance.create_2d(ctx, psi0, V, dx, dy, dt, order, precision, mass, hbar)
+
+    def GetPsi(self):
+        if self._psi_cache is None:
+            self._psi_cache = self._inst.get_psi()
+        return self._psi_cache
+
+    def GetV(self):
+        return self._V
+
+    def GetNx(self):
+        return self._nx
+
+    def GetNy(self):
+        return self._ny
+
+
+__all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Evolver1D",
+           "Evolver2D", "QsgError", "default_context"]

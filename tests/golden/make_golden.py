@@ -61,9 +61,9 @@ def main():
 
     # 2D evolutions.  (name, nx, ny, half_x, half_y, order, dt, batch, calls, fnes)
     cases_2d = [
-        ("evolve2d_64x128_o2_50", 64, 128, 20.0, 40.0, 2, 0.02, 50, 1, False),
-        ("evolve2d_128x128_o4_20", 128, 128, 30.0, 30.0, 4, 0.02, 20, 1, False),
-        ("evolve2d_32x64_o4_b5x2_fnes", 32, 64, 10.0, 20.0, 4, 0.01 - 0.002j, 5, 2, True),
+        ("evolve2d_128x256_o2_50", 128, 256, 20.0, 40.0, 2, 0.02, 50, 1, False),
+        ("evolve2d_256x128_o4_20", 256, 128, 30.0, 30.0, 4, 0.02, 20, 1, False),
+        ("evolve2d_128x128_o4_b5x2_fnes", 128, 128, 10.0, 20.0, 4, 0.01 - 0.002j, 5, 2, True),
     ]
     for name, nx, ny, hx, hy, order, dt, batch, calls, fnes in cases_2d:
         x0, x1, y0, y1 = -hx, hx, -hy, hy

@@ -1,0 +1,188 @@
+"""GPU parity: the CUDA engine through its C ABI (libqsg.so) against the oracle.
+
+The bar (complex128 "plain" form): relative L2 error <= 1e-12 against the
+reference's own CPU evolution on the same inputs (golden fixtures made by the
+reference; the C oracle, bit-exact with the reference on every fixture, for
+shapes computed live).  The complex64 "mixed" form is held to relative L2
+<= 1e-5 against the same FP64 result.
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import load_golden
+from tests.workloads import gauss_packet_1d, gauss_packet_2d, gaussian_bumps_2d
+
+pytestmark = pytest.mark.gpu
+
+PLAIN_TOL = 1e-12
+MIXED_TOL = 1e-5
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.fixture(scope="module")
+def qsg():
+    import qusim_gb300 as q
+    q.load()
+    return q
+
+
+@pytest.fixture(scope="module")
+def ctx(qsg):
+    return qsg.Context(0)
+
+
+def run_1d(qsg, ctx, g, precision):
+    n, x0, x1, order, wall, batch, calls, fnes = g["params"]
+    n, order, batch, calls = int(n), int(order), int(batch), int(calls)
+    dx = (x1 - x0) / n
+    inst = qsg.Instance.create_1d(ctx, g["psi0"], g["V"], dx, complex(g["dt"]), order=order,
+                                  precision=precision)
+    for _ in range(calls):
+        inst.step(batch, renormalize=bool(fnes))
+    return inst, dx
+
+
+GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
+             "evolve1d_n1024_o4_imag"]
+GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_1D)
+def test_evolve1d_plain_matches_reference(qsg, ctx, name):
+    g = load_golden(name)
+    inst, dx = run_1d(qsg, ctx, g, "fp64")
+    psi = inst.get_psi()
+    assert rel_l2(psi, g["psi"]) <= PLAIN_TOL
+    assert abs(inst.norm2() - g["norm2"]) <= 1e-12 * abs(g["norm2"])
+    kin, pot = inst.energies()
+    assert abs(kin - g["kin"]) <= 1e-11 * max(1.0, abs(g["kin"]))
+    assert abs(pot - g["pot"]) <= 1e-11 * max(1.0, abs(g["pot"]))
+
+
+@pytest.mark.parametrize("name", GOLDEN_1D)
+def test_evolve1d_mixed_close_to_reference(qsg, ctx, name):
+    g = load_golden(name)
+    inst, dx = run_1d(qsg, ctx, g, "mixed")
+    assert rel_l2(inst.get_psi(), g["psi"]) <= MIXED_TOL
+    assert abs(inst.norm2() - g["norm2"]) <= 1e-5
+
+
+@pytest.mark.parametrize("name", GOLDEN_2D)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_evolve2d_matches_reference(qsg, ctx, name, precision):
+    g = load_golden(name)
+    nx, ny, x0, x1, y0, y1, order, batch, calls, fnes = g["params"]
+    nx, ny, order, batch, calls = int(nx), int(ny), int(order), int(batch), int(calls)
+    dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+    inst = qsg.Instance.create_2d(ctx, g["psi0"], g["V"], dx, dy, complex(g["dt"]), order=order,
+                                  precision=precision)
+    for _ in range(calls):
+        inst.step(batch, renormalize=bool(fnes))
+    tol = PLAIN_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_l2(inst.get_psi(), g["psi"]) <= tol
+    assert abs(inst.norm2() - g["norm2"]) <= (1e-12 if precision == "fp64" else 1e-5)
+    kin, pot = inst.energies()
+    etol = 1e-10 if precision == "fp64" else 1e-4
+    assert abs(kin - g["kin"]) <= etol * max(1.0, abs(g["kin"]))
+    assert abs(pot - g["pot"]) <= etol * max(1.0, abs(g["pot"]))
+
+
+# shapes that exercise every x-split (G = 1, 2, 4) and row/column tile shape
+SPLIT_SHAPES = [(4096, 128, 4), (2048, 256, 2), (128, 4096, 4), (512, 512, 2), (1024, 128, 2)]
+
+
+@pytest.mark.parametrize("nx,ny,order", SPLIT_SHAPES)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_evolve2d_shapes_vs_oracle(qsg, ctx, oracle, nx, ny, order, precision):
+    hx, hy = 0.05 * nx, 0.05 * ny
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=0.08 * min(hx, hy))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=8, seed=1, spread=0.5 * min(hx, hy))
+    nsteps = 3
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.01, nsteps, order=order)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=order, precision=precision)
+    inst.step(nsteps)
+    tol = PLAIN_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_l2(inst.get_psi(), ref) <= tol
+
+
+@pytest.mark.parametrize("n", [64, 128, 512, 2048, 4096])
+@pytest.mark.parametrize("order", [2, 4])
+def test_evolve1d_sizes_vs_oracle(qsg, ctx, oracle, n, order):
+    psi0, V, dx = gauss_packet_1d(n, -0.05 * n, 0.05 * n, 1.5, -0.01 * n, 0.01 * n + 1, barrier=0.7)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02, 25, order=order)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision)
+        inst.step(25)
+        assert rel_l2(inst.get_psi(), ref) <= tol, precision
+
+
+def test_batch_equals_repeated_steps(qsg, ctx):
+    psi0, V, dx = gauss_packet_1d(1024, -50, 50, 1.0, -10, 3.0)
+    a = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=4)
+    b = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=4)
+    a.step(10)
+    for _ in range(10):
+        b.step(1)
+    assert rel_l2(a.get_psi(), b.get_psi()) <= 1e-13
+    assert a.steps_taken() == b.steps_taken() == 10
+
+
+def test_tunnelling_known_answer_gpu(qsg, ctx):
+    """QuSimPrecision.cpp:82: transmission 0.15937744085 at t=64."""
+    ref = (0.1593774409 + 0.1593774408) / 2
+    n, x0, x1, dt = 2048, -100.0, 100.0, 0.02
+    dx = (x1 - x0) / n
+    xs = x0 + dx * np.arange(n)
+    psi = np.exp(-0.5 * ((xs + 20) / 5) ** 2) * np.exp(1j * xs)
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx)
+    for precision, tol in (("fp64", 1e-9), ("mixed", 2e-6)):
+        inst = qsg.Instance.create_1d(ctx, psi, np.exp(-xs * xs), dx, dt, order=4, precision=precision)
+        inst.step(3200)
+        assert abs(inst.norm2_range(x0, 0.0, x1) - ref) < tol, precision
+
+
+def test_unsupported_sizes_are_reported(qsg, ctx):
+    psi0, V, dx = gauss_packet_1d(1000, -50, 50, 1.0, -10, 3.0)
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02)
+    assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:512], V[:512], dx, 0.02, order=3)
+    assert e.value.code == 1
+    z = np.zeros((100, 128), np.complex128)
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_2d(ctx, z, z.real, 0.1, 0.1, 0.02)
+    assert e.value.code == 5
+
+
+def test_budget_rejects_oversize(qsg):
+    c = qsg.Context(0, hbm_budget=1 << 20)
+    psi0, V, dx = gauss_packet_1d(4096, -50, 50, 1.0, -10, 3.0)
+    qsg.Instance.create_1d(c, psi0, V, dx, 0.02)  # ~ 0.3 MB, fits
+    z = np.zeros((1024, 1024), np.complex128)
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_2d(c, z, z.real, 0.1, 0.1, 0.02)
+    assert e.value.code == 2
+
+
+def test_evolver_api_mirror(qsg):
+    """The Evolver1D API mirror: init with functors, batch, force-normalise."""
+    from qusim_gb300 import BoundaryCondition, Evolver1D, Options, SolverMethod
+    e = Evolver1D()
+    opts = Options().Gb300().Batch(10)
+    e.init(lambda x: np.exp(-0.5 * ((x + 20) / 5) ** 2) * np.exp(1j * x), True, 0.02, False,
+           lambda x: np.exp(-x * x), -100.0, 100.0, 2048, BoundaryCondition.Period,
+           SolverMethod.SplittingMethodO2, 1.0, 1.0, opts)
+    assert abs(e.Norm2() - 1) < 1e-13
+    x0 = e.Xavg()
+    e.step()
+    assert abs(e.Time() - 0.2) < 1e-15
+    assert e.GetPsi().shape == (2048,)
+    assert e.Xavg() > x0
+    with pytest.raises(ValueError):
+        Evolver1D().init(lambda x: 0j, True, 0.02, False, lambda x: 0.0, -1, 1, 64,
+                         BoundaryCondition.Period, SolverMethod.SplittingMethodO2, 1, 1, Options())

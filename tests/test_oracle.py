@@ -11,7 +11,7 @@ from tests.conftest import load_golden
 
 EVOLVE_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1000_o2"]
-EVOLVE_2D = ["evolve2d_64x128_o2_50", "evolve2d_128x128_o4_20", "evolve2d_32x64_o4_b5x2_fnes"]
+EVOLVE_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes"]
 
 
 def rel_l2(a, b):
