@@ -42,10 +42,11 @@ from tests.workloads import double_slit_2d, gauss_packet_1d, gauss_packet_2d, ga
 
 WORKLOADS = {
     "2d4096": dict(desc="2D 4096x4096 double slit, O4, dt=0.01", dim=2, nx=4096, ny=4096, half=200.0,
-                   k=(2.0, 0.0), c=(-60.0, 0.0), s=10.0, dt=0.01, order=4),
+                   k=(2.0, 0.0), c=(-60.0, 0.0), s=10.0, dt=0.01, order=4, full_steps=2000),
     "2d1024": dict(desc="2D 1024x1024 16 Gaussian bumps (seed 0), O4, dt=0.02", dim=2, nx=1024, ny=1024,
-                   half=100.0, k=(1.5, 0.0), c=(-40.0, 0.0), s=8.0, dt=0.02, order=4),
-    "1d4096": dict(desc="1D N=4096 barrier 0.5 exp(-x^2/2), O2, dt=0.05", dim=1, n=4096, dt=0.05, order=2),
+                   half=100.0, k=(1.5, 0.0), c=(-40.0, 0.0), s=8.0, dt=0.02, order=4, full_steps=1000),
+    "1d4096": dict(desc="1D N=4096 barrier 0.5 exp(-x^2/2), O2, dt=0.05", dim=1, n=4096, dt=0.05, order=2,
+                   full_steps=2000),
 }
 
 
@@ -261,7 +262,10 @@ def main():
     ap.add_argument("--workload", default="2d4096", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plain", action="store_true", help="skip the fp64 comparison run")
+    ap.add_argument("--no-plain", action="store_true", help="skip the fp64 comparison runs")
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the mixed-vs-fp64 accuracy run (default: the configuration's own count)")
+    ap.add_argument("--no-tune", action="store_true", help="use the default plan instead of autotuning")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.warmup < 3:
@@ -287,7 +291,19 @@ def main():
             return q.Instance.create_1d(ctx, psi0, V, d[0], w["dt"], order=w["order"], precision=precision)
         return q.Instance.create_2d(ctx, psi0, V, d[0], d[1], w["dt"], order=w["order"], precision=precision)
 
-    inst = create(args.precision)
+    tuned = {}
+
+    def tuned_instance(precision):
+        i = create(precision)
+        if w["dim"] == 2 and not args.no_tune:
+            if precision not in tuned:
+                p, ms_tr = i.autotune(trial_steps=3, persist=True)
+                tuned[precision] = {"plan": list(p.as_tuple()), "trial_ms_per_step": ms_tr}
+            else:
+                i.set_plan(tuned[precision]["plan"])
+        return i
+
+    inst = tuned_instance(args.precision)
     inst.step(args.warmup)
     inst.sync()
 
@@ -343,12 +359,12 @@ def main():
     step_roof = {"algorithmic_bytes_per_site_step": ab, "achieved_gbs": ab * value / world / 1e9,
                  "frac": ab * value / world / 1e9 / peak} if ab else None
 
-    # accuracy against the fp64 path run for the same steps
+    # the fp64 path on the same workload (site-steps/s), and the accuracy of the
+    # mixed form against it over the configuration's full step count
     acc = None
     plain = None
     if not args.no_plain and args.precision == "mixed":
-        ref = create("fp64")
-        k0, p0 = ref.energies()
+        ref = tuned_instance("fp64")
         ref.step(args.warmup)
         ref.sync()
         torch.cuda.synchronize()
@@ -361,18 +377,29 @@ def main():
         f1.synchronize()
         pms = f0.elapsed_time(f1)
         plain = {"value": sites * psteps / (pms / 1e3), "unit": "site-steps/s", "steps": psteps,
-                 "dtype": "c128"}
-        if psteps < args.steps:
-            ref.step(args.steps - psteps)
-        a, b = inst.get_psi(), ref.get_psi()
-        km, pm = inst.energies()
-        kr, pr = ref.energies()
-        dv = np.prod(d)
-        acc = {"rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-               "norm_drift": float(inst.norm2() - np.sum(np.abs(psi0) ** 2) * dv),
-               "energy_drift_vs_fp64": float((km + pm) - (kr + pr)),
-               "energy_fp64_start": float(k0 + p0), "steps": args.steps + args.warmup}
+                 "dtype": "c128", "plan": tuned.get("fp64", {}).get("plan")}
         ref.close()
+        nacc = args.accuracy_steps if args.accuracy_steps is not None else w["full_steps"]
+        a_m, a_p = tuned_instance("mixed"), tuned_instance("fp64")
+        k0, p0 = a_p.energies()
+        n0 = a_p.norm2()
+        chunk = 250
+        done = 0
+        while done < nacc:
+            c = min(chunk, nacc - done)
+            a_m.step(c)
+            a_p.step(c)
+            done += c
+        a, b = a_m.get_psi(), a_p.get_psi()
+        km, pm = a_m.energies()
+        kr, pr = a_p.energies()
+        acc = {"steps": nacc, "rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+               "norm_drift_mixed": float(a_m.norm2() - n0), "norm_drift_fp64": float(a_p.norm2() - n0),
+               "energy_drift_mixed": float((km + pm) - (k0 + p0)),
+               "energy_drift_fp64": float((kr + pr) - (k0 + p0)),
+               "energy_mixed_minus_fp64": float((km + pm) - (kr + pr)), "energy_start": float(k0 + p0)}
+        a_m.close()
+        a_p.close()
 
     # end to end through the public API: H2D of psi0 and V from pinned memory,
     # K x (step + Norm2 read back), final psi read back
@@ -389,6 +416,7 @@ def main():
         e2 = q.Instance.create_1d(ctx, psi_pinned, V_pinned, d[0], w["dt"], order=w["order"],
                                   precision=args.precision)
     else:
+        # a new instance picks up the plan tuned above (the context remembers it)
         e2 = q.Instance.create_2d(ctx, psi_pinned, V_pinned, d[0], d[1], w["dt"], order=w["order"],
                                   precision=args.precision)
     for _ in range(args.steps):
@@ -419,6 +447,7 @@ def main():
                 "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
                 "roofline": roof, "step_roofline": step_roof, "accuracy": acc, "plain_fp64": plain,
+                "plan": tuned.get(args.precision),
                 "e2e": e2e, "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]}
                                                                   for k, v in prof.items()},
                 "cpu_baseline": cpu, "clocks": clk}

@@ -116,6 +116,33 @@ int qsg_steps_taken(qsg_inst *inst, uint64_t *out);
 
 void qsg_destroy(qsg_inst *inst);
 
+/* 2D execution plan: the x split (Nx = g * m, column transforms of length m,
+ * a radix-g stage folded into the row pass), the elements per thread (radix)
+ * of the row and column transforms, and the columns per column-pass CTA.
+ * Every plan computes the same result to rounding; they differ in speed.
+ * New to this engine (the reference has one fixed cuFFT / KISS path). */
+typedef struct {
+    int32_t g;
+    int32_t row_e;
+    int32_t col_e;
+    int32_t col_w;
+} qsg_plan2d;
+
+/* Plans compiled for an nx x ny grid at `precision`; fills up to cap, returns
+ * the count. */
+int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out, int cap);
+int qsg_get_plan(qsg_inst *inst, qsg_plan2d *out);
+int qsg_set_plan(qsg_inst *inst, const qsg_plan2d *plan);
+
+/* Time every candidate plan for trial_steps steps on a copy of the
+ * instance's state (psi and the step count are left unchanged), switch the
+ * instance to the fastest, remember it for later instances of the same grid in
+ * this context, and if persist append it to the plan cache file
+ * ($QSG_PLAN_CACHE, default ~/.cache/qusim_gb300/plans.tsv) that new contexts
+ * read.  Either out pointer may be null. */
+int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
+                 double *best_ms_per_step);
+
 /* Per-kernel timing of this context's launches (CUDA events around every
  * launch on the context stream), for roofline reporting.  Enabling resets the
  * counters.  qsg_profile_read fills up to cap entries of name / launches /

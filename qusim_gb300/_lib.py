@@ -32,8 +32,21 @@ EXPORTS = [
     "qsg_version", "qsg_last_error", "qsg_init", "qsg_ctx_destroy", "qsg_ctx_stream",
     "qsg_ctx_bytes_in_use", "qsg_create_1d", "qsg_create_2d", "qsg_step", "qsg_sync",
     "qsg_norm2", "qsg_energies", "qsg_xavg", "qsg_norm2_range", "qsg_get_psi", "qsg_set_psi",
-    "qsg_steps_taken", "qsg_destroy", "qsg_profile_enable", "qsg_profile_read",
+    "qsg_steps_taken", "qsg_destroy", "qsg_candidate_plans", "qsg_get_plan", "qsg_set_plan",
+    "qsg_autotune", "qsg_profile_enable", "qsg_profile_read",
 ]
+
+
+class Plan2D(ctypes.Structure):
+    """qsg_plan2d: x split g, row / column elements per thread, column tile width."""
+    _fields_ = [("g", ctypes.c_int32), ("row_e", ctypes.c_int32), ("col_e", ctypes.c_int32),
+                ("col_w", ctypes.c_int32)]
+
+    def as_tuple(self):
+        return (self.g, self.row_e, self.col_e, self.col_w)
+
+    def __repr__(self):
+        return f"Plan2D(g={self.g}, row_e={self.row_e}, col_e={self.col_e}, col_w={self.col_w})"
 
 
 class QsgError(RuntimeError):
@@ -77,6 +90,10 @@ def _declare(lib):
     lib.qsg_steps_taken.argtypes = [_vp, ctypes.POINTER(_u64)]
     lib.qsg_destroy.argtypes = [_vp]
     lib.qsg_destroy.restype = None
+    lib.qsg_candidate_plans.argtypes = [_i, _u64, _u64, ctypes.POINTER(Plan2D), _i]
+    lib.qsg_get_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
+    lib.qsg_set_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
+    lib.qsg_autotune.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan2D), _dp]
     lib.qsg_profile_enable.argtypes = [_vp, _i]
     lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
 

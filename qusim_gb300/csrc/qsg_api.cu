@@ -13,12 +13,16 @@
 //        space; "V V" multiplies by the same table twice (the reference's two
 //        ExpV calls at the step boundary).
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <sstream>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -29,6 +33,7 @@
 #include "qsg_launch.h"
 
 using qsg::Geom2D;
+using qsg::Plan2D;
 using cd = std::complex<double>;
 
 namespace {
@@ -90,6 +95,9 @@ struct qsg_ctx {
     std::vector<cudaEvent_t> event_pool;
     std::map<std::string, ProfStat> prof_stats;
     std::vector<std::string> prof_names;  // stable storage for returned names
+    std::string device_name;
+    std::map<std::tuple<int, int, int>, Plan2D> plans;  // tuned plans: (prec, nx, ny) -> plan
+    bool plans_loaded = false;
 };
 
 struct qsg_inst {
@@ -105,7 +113,8 @@ struct qsg_inst {
     void *vtab[2] = {nullptr, nullptr};
     void *ktab[2] = {nullptr, nullptr};  // 1D kinetic tables, or 2D fp64 full tables
     void *kx[2] = {nullptr, nullptr}, *ky[2] = {nullptr, nullptr};  // 2D complex64 separable
-    const void *tw = nullptr, *tw_row = nullptr, *tw_col = nullptr, *tw_nx = nullptr;
+    const void *tw = nullptr, *tw_row = nullptr, *tw_col = nullptr, *tw_nx = nullptr, *tw_kin = nullptr;
+    Plan2D plan{};
     Geom2D geom{};
     uint64_t steps = 0;
     std::vector<void *> allocs;
@@ -313,8 +322,10 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     a.partials = partials;
     a.nx = in->nx;
     a.m = in->geom.m;
+    a.in_split = is ? 1 : 0;
+    a.out_split = os ? 1 : 0;
     ProfScope ps(in->ctx, "row_pass");
-    QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, is, os, a, in->ctx->st));
+    QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, a, in->ctx->st));
     return QSG_OK;
 }
 
@@ -477,6 +488,76 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     return QSG_OK;
 }
 
+
+// --- plans -----------------------------------------------------------------
+
+std::string plan_cache_path()
+{
+    if (const char *p = std::getenv("QSG_PLAN_CACHE")) return p;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : ".") + "/.cache/qusim_gb300/plans.tsv";
+}
+
+// lines: device \t prec \t nx \t ny \t g \t row_e \t col_e \t col_w \t ms_per_step
+void load_plans(qsg_ctx *ctx)
+{
+    if (ctx->plans_loaded) return;
+    ctx->plans_loaded = true;
+    std::ifstream f(plan_cache_path());
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream is(line);
+        std::string dev;
+        int prec, nx, ny;
+        Plan2D p;
+        double ms;
+        if (!std::getline(is, dev, '\t')) continue;
+        if (!(is >> prec >> nx >> ny >> p.g >> p.row_e >> p.col_e >> p.col_w >> ms)) continue;
+        Geom2D g;
+        if (dev == ctx->device_name && qsg::geom2d(prec, nx, ny, p, &g)) ctx->plans[std::make_tuple(prec, nx, ny)] = p;
+    }
+}
+
+void save_plan(qsg_ctx *ctx, int prec, int nx, int ny, const Plan2D &p, double ms)
+{
+    const std::string path = plan_cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        // create the directory chain (best effort)
+        std::string dir = path.substr(0, slash);
+        for (size_t i = 1; i <= dir.size(); ++i)
+            if (i == dir.size() || dir[i] == '/') {
+                std::string d = dir.substr(0, i);
+                mkdir(d.c_str(), 0755);
+            }
+    }
+    std::ofstream f(path, std::ios::app);
+    if (!f) return;
+    f << ctx->device_name << '\t' << prec << '\t' << nx << '\t' << ny << '\t' << p.g << '\t' << p.row_e << '\t'
+      << p.col_e << '\t' << p.col_w << '\t' << ms << '\n';
+}
+
+// point the instance at a plan: geometry + the twiddle tables it needs
+int apply_plan(qsg_inst *in, const Plan2D &p)
+{
+    Geom2D g;
+    if (!qsg::geom2d(in->prec, in->nx, in->ny, p, &g))
+        return fail(QSG_ERR_UNSUPPORTED, "plan not available for this grid");
+    const void *tr, *tc, *tn, *tk;
+    int rc;
+    if ((rc = get_twiddles(in->ctx, in->prec, in->ny, p.row_e, &tr))) return rc;
+    if ((rc = get_twiddles(in->ctx, in->prec, g.m, p.col_e, &tc))) return rc;
+    if ((rc = get_circle(in->ctx, in->prec, in->nx, &tn))) return rc;
+    if ((rc = get_twiddles(in->ctx, in->prec, g.m, g.kin_e, &tk))) return rc;
+    in->plan = p;
+    in->geom = g;
+    in->tw_row = tr;
+    in->tw_col = tc;
+    in->tw_nx = tn;
+    in->tw_kin = tk;
+    return QSG_OK;
+}
+
 bool finite_pos(double v) { return std::isfinite(v) && v > 0; }
 
 }  // namespace
@@ -508,6 +589,7 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
                                              " is not a Blackwell (sm_10x) GPU");
     qsg_ctx *ctx = new qsg_ctx();
     ctx->dev = device_ordinal;
+    ctx->device_name = prop.name;
     ctx->budget = hbm_budget_bytes;
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -618,8 +700,8 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     if (!finite_pos(dx) || !finite_pos(dy) || !finite_pos(mass) || !finite_pos(hbar) ||
         !std::isfinite(dt_re) || !std::isfinite(dt_im))
         return fail(QSG_ERR_ARG, "qsg_create_2d: dx, dy, mass, hbar must be finite and > 0, dt finite");
-    Geom2D g{};
-    if (nx > 65536 || ny > 65536 || !qsg::geom2d(precision, (int)nx, (int)ny, &g))
+    Plan2D plan{};
+    if (nx > 8192 || ny > 8192 || !qsg::default_plan(precision, (int)nx, (int)ny, &plan))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" +
                                              std::to_string(ny) +
                                              " (supported: powers of two, 128 .. 4096 per side)");
@@ -639,11 +721,10 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     in->dt = cd(dt_re, dt_im);
     in->order = order;
     in->prec = precision;
-    in->geom = g;
-    const int E = qsg::elems_per_thread(precision);
-    int rc = get_twiddles(ctx, precision, (int)ny, E, &in->tw_row);
-    if (!rc) rc = get_twiddles(ctx, precision, g.m, E, &in->tw_col);
-    if (!rc) rc = get_circle(ctx, precision, (int)nx, &in->tw_nx);
+    load_plans(ctx);
+    auto it = ctx->plans.find(std::make_tuple(precision, (int)nx, (int)ny));
+    if (it != ctx->plans.end()) plan = it->second;
+    int rc = apply_plan(in, plan);
     if (!rc) rc = common_create(in, psi0, V);
     if (rc) {
         std::string msg = g_last_error;
@@ -723,11 +804,11 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             if ((rc = row_pass(in, false, true, nullptr, false, nullptr, in->psi, ctx->scratch))) return rc;
             qsg::ColPassArgs a{};
             a.psi = ctx->scratch;
-            a.tw_col = in->tw_col;
+            a.tw_col = in->tw_kin;
             a.nx = in->nx;
             a.ny = in->ny;
             a.g = in->geom.g;
-            const int nblk = (in->ny / in->geom.col_w) * in->geom.g;
+            const int nblk = (in->ny / in->geom.kin_w) * in->geom.g;
             if (nblk > ctx->max_partials) return fail(QSG_ERR_STATE, "partials buffer too small");
             QSG_CUDA(qsg::launch_col_kinetic(in->prec, in->geom, a, DTx, DTy, ctx->partials, ctx->st));
             QSG_CUDA(qsg::launch_finalize(ctx->partials, nblk, 2, ctx->sums, ctx->st));
@@ -811,6 +892,88 @@ void qsg_destroy(qsg_inst *in)
     if (!in) return;
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     free_inst(in);
+}
+
+int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out, int cap)
+{
+    if (nx > 8192 || ny > 8192) return 0;
+    std::vector<Plan2D> v(256);
+    const int n = qsg::candidate_plans(precision, (int)nx, (int)ny, v.data(), (int)v.size());
+    for (int i = 0; i < n && i < cap && out; ++i) out[i] = qsg_plan2d{v[i].g, v[i].row_e, v[i].col_e, v[i].col_w};
+    return n;
+}
+
+int qsg_get_plan(qsg_inst *in, qsg_plan2d *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_plan: null argument");
+    if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_get_plan: 2D instances only");
+    *out = qsg_plan2d{in->plan.g, in->plan.row_e, in->plan.col_e, in->plan.col_w};
+    return QSG_OK;
+}
+
+int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
+{
+    if (!in || !p) return fail(QSG_ERR_ARG, "qsg_set_plan: null argument");
+    if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_set_plan: 2D instances only");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    QSG_CUDA(cudaSetDevice(in->ctx->dev));
+    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    return apply_plan(in, Plan2D{p->g, p->row_e, p->col_e, p->col_w});
+}
+
+int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, double *best_ms_per_step)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_autotune: null instance");
+    if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_autotune: 2D instances only");
+    if (trial_steps < 1) trial_steps = 4;
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    qsg_ctx *ctx = in->ctx;
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    std::vector<Plan2D> cands(256);
+    const int n = qsg::candidate_plans(in->prec, in->nx, in->ny, cands.data(), (int)cands.size());
+    if (n <= 0) return fail(QSG_ERR_UNSUPPORTED, "qsg_autotune: no plan for this grid");
+    cands.resize(n);
+    // the trials evolve a copy; psi and the step count are restored afterwards
+    const size_t bytes = in->n * csize(in->prec);
+    int rc = ensure_scratch(ctx, bytes);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    const Plan2D keep = in->plan;
+    const bool prof = ctx->prof;
+    ctx->prof = false;
+    cudaEvent_t e0, e1;
+    QSG_CUDA(cudaEventCreate(&e0));
+    QSG_CUDA(cudaEventCreate(&e1));
+    double best_ms = 1e30;
+    Plan2D best_p = keep;
+    for (const Plan2D &p : cands) {
+        if (apply_plan(in, p)) continue;
+        if (step2d(in, 1, 0)) continue;  // warm-up (also loads the module)
+        cudaEventRecord(e0, ctx->st);
+        if (step2d(in, (uint64_t)trial_steps, 0)) continue;
+        cudaEventRecord(e1, ctx->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double per = ms / trial_steps;
+        if (per < best_ms) {
+            best_ms = per;
+            best_p = p;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->prof = prof;
+    cudaError_t err = cudaGetLastError();
+    QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    if (err != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_autotune: ") + cudaGetErrorString(err));
+    if ((rc = apply_plan(in, best_p))) return rc;
+    ctx->plans[std::make_tuple(in->prec, in->nx, in->ny)] = best_p;
+    if (persist) save_plan(ctx, in->prec, in->nx, in->ny, best_p, best_ms);
+    if (best) *best = qsg_plan2d{best_p.g, best_p.row_e, best_p.col_e, best_p.col_w};
+    if (best_ms_per_step) *best_ms_per_step = best_ms;
+    return QSG_OK;
 }
 
 int qsg_profile_enable(qsg_ctx *ctx, int on)

@@ -1,48 +1,45 @@
-// 2D column passes: instantiations + launchers.
+// 2D column passes: instantiations, launchers, planner.
 #include "qsg_dispatch.cuh"
 
 namespace qsg {
 
 template <class T, int M>
-static cudaError_t run_col(const Geom2D &g, const ColPassArgs &a, cudaStream_t st)
-{
-    constexpr int E = sizeof(T) == 4 ? 16 : 8;
-    constexpr int W = col_w_for(M, E, sizeof(T) == 4 ? 1 : 0);
-    auto k = k_col_pass<T, M, E, W>;
-    cudaError_t e = prepare_smem(k, g.col_smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid(g.ny / W, g.g);
-    k<<<grid, W * (M / E), g.col_smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-template <class T, int M>
 static cudaError_t run_colkin(const Geom2D &g, const ColPassArgs &a, double dtx, double dty,
                               double *partials, cudaStream_t st)
 {
-    constexpr int E = sizeof(T) == 4 ? 16 : 8;
-    constexpr int W = col_w_for(M, E, sizeof(T) == 4 ? 1 : 0);
+    constexpr int P = sizeof(T) == 4 ? 1 : 0;
+    constexpr int E = kin_e_for(P);
+    constexpr int W = kin_w_for(P, M);
     auto k = k_col_kinetic<T, M, E, W>;
-    cudaError_t e = prepare_smem(k, g.col_smem);
+    cudaError_t e = prepare_smem(k, g.kin_smem);
     if (e != cudaSuccess) return e;
     dim3 grid(g.ny / W, g.g);
-    k<<<grid, W * (M / E), g.col_smem, st>>>(a, dtx, dty, partials);
+    k<<<grid, W * (M / E), g.kin_smem, st>>>(a, dtx, dty, partials);
     return cudaGetLastError();
 }
 
-#define QSG_M_CASES(X, T) X(T, 128) X(T, 256) X(T, 512) X(T, 1024)
+static bool col_variant_exists(int prec, int m, int e, int w)
+{
+#define C(T, M, E, W) \
+    if (m == M && e == E && w == W) return true;
+    if (prec == 1) {
+        QSG_COL_VARIANTS_F32(C)
+    } else {
+        QSG_COL_VARIANTS_F64(C)
+    }
+#undef C
+    return false;
+}
+
+cudaError_t launch_col_pass_f32(const Geom2D &, const ColPassArgs &, cudaStream_t);
+cudaError_t launch_col_pass_f64(const Geom2D &, const ColPassArgs &, cudaStream_t);
 
 cudaError_t launch_col_pass(int prec, const Geom2D &g, const ColPassArgs &a, cudaStream_t st)
 {
-#define X(T, M) case M: return run_col<T, M>(g, a, st);
-    if (prec == 1) {
-        switch (g.m) { QSG_M_CASES(X, float) default: break; }
-    } else {
-        switch (g.m) { QSG_M_CASES(X, double) X(double, 2048) default: break; }
-    }
-#undef X
-    return cudaErrorNotSupported;
+    return prec == 1 ? launch_col_pass_f32(g, a, st) : launch_col_pass_f64(g, a, st);
 }
+
+#define QSG_M_CASES(X, T) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
 
 cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, double dtx,
                                double dty, double *partials, cudaStream_t st)
@@ -51,45 +48,108 @@ cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, 
     if (prec == 1) {
         switch (g.m) { QSG_M_CASES(X, float) default: break; }
     } else {
-        switch (g.m) { QSG_M_CASES(X, double) X(double, 2048) default: break; }
+        switch (g.m) { QSG_M_CASES(X, double) default: break; }
     }
 #undef X
     return cudaErrorNotSupported;
 }
 
-cudaError_t launch_row_pass_f32(const Geom2D &, bool, bool, const RowPassArgs &, cudaStream_t);
-cudaError_t launch_row_pass_f64(const Geom2D &, bool, bool, const RowPassArgs &, cudaStream_t);
+cudaError_t launch_row_pass_f32a(const Geom2D &, const RowPassArgs &, cudaStream_t);
+cudaError_t launch_row_pass_f32b(const Geom2D &, const RowPassArgs &, cudaStream_t);
+cudaError_t launch_row_pass_f64(const Geom2D &, const RowPassArgs &, cudaStream_t);
+bool row_variant_exists_f32a(int ny, int e, int g);
+bool row_variant_exists_f32b(int ny, int e, int g);
+bool row_variant_exists_f64(int ny, int e, int g);
 
-cudaError_t launch_row_pass(int prec, const Geom2D &g, bool in_split, bool out_split,
-                            const RowPassArgs &a, cudaStream_t st)
+cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
 {
-    return prec == 1 ? launch_row_pass_f32(g, in_split, out_split, a, st)
-                     : launch_row_pass_f64(g, in_split, out_split, a, st);
+    if (prec == 0) return launch_row_pass_f64(g, a, st);
+    return g.row_e == 16 ? launch_row_pass_f32a(g, a, st) : launch_row_pass_f32b(g, a, st);
 }
 
-bool geom2d(int prec, int nx, int ny, Geom2D *g)
+bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
 {
     auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
-    if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 4096 || nx < 128 || nx > 4096) return false;
-    const int E = elems_per_thread(prec);
+    if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 4096 || nx < 128 || nx > 8192) return false;
+    if (!pow2(p.g) || p.g > 4 || nx % p.g) return false;
     const int csz = prec == 1 ? 8 : 16;
-    const int pads = prec == 1 ? 4 : 3;
+    const bool row_ok = prec == 1 ? (row_variant_exists_f32a(ny, p.row_e, p.g) || row_variant_exists_f32b(ny, p.row_e, p.g))
+                                   : row_variant_exists_f64(ny, p.row_e, p.g);
+    if (!row_ok) return false;
     g->nx = nx;
     g->ny = ny;
-    g->g = split_g_for(prec, nx);
-    g->m = nx / g->g;
-    g->row_b = row_b_for(ny, E, g->g);
-    const int rs = row_rs_for(ny, E, g->g);
-    g->row_threads = g->row_b * g->g * (ny / E) / rs;
+    g->g = p.g;
+    g->m = nx / p.g;
+    if (!col_variant_exists(prec, g->m, p.col_e, p.col_w)) return false;
+    g->row_e = p.row_e;
+    g->row_b = row_b_for(ny, p.row_e, p.g);
+    g->row_rs = row_rs_for(ny, p.row_e, p.g);
+    g->row_threads = g->row_b * p.g * (ny / p.row_e) / g->row_rs;
     if (g->m % g->row_b) return false;
     g->row_blocks = g->m / g->row_b;
-    g->row_smem = (size_t)csz * g->row_b * g->g * (ny + (ny >> pads));
-    g->col_w = col_w_for(g->m, E, prec);
-    if (ny % g->col_w) return false;
-    g->col_threads = g->col_w * (g->m / E);
-    g->col_smem = (size_t)csz * col_tile_elems(csz, g->m, g->col_w);
-    return g->row_threads <= 512 && g->col_threads <= 512 && g->row_smem <= 200 * 1024 &&
-           g->col_smem <= 200 * 1024;
+    g->row_smem = row_smem_for(csz, ny, p.row_e, p.g);
+    g->col_e = p.col_e;
+    g->col_w = p.col_w;
+    if (ny % p.col_w) return false;
+    g->col_threads = p.col_w * (g->m / p.col_e);
+    g->col_smem = (size_t)csz * col_tile_elems(csz, g->m, p.col_w);
+    g->kin_e = kin_e_for(prec);
+    g->kin_w = kin_w_for(prec, g->m);
+    if (ny % g->kin_w) return false;
+    g->kin_threads = g->kin_w * (g->m / g->kin_e);
+    g->kin_smem = (size_t)csz * col_tile_elems(csz, g->m, g->kin_w);
+    const size_t smem_max = 227 * 1024 - 1024;
+    return g->row_threads <= 512 && g->col_threads <= 512 && g->kin_threads <= 512 &&
+           g->row_smem <= smem_max && g->col_smem <= smem_max && g->kin_smem <= smem_max &&
+           g->m >= 128 && g->m <= 2048;
+}
+
+int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap)
+{
+    int n = 0;
+    const int es[2] = {16, 8};
+    const int ws[5] = {4, 8, 16, 32, 2};
+    for (int g = 1; g <= 4; g *= 2)
+        for (int re : es)
+            for (int ce : es)
+                for (int w : ws) {
+                    Plan2D p{g, re, ce, w};
+                    Geom2D gm;
+                    if (!geom2d(prec, nx, ny, p, &gm)) continue;
+                    if (n < cap) out[n] = p;
+                    ++n;
+                }
+    return n;
+}
+
+bool default_plan(int prec, int nx, int ny, Plan2D *p)
+{
+    // complex64: column blocks of <= 1024 rows with 64-byte column segments
+    // (radix 16); complex128: blocks of <= 2048 rows (radix 8)
+    Plan2D c;
+    if (prec == 1) {
+        c.g = nx > 1024 ? nx / 1024 : 1;
+        c.row_e = 16;
+        c.col_e = 16;
+        const int m = nx / c.g;
+        c.col_w = m >= 512 ? 8 : (m == 256 ? 16 : 32);
+    } else {
+        c.g = nx > 2048 ? nx / 2048 : 1;
+        c.row_e = 8;
+        c.col_e = 8;
+        const int m = nx / c.g;
+        c.col_w = m >= 2048 ? 2 : (m >= 512 ? 4 : (m == 256 ? 8 : 16));
+    }
+    Geom2D g;
+    if (geom2d(prec, nx, ny, c, &g)) {
+        *p = c;
+        return true;
+    }
+    Plan2D cands[64];
+    const int n = candidate_plans(prec, nx, ny, cands, 64);
+    if (n <= 0) return false;
+    *p = cands[0];
+    return true;
 }
 
 }  // namespace qsg

@@ -1,0 +1,26 @@
+// 2D column passes (float): instantiations + launcher.
+#include "qsg_dispatch.cuh"
+
+namespace qsg {
+
+template <class T, int M, int E, int W>
+static cudaError_t run_col_f32(const Geom2D &g, const ColPassArgs &a, cudaStream_t st)
+{
+    auto k = k_col_pass<T, M, E, W>;
+    cudaError_t e = prepare_smem(k, g.col_smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(g.ny / W, g.g);
+    k<<<grid, W * (M / E), g.col_smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col_pass_f32(const Geom2D &g, const ColPassArgs &a, cudaStream_t st)
+{
+#define C(T, M, E, W) \
+    if (g.m == M && g.col_e == E && g.col_w == W) return run_col_f32<T, M, E, W>(g, a, st);
+    QSG_COL_VARIANTS_F32(C)
+#undef C
+    return cudaErrorNotSupported;
+}
+
+}  // namespace qsg

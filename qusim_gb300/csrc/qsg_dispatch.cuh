@@ -1,4 +1,5 @@
-// qsg_dispatch.cuh -- helpers shared by the instantiation units.
+// qsg_dispatch.cuh -- variant tables and geometry rules shared by the
+// instantiation units and the host planner.
 #pragma once
 #include "qsg_launch.h"
 
@@ -12,16 +13,8 @@ static inline cudaError_t prepare_smem(K kernel, size_t smem)
     return cudaSuccess;
 }
 
-// Geometry rules (shared by the launchers and geom2d):
-//  * x split G: complex64 keeps column blocks M = Nx/G <= 1024, complex128 <= 2048
-//  * row pass: B groups of G rows per CTA so a CTA holds >= 256 threads of
-//    line work; RS sequential rounds keep the CTA at <= 512 threads
-//  * column pass: W adjacent columns per CTA (64 B rows for complex64),
-//    <= 512 threads
-constexpr int split_g_for(int prec, int nx)
-{
-    return prec == 1 ? (nx > 1024 ? nx / 1024 : 1) : (nx > 2048 ? nx / 2048 : 1);
-}
+// Row pass: B groups of G rows per CTA so a CTA holds >= 256 threads of line
+// work; RS sequential rounds keep the CTA at <= 512 threads.
 constexpr int row_b_for(int ny, int e, int g)
 {
     return (256 / (g * (ny / e))) > 1 ? 256 / (g * (ny / e)) : 1;
@@ -30,10 +23,44 @@ constexpr int row_rs_for(int ny, int e, int g)
 {
     return (row_b_for(ny, e, g) * g * (ny / e)) > 512 ? row_b_for(ny, e, g) * g * (ny / e) / 512 : 1;
 }
-constexpr int col_w_for(int m, int e, int prec)
+constexpr size_t row_smem_for(int csz, int ny, int e, int g)
 {
-    return prec == 1 ? (512 / (m / e) < 8 ? 8 : (256 / (m / e) > 8 ? 256 / (m / e) : 8))
-                     : (m >= 2048 ? 2 : (256 / (m / e) > 4 ? 256 / (m / e) : 4));
+    return (size_t)csz * row_b_for(ny, e, g) * g * (ny + (ny >> (csz == 8 ? 4 : 3)));
+}
+
+// Instantiated variants.  X(T, NY, E, G) for the row pass,
+// C(T, M, E, W) for the column pass (W*M/E threads, 128..512).
+#define QSG_ROW_NY(X, T, E, G) X(T, 128, E, G) X(T, 256, E, G) X(T, 512, E, G) X(T, 1024, E, G) X(T, 2048, E, G) X(T, 4096, E, G)
+#define QSG_ROW_VARIANTS_F32A(X) \
+    QSG_ROW_NY(X, float, 16, 1) QSG_ROW_NY(X, float, 16, 2) QSG_ROW_NY(X, float, 16, 4)
+#define QSG_ROW_VARIANTS_F32B(X) \
+    QSG_ROW_NY(X, float, 8, 1) QSG_ROW_NY(X, float, 8, 2) QSG_ROW_NY(X, float, 8, 4)
+#define QSG_ROW_VARIANTS_F64(X) \
+    QSG_ROW_NY(X, double, 8, 1) QSG_ROW_NY(X, double, 8, 2) QSG_ROW_NY(X, double, 8, 4)
+
+#define QSG_COL_VARIANTS_F32(C) \
+    C(float, 128, 16, 16) C(float, 128, 16, 32) \
+    C(float, 256, 16, 8) C(float, 256, 16, 16) C(float, 256, 16, 32) \
+    C(float, 512, 16, 4) C(float, 512, 16, 8) C(float, 512, 16, 16) \
+    C(float, 1024, 16, 4) C(float, 1024, 16, 8) \
+    C(float, 2048, 16, 4) \
+    C(float, 128, 8, 8) C(float, 128, 8, 16) C(float, 128, 8, 32) \
+    C(float, 256, 8, 4) C(float, 256, 8, 8) C(float, 256, 8, 16) \
+    C(float, 512, 8, 4) C(float, 512, 8, 8) \
+    C(float, 1024, 8, 4)
+#define QSG_COL_VARIANTS_F64(C) \
+    C(double, 128, 8, 8) C(double, 128, 8, 16) \
+    C(double, 256, 8, 4) C(double, 256, 8, 8) \
+    C(double, 512, 8, 4) \
+    C(double, 1024, 8, 4) \
+    C(double, 2048, 8, 2)
+
+// the kinetic-energy column transform: one variant per (precision, M)
+constexpr int kin_e_for(int prec) { return prec == 1 ? 16 : 8; }
+constexpr int kin_w_for(int prec, int m)
+{
+    return prec == 1 ? (m >= 2048 ? 4 : (m >= 512 ? 8 : 256 / (m / 16)))
+                     : (m >= 2048 ? 2 : (m >= 512 ? 4 : 256 / (m / 8)));
 }
 
 }  // namespace qsg

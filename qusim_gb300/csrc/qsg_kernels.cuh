@@ -194,16 +194,18 @@ struct RowPassArgs {
     const void *tw_nx;      // full circle exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
     double *partials;       // per-CTA sum |psi|^2 (natural-output passes), or null
     int nx, m;              // Nx and M = Nx / G
+    int in_split, out_split;
 };
 
-// IN_SPLIT: input is in split-k space (inverse x-split stage + row iFFT first);
-//           otherwise natural real-space rows.
-// OUT_SPLIT: output goes back to split-k space (row FFT + forward x-split
-//           stage); otherwise natural real-space rows (+ norm partials).
+// in_split:  input is in split-k space (inverse x-split stage + row iFFT first);
+//            otherwise natural real-space rows.
+// out_split: output goes back to split-k space (row FFT + forward x-split
+//            stage); otherwise natural real-space rows (+ norm partials).
+// (Runtime flags: one instantiation serves the three pass kinds of a step.)
 // One CTA handles B row groups; group b has the G rows n1 + j*M, j < G,
 // n1 = blockIdx.x*B + b, i.e. NL = B*G lines of NY.  The NT threads work on
 // NL/RS lines at a time and go over the CTA's lines in RS rounds.
-template <class T, int NY, int E, int G, int B, int RS, bool IN_SPLIT, bool OUT_SPLIT>
+template <class T, int NY, int E, int G, int B, int RS>
 __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
 {
     using C = cplx_t<T>;
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     C *sm = reinterpret_cast<C *>(smraw);
     __shared__ double red[32];
 
+    const bool in_split = a.in_split != 0, out_split = a.out_split != 0;
     const int tid = threadIdx.x;
     const int grp = tid / TL;  // line slot within a round
     const int t = tid - grp * TL;
@@ -233,25 +236,27 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
     LineBar lbar;
     if constexpr (NAMED) lbar = NamedBarrier{1 + grp, TL};
-    constexpr bool VIA_SMEM_IN = IN_SPLIT && G > 1;
-    constexpr bool VIA_SMEM_OUT = OUT_SPLIT && G > 1;
+    const bool via_smem_in = in_split && G > 1;
+    const bool via_smem_out = out_split && G > 1;
 
-    if constexpr (VIA_SMEM_IN) {
-        // inverse x-split stage over every column of every group of this CTA
-#pragma unroll 4
-        for (int u = 0; u < B * NY / NT; ++u) {
-            const int gc = tid + u * NT;
-            const int bb = gc / NY, c = gc - bb * NY;
-            const int nn1 = blockIdx.x * B + bb;
-            C y[G];
+    if (via_smem_in) {
+        if constexpr (G > 1) {
+            // inverse x-split stage over every column of every group of this CTA
+#pragma unroll 2
+            for (int u = 0; u < B * NY / NT; ++u) {
+                const int gc = tid + u * NT;
+                const int bb = gc / NY, c = gc - bb * NY;
+                const int nn1 = blockIdx.x * B + bb;
+                C y[G];
 #pragma unroll
-            for (int q = 0; q < G; ++q) {
-                y[q] = ld_stream(in + (size_t)(q * a.m + nn1) * NY + c);
-                if (q > 0) y[q] = twmul<true>(y[q], __ldg(twx + nn1 * q));
+                for (int q = 0; q < G; ++q) {
+                    y[q] = ld_stream(in + (size_t)(q * a.m + nn1) * NY + c);
+                    if (q > 0) y[q] = twmul<true>(y[q], __ldg(twx + nn1 * q));
+                }
+                dftg<G, true>(y);
+#pragma unroll
+                for (int q = 0; q < G; ++q) sm[(bb * G + q) * LINE + c + (c >> PADS)] = y[q];
             }
-            dftg<G, true>(y);
-#pragma unroll
-            for (int q = 0; q < G; ++q) sm[(bb * G + q) * LINE + c + (c >> PADS)] = y[q];
         }
         cbar();
     }
@@ -264,24 +269,25 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
         const int row = blockIdx.x * B + b + j * a.m;
         const RowLayout<PADS> lay{line * LINE};
         C x[E];
-        if constexpr (VIA_SMEM_IN) {
+        if (via_smem_in) {
 #pragma unroll
             for (int e = 0; e < E; ++e) x[e] = sm[lay(t + e * TL)];
         } else {
+            const C *ir = in + (size_t)row * NY + t;
 #pragma unroll
-            for (int e = 0; e < E; ++e) x[e] = ld_stream(in + (size_t)row * NY + t + e * TL);
+            for (int e = 0; e < E; ++e) x[e] = ld_stream(ir + e * TL);
         }
         // [row iFFT] -> V -> [row FFT], the iFFT as conj(FFT(conj(x)))
-        constexpr int NPASS = (IN_SPLIT ? 1 : 0) + (OUT_SPLIT ? 1 : 0);
-        constexpr int VPOS = IN_SPLIT ? 1 : 0;
-        if constexpr (IN_SPLIT) {
+        const int npass = (in_split ? 1 : 0) + (out_split ? 1 : 0);
+        const int vpos = in_split ? 1 : 0;
+        if (in_split) {
 #pragma unroll
             for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
         }
 #pragma unroll 1
-        for (int p = 0; p <= NPASS; ++p) {
-            if (p == VPOS) {
-                if constexpr (IN_SPLIT) {
+        for (int p = 0; p <= npass; ++p) {
+            if (p == vpos) {
+                if (in_split) {
 #pragma unroll
                     for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
                 }
@@ -295,49 +301,49 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
                     }
                 }
             }
-            if (p < NPASS) line_fft<C, NY, E, false>(x, sm, lay, lbar, t, tw);
+            if (p < npass) line_fft<C, NY, E, false>(x, sm, lay, lbar, t, tw);
         }
-        if constexpr (!OUT_SPLIT) {
+        if (!out_split) {
+            C *orow = const_cast<C *>(opaque(out)) + (size_t)row * NY + t;
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                st_stream(out + (size_t)row * NY + t + e * TL, x[e]);
+                st_stream(orow + e * TL, x[e]);
                 nsum += abs2d(x[e]);
             }
+        } else if (via_smem_out) {
+            lbar();  // this line's readers of the last exchange are done
+#pragma unroll
+            for (int e = 0; e < E; ++e) sm[lay(t + e * TL)] = x[e];
         } else {
-            if constexpr (VIA_SMEM_OUT) {
-                lbar();  // this line's readers of the last exchange are done
+            C *orow = const_cast<C *>(opaque(out)) + (size_t)row * NY + t;
 #pragma unroll
-                for (int e = 0; e < E; ++e) sm[lay(t + e * TL)] = x[e];
-            } else {
-#pragma unroll
-                for (int e = 0; e < E; ++e) st_stream(out + (size_t)row * NY + t + e * TL, x[e]);
-            }
+            for (int e = 0; e < E; ++e) st_stream(orow + e * TL, x[e]);
         }
     }
 
-    if constexpr (VIA_SMEM_OUT) {
-        cbar();
-#pragma unroll 4
-        for (int u = 0; u < B * NY / NT; ++u) {
-            const int gc = tid + u * NT;
-            const int bb = gc / NY, c = gc - bb * NY;
-            const int nn1 = blockIdx.x * B + bb;
-            C y[G];
+    if (via_smem_out) {
+        if constexpr (G > 1) {
+            cbar();
+#pragma unroll 2
+            for (int u = 0; u < B * NY / NT; ++u) {
+                const int gc = tid + u * NT;
+                const int bb = gc / NY, c = gc - bb * NY;
+                const int nn1 = blockIdx.x * B + bb;
+                C y[G];
 #pragma unroll
-            for (int q = 0; q < G; ++q) y[q] = sm[(bb * G + q) * LINE + c + (c >> PADS)];
-            dftg<G, false>(y);
+                for (int q = 0; q < G; ++q) y[q] = sm[(bb * G + q) * LINE + c + (c >> PADS)];
+                dftg<G, false>(y);
 #pragma unroll
-            for (int q = 0; q < G; ++q) {
-                if (q > 0) y[q] = twmul<false>(y[q], __ldg(twx + nn1 * q));
-                st_stream(out + (size_t)(q * a.m + nn1) * NY + c, y[q]);
+                for (int q = 0; q < G; ++q) {
+                    if (q > 0) y[q] = twmul<false>(y[q], __ldg(twx + nn1 * q));
+                    st_stream(out + (size_t)(q * a.m + nn1) * NY + c, y[q]);
+                }
             }
         }
     }
-    if constexpr (!OUT_SPLIT) {
-        if (a.partials) {
-            nsum = block_sum<NT>(nsum, red);
-            if (tid == 0) a.partials[blockIdx.x] = nsum;
-        }
+    if (!out_split && a.partials) {
+        nsum = block_sum<NT>(nsum, red);
+        if (tid == 0) a.partials[blockIdx.x] = nsum;
     }
 }
 

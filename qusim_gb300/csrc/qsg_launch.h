@@ -8,27 +8,42 @@
 
 namespace qsg {
 
-// elements per thread of every line transform, per precision (0 fp64, 1 mixed)
+// elements per thread of the 1D resident transforms and of the default plans,
+// per precision (0 fp64, 1 mixed)
 inline int elems_per_thread(int prec) { return prec == 1 ? 16 : 8; }
 
 // 1D resident evolver: supported n (power of two)
 bool evolve1d_supported(int prec, uint64_t n);
 cudaError_t launch_evolve1d(int prec, int n, const Evolve1DArgs &a, cudaStream_t st);
 
-// 2D geometry chosen for a grid
-struct Geom2D {
-    int nx, ny, g, m;   // x split: nx = g * m
-    int row_b;          // row groups per CTA
-    int row_threads, row_blocks;
-    size_t row_smem;
-    int col_w, col_threads;
-    size_t col_smem;
+// A 2D plan: the x split and the kernel variants of the two passes.
+struct Plan2D {
+    int g;          // x split: Nx = g * m, column transforms of length m
+    int row_e;      // elements per thread of the row transforms (radix)
+    int col_e;      // elements per thread of the column transforms
+    int col_w;      // adjacent columns per column-pass CTA
 };
-bool geom2d(int prec, int nx, int ny, Geom2D *g);
-cudaError_t launch_row_pass(int prec, const Geom2D &g, bool in_split, bool out_split,
-                            const RowPassArgs &a, cudaStream_t st);
+
+// Launch geometry of a plan for a grid
+struct Geom2D {
+    int nx, ny, g, m;
+    int row_e, row_b, row_rs, row_threads, row_blocks;
+    size_t row_smem;
+    int col_e, col_w, col_threads;
+    size_t col_smem;
+    int kin_e, kin_w, kin_threads;  // kinetic-energy column transform
+    size_t kin_smem;
+};
+// Valid (compiled, fits the SM) geometry for the plan?
+bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g);
+// Plans compiled for this grid (up to cap); returns the count.
+int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap);
+// The plan used when no tuned plan is known.
+bool default_plan(int prec, int nx, int ny, Plan2D *p);
+
+cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cudaStream_t st);
 cudaError_t launch_col_pass(int prec, const Geom2D &g, const ColPassArgs &a, cudaStream_t st);
-// forward transform of the column pass with the kinetic-energy reduction
+// forward column transform with the kinetic-energy reduction (uses kin_* geometry)
 cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, double dtx,
                                double dty, double *partials, cudaStream_t st);
 // 1D forward transform with the kinetic-energy reduction (one CTA)

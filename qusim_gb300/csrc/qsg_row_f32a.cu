@@ -1,0 +1,36 @@
+// 2D row passes (float, radix 16): instantiations + launcher.
+#include "qsg_dispatch.cuh"
+
+namespace qsg {
+
+template <int NY, int E, int G>
+static cudaError_t run_row_f32a(const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
+{
+    constexpr int B = row_b_for(NY, E, G);
+    constexpr int RS = row_rs_for(NY, E, G);
+    auto k = k_row_pass<float, NY, E, G, B, RS>;
+    cudaError_t e = prepare_smem(k, g.row_smem);
+    if (e != cudaSuccess) return e;
+    k<<<g.row_blocks, g.row_threads, g.row_smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_pass_f32a(const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
+{
+#define X(T, NY, E, G) \
+    if (g.ny == NY && g.row_e == E && g.g == G) return run_row_f32a<NY, E, G>(g, a, st);
+    QSG_ROW_VARIANTS_F32A(X)
+#undef X
+    return cudaErrorNotSupported;
+}
+
+bool row_variant_exists_f32a(int ny, int e, int g)
+{
+#define X(T, NY, E, G) \
+    if (ny == NY && e == E && g == G) return true;
+    QSG_ROW_VARIANTS_F32A(X)
+#undef X
+    return false;
+}
+
+}  // namespace qsg

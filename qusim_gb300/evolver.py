@@ -136,11 +136,12 @@ def _dptr(a: np.ndarray):
 class Instance:
     """One qsg_inst: a wavefunction resident on the device."""
 
-    def __init__(self, ctx: Context, handle, shape, dv):
+    def __init__(self, ctx: Context, handle, shape, dv, prec=0):
         self.ctx = ctx
         self.h = handle
         self.shape = shape
         self.dv = dv
+        self._prec = prec
 
     @classmethod
     def create_1d(cls, ctx, psi0, V, dx, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
@@ -155,7 +156,7 @@ class Instance:
                                     _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
                                     boundary.value, _dptr(psi0.view(np.float64)), _dptr(V),
                                     ctypes.byref(h)))
-        return cls(ctx, h, psi0.shape, dx)
+        return cls(ctx, h, psi0.shape, dx, 1 if precision == "mixed" else 0)
 
     @classmethod
     def create_2d(cls, ctx, psi0, V, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
@@ -169,7 +170,7 @@ class Instance:
         check(ctx.lib.qsg_create_2d(ctx.h, nx, ny, dx, dy, mass, hbar, dt.real, dt.imag, order,
                                     _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
                                     _dptr(psi0.view(np.float64)), _dptr(V), ctypes.byref(h)))
-        return cls(ctx, h, psi0.shape, dx * dy)
+        return cls(ctx, h, psi0.shape, dx * dy, 1 if precision == "mixed" else 0)
 
     def step(self, nsteps: int, renormalize: bool = False):
         check(self.ctx.lib.qsg_step(self.h, nsteps, int(renormalize)))
@@ -206,6 +207,32 @@ class Instance:
     def set_psi(self, psi):
         psi = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
         check(self.ctx.lib.qsg_set_psi(self.h, _dptr(psi.view(np.float64))))
+
+    def plan(self):
+        p = _lib.Plan2D()
+        check(self.ctx.lib.qsg_get_plan(self.h, ctypes.byref(p)))
+        return p
+
+    def set_plan(self, plan):
+        if not isinstance(plan, _lib.Plan2D):
+            plan = _lib.Plan2D(*plan)
+        check(self.ctx.lib.qsg_set_plan(self.h, ctypes.byref(plan)))
+
+    def candidate_plans(self, precision=None):
+        lib = self.ctx.lib
+        prec = self._prec if precision is None else (1 if precision == "mixed" else 0)
+        nx, ny = self.shape
+        n = lib.qsg_candidate_plans(prec, nx, ny, None, 0)
+        arr = (_lib.Plan2D * max(n, 1))()
+        n = lib.qsg_candidate_plans(prec, nx, ny, arr, n)
+        return [arr[i] for i in range(n)]
+
+    def autotune(self, trial_steps: int = 4, persist: bool = True):
+        """Time every plan on a copy of the state, switch to the fastest; returns (plan, ms/step)."""
+        p = _lib.Plan2D()
+        ms = ctypes.c_double()
+        check(self.ctx.lib.qsg_autotune(self.h, trial_steps, int(persist), ctypes.byref(p), ctypes.byref(ms)))
+        return p, ms.value
 
     def steps_taken(self) -> int:
         v = ctypes.c_uint64()

@@ -186,3 +186,38 @@ def test_evolver_api_mirror(qsg):
     with pytest.raises(ValueError):
         Evolver1D().init(lambda x: 0j, True, 0.02, False, lambda x: 0.0, -1, 1, 64,
                          BoundaryCondition.Period, SolverMethod.SplittingMethodO2, 1, 1, Options())
+
+
+@pytest.mark.parametrize("nx,ny", [(4096, 128), (2048, 256), (256, 1024)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_every_plan_matches_oracle(qsg, ctx, oracle, nx, ny, precision):
+    hx, hy = 0.05 * nx, 0.05 * ny
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=0.08 * min(hx, hy))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=8, seed=2, spread=0.5 * min(hx, hy))
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.01, 2, order=4)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision=precision)
+    plans = inst.candidate_plans()
+    assert len(plans) >= 1
+    tol = PLAIN_TOL if precision == "fp64" else MIXED_TOL
+    for p in plans:
+        inst.set_psi(psi0)
+        inst.set_plan(p)
+        inst.step(2)
+        err = rel_l2(inst.get_psi(), ref)
+        assert err <= tol, (p, err)
+
+
+def test_autotune_keeps_state(qsg, ctx):
+    nx = ny = 1024
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -50, 50, -50, 50, 1.0, 0.0, -10.0, 0.0, 4.0)
+    V = gaussian_bumps_2d(nx, ny, -50, 50, -50, 50, nbumps=8, seed=3, spread=20.0)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    inst.step(3)
+    before = inst.get_psi().copy()
+    plan, ms = inst.autotune(trial_steps=2, persist=False)
+    assert ms > 0
+    assert plan.as_tuple() in [p.as_tuple() for p in inst.candidate_plans()]
+    assert inst.plan().as_tuple() == plan.as_tuple()
+    assert np.array_equal(inst.get_psi(), before)
+    assert inst.steps_taken() == 3
