@@ -118,12 +118,14 @@ void qsg_destroy(qsg_inst *inst);
 
 /* 2D execution plan: the x split (Nx = g * m, column transforms of length m,
  * a radix-g stage folded into the row pass), the elements per thread (radix)
- * of the row and column transforms, and the columns per column-pass CTA.
+ * of the row and column transforms, the threads per row-pass CTA, and the
+ * columns per column-pass CTA.
  * Every plan computes the same result to rounding; they differ in speed.
  * New to this engine (the reference has one fixed cuFFT / KISS path). */
 typedef struct {
     int32_t g;
     int32_t row_e;
+    int32_t row_nt;
     int32_t col_e;
     int32_t col_w;
 } qsg_plan2d;

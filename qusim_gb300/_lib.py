@@ -38,15 +38,16 @@ EXPORTS = [
 
 
 class Plan2D(ctypes.Structure):
-    """qsg_plan2d: x split g, row / column elements per thread, column tile width."""
-    _fields_ = [("g", ctypes.c_int32), ("row_e", ctypes.c_int32), ("col_e", ctypes.c_int32),
-                ("col_w", ctypes.c_int32)]
+    """qsg_plan2d: x split g, row radix and CTA threads, column radix and tile width."""
+    _fields_ = [("g", ctypes.c_int32), ("row_e", ctypes.c_int32), ("row_nt", ctypes.c_int32),
+                ("col_e", ctypes.c_int32), ("col_w", ctypes.c_int32)]
 
     def as_tuple(self):
-        return (self.g, self.row_e, self.col_e, self.col_w)
+        return (self.g, self.row_e, self.row_nt, self.col_e, self.col_w)
 
     def __repr__(self):
-        return f"Plan2D(g={self.g}, row_e={self.row_e}, col_e={self.col_e}, col_w={self.col_w})"
+        return (f"Plan2D(g={self.g}, row_e={self.row_e}, row_nt={self.row_nt}, col_e={self.col_e}, "
+                f"col_w={self.col_w})")
 
 
 class QsgError(RuntimeError):

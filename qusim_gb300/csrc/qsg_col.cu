@@ -57,9 +57,9 @@ cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, 
 cudaError_t launch_row_pass_f32a(const Geom2D &, const RowPassArgs &, cudaStream_t);
 cudaError_t launch_row_pass_f32b(const Geom2D &, const RowPassArgs &, cudaStream_t);
 cudaError_t launch_row_pass_f64(const Geom2D &, const RowPassArgs &, cudaStream_t);
-bool row_variant_exists_f32a(int ny, int e, int g);
-bool row_variant_exists_f32b(int ny, int e, int g);
-bool row_variant_exists_f64(int ny, int e, int g);
+bool row_variant_exists_f32a(int ny, int e, int g, int nt);
+bool row_variant_exists_f32b(int ny, int e, int g, int nt);
+bool row_variant_exists_f64(int ny, int e, int g, int nt);
 
 cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
 {
@@ -73,8 +73,9 @@ bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
     if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 4096 || nx < 128 || nx > 8192) return false;
     if (!pow2(p.g) || p.g > 4 || nx % p.g) return false;
     const int csz = prec == 1 ? 8 : 16;
-    const bool row_ok = prec == 1 ? (row_variant_exists_f32a(ny, p.row_e, p.g) || row_variant_exists_f32b(ny, p.row_e, p.g))
-                                   : row_variant_exists_f64(ny, p.row_e, p.g);
+    const bool row_ok = prec == 1 ? (row_variant_exists_f32a(ny, p.row_e, p.g, p.row_nt) ||
+                                     row_variant_exists_f32b(ny, p.row_e, p.g, p.row_nt))
+                                   : row_variant_exists_f64(ny, p.row_e, p.g, p.row_nt);
     if (!row_ok) return false;
     g->nx = nx;
     g->ny = ny;
@@ -83,8 +84,8 @@ bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
     if (!col_variant_exists(prec, g->m, p.col_e, p.col_w)) return false;
     g->row_e = p.row_e;
     g->row_b = row_b_for(ny, p.row_e, p.g);
-    g->row_rs = row_rs_for(ny, p.row_e, p.g);
-    g->row_threads = g->row_b * p.g * (ny / p.row_e) / g->row_rs;
+    g->row_threads = p.row_nt;
+    g->row_rs = row_work_for(ny, p.row_e, p.g) / p.row_nt;
     if (g->m % g->row_b) return false;
     g->row_blocks = g->m / g->row_b;
     g->row_smem = row_smem_for(csz, ny, p.row_e, p.g);
@@ -109,16 +110,18 @@ int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap)
     int n = 0;
     const int es[2] = {16, 8};
     const int ws[5] = {4, 8, 16, 32, 2};
+    const int nts[2] = {512, 256};
     for (int g = 1; g <= 4; g *= 2)
         for (int re : es)
-            for (int ce : es)
-                for (int w : ws) {
-                    Plan2D p{g, re, ce, w};
-                    Geom2D gm;
-                    if (!geom2d(prec, nx, ny, p, &gm)) continue;
-                    if (n < cap) out[n] = p;
-                    ++n;
-                }
+            for (int nt : nts)
+                for (int ce : es)
+                    for (int w : ws) {
+                        Plan2D p{g, re, nt, ce, w};
+                        Geom2D gm;
+                        if (!geom2d(prec, nx, ny, p, &gm)) continue;
+                        if (n < cap) out[n] = p;
+                        ++n;
+                    }
     return n;
 }
 
@@ -130,12 +133,14 @@ bool default_plan(int prec, int nx, int ny, Plan2D *p)
     if (prec == 1) {
         c.g = nx > 1024 ? nx / 1024 : 1;
         c.row_e = 16;
+        c.row_nt = (ny >= 4096 && c.g >= 2) || (ny >= 2048 && c.g >= 4) ? 512 : 256;
         c.col_e = 16;
         const int m = nx / c.g;
         c.col_w = m >= 512 ? 8 : (m == 256 ? 16 : 32);
     } else {
         c.g = nx > 2048 ? nx / 2048 : 1;
         c.row_e = 8;
+        c.row_nt = row_work_for(ny, 8, c.g) >= 512 ? 512 : 256;
         c.col_e = 8;
         const int m = nx / c.g;
         c.col_w = m >= 2048 ? 2 : (m >= 512 ? 4 : (m == 256 ? 8 : 16));

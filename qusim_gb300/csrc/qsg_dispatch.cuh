@@ -14,29 +14,41 @@ static inline cudaError_t prepare_smem(K kernel, size_t smem)
 }
 
 // Row pass: B groups of G rows per CTA so a CTA holds >= 256 threads of line
-// work; RS sequential rounds keep the CTA at <= 512 threads.
+// work; the NT threads of a CTA (256 or 512) go over its NL = B*G lines in
+// RS = NL*(NY/E)/NT rounds (NT >= NY/E: a line is never split across rounds).
 constexpr int row_b_for(int ny, int e, int g)
 {
     return (256 / (g * (ny / e))) > 1 ? 256 / (g * (ny / e)) : 1;
 }
-constexpr int row_rs_for(int ny, int e, int g)
-{
-    return (row_b_for(ny, e, g) * g * (ny / e)) > 512 ? row_b_for(ny, e, g) * g * (ny / e) / 512 : 1;
-}
+constexpr int row_work_for(int ny, int e, int g) { return row_b_for(ny, e, g) * g * (ny / e); }
 constexpr size_t row_smem_for(int csz, int ny, int e, int g)
 {
     return (size_t)csz * row_b_for(ny, e, g) * g * (ny + (ny >> (csz == 8 ? 4 : 3)));
 }
 
-// Instantiated variants.  X(T, NY, E, G) for the row pass,
+// Instantiated variants.  X(T, NY, E, G, NT) for the row pass (NT threads),
 // C(T, M, E, W) for the column pass (W*M/E threads, 128..512).
-#define QSG_ROW_NY(X, T, E, G) X(T, 128, E, G) X(T, 256, E, G) X(T, 512, E, G) X(T, 1024, E, G) X(T, 2048, E, G) X(T, 4096, E, G)
+#define QSG_ROW_SMALL(X, T, E) \
+    X(T, 128, E, 1, 256) X(T, 128, E, 2, 256) X(T, 128, E, 4, 256) \
+    X(T, 256, E, 1, 256) X(T, 256, E, 2, 256) X(T, 256, E, 4, 256) \
+    X(T, 512, E, 1, 256) X(T, 512, E, 2, 256) X(T, 512, E, 4, 256) \
+    X(T, 1024, E, 1, 256) X(T, 1024, E, 2, 256) X(T, 1024, E, 4, 256)
 #define QSG_ROW_VARIANTS_F32A(X) \
-    QSG_ROW_NY(X, float, 16, 1) QSG_ROW_NY(X, float, 16, 2) QSG_ROW_NY(X, float, 16, 4)
+    QSG_ROW_SMALL(X, float, 16) \
+    X(float, 2048, 16, 1, 256) X(float, 2048, 16, 2, 256) X(float, 2048, 16, 4, 256) X(float, 2048, 16, 4, 512) \
+    X(float, 4096, 16, 1, 256) X(float, 4096, 16, 2, 256) X(float, 4096, 16, 2, 512) \
+    X(float, 4096, 16, 4, 256) X(float, 4096, 16, 4, 512)
 #define QSG_ROW_VARIANTS_F32B(X) \
-    QSG_ROW_NY(X, float, 8, 1) QSG_ROW_NY(X, float, 8, 2) QSG_ROW_NY(X, float, 8, 4)
+    X(float, 128, 8, 1, 256) X(float, 128, 8, 2, 256) X(float, 128, 8, 4, 256) \
+    X(float, 256, 8, 1, 256) X(float, 256, 8, 2, 256) X(float, 256, 8, 4, 256) \
+    X(float, 512, 8, 1, 256) X(float, 512, 8, 2, 256) X(float, 512, 8, 4, 256) \
+    X(float, 1024, 8, 1, 256) X(float, 1024, 8, 2, 256) X(float, 1024, 8, 4, 256) X(float, 1024, 8, 4, 512) \
+    X(float, 2048, 8, 1, 256) X(float, 2048, 8, 2, 256) X(float, 2048, 8, 2, 512) X(float, 2048, 8, 4, 512) \
+    X(float, 4096, 8, 1, 512) X(float, 4096, 8, 2, 512) X(float, 4096, 8, 4, 512)
 #define QSG_ROW_VARIANTS_F64(X) \
-    QSG_ROW_NY(X, double, 8, 1) QSG_ROW_NY(X, double, 8, 2) QSG_ROW_NY(X, double, 8, 4)
+    QSG_ROW_SMALL(X, double, 8) \
+    X(double, 2048, 8, 1, 256) X(double, 2048, 8, 2, 512) X(double, 2048, 8, 4, 512) \
+    X(double, 4096, 8, 1, 512) X(double, 4096, 8, 2, 512)
 
 #define QSG_COL_VARIANTS_F32(C) \
     C(float, 128, 16, 16) C(float, 128, 16, 32) \

@@ -42,7 +42,21 @@ template <> struct PhaseOps<float2> {
 };
 
 template <class C> __device__ __forceinline__ C ld_c(const C *p) { return __ldg(p); }
-template <class C> __device__ __forceinline__ C ld_stream(const C *p) { return __ldcs(p); }
+// Streaming loads of psi and of the V tables bypass L1: each element is read
+// once per pass, and letting them allocate evicts the twiddle tables that
+// every butterfly stage re-reads from L1.
+__device__ __forceinline__ float2 ld_stream(const float2 *p)
+{
+    float2 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ double2 ld_stream(const double2 *p)
+{
+    double2 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+    return r;
+}
 template <class C> __device__ __forceinline__ void st_stream(C *p, C v) { __stcs(p, v); }
 
 template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, -a.y); }

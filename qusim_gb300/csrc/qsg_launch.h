@@ -20,6 +20,7 @@ cudaError_t launch_evolve1d(int prec, int n, const Evolve1DArgs &a, cudaStream_t
 struct Plan2D {
     int g;          // x split: Nx = g * m, column transforms of length m
     int row_e;      // elements per thread of the row transforms (radix)
+    int row_nt;     // threads per row-pass CTA (256 or 512)
     int col_e;      // elements per thread of the column transforms
     int col_w;      // adjacent columns per column-pass CTA
 };

@@ -35,7 +35,8 @@ def test_cpp_api_tunnelling_known_answer(exe, precision, tol):
     out = subprocess.run([exe, precision], capture_output=True, text=True, check=True).stdout
     r = json.loads(out.strip().splitlines()[-1])
     ref = (0.1593774409 + 0.1593774408) / 2
-    assert abs(r["norm0"] - 1) < 1e-12
+    # complex64 state: the initial norm carries the float rounding of psi0
+    assert abs(r["norm0"] - 1) < (1e-12 if precision == "fp64" else 1e-7)
     assert abs(r["time"] - 64.0) < 1e-9
     assert abs(r["transmission"] - ref) < tol
     assert abs(r["norm2d"] - 1) < 1e-5
