@@ -64,7 +64,7 @@ void *qsg_ctx_stream(qsg_ctx *ctx);
 /* Device bytes currently held by the context's instances and scratch. */
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
 
-/* Create a 1D instance.  psi0: n complex (re,im); V: n real (the reference keeps
+/* Create a 1D instance (n a power of two, 64 .. 262144).  psi0: n complex (re,im); V: n real (the reference keeps
  * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
@@ -144,6 +144,23 @@ int qsg_set_plan(qsg_inst *inst, const qsg_plan2d *plan);
  * read.  Either out pointer may be null. */
 int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
                  double *best_ms_per_step);
+
+/* A batch of independent 1D instances of (possibly) different sizes, shared
+ * order / precision / mass / hbar, per-instance dx, dt, psi0, V -- advanced
+ * together.  Instances of one size are evolved by launches over all of them
+ * (one CTA per instance for resident sizes, the four-step passes for the
+ * others), each size on a stream of its own.  Each member is a qsg_inst owned
+ * by the batch (qsg_batch_instance), usable with qsg_get_psi, qsg_norm2, ...
+ * New to this engine (the reference evolves one system per Evolver). */
+typedef struct qsg_batch qsg_batch;
+int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double *dx, const double *dt_re,
+                        const double *dt_im, double mass, double hbar, int order, int precision,
+                        const double *const *psi0, const double *const *V, qsg_batch **out);
+int qsg_batch_step(qsg_batch *batch, uint64_t nsteps);
+int qsg_batch_sync(qsg_batch *batch);
+int qsg_batch_size(qsg_batch *batch, int *count, uint64_t *sites);
+int qsg_batch_instance(qsg_batch *batch, int i, qsg_inst **out);
+void qsg_batch_destroy(qsg_batch *batch);
 
 /* Per-kernel timing of this context's launches (CUDA events around every
  * launch on the context stream), for roofline reporting.  Enabling resets the

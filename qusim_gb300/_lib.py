@@ -33,7 +33,8 @@ EXPORTS = [
     "qsg_ctx_bytes_in_use", "qsg_create_1d", "qsg_create_2d", "qsg_step", "qsg_sync",
     "qsg_norm2", "qsg_energies", "qsg_xavg", "qsg_norm2_range", "qsg_get_psi", "qsg_set_psi",
     "qsg_steps_taken", "qsg_destroy", "qsg_candidate_plans", "qsg_get_plan", "qsg_set_plan",
-    "qsg_autotune", "qsg_profile_enable", "qsg_profile_read",
+    "qsg_autotune", "qsg_batch_create_1d", "qsg_batch_step", "qsg_batch_sync", "qsg_batch_size",
+    "qsg_batch_instance", "qsg_batch_destroy", "qsg_profile_enable", "qsg_profile_read",
 ]
 
 
@@ -95,6 +96,15 @@ def _declare(lib):
     lib.qsg_get_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
     lib.qsg_set_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
     lib.qsg_autotune.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan2D), _dp]
+    _pp = ctypes.POINTER(_dp)
+    lib.qsg_batch_create_1d.argtypes = [_vp, _i, ctypes.POINTER(_u64), _dp, _dp, _dp, _d, _d, _i, _i, _pp, _pp,
+                                        ctypes.POINTER(_vp)]
+    lib.qsg_batch_step.argtypes = [_vp, _u64]
+    lib.qsg_batch_sync.argtypes = [_vp]
+    lib.qsg_batch_size.argtypes = [_vp, ctypes.POINTER(_i), ctypes.POINTER(_u64)]
+    lib.qsg_batch_instance.argtypes = [_vp, _i, ctypes.POINTER(_vp)]
+    lib.qsg_batch_destroy.argtypes = [_vp]
+    lib.qsg_batch_destroy.restype = None
     lib.qsg_profile_enable.argtypes = [_vp, _i]
     lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
 

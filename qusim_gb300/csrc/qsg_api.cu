@@ -18,6 +18,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -116,6 +117,13 @@ struct qsg_inst {
     const void *tw = nullptr, *tw_row = nullptr, *tw_col = nullptr, *tw_nx = nullptr, *tw_kin = nullptr;
     Plan2D plan{};
     Geom2D geom{};
+    // 1D: resident (one CTA holds the instance) or four-step (two passes per substep)
+    bool fourstep = false;
+    qsg::FsGeom fsg{};
+    const void *tw_fs_col = nullptr, *tw_fs_row = nullptr, *tw_n = nullptr;
+    qsg::FsInst *desc = nullptr;   // device descriptor of this instance
+    double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
+    double *parts = nullptr;       // four-step norm partials (col_blocks)
     uint64_t steps = 0;
     std::vector<void *> allocs;
     size_t bytes = 0;
@@ -254,19 +262,20 @@ cudaEvent_t take_event(qsg_ctx *ctx)
 struct ProfScope {
     qsg_ctx *ctx;
     const char *name;
+    cudaStream_t st;
     cudaEvent_t e0 = nullptr;
-    ProfScope(qsg_ctx *c, const char *n) : ctx(c), name(n)
+    ProfScope(qsg_ctx *c, const char *n, cudaStream_t s = nullptr) : ctx(c), name(n), st(s ? s : c->st)
     {
         if (ctx->prof) {
             e0 = take_event(ctx);
-            cudaEventRecord(e0, ctx->st);
+            cudaEventRecord(e0, st);
         }
     }
     ~ProfScope()
     {
         if (e0) {
             cudaEvent_t e1 = take_event(ctx);
-            cudaEventRecord(e1, ctx->st);
+            cudaEventRecord(e1, st);
             ctx->prof_pending.emplace_back(name, e0, e1);
         }
     }
@@ -275,7 +284,7 @@ struct ProfScope {
 void prof_drain(qsg_ctx *ctx)
 {
     if (ctx->prof_pending.empty()) return;
-    cudaStreamSynchronize(ctx->st);
+    cudaDeviceSynchronize();
     for (auto &p : ctx->prof_pending) {
         float ms = 0;
         cudaEventElapsedTime(&ms, std::get<1>(p), std::get<2>(p));
@@ -290,22 +299,84 @@ void prof_drain(qsg_ctx *ctx)
 
 // --- steps -----------------------------------------------------------------
 
+int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out_k, int vsel, bool vtwice,
+           cudaStream_t st)
+{
+    qsg::FsColArgs a{};
+    a.inst = desc;
+    a.tw_col = in->tw_fs_col;
+    a.tw_n = in->tw_n;
+    a.n1 = in->fsg.n1;
+    a.vsel = vsel;
+    a.vtwice = vtwice ? 1 : 0;
+    a.in_k = in_k ? 1 : 0;
+    a.out_k = out_k ? 1 : 0;
+    ProfScope ps(in->ctx, "fs_col_pass", st);
+    QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, a, ninst, st));
+    return QSG_OK;
+}
+
+int fs_row(qsg_inst *in, const qsg::FsInst *desc, int ninst, int ksel, cudaStream_t st)
+{
+    qsg::FsRowArgs a{};
+    a.inst = desc;
+    a.tw_row = in->tw_fs_row;
+    a.ksel = ksel;
+    a.inv_n = (float)(1.0 / (double)in->n);
+    ProfScope ps(in->ctx, "fs_row_pass", st);
+    QSG_CUDA(qsg::launch_fs_row(in->prec, in->fsg, a, ninst, st));
+    return QSG_OK;
+}
+
+// Four-step schedule over ninst instances sharing in's geometry and tables
+// layout (descriptors `desc`): like the 2D schedule with the roles of the
+// passes swapped -- the column pass is the real-space one.
+int step_fs(qsg_inst *in, const qsg::FsInst *desc, int ninst, uint64_t nsteps, cudaStream_t st)
+{
+    int rc;
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        const bool last = s + 1 == nsteps;
+        if (s == 0 && (rc = fs_col(in, desc, ninst, false, true, 0, false, st))) return rc;
+        if (in->order == 2) {
+            if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
+        } else {
+            if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
+            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st))) return rc;
+            if ((rc = fs_row(in, desc, ninst, 1, st))) return rc;
+            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st))) return rc;
+            if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
+        }
+        rc = last ? fs_col(in, desc, ninst, true, false, 0, false, st)
+                  : fs_col(in, desc, ninst, true, true, 0, true, st);
+        if (rc) return rc;
+    }
+    return QSG_OK;
+}
+
 int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
-    qsg::Evolve1DArgs a{};
-    a.psi = in->psi;
-    a.vtab[0] = in->vtab[0];
-    a.vtab[1] = in->vtab[1];
-    a.ktab[0] = in->ktab[0];
-    a.ktab[1] = in->ktab[1];
-    a.tw = in->tw;
-    a.norm_out = nullptr;
-    a.dv = in->dv;
-    a.nsteps = nsteps;
-    a.order = in->order;
-    a.renormalize = renorm;
-    ProfScope ps(in->ctx, "evolve1d_resident");
-    QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, in->ctx->st));
+    qsg_ctx *ctx = in->ctx;
+    if (!in->fourstep) {
+        qsg::Evolve1DBatchArgs a{};
+        a.inst = in->desc;
+        a.tw = in->tw;
+        a.norm_out = nullptr;
+        a.dv = in->d_dv;
+        a.nsteps = nsteps;
+        a.order = in->order;
+        a.renormalize = renorm;
+        a.count = 1;
+        ProfScope ps(ctx, "evolve1d_resident");
+        QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, ctx->st));
+        return QSG_OK;
+    }
+    int rc = step_fs(in, in->desc, 1, nsteps, ctx->st);
+    if (rc) return rc;
+    if (renorm) {
+        ProfScope ps(ctx, "renorm");
+        QSG_CUDA(qsg::launch_finalize(in->parts, in->fsg.col_blocks, 1, ctx->sums, ctx->st));
+        QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
+    }
     return QSG_OK;
 }
 
@@ -421,8 +492,13 @@ int build_tables(qsg_inst *in)
         for (int k = 0; k < ntab; ++k) {
             const cd f = -I * DT * in->dt * tc[k] / in->hbar;
             if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
-            QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
-                                          1.0 / (double)in->n, ctx->st));
+            if (in->fourstep) {
+                QSG_CUDA(qsg::launch_ktable_fs(in->prec, in->ktab[k], in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
+                                               1.0 / (double)in->n, ctx->st));
+            } else {
+                QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
+                                              1.0 / (double)in->n, ctx->st));
+            }
         }
     } else {
         // SplittingMethod2D::InitExpT (src/SplittingMethod2D.cpp:56-79)
@@ -484,6 +560,24 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyHostToDevice, ctx->st));
     if ((rc = upload_psi(in, psi0))) return rc;
     if ((rc = build_tables(in))) return rc;
+    if (in->dim == 1) {
+        // device descriptor (+ dv, + four-step norm partials) for the 1D kernels
+        const int nparts = in->fourstep ? in->fsg.col_blocks : 0;
+        void *blk = nullptr;
+        if ((rc = inst_alloc(in, sizeof(qsg::FsInst) + sizeof(double) * (1 + nparts), &blk))) return rc;
+        in->desc = static_cast<qsg::FsInst *>(blk);
+        in->d_dv = reinterpret_cast<double *>(in->desc + 1);
+        in->parts = nparts ? in->d_dv + 1 : nullptr;
+        qsg::FsInst h{};
+        h.psi = in->psi;
+        h.vtab[0] = in->vtab[0];
+        h.vtab[1] = in->vtab[1];
+        h.ktab[0] = in->ktab[0];
+        h.ktab[1] = in->ktab[1];
+        h.partials = in->parts;
+        QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    }
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     return QSG_OK;
 }
@@ -643,9 +737,22 @@ void *qsg_ctx_stream(qsg_ctx *ctx) { return ctx ? (void *)ctx->st : nullptr; }
 
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx) { return ctx ? ctx->in_use : 0; }
 
+static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
+                            double dt_im, int order, int precision, int boundary, const double *psi0,
+                            const double *V, qsg_inst **out);
+
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
                   double dt_im, int order, int precision, int boundary, const double *psi0,
                   const double *V, qsg_inst **out)
+{
+    if (!ctx) return fail(QSG_ERR_ARG, "qsg_create_1d: null argument");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return create_1d_locked(ctx, n, dx, mass, hbar, dt_re, dt_im, order, precision, boundary, psi0, V, out);
+}
+
+static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
+                            double dt_im, int order, int precision, int boundary, const double *psi0,
+                            const double *V, qsg_inst **out)
 {
     if (!ctx || !out || !psi0 || !V) return fail(QSG_ERR_ARG, "qsg_create_1d: null argument");
     *out = nullptr;
@@ -658,11 +765,11 @@ int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
     if (boundary == QSG_INFINITE_WALL)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall boundary is not built");
     if (boundary != QSG_PERIOD) return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
-    if (!qsg::evolve1d_supported(precision, n))
+    qsg::FsGeom fsg{};
+    const bool resident = qsg::evolve1d_supported(precision, n);
+    if (!resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
-                                             " (supported: powers of two, 64 .. " +
-                                             (precision == 1 ? "8192" : "4096") + ")");
-    std::lock_guard<std::mutex> lk(ctx->mu);
+                                             " (supported: powers of two, 64 .. 262144)");
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();
     in->ctx = ctx;
@@ -677,7 +784,17 @@ int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
     in->order = order;
     in->prec = precision;
     in->boundary = boundary;
-    int rc = get_twiddles(ctx, precision, (int)n, qsg::elems_per_thread(precision), &in->tw);
+    in->fourstep = !resident;
+    in->fsg = fsg;
+    int rc = QSG_OK;
+    if (resident) {
+        rc = get_twiddles(ctx, precision, (int)n, qsg::elems_per_thread(precision), &in->tw);
+    } else {
+        rc = get_twiddles(ctx, precision, fsg.n2, fsg.col_e, &in->tw_fs_col);
+        if (!rc) rc = get_twiddles(ctx, precision, fsg.n1, fsg.row_e, &in->tw_fs_row);
+        if (!rc) rc = get_circle(ctx, precision, (int)n, &in->tw_n);
+        if (!rc) rc = get_twiddles(ctx, precision, (int)fsg.n1, qsg::elems_per_thread(precision), &in->tw);
+    }
     if (!rc) rc = common_create(in, psi0, V);
     if (rc) {
         std::string msg = g_last_error;
@@ -791,7 +908,34 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102)
             const double dk = 2 * kPi / (in->dx * in->n);
             const double DT = dk * dk / (2 * in->mass);
-            QSG_CUDA(qsg::launch_kinetic1d(in->prec, (int)in->n, in->psi, in->tw, DT, ctx->sums, ctx->st));
+            if (!in->fourstep) {
+                QSG_CUDA(qsg::launch_kinetic1d(in->prec, (int)in->n, in->psi, in->tw, DT, ctx->sums, ctx->st));
+            } else {
+                // forward transform of a copy: column pass (natural -> k layout), then row
+                // FFTs with the reductions
+                const size_t bytes = in->n * csize(in->prec);
+                if ((rc = ensure_scratch(ctx, bytes + 2 * sizeof(qsg::FsInst)))) return rc;
+                qsg::FsInst h{};
+                h.psi = ctx->scratch;
+                qsg::FsInst *dd = reinterpret_cast<qsg::FsInst *>(static_cast<char *>(ctx->scratch) + bytes);
+                QSG_CUDA(cudaMemcpyAsync(dd, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
+                QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+                qsg::FsColArgs ca{};
+                ca.inst = dd;
+                ca.tw_col = in->tw_fs_col;
+                ca.tw_n = in->tw_n;
+                ca.n1 = in->fsg.n1;
+                ca.vsel = 0;
+                ca.in_k = 0;
+                ca.out_k = 1;
+                QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, ca, 1, ctx->st));
+                qsg::FsRowArgs ra{};
+                ra.inst = dd;
+                ra.tw_row = in->tw_fs_row;
+                if (2 * in->fsg.row_blocks > 2 * ctx->max_partials) return fail(QSG_ERR_STATE, "partials buffer too small");
+                QSG_CUDA(qsg::launch_fs_row_kinetic(in->prec, in->fsg, ra, DT, ctx->partials, ctx->st));
+                QSG_CUDA(qsg::launch_finalize(ctx->partials, in->fsg.row_blocks, 2, ctx->sums, ctx->st));
+            }
             QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                                      ctx->st));
             QSG_CUDA(cudaStreamSynchronize(ctx->st));
@@ -974,6 +1118,187 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     if (best) *best = qsg_plan2d{best_p.g, best_p.row_e, best_p.row_nt, best_p.col_e, best_p.col_w};
     if (best_ms_per_step) *best_ms_per_step = best_ms;
     return QSG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of 1D instances: grouped by size; each size class is advanced by
+// launches over all its instances (resident: one launch per qsg_batch_step;
+// four-step: one launch per pass), on a stream of its own so classes overlap.
+// ---------------------------------------------------------------------------
+
+}  // extern "C"
+
+struct qsg_batch {
+    qsg_ctx *ctx = nullptr;
+    std::vector<qsg_inst *> insts;
+    struct Class {
+        uint64_t n = 0;
+        std::vector<int> members;
+        qsg::FsInst *d_desc = nullptr;
+        double *d_dv = nullptr;
+        cudaStream_t st = nullptr;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Class> classes;
+    uint64_t sites = 0;
+};
+
+static void batch_free(qsg_batch *b)
+{
+    if (!b) return;
+    if (b->ctx) cudaSetDevice(b->ctx->dev);
+    for (auto &c : b->classes) {
+        if (c.st) cudaStreamSynchronize(c.st);
+        if (c.d_desc) cudaFree(c.d_desc);
+        if (c.done) cudaEventDestroy(c.done);
+        if (c.st) cudaStreamDestroy(c.st);
+    }
+    for (qsg_inst *in : b->insts) free_inst(in);
+    delete b;
+}
+
+extern "C" {
+
+int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double *dx, const double *dt_re,
+                        const double *dt_im, double mass, double hbar, int order, int precision,
+                        const double *const *psi0, const double *const *V, qsg_batch **out)
+{
+    if (!ctx || !out || !n || !dx || !dt_re || !psi0 || !V || count <= 0)
+        return fail(QSG_ERR_ARG, "qsg_batch_create_1d: null argument or empty batch");
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    qsg_batch *b = new qsg_batch();
+    b->ctx = ctx;
+    std::map<uint64_t, int> cls;
+    for (int i = 0; i < count; ++i) {
+        qsg_inst *in = nullptr;
+        int rc = create_1d_locked(ctx, n[i], dx[i], mass, hbar, dt_re[i], dt_im ? dt_im[i] : 0.0, order, precision,
+                                  QSG_PERIOD, psi0[i], V[i], &in);
+        if (rc) {
+            std::string msg = g_last_error;
+            batch_free(b);
+            return fail(rc, "qsg_batch_create_1d: instance " + std::to_string(i) + ": " + msg);
+        }
+        b->insts.push_back(in);
+        b->sites += n[i];
+        auto it = cls.find(n[i]);
+        if (it == cls.end()) {
+            cls[n[i]] = (int)b->classes.size();
+            b->classes.emplace_back();
+            b->classes.back().n = n[i];
+            it = cls.find(n[i]);
+        }
+        b->classes[it->second].members.push_back(i);
+    }
+    for (auto &c : b->classes) {
+        std::vector<qsg::FsInst> h(c.members.size());
+        std::vector<double> dv(c.members.size());
+        for (size_t k = 0; k < c.members.size(); ++k) {
+            qsg_inst *in = b->insts[c.members[k]];
+            h[k].psi = in->psi;
+            h[k].vtab[0] = in->vtab[0];
+            h[k].vtab[1] = in->vtab[1];
+            h[k].ktab[0] = in->ktab[0];
+            h[k].ktab[1] = in->ktab[1];
+            h[k].partials = nullptr;
+            dv[k] = in->dv;
+        }
+        void *p = nullptr;
+        const size_t bytes = sizeof(qsg::FsInst) * h.size() + sizeof(double) * dv.size();
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) {
+            c.d_desc = static_cast<qsg::FsInst *>(p);
+            c.d_dv = reinterpret_cast<double *>(c.d_desc + h.size());
+            e = cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice);
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(c.d_dv, dv.data(), sizeof(double) * dv.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            batch_free(b);
+            return fail(QSG_ERR_CUDA, std::string("qsg_batch_create_1d: ") + cudaGetErrorString(e));
+        }
+    }
+    *out = b;
+    return QSG_OK;
+}
+
+int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
+{
+    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_step: null batch");
+    if (nsteps == 0) return QSG_OK;
+    qsg_ctx *ctx = b->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    // classes start after everything already queued on the context stream
+    cudaEvent_t start;
+    QSG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    QSG_CUDA(cudaEventRecord(start, ctx->st));
+    // biggest classes first, so their long launches start earliest
+    std::vector<int> order(b->classes.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+        return b->classes[x].n * b->classes[x].members.size() > b->classes[y].n * b->classes[y].members.size();
+    });
+    int rc = QSG_OK;
+    for (int ci : order) {
+        auto &c = b->classes[ci];
+        qsg_inst *proto = b->insts[c.members[0]];
+        cudaStreamWaitEvent(c.st, start, 0);
+        if (!proto->fourstep) {
+            qsg::Evolve1DBatchArgs a{};
+            a.inst = c.d_desc;
+            a.tw = proto->tw;
+            a.dv = c.d_dv;
+            a.nsteps = nsteps;
+            a.order = proto->order;
+            a.count = (int)c.members.size();
+            ProfScope ps(ctx, "evolve1d_resident", c.st);
+            cudaError_t e = qsg::launch_evolve1d(proto->prec, (int)proto->n, a, c.st);
+            if (e != cudaSuccess) {
+                rc = fail(QSG_ERR_CUDA, std::string("qsg_batch_step: ") + cudaGetErrorString(e));
+                break;
+            }
+        } else if ((rc = step_fs(proto, c.d_desc, (int)c.members.size(), nsteps, c.st))) {
+            break;
+        }
+        cudaEventRecord(c.done, c.st);
+        cudaStreamWaitEvent(ctx->st, c.done, 0);
+    }
+    cudaEventDestroy(start);
+    if (rc) return rc;
+    for (qsg_inst *in : b->insts) in->steps += nsteps;
+    return QSG_OK;
+}
+
+int qsg_batch_size(qsg_batch *b, int *count, uint64_t *sites)
+{
+    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_size: null batch");
+    if (count) *count = (int)b->insts.size();
+    if (sites) *sites = b->sites;
+    return QSG_OK;
+}
+
+int qsg_batch_instance(qsg_batch *b, int i, qsg_inst **out)
+{
+    if (!b || !out || i < 0 || i >= (int)b->insts.size()) return fail(QSG_ERR_ARG, "qsg_batch_instance: bad index");
+    *out = b->insts[i];
+    return QSG_OK;
+}
+
+int qsg_batch_sync(qsg_batch *b)
+{
+    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_sync: null batch");
+    QSG_CUDA(cudaStreamSynchronize(b->ctx->st));
+    return QSG_OK;
+}
+
+void qsg_batch_destroy(qsg_batch *b)
+{
+    if (!b) return;
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    batch_free(b);
 }
 
 int qsg_profile_enable(qsg_ctx *ctx, int on)

@@ -62,6 +62,19 @@ __global__ void k_ktable1d(C *out, int n, double fre, double fim, double scale)
     }
 }
 
+template <class C>
+__global__ void k_ktable_fs(C *out, int n1, int n2, double fre, double fim, double scale)
+{
+    const long n = (long)n1 * n2;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < n; idx += (long)gridDim.x * blockDim.x) {
+        const long k2 = idx / n1, k1 = idx % n1;
+        const long k = k2 + (long)n2 * k1;
+        const double f = double(k > n / 2 ? n - k : k);
+        const double s = f * f;
+        out[idx] = phase_entry<C>(fre * s, fim * s, scale);
+    }
+}
+
 __global__ void k_ktable2d(double2 *out, int nx, int ny, double are, double aim, double dtx, double dty,
                            double scale)
 {
@@ -148,6 +161,17 @@ cudaError_t launch_ktable1d(int prec, void *out, int n, double fre, double fim, 
         k_ktable1d<float2><<<blocks_for(n), kThreads, 0, st>>>((float2 *)out, n, fre, fim, scale);
     else
         k_ktable1d<double2><<<blocks_for(n), kThreads, 0, st>>>((double2 *)out, n, fre, fim, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ktable_fs(int prec, void *out, int n1, int n2, double fre, double fim, double scale,
+                             cudaStream_t st)
+{
+    const size_t n = (size_t)n1 * n2;
+    if (prec == 1)
+        k_ktable_fs<float2><<<blocks_for(n), kThreads, 0, st>>>((float2 *)out, n1, n2, fre, fim, scale);
+    else
+        k_ktable_fs<double2><<<blocks_for(n), kThreads, 0, st>>>((double2 *)out, n1, n2, fre, fim, scale);
     return cudaGetLastError();
 }
 

@@ -14,6 +14,10 @@ cudaError_t launch_vtable(int prec, void *out, const double *V, size_t n, double
 // i < n; fold(i) = i > n/2 ? n - i : i (src/DeviceTemplate.h:544-547, 754-769).
 cudaError_t launch_ktable1d(int prec, void *out, int n, double fre, double fim, double scale,
                             cudaStream_t st);
+// four-step kinetic table in row layout: entry k2*n1 + k1 holds the factor of
+// frequency k = k2 + n2*k1 (same forms as launch_ktable1d)
+cudaError_t launch_ktable_fs(int prec, void *out, int n1, int n2, double fre, double fim, double scale,
+                             cudaStream_t st);
 // fp64 2D kinetic table: scale * exp(alpha (fold(i)^2 DTx + fold(j)^2 DTy)), index j + i*ny
 // (MulExpK2D on ones, src/SplittingMethod2D.cpp:56-79, src/DeviceTemplate.h:794-819).
 cudaError_t launch_ktable2d(void *out, int nx, int ny, double are, double aim, double dtx,

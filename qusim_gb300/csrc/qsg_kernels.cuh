@@ -106,94 +106,14 @@ template <int G, bool INV, class C> __device__ __forceinline__ void dftg(C (&v)[
 // 1D resident evolution
 // ---------------------------------------------------------------------------
 
-struct Evolve1DArgs {
-    void *psi;              // N complex, natural order, in/out
-    const void *vtab[2];    // V phase tables: O2 {1/2}, O4 {C1, C2}
-    const void *ktab[2];    // kinetic tables with 1/N folded in (complex128) or
-                            // factor - 1 (complex64): O2 {1}, O4 {D1, D2}
-    const void *tw;         // stage-major twiddles for (N, E)
-    double *norm_out;       // if set: sum |psi|^2 after the run (before renormalisation)
-    double dv;              // grid volume element for renormalisation
-    uint64_t nsteps;
-    int order;              // 2 or 4
-    int renormalize;        // scale to Norm2 == 1 after the run
-};
+struct FsInst;
+struct Evolve1DBatchArgs;
 
-template <class T, int L, int E>
-__global__ void __launch_bounds__(L / E) k_evolve1d_resident(Evolve1DArgs a)
-{
-    using C = cplx_t<T>;
-    using P = Plan<L, E>;
-    constexpr int TL = P::TL;
-    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    C *sm = reinterpret_cast<C *>(smraw);
-    __shared__ double red[32];
-    const int t = threadIdx.x;
-    C *psi = static_cast<C *>(a.psi);
-    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
-    const C *v0 = static_cast<const C *>(a.vtab[0]);
-    const C *v1 = static_cast<const C *>(a.vtab[1]);
-    const C *k0 = static_cast<const C *>(a.ktab[0]);
-    const C *k1 = static_cast<const C *>(a.ktab[1]);
-    const RowLayout<PADS> lay{0};
-    const CtaBarrier bar{};
-    constexpr T inv_n = T(1) / T(L);
-
-    C x[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = psi[t + e * TL];
-
-    // substep schedule: V(v[0]) T(k[0]) V(v[1]) T(k[1]) ... V(v[nsub])
-    // O2: V1/2 T1 V1/2;  O4: VC1 TD1 VC2 TD2 VC2 TD1 VC1
-    // T(k) = iFFT(k * FFT(x)) = conj(FFT(conj(k * FFT(x)))): each half-substep
-    // is one forward transform followed by a conjugating multiply.
-    const int nsub = a.order == 2 ? 1 : 3;
-#pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], ld_c(v0 + t + e * TL));
-    for (uint64_t s = 0; s < a.nsteps; ++s) {
-#pragma unroll 1
-        for (int h = 0; h < 2 * nsub; ++h) {
-            line_fft<C, L, E, false>(x, sm, lay, bar, t, tw);
-            const int u = h >> 1;
-            if ((h & 1) == 0) {
-                const C *kt = (a.order == 4 && u == 1) ? k1 : k0;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    if constexpr (sizeof(C) == 8) x[e] = cscale(x[e], inv_n);
-                    x[e] = cconj(PhaseOps<C>::apply(x[e], ld_c(kt + t + e * TL)));
-                }
-            } else {
-                // the next V: the step's own closing factor, then (if more
-                // steps follow) the next step's opening factor
-                const bool last = u == nsub - 1;
-                const C *vt = (a.order == 4 && !last) ? v1 : v0;
-                const bool twice = last && s + 1 < a.nsteps;
-#pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const C m = ld_c(vt + t + e * TL);
-                    x[e] = PhaseOps<C>::apply(cconj(x[e]), m);
-                    if (twice) x[e] = PhaseOps<C>::apply(x[e], m);
-                }
-            }
-        }
-    }
-
-    if (a.norm_out || a.renormalize) {
-        double s = 0;
-#pragma unroll
-        for (int e = 0; e < E; ++e) s += abs2d(x[e]);
-        s = block_sum<L / E>(s, red);
-        if (t == 0 && a.norm_out) *a.norm_out = s;
-        if (a.renormalize) {
-            const T sc = T(1.0 / sqrt(s * a.dv));
-#pragma unroll
-            for (int e = 0; e < E; ++e) x[e] = cscale(x[e], sc);
-        }
-    }
-#pragma unroll
-    for (int e = 0; e < E; ++e) psi[t + e * TL] = x[e];
-}
+// NI instances per CTA (instance blockIdx.x*NI + line); all instances of one
+// launch share N and the order.  V tables vtab[0..1], kinetic tables ktab[0..1] (natural layout,
+// 1/N folded in for complex128, factor - 1 for complex64).
+template <class T, int L, int E, int NI>
+__global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatchArgs a);
 
 // ---------------------------------------------------------------------------
 // 2D passes
@@ -516,6 +436,317 @@ __global__ void __launch_bounds__(W *(M / E)) k_col_kinetic(ColPassArgs a, doubl
         const int cta = blockIdx.y * gridDim.x + blockIdx.x;
         partials[2 * cta] = k;
         partials[2 * cta + 1] = nn;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1D four-step passes (N = N1 * N2 too large for one CTA)
+//
+// psi[n], n = n1 + N1*n2, is viewed as an N2 x N1 row-major array (row n2,
+// column n1).  Forward transform: column FFTs (length N2) -> twiddle
+// exp(-2 pi i n1 k2 / N) -> row FFTs (length N1); frequency k = k2 + N2*k1
+// sits at row k2, column k1.  A step is then
+//   column pass (real space): [conj twiddle, column iFFT] -> V -> [column FFT, twiddle]
+//   row pass    (k space):    row FFT -> K(k)/N -> row iFFT
+// so an O2 step costs two HBM round trips, an O4 step six (as in 2D).
+// Instances of one size are batched: blockIdx.y selects the instance.
+// ---------------------------------------------------------------------------
+
+struct FsInst {
+    void *psi;
+    const void *vtab[2];    // V phase tables, natural layout
+    const void *ktab[2];    // kinetic tables in row layout: entry k2*N1 + k1 for k = k2 + N2*k1
+    double *partials;       // per-CTA norm partials of natural-output passes (or null)
+};
+
+struct FsColArgs {
+    const FsInst *inst;
+    const void *tw_col;     // stage twiddles for (N2, E)
+    const void *tw_n;       // circle exp(-2 pi i m / N), m < N
+    int n1;
+    int vsel, vtwice;       // V table index; apply it twice
+    int in_k, out_k;        // input in k layout / output to k layout
+};
+
+template <class T, int N2, int E, int W>
+__global__ void __launch_bounds__(W *(N2 / E)) k_fs_col(FsColArgs a)
+{
+    using C = cplx_t<T>;
+    constexpr int TM = Plan<N2, E>::TL;
+    constexpr int NT = W * TM;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const FsInst in = a.inst[blockIdx.y];
+    const bool in_k = a.in_k != 0, out_k = a.out_k != 0;
+    const int tid = threadIdx.x;
+    const int c = tid % W, t = tid / W;
+    const int col = blockIdx.x * W + c;
+    const int n1 = a.n1;
+    C *psi = static_cast<C *>(in.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_col);
+    const tw_t<C> *twn = static_cast<const tw_t<C> *>(a.tw_n);
+    constexpr ColPad CP = col_pad(sizeof(C), N2, W);
+    const ColLayout<W, CP.sh, CP.p> lay{c};
+    const CtaBarrier bar{};
+    const size_t base = (size_t)t * n1 + col;
+    const size_t stride = (size_t)TM * n1;
+
+    C x[E];
+    {
+        const C *p = psi + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = ld_stream(p + e * stride);
+    }
+    if (in_k) {
+        // iFFT(y * conj(w)) = conj(FFT(conj(y) * w))
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = twmul<false>(cconj(x[e]), __ldg(twn + (size_t)col * (t + e * TM)));
+    }
+    const int npass = (in_k ? 1 : 0) + (out_k ? 1 : 0);
+    const int vpos = in_k ? 1 : 0;
+#pragma unroll 1
+    for (int p = 0; p <= npass; ++p) {
+        if (p == vpos) {
+            if (in_k) {
+#pragma unroll
+                for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+            }
+            const C *vt = static_cast<const C *>(in.vtab[a.vsel]);
+            if (vt) {
+                const C *vr = opaque(vt) + base;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const C m = ld_stream(vr + e * stride);
+                    x[e] = PhaseOps<C>::apply(x[e], m);
+                    if (a.vtwice) x[e] = PhaseOps<C>::apply(x[e], m);
+                }
+            }
+        }
+        if (p < npass) line_fft<C, N2, E, false>(x, sm, lay, bar, t, tw);
+    }
+    double nsum = 0;
+    if (out_k) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = twmul<false>(x[e], __ldg(opaque(twn) + (size_t)col * (t + e * TM)));
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) nsum += abs2d(x[e]);
+    }
+    {
+        C *p = const_cast<C *>(opaque(psi)) + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) st_stream(p + e * stride, x[e]);
+    }
+    if (!out_k && in.partials) {
+        nsum = block_sum<NT>(nsum, red);
+        if (tid == 0) in.partials[blockIdx.x] = nsum;
+    }
+}
+
+struct FsRowArgs {
+    const FsInst *inst;
+    const void *tw_row;     // stage twiddles for (N1, E)
+    int ksel;
+    float inv_n;            // 1/N (complex64 path; complex128 tables carry it)
+};
+
+// B rows of N1 per CTA (B * N1/E threads)
+template <class T, int N1, int E, int B>
+__global__ void __launch_bounds__(B *(N1 / E)) k_fs_row(FsRowArgs a)
+{
+    using C = cplx_t<T>;
+    constexpr int TL = Plan<N1, E>::TL;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    constexpr int LINE = padded<N1, PADS>(N1);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    const FsInst in = a.inst[blockIdx.y];
+    const int tid = threadIdx.x;
+    const int line = tid / TL, t = tid - line * TL;
+    const int row = blockIdx.x * B + line;
+    const RowLayout<PADS> lay{line * LINE};
+    constexpr bool NAMED = (TL % 32 == 0) && (B <= 15) && (B > 1);
+    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
+    LineBar lbar;
+    if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    C *psi = static_cast<C *>(in.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_row);
+    const size_t base = (size_t)row * N1 + t;
+
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = ld_stream(psi + base + e * TL);
+    // FFT -> K -> iFFT, the iFFT as conj(FFT(conj(x)))
+#pragma unroll 1
+    for (int p = 0; p < 2; ++p) {
+        line_fft<C, N1, E, false>(x, sm, lay, lbar, t, tw);
+        if (p == 1) continue;
+        const C *kt = opaque(static_cast<const C *>(in.ktab[a.ksel])) + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            C v = x[e];
+            if constexpr (sizeof(C) == 8) v = cscale(v, a.inv_n);
+            x[e] = cconj(PhaseOps<C>::apply(v, ld_stream(kt + e * TL)));
+        }
+    }
+    C *p = const_cast<C *>(opaque(psi)) + base;
+#pragma unroll
+    for (int e = 0; e < E; ++e) st_stream(p + e * TL, cconj(x[e]));
+}
+
+
+// Four-step kinetic energy: the row FFT of a k-layout array (after a column
+// pass) with partials[2*cta] = sum |X|^2 fold(k)^2 dtk, [2*cta+1] = sum |X|^2.
+template <class T, int N1, int E, int B>
+__global__ void __launch_bounds__(B *(N1 / E)) k_fs_row_kinetic(FsRowArgs a, int n2, double dtk, double *partials)
+{
+    using C = cplx_t<T>;
+    constexpr int TL = Plan<N1, E>::TL;
+    constexpr int NT = B * TL;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    constexpr int LINE = padded<N1, PADS>(N1);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const FsInst in = a.inst[0];
+    const int tid = threadIdx.x;
+    const int line = tid / TL, t = tid - line * TL;
+    const int row = blockIdx.x * B + line;
+    const C *psi = static_cast<const C *>(in.psi);
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = psi[(size_t)row * N1 + t + e * TL];
+    line_fft<C, N1, E, false>(x, sm, RowLayout<PADS>{line * LINE}, CtaBarrier{}, t,
+                              static_cast<const tw_t<C> *>(a.tw_row));
+    const long n = (long)N1 * n2;
+    double k = 0, nn = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const long kk = row + (long)n2 * (t + e * TL);
+        const double f = double(kk > n / 2 ? n - kk : kk);
+        const double a2 = abs2d(x[e]);
+        k += a2 * (f * f) * dtk;
+        nn += a2;
+    }
+    k = block_sum<NT>(k, red);
+    nn = block_sum<NT>(nn, red);
+    if (tid == 0) {
+        partials[2 * blockIdx.x] = k;
+        partials[2 * blockIdx.x + 1] = nn;
+    }
+}
+
+// Batched 1D resident evolution: one CTA per instance (blockIdx.x), all
+// instances of the same N and order.
+struct Evolve1DBatchArgs {
+    const FsInst *inst;     // psi, vtab[0..1], ktab[0..1] (natural layout)
+    const void *tw;
+    double *norm_out;       // per-instance sum |psi|^2 (before renormalisation) or null
+    const double *dv;       // per-instance volume element (renormalisation)
+    uint64_t nsteps;
+    int order, renormalize;
+    int count;              // instances in the launch
+};
+
+template <class T, int L, int E, int NI>
+__global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatchArgs a)
+{
+    using C = cplx_t<T>;
+    using P = Plan<L, E>;
+    constexpr int TL = P::TL;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    const int line = threadIdx.x / TL;
+    const int t = threadIdx.x - line * TL;
+    const int idx = blockIdx.x * NI + line;
+    const bool active = idx < a.count;
+    const FsInst in = a.inst[active ? idx : 0];
+    C *psi = static_cast<C *>(in.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
+    const C *v0 = static_cast<const C *>(in.vtab[0]);
+    const C *v1 = static_cast<const C *>(in.vtab[1]);
+    const C *k0 = static_cast<const C *>(in.ktab[0]);
+    const C *k1 = static_cast<const C *>(in.ktab[1]);
+    const RowLayout<PADS> lay{line * padded<L, PADS>(L)};
+    // instances are independent: lines of whole warps synchronise on their own
+    constexpr bool NAMED = (TL % 32 == 0) && NI > 1 && NI <= 15;
+    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
+    LineBar bar;
+    if constexpr (NAMED) bar = NamedBarrier{1 + line, TL};
+    constexpr T inv_n = T(1) / T(L);
+
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = psi[t + e * TL];
+
+    // substep schedule: V(v[0]) T(k[0]) V(v[1]) T(k[1]) ... V(v[nsub])
+    // O2: V1/2 T1 V1/2;  O4: VC1 TD1 VC2 TD2 VC2 TD1 VC1
+    // T(k) = iFFT(k * FFT(x)) = conj(FFT(conj(k * FFT(x)))): each half-substep
+    // is one forward transform followed by a conjugating multiply.
+    const int nsub = a.order == 2 ? 1 : 3;
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], ld_c(v0 + t + e * TL));
+    for (uint64_t s = 0; s < a.nsteps; ++s) {
+#pragma unroll 1
+        for (int h = 0; h < 2 * nsub; ++h) {
+            line_fft<C, L, E, false>(x, sm, lay, bar, t, tw);
+            const int u = h >> 1;
+            if ((h & 1) == 0) {
+                const C *kt = (a.order == 4 && u == 1) ? k1 : k0;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    if constexpr (sizeof(C) == 8) x[e] = cscale(x[e], inv_n);
+                    x[e] = cconj(PhaseOps<C>::apply(x[e], ld_c(kt + t + e * TL)));
+                }
+            } else {
+                // the next V: the step's own closing factor, then (if more
+                // steps follow) the next step's opening factor
+                const bool last = u == nsub - 1;
+                const C *vt = (a.order == 4 && !last) ? v1 : v0;
+                const bool twice = last && s + 1 < a.nsteps;
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const C m = ld_c(vt + t + e * TL);
+                    x[e] = PhaseOps<C>::apply(cconj(x[e]), m);
+                    if (twice) x[e] = PhaseOps<C>::apply(x[e], m);
+                }
+            }
+        }
+    }
+
+    if (a.norm_out || a.renormalize) {
+        // per-instance sum |psi|^2: shuffles within the line's lanes, then
+        // (lines of whole warps) across the line's warps via shared memory
+        double s = 0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) s += abs2d(x[e]);
+        double tot = 0;
+        if constexpr (TL < 32) {
+#pragma unroll
+            for (int o = TL / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            tot = s;
+        } else {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            __shared__ double wsum[32];
+            __syncthreads();
+            if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = s;
+            __syncthreads();
+            constexpr int WPL = TL / 32;  // warps per line
+            for (int w = 0; w < WPL; ++w) tot += wsum[line * WPL + w];
+        }
+        if (t == 0 && a.norm_out && active) a.norm_out[idx] = tot;
+        if (a.renormalize && active) {
+            const T sc = T(1.0 / sqrt(tot * a.dv[idx]));
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = cscale(x[e], sc);
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) psi[t + e * TL] = x[e];
     }
 }
 

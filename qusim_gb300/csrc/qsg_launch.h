@@ -12,9 +12,23 @@ namespace qsg {
 // per precision (0 fp64, 1 mixed)
 inline int elems_per_thread(int prec) { return prec == 1 ? 16 : 8; }
 
-// 1D resident evolver: supported n (power of two)
+// 1D resident evolver: supported n (power of two); a.count instances
 bool evolve1d_supported(int prec, uint64_t n);
-cudaError_t launch_evolve1d(int prec, int n, const Evolve1DArgs &a, cudaStream_t st);
+cudaError_t launch_evolve1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);
+
+// 1D four-step geometry (n = n1 * n2, 2^13 .. 2^18) and passes over ninst instances
+struct FsGeom {
+    int n, n1, n2;
+    int col_e, col_w, col_threads, col_blocks;
+    size_t col_smem;
+    int row_e, row_b, row_threads, row_blocks;
+    size_t row_smem;
+};
+bool fs_geom(int prec, uint64_t n, FsGeom *g);
+cudaError_t launch_fs_col(int prec, const FsGeom &g, const FsColArgs &a, int ninst, cudaStream_t st);
+cudaError_t launch_fs_row(int prec, const FsGeom &g, const FsRowArgs &a, int ninst, cudaStream_t st);
+cudaError_t launch_fs_row_kinetic(int prec, const FsGeom &g, const FsRowArgs &a, double dtk,
+                                  double *partials, cudaStream_t st);
 
 // A 2D plan: the x split and the kernel variants of the two passes.
 struct Plan2D {

@@ -240,8 +240,68 @@ class Instance:
         return v.value
 
     def close(self):
-        if self.h:
+        # views of batch members (Batch.instance) do not own their handle
+        if self.h and getattr(self, "_owned", True):
             self.ctx.lib.qsg_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """qsg_batch: many independent 1D instances (mixed sizes) advanced together."""
+
+    def __init__(self, ctx: Context, psis, Vs, dxs, dts, order=2, precision="fp64", mass=1.0, hbar=1.0):
+        lib = ctx.lib
+        self.ctx = ctx
+        psis = [np.ascontiguousarray(p, dtype=np.complex128) for p in psis]
+        Vs = [np.ascontiguousarray(v, dtype=np.float64) for v in Vs]
+        cnt = len(psis)
+        if not (len(Vs) == len(dxs) == len(dts) == cnt):
+            raise ValueError("psis, Vs, dxs, dts must have the same length")
+        n = (ctypes.c_uint64 * cnt)(*[p.size for p in psis])
+        dx = (ctypes.c_double * cnt)(*[float(v) for v in dxs])
+        dtr = (ctypes.c_double * cnt)(*[complex(v).real for v in dts])
+        dti = (ctypes.c_double * cnt)(*[complex(v).imag for v in dts])
+        pp = (ctypes.POINTER(ctypes.c_double) * cnt)(*[_dptr(p.view(np.float64)) for p in psis])
+        vp = (ctypes.POINTER(ctypes.c_double) * cnt)(*[_dptr(v) for v in Vs])
+        h = ctypes.c_void_p()
+        check(lib.qsg_batch_create_1d(ctx.h, cnt, n, dx, dtr, dti, mass, hbar, order,
+                                      _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64, pp, vp,
+                                      ctypes.byref(h)))
+        self.h = h
+        self._keep = (psis, Vs)
+        self.count = cnt
+        self.sizes = [p.size for p in psis]
+        self._prec = 1 if precision == "mixed" else 0
+
+    def step(self, nsteps: int):
+        check(self.ctx.lib.qsg_batch_step(self.h, nsteps))
+
+    def sync(self):
+        check(self.ctx.lib.qsg_batch_sync(self.h))
+
+    def sites(self) -> int:
+        c, s = ctypes.c_int(), ctypes.c_uint64()
+        check(self.ctx.lib.qsg_batch_size(self.h, ctypes.byref(c), ctypes.byref(s)))
+        return s.value
+
+    def instance(self, i: int) -> "Instance":
+        """A non-owning view of member i (get_psi, norm2, energies, ...)."""
+        p = ctypes.c_void_p()
+        check(self.ctx.lib.qsg_batch_instance(self.h, i, ctypes.byref(p)))
+        v = Instance.__new__(Instance)
+        v._owned = False
+        v.__init__(self.ctx, p, (self.sizes[i],), 0.0, self._prec)
+        return v
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.qsg_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -386,5 +446,5 @@ class Evolver2D(Evolver):
         return self._ny
 
 
-__all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Evolver1D",
+__all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Batch", "Evolver1D",
            "Evolver2D", "QsgError", "default_context"]

@@ -221,3 +221,54 @@ def test_autotune_keeps_state(qsg, ctx):
     assert inst.plan().as_tuple() == plan.as_tuple()
     assert np.array_equal(inst.get_psi(), before)
     assert inst.steps_taken() == 3
+
+
+@pytest.mark.parametrize("n", [8192, 16384, 32768, 65536, 131072, 262144])
+@pytest.mark.parametrize("order", [2, 4])
+def test_evolve1d_fourstep_vs_oracle(qsg, ctx, oracle, n, order):
+    """Sizes above one CTA run as four-step column / row passes."""
+    psi0, V, dx = gauss_packet_1d(n, -0.05 * n, 0.05 * n, 1.5, -0.01 * n, 0.005 * n, barrier=0.7)
+    nsteps = 4
+    ref = oracle.evolve1d(psi0, V, dx, 0.01, nsteps, order=order)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01, order=order, precision=precision)
+        inst.step(nsteps)
+        assert rel_l2(inst.get_psi(), ref) <= tol, precision
+        if precision == "fp64":
+            kin, pot = inst.energies()
+            assert abs(kin - oracle.kinen1d(ref, dx)) <= 1e-10 * abs(kin)
+            assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-10 * max(1, abs(pot))
+
+
+def test_fourstep_renormalize(qsg, ctx, oracle):
+    n = 65536
+    psi0, V, dx = gauss_packet_1d(n, -0.05 * n, 0.05 * n, 1.0, -100.0, 40.0, barrier=0.5)
+    ref = oracle.evolve1d(psi0 * 1.5, V, dx, 0.01 - 0.002j, 3, order=2, renormalize=True)
+    inst = qsg.Instance.create_1d(ctx, psi0 * 1.5, V, dx, 0.01 - 0.002j, order=2)
+    inst.step(3, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_solo_runs(qsg, ctx, precision):
+    """Each member of a mixed-size batch evolves exactly as it does alone."""
+    rng = np.random.default_rng(7)
+    sizes = [1024, 2048, 1024, 8192, 4096, 16384, 65536, 16384, 512]
+    psis, Vs, dxs, dts = [], [], [], []
+    for n in sizes:
+        box = 0.05 * n
+        p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
+        psis.append(p), Vs.append(v), dxs.append(dx), dts.append(0.01)
+    b = qsg.Batch(ctx, psis, Vs, dxs, dts, order=2, precision=precision)
+    b.step(7)
+    b.step(5)
+    assert b.sites() == sum(sizes)
+    for i, n in enumerate(sizes):
+        solo = qsg.Instance.create_1d(ctx, psis[i], Vs[i], dxs[i], dts[i], order=2, precision=precision)
+        solo.step(7)
+        solo.step(5)
+        got = b.instance(i).get_psi()
+        assert np.array_equal(got, solo.get_psi()), (i, n)
+        assert b.instance(i).steps_taken() == 12
+    b.close()

@@ -78,3 +78,36 @@ def config_2d_4096():
     psi, dx, dy = gauss_packet_2d(4096, 4096, -200, 200, -200, 200, 2.0, 0.0, -60.0, 0.0, 10.0)
     V, _, _ = double_slit_2d()
     return dict(psi=psi, V=V, dx=dx, dy=dy, dt=0.01, steps=2000, order=4)
+
+
+def gaussian_bumps_1d(xs, nbumps, rng, lo, hi, hmin=-1.0, hmax=1.0, wmin=1.0, wmax=5.0):
+    """Sum of nbumps Gaussian bumps h exp(-(x-c)^2/(2w^2)), c ~ U[lo, hi]."""
+    c = rng.uniform(lo, hi, size=nbumps)
+    h = rng.uniform(hmin, hmax, size=nbumps)
+    w = rng.uniform(wmin, wmax, size=nbumps)
+    V = np.zeros_like(xs)
+    for i in range(nbumps):
+        V += h[i] * np.exp(-((xs - c[i]) ** 2) / (2 * w[i] ** 2))
+    return V
+
+
+def batch_1d(count=2048, emin=10, emax=17, seed=0):
+    """The batched 1D configuration: N = 2^e, e ~ U{emin..emax}; box [-0.05N, 0.05N)
+    (dx = 0.1); packet k0 ~ U[0.5,3], s ~ U[2,20] at -0.25 of the box; 8 bumps
+    (heights U[-1,1], widths U[1,5]) with centres inside the box; dt = 0.01, O2."""
+    rng = np.random.default_rng(seed)
+    es = rng.integers(emin, emax + 1, size=count)
+    psis, Vs, dxs = [], [], []
+    for e in es:
+        n = 1 << int(e)
+        half = 0.05 * n
+        xs, dx = grid(n, -half, half)
+        k0 = rng.uniform(0.5, 3.0)
+        s = rng.uniform(2.0, 20.0)
+        xc = -0.25 * 2 * half * 0.5
+        psi = np.exp(1j * k0 * xs) * np.exp(-((xs - xc) ** 2) / (4 * s * s))
+        psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * dx)
+        psis.append(psi.astype(np.complex128))
+        Vs.append(gaussian_bumps_1d(xs, 8, rng, -half, half))
+        dxs.append(dx)
+    return psis, Vs, dxs
