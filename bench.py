@@ -49,6 +49,9 @@ WORKLOADS = {
                    full_steps=2000),
     "batch1d": dict(desc="batched 1D: 2048 instances, N=2^e e~U{10..17} (seed 0), 8 bumps, O2, dt=0.01",
                     dim=0, count=2048, dt=0.01, order=2, full_steps=500),
+    "serving": dict(desc="serving: seeded Poisson arrivals; 70% 1D N log-uniform 2^10..2^18, 30% 2D side "
+                         "log-uniform 256..2048 (both rounded to powers of two); steps U{100..5000}; O2/O4 50/50; "
+                         "complex64; 120 GB budget", dim=-1),
 }
 
 
@@ -332,6 +335,105 @@ def run_batch(args, w):
         print(json.dumps(line), flush=True)
 
 
+def serving_inputs(seed=0):
+    """A pool of seeded inputs per power-of-two size (4 variants each): a packet
+    and an 8-bump potential as in the batched configuration."""
+    from tests.workloads import gaussian_bumps_1d, grid
+    rng = np.random.default_rng(seed)
+    pool = {}
+    for e in range(10, 19):
+        n = 1 << e
+        half = 0.05 * n
+        xs, dx = grid(n, -half, half)
+        lst = []
+        for _ in range(4):
+            k0, s0 = rng.uniform(0.5, 3.0), rng.uniform(2.0, 20.0)
+            p = np.exp(1j * k0 * xs) * np.exp(-((xs + 0.25 * half) ** 2) / (4 * s0 * s0))
+            p /= np.sqrt(np.sum(np.abs(p) ** 2) * dx)
+            lst.append((p, gaussian_bumps_1d(xs, 8, rng, -half, half), dx))
+        pool[(1, n)] = lst
+    for e in range(8, 12):
+        side = 1 << e
+        h = 0.05 * side
+        lst = []
+        for v in range(2):
+            p, dx, dy = gauss_packet_2d(side, side, -h, h, -h, h, rng.uniform(0.5, 3), 0.0, -0.25 * h, 0.0,
+                                        rng.uniform(2, 20))
+            V = gaussian_bumps_2d(side, side, -h, h, -h, h, nbumps=8, seed=int(rng.integers(1 << 30)),
+                                  spread=0.8 * h)
+            lst.append((p, V, dx))
+        pool[(2, side)] = lst
+    return pool
+
+
+def run_serving(args, w):
+    """Requests arrive at Poisson times; the server admits them against its HBM
+    budget and batches them continuously.  Reports latency percentiles and the
+    aggregate site-steps/s from first submit to last completion."""
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    import qusim_gb300 as q
+    pool = serving_inputs(seed=rank)
+    rng = np.random.default_rng(1000 + rank)
+    nreq = int(args.serve_rate * args.serve_seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=nreq))
+    reqs = []
+    for i in range(nreq):
+        if rng.uniform() < 0.7:
+            n = 1 << int(np.clip(np.round(rng.uniform(10, 18)), 10, 18))
+            key = (1, n)
+        else:
+            side = 1 << int(np.clip(np.round(rng.uniform(8, 11)), 8, 11))
+            key = (2, side)
+        reqs.append((key, int(rng.integers(0, len(pool[key]))), int(rng.integers(100, 5001)),
+                     2 if rng.uniform() < 0.5 else 4))
+    srv = q.Server(local, hbm_budget=120 << 30, max_running=256)
+    # warm-up: one small request of each kind, so module loading is not in the latencies
+    for key in [(1, 1024), (1, 65536), (2, 256)]:
+        p, V, dx = pool[key][0]
+        rid = srv.submit(p, V, dx, 0.01, 10, precision="mixed", dy=dx)
+        srv.wait(rid, 120)
+        srv.take(rid)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    ids = []
+    site_steps = 0
+    for i, (key, var, steps, order) in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if arrivals[i] > now:
+            time.sleep(arrivals[i] - now)
+        p, V, dx = pool[key][var]
+        ids.append(srv.submit(p, V, dx, 0.01, steps, order=order, precision="mixed", dy=dx))
+        site_steps += p.size * steps
+    lats = []
+    for rid in ids:
+        srv.wait(rid, 3600)
+        lats.append(srv.take(rid)[1])
+    t_end = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    lats = np.array(lats)
+    if rank == 0:
+        value = site_steps * world / t_end
+        line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+                "steps": nreq, "warmup": 3, "ms_per_step": 1e3 * t_end / max(1, nreq),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+                "data": "synthetic",
+                "config": {"workload": w["desc"], "rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
+                           "requests": nreq, "budget_bytes": 120 << 30, "parallelism": f"replicas x{world}",
+                           "l2": "requests' state far larger than L2"},
+                "latency_s": {"p50": float(np.percentile(lats, 50)), "p90": float(np.percentile(lats, 90)),
+                              "p99": float(np.percentile(lats, 99)), "max": float(lats.max())},
+                "offered_site_steps_per_s": site_steps / max(arrivals[-1], 1e-9),
+                "makespan_s": t_end, "peak_device_bytes": st["peak_device_bytes"],
+                "completed": st["completed"], "failed": st["failed"], "clocks": clk,
+                "note": "a 'step' here is one request; ms_per_step = makespan / requests"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -345,6 +447,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="steps of the mixed-vs-fp64 accuracy run (default: the configuration's own count)")
     ap.add_argument("--no-tune", action="store_true", help="use the default plan instead of autotuning")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: requests per second")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving: length of the arrival stream")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.warmup < 3:
@@ -353,6 +457,8 @@ def main():
         return run_reference(args, w)
     if w["dim"] == 0:
         return run_batch(args, w)
+    if w["dim"] == -1:
+        return run_serving(args, w)
 
     rank, world, local = dist_env()
     import torch

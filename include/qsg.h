@@ -162,6 +162,41 @@ int qsg_batch_size(qsg_batch *batch, int *count, uint64_t *sites);
 int qsg_batch_instance(qsg_batch *batch, int i, qsg_inst **out);
 void qsg_batch_destroy(qsg_batch *batch);
 
+/* Serving: evolution requests submitted as they arrive, run by a scheduler
+ * thread with continuous batching under an HBM budget (new to this engine).
+ * A request is a 1D (ny ignored) or 2D grid with its initial state, potential,
+ * dt, step count and order; psi0 / V are copied at submit.  States: 0 queued,
+ * 1 running, 2 done, 3 failed.  Requests are admitted first-in first-out while
+ * the budget allows; running requests stay resident and advance in chunks, the
+ * resident-size 1D ones of equal size batched into one launch; work of
+ * different requests overlaps on the device.  A request's result does not
+ * depend on what else runs. */
+typedef struct qsg_server qsg_server;
+typedef struct {
+    int32_t dim;        /* 1 or 2 */
+    int32_t order;      /* 2 or 4 */
+    int32_t precision;  /* QSG_FP64 or QSG_MIXED */
+    int32_t reserved;
+    uint64_t nx, ny;
+    double dx, dy, mass, hbar, dt_re, dt_im;
+    uint64_t nsteps;
+    const double *psi0; /* nx*ny complex */
+    const double *V;    /* nx*ny real */
+} qsg_request;
+typedef struct {
+    uint64_t completed, failed, site_steps;
+    size_t peak_device_bytes, budget_bytes;
+} qsg_server_info;
+int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_running, qsg_server **out);
+int qsg_server_submit(qsg_server *server, const qsg_request *req, uint64_t *id);
+int qsg_server_poll(qsg_server *server, uint64_t id, int *state);
+int qsg_server_wait(qsg_server *server, uint64_t id, double timeout_s, int *state);
+/* Copy the result (psi, complex128) and the submit-to-done latency; releases
+ * the request.  A failed request returns its error here. */
+int qsg_server_take(qsg_server *server, uint64_t id, double *psi_out, double *latency_s);
+int qsg_server_stats(qsg_server *server, qsg_server_info *out);
+void qsg_server_destroy(qsg_server *server);
+
 /* Per-kernel timing of this context's launches (CUDA events around every
  * launch on the context stream), for roofline reporting.  Enabling resets the
  * counters.  qsg_profile_read fills up to cap entries of name / launches /

@@ -7,4 +7,4 @@ Evolver/Options API (evolver.py).
 """
 from ._lib import QsgError, load  # noqa: F401
 from .evolver import (Batch, BoundaryCondition, Context, Evolver1D, Evolver2D, Instance,  # noqa: F401
-                      Options, SolverMethod, default_context)
+                      Options, Server, SolverMethod, default_context)

@@ -34,8 +34,25 @@ EXPORTS = [
     "qsg_norm2", "qsg_energies", "qsg_xavg", "qsg_norm2_range", "qsg_get_psi", "qsg_set_psi",
     "qsg_steps_taken", "qsg_destroy", "qsg_candidate_plans", "qsg_get_plan", "qsg_set_plan",
     "qsg_autotune", "qsg_batch_create_1d", "qsg_batch_step", "qsg_batch_sync", "qsg_batch_size",
-    "qsg_batch_instance", "qsg_batch_destroy", "qsg_profile_enable", "qsg_profile_read",
+    "qsg_batch_instance", "qsg_batch_destroy", "qsg_server_create", "qsg_server_submit",
+    "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_destroy",
+    "qsg_profile_enable", "qsg_profile_read",
 ]
+
+
+class Request(ctypes.Structure):
+    """qsg_request."""
+    _fields_ = [("dim", ctypes.c_int32), ("order", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("nx", ctypes.c_uint64), ("ny", ctypes.c_uint64),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("mass", ctypes.c_double),
+                ("hbar", ctypes.c_double), ("dt_re", ctypes.c_double), ("dt_im", ctypes.c_double),
+                ("nsteps", ctypes.c_uint64), ("psi0", ctypes.POINTER(ctypes.c_double)),
+                ("V", ctypes.POINTER(ctypes.c_double))]
+
+
+class ServerInfo(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("site_steps", ctypes.c_uint64),
+                ("peak_device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t)]
 
 
 class Plan2D(ctypes.Structure):
@@ -105,6 +122,14 @@ def _declare(lib):
     lib.qsg_batch_instance.argtypes = [_vp, _i, ctypes.POINTER(_vp)]
     lib.qsg_batch_destroy.argtypes = [_vp]
     lib.qsg_batch_destroy.restype = None
+    lib.qsg_server_create.argtypes = [_i, _sz, _i, ctypes.POINTER(_vp)]
+    lib.qsg_server_submit.argtypes = [_vp, ctypes.POINTER(Request), ctypes.POINTER(_u64)]
+    lib.qsg_server_poll.argtypes = [_vp, _u64, ctypes.POINTER(_i)]
+    lib.qsg_server_wait.argtypes = [_vp, _u64, _d, ctypes.POINTER(_i)]
+    lib.qsg_server_take.argtypes = [_vp, _u64, _dp, _dp]
+    lib.qsg_server_stats.argtypes = [_vp, ctypes.POINTER(ServerInfo)]
+    lib.qsg_server_destroy.argtypes = [_vp]
+    lib.qsg_server_destroy.restype = None
     lib.qsg_profile_enable.argtypes = [_vp, _i]
     lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
 

@@ -117,6 +117,7 @@ struct qsg_inst {
     const void *tw = nullptr, *tw_row = nullptr, *tw_col = nullptr, *tw_nx = nullptr, *tw_kin = nullptr;
     Plan2D plan{};
     Geom2D geom{};
+    cudaStream_t st = nullptr;     // launch stream of the stepping kernels (the context's unless set)
     // 1D: resident (one CTA holds the instance) or four-step (two passes per substep)
     bool fourstep = false;
     qsg::FsGeom fsg{};
@@ -141,8 +142,9 @@ int dev_alloc(qsg_ctx *ctx, size_t bytes, void **p, size_t *acct, bool budgeted 
     if (budgeted && ctx->budget && ctx->in_use + bytes > ctx->budget)
         return fail(QSG_ERR_BUDGET, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
                                         std::to_string(ctx->budget - ctx->in_use) + " left");
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    // stream-ordered: a free does not stall other streams (cudaFree synchronises the device)
+    cudaError_t e = cudaMallocAsync(p, bytes, ctx->st);
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
     if (budgeted) ctx->in_use += bytes;
     if (acct) *acct += bytes;
     return QSG_OK;
@@ -159,8 +161,7 @@ int ensure_scratch(qsg_ctx *ctx, size_t bytes)
 {
     if (ctx->scratch_bytes >= bytes) return QSG_OK;
     if (ctx->scratch) {
-        cudaStreamSynchronize(ctx->st);
-        cudaFree(ctx->scratch);
+        cudaFreeAsync(ctx->scratch, ctx->st);
         ctx->in_use -= ctx->scratch_bytes;
         ctx->scratch = nullptr;
         ctx->scratch_bytes = 0;
@@ -215,7 +216,8 @@ int get_twiddles(qsg_ctx *ctx, int prec, int L, int E, const void **out)
     void *d = nullptr;
     int rc = dev_alloc(ctx, host.size(), &d, nullptr);
     if (rc) return rc;
-    QSG_CUDA(cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice));
+    QSG_CUDA(cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
     ctx->tw_cache[key] = d;
     *out = d;
     return QSG_OK;
@@ -239,7 +241,8 @@ int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
     void *d = nullptr;
     int rc = dev_alloc(ctx, host.size(), &d, nullptr);
     if (rc) return rc;
-    QSG_CUDA(cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice));
+    QSG_CUDA(cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
     ctx->circle_cache[key] = d;
     *out = d;
     return QSG_OK;
@@ -366,11 +369,11 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         a.order = in->order;
         a.renormalize = renorm;
         a.count = 1;
-        ProfScope ps(ctx, "evolve1d_resident");
-        QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, ctx->st));
+        ProfScope ps(ctx, "evolve1d_resident", in->st);
+        QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, in->st));
         return QSG_OK;
     }
-    int rc = step_fs(in, in->desc, 1, nsteps, ctx->st);
+    int rc = step_fs(in, in->desc, 1, nsteps, in->st);
     if (rc) return rc;
     if (renorm) {
         ProfScope ps(ctx, "renorm");
@@ -395,8 +398,8 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     a.m = in->geom.m;
     a.in_split = is ? 1 : 0;
     a.out_split = os ? 1 : 0;
-    ProfScope ps(in->ctx, "row_pass");
-    QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, a, in->ctx->st));
+    ProfScope ps(in->ctx, "row_pass", in->st);
+    QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;
 }
 
@@ -412,8 +415,8 @@ int col_pass(qsg_inst *in, int d)
     a.ny = in->ny;
     a.g = in->geom.g;
     a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
-    ProfScope ps(in->ctx, "col_pass");
-    QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->ctx->st));
+    ProfScope ps(in->ctx, "col_pass", in->st);
+    QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;
 }
 
@@ -542,8 +545,9 @@ void free_inst(qsg_inst *in)
 {
     if (!in) return;
     if (in->ctx) {
-        cudaStreamSynchronize(in->ctx->st);
-        for (void *p : in->allocs) cudaFree(p);
+        // ordered after everything queued on the context stream (work on other
+        // streams is joined into it before an instance is released)
+        for (void *p : in->allocs) cudaFreeAsync(p, in->ctx->st);
         in->ctx->in_use -= in->bytes;
     }
     delete in;
@@ -690,6 +694,14 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
         delete ctx;
         return fail(QSG_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
     }
+    {
+        // keep freed blocks in the device pool for reuse instead of returning them
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device_ordinal) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    }
     ctx->max_partials = 65536;
     void *p = nullptr;
     int rc = dev_alloc(ctx, sizeof(double) * 2 * ctx->max_partials, &p, nullptr, false);
@@ -718,11 +730,12 @@ void qsg_ctx_destroy(qsg_ctx *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->dev);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (auto &kv : ctx->tw_cache) cudaFree(kv.second);
-    for (auto &kv : ctx->circle_cache) cudaFree(kv.second);
-    if (ctx->scratch) cudaFree(ctx->scratch);
-    if (ctx->partials) cudaFree(ctx->partials);
-    if (ctx->sums) cudaFree(ctx->sums);
+    for (auto &kv : ctx->tw_cache) cudaFreeAsync(kv.second, ctx->st);
+    for (auto &kv : ctx->circle_cache) cudaFreeAsync(kv.second, ctx->st);
+    if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->st);
+    if (ctx->partials) cudaFreeAsync(ctx->partials, ctx->st);
+    if (ctx->sums) cudaFreeAsync(ctx->sums, ctx->st);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
     if (ctx->host_sums) cudaFreeHost(ctx->host_sums);
     for (auto &p : ctx->prof_pending) {
         cudaEventDestroy(std::get<1>(p));
@@ -784,6 +797,7 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     in->order = order;
     in->prec = precision;
     in->boundary = boundary;
+    in->st = ctx->st;
     in->fourstep = !resident;
     in->fsg = fsg;
     int rc = QSG_OK;
@@ -838,6 +852,7 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     in->dt = cd(dt_re, dt_im);
     in->order = order;
     in->prec = precision;
+    in->st = ctx->st;
     load_plans(ctx);
     auto it = ctx->plans.find(std::make_tuple(precision, (int)nx, (int)ny));
     if (it != ctx->plans.end()) plan = it->second;
@@ -1149,7 +1164,7 @@ static void batch_free(qsg_batch *b)
     if (b->ctx) cudaSetDevice(b->ctx->dev);
     for (auto &c : b->classes) {
         if (c.st) cudaStreamSynchronize(c.st);
-        if (c.d_desc) cudaFree(c.d_desc);
+        if (c.d_desc) cudaFreeAsync(c.d_desc, b->ctx->st);
         if (c.done) cudaEventDestroy(c.done);
         if (c.st) cudaStreamDestroy(c.st);
     }
@@ -1206,7 +1221,8 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
         }
         void *p = nullptr;
         const size_t bytes = sizeof(qsg::FsInst) * h.size() + sizeof(double) * dv.size();
-        cudaError_t e = cudaMalloc(&p, bytes);
+        cudaError_t e = cudaMallocAsync(&p, bytes, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
         if (e == cudaSuccess) {
             c.d_desc = static_cast<qsg::FsInst *>(p);
             c.d_dv = reinterpret_cast<double *>(c.d_desc + h.size());
@@ -1299,6 +1315,418 @@ void qsg_batch_destroy(qsg_batch *b)
     if (!b) return;
     std::lock_guard<std::mutex> lk(b->ctx->mu);
     batch_free(b);
+}
+
+// ---------------------------------------------------------------------------
+// Serving: a scheduler thread with continuous batching.
+//
+//   submit -> queued (host copies of psi0 / V)
+//   admission (FIFO, while the server context's HBM budget allows): the
+//     instance is created on the device and stays resident until done
+//   each scheduler round, every running request whose previous chunk has
+//     finished gets its next chunk:
+//       resident 1D: requests of one (n, order, precision) advance together by
+//                    the same step count in one batched launch
+//       four-step 1D and 2D: a chunk of steps (about 1e8 site-steps) on the
+//                    request's stream
+//     launches go to a pool of streams, so work of different requests
+//     overlaps on the device
+//   done: psi copied back, device memory released, latency recorded
+//
+// Splitting a request's steps into chunks does not change its result: a
+// chunk boundary performs the same multiplies as the fused step boundary
+// inside a chunk, and every kernel is deterministic -- a request's result is
+// the same alone or in any mix.
+// ---------------------------------------------------------------------------
+
+}  // extern "C"
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+struct SrvRequest {
+    uint64_t id = 0;
+    qsg_request req{};
+    std::vector<double> psi0, V, result;
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+    int error = 0;
+    std::string message;
+    clk::time_point submit, finish;
+    qsg_inst *inst = nullptr;
+    uint64_t dispatched = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool in_flight = false;
+};
+
+}  // namespace
+
+struct qsg_server {
+    qsg_ctx *ctx = nullptr;
+    int max_running = 64;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<std::shared_ptr<SrvRequest>> incoming;
+    std::unordered_map<uint64_t, std::shared_ptr<SrvRequest>> all;
+    uint64_t next_id = 1;
+    bool stop = false;
+    std::thread th;
+    std::vector<cudaStream_t> streams;
+    // device descriptor ring for batched resident launches
+    qsg::FsInst *ring = nullptr, *ring_host = nullptr;  // device ring + pinned staging
+    int ring_size = 4096, ring_pos = 0;
+    // statistics
+    uint64_t done_site_steps = 0, completed = 0, failed = 0;
+    size_t peak_bytes = 0;
+};
+
+namespace {
+
+size_t request_bytes(const qsg_request &r)
+{
+    const size_t n = (size_t)r.nx * (r.dim == 2 ? r.ny : 1);
+    const size_t cs = r.precision == QSG_MIXED ? 8 : 16;
+    const int ntab = r.order == 2 ? 1 : 2;
+    return n * (cs + 8 + ntab * cs * 2) + n * 16;  // psi, V, V and K tables, import staging
+}
+
+int srv_create(qsg_server *S, SrvRequest &q)
+{
+    const qsg_request &r = q.req;
+    qsg_ctx *ctx = S->ctx;
+    if (r.dim == 1)
+        return create_1d_locked(ctx, r.nx, r.dx, r.mass, r.hbar, r.dt_re, r.dt_im, r.order, r.precision, QSG_PERIOD,
+                                q.psi0.data(), q.V.data(), &q.inst);
+    ctx->mu.unlock();  // qsg_create_2d takes the context lock itself
+    int rc = qsg_create_2d(ctx, r.nx, r.ny, r.dx, r.dy, r.mass, r.hbar, r.dt_re, r.dt_im, r.order, r.precision,
+                           q.psi0.data(), q.V.data(), &q.inst);
+    ctx->mu.lock();
+    return rc;
+}
+
+void srv_finish(qsg_server *S, SrvRequest &q, int err, const std::string &msg)
+{
+    if (q.inst) {
+        if (!err) {
+            q.result.resize(2 * (size_t)q.inst->n);
+            q.inst->st = S->ctx->st;
+            cudaStreamWaitEvent(S->ctx->st, q.ev, 0);
+            S->ctx->mu.unlock();
+            int rc = qsg_get_psi(q.inst, q.result.data());
+            S->ctx->mu.lock();
+            if (rc) {
+                err = rc;
+                q.message = g_last_error;
+            }
+        }
+        free_inst(q.inst);
+        q.inst = nullptr;
+    }
+    if (q.ev) {
+        cudaEventDestroy(q.ev);
+        q.ev = nullptr;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    q.finish = clk::now();
+    q.error = err;
+    if (err && q.message.empty()) q.message = msg;
+    q.state = err ? 3 : 2;
+    q.psi0.clear();
+    q.psi0.shrink_to_fit();
+    q.V.clear();
+    q.V.shrink_to_fit();
+    if (err) {
+        ++S->failed;
+    } else {
+        ++S->completed;
+        S->done_site_steps += q.req.nx * (q.req.dim == 2 ? q.req.ny : 1) * q.req.nsteps;
+    }
+    S->cv.notify_all();
+}
+
+void srv_loop(qsg_server *S)
+{
+    qsg_ctx *ctx = S->ctx;
+    cudaSetDevice(ctx->dev);
+    std::deque<std::shared_ptr<SrvRequest>> pending;
+    std::vector<std::shared_ptr<SrvRequest>> running;
+    uint64_t rr = 0;
+    std::vector<cudaEvent_t> ring_events(S->ring_size, nullptr);
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            if (S->stop) break;
+            if (S->incoming.empty() && pending.empty() && running.empty())
+                S->cv.wait_for(lk, std::chrono::milliseconds(5));
+            while (!S->incoming.empty()) {
+                pending.push_back(S->incoming.front());
+                S->incoming.pop_front();
+            }
+        }
+        std::unique_lock<std::mutex> clk_ctx(ctx->mu);
+        bool progress = false;
+        // admission, FIFO while memory allows
+        while (!pending.empty() && (int)running.size() < S->max_running) {
+            auto q = pending.front();
+            const int rc = srv_create(S, *q);
+            if (rc == QSG_ERR_BUDGET) {
+                if (running.empty()) {  // can never fit
+                    pending.pop_front();
+                    srv_finish(S, *q, rc, "request does not fit the server's HBM budget");
+                    progress = true;
+                    continue;
+                }
+                break;  // wait for running requests to release memory
+            }
+            pending.pop_front();
+            progress = true;
+            if (rc) {
+                srv_finish(S, *q, rc, g_last_error);
+                continue;
+            }
+            q->st = S->streams[rr++ % S->streams.size()];
+            q->inst->st = q->st;
+            cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming);
+            {
+                std::lock_guard<std::mutex> lk(S->mu);
+                q->state = 1;
+            }
+            running.push_back(q);
+        }
+        S->peak_bytes = std::max(S->peak_bytes, ctx->in_use);
+        // completions
+        for (size_t i = 0; i < running.size();) {
+            auto &q = running[i];
+            if (q->in_flight && cudaEventQuery(q->ev) == cudaSuccess) q->in_flight = false;
+            if (!q->in_flight && q->dispatched >= q->req.nsteps) {
+                srv_finish(S, *q, 0, "");
+                running.erase(running.begin() + i);
+                progress = true;
+                continue;
+            }
+            ++i;
+        }
+        // dispatch: batched resident groups
+        std::map<std::tuple<uint64_t, int, int>, std::vector<SrvRequest *>> groups;
+        for (auto &q : running)
+            if (!q->in_flight && q->dispatched < q->req.nsteps && q->req.dim == 1 && !q->inst->fourstep)
+                groups[std::make_tuple(q->req.nx, q->req.order, q->req.precision)].push_back(q.get());
+        for (auto &kv : groups) {
+            auto &g = kv.second;
+            uint64_t chunk = 1024;
+            for (auto *q : g) chunk = std::min(chunk, q->req.nsteps - q->dispatched);
+            const int cnt = (int)g.size();
+            if (cnt > S->ring_size) continue;
+            if (S->ring_pos + cnt > S->ring_size) S->ring_pos = 0;
+            // the slots must not be in use by a launch still running
+            bool busy = false;
+            for (int k = 0; k < cnt; ++k) {
+                cudaEvent_t e = ring_events[S->ring_pos + k];
+                if (e && cudaEventQuery(e) != cudaSuccess) busy = true;
+            }
+            if (busy) continue;
+            qsg::FsInst *h = S->ring_host + S->ring_pos;
+            for (int k = 0; k < cnt; ++k) {
+                qsg_inst *in = g[k]->inst;
+                h[k] = qsg::FsInst{};
+                h[k].psi = in->psi;
+                h[k].vtab[0] = in->vtab[0];
+                h[k].vtab[1] = in->vtab[1];
+                h[k].ktab[0] = in->ktab[0];
+                h[k].ktab[1] = in->ktab[1];
+            }
+            qsg::FsInst *d = S->ring + S->ring_pos;
+            cudaStream_t st = g[0]->st;
+            for (int k = 1; k < cnt; ++k) cudaStreamWaitEvent(st, g[k]->ev, 0);
+            cudaMemcpyAsync(d, h, sizeof(qsg::FsInst) * cnt, cudaMemcpyHostToDevice, st);
+            qsg::Evolve1DBatchArgs a{};
+            a.inst = d;
+            a.tw = g[0]->inst->tw;
+            a.nsteps = chunk;
+            a.order = g[0]->req.order;
+            a.count = cnt;
+            cudaError_t e = qsg::launch_evolve1d(g[0]->req.precision, (int)g[0]->req.nx, a, st);
+            // ring slots (device and pinned staging) stay busy until this event
+            cudaEvent_t done = g[0]->ev;
+            cudaEventRecord(done, st);
+            for (int k = 0; k < cnt; ++k) {
+                ring_events[S->ring_pos + k] = done;
+                if (e != cudaSuccess) continue;
+                g[k]->dispatched += chunk;
+                g[k]->in_flight = true;
+                if (k) cudaEventRecord(g[k]->ev, st);
+            }
+            S->ring_pos += cnt;
+            progress = true;
+        }
+        // dispatch: stepped requests (four-step 1D, 2D), one chunk each
+        for (auto &q : running) {
+            if (q->in_flight || q->dispatched >= q->req.nsteps) continue;
+            if (q->req.dim == 1 && !q->inst->fourstep) continue;
+            const double sites = (double)q->inst->n;
+            uint64_t chunk = (uint64_t)std::max(1.0, 1e8 / (sites * (q->req.order == 4 ? 3 : 1)));
+            chunk = std::min(chunk, q->req.nsteps - q->dispatched);
+            int rc = q->req.dim == 1 ? step1d(q->inst, chunk, 0) : step2d(q->inst, chunk, 0);
+            if (rc) {
+                q->dispatched = q->req.nsteps;
+                q->in_flight = false;
+                continue;
+            }
+            q->dispatched += chunk;
+            q->inst->steps += chunk;
+            cudaEventRecord(q->ev, q->st);
+            q->in_flight = true;
+            progress = true;
+        }
+        clk_ctx.unlock();
+        if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    // shut down: wait for the device, release everything still held
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaDeviceSynchronize();
+    for (auto &q : running) srv_finish(S, *q, QSG_ERR_STATE, "server stopped");
+    for (auto &q : pending) srv_finish(S, *q, QSG_ERR_STATE, "server stopped");
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_running, qsg_server **out)
+{
+    if (!out) return fail(QSG_ERR_ARG, "qsg_server_create: out is null");
+    *out = nullptr;
+    qsg_ctx *ctx = nullptr;
+    int rc = qsg_init(device_ordinal, hbm_budget_bytes, &ctx);
+    if (rc) return rc;
+    qsg_server *S = new qsg_server();
+    S->ctx = ctx;
+    if (max_running > 0) S->max_running = max_running;
+    for (int i = 0; i < 8; ++i) {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) break;
+        S->streams.push_back(st);
+    }
+    void *p = nullptr, *ph = nullptr;
+    if (S->streams.empty() || cudaMalloc(&p, sizeof(qsg::FsInst) * S->ring_size) != cudaSuccess ||
+        cudaMallocHost(&ph, sizeof(qsg::FsInst) * S->ring_size) != cudaSuccess) {
+        for (auto st : S->streams) cudaStreamDestroy(st);
+        qsg_ctx_destroy(ctx);
+        delete S;
+        return fail(QSG_ERR_CUDA, "qsg_server_create: stream / descriptor allocation failed");
+    }
+    S->ring = static_cast<qsg::FsInst *>(p);
+    S->ring_host = static_cast<qsg::FsInst *>(ph);
+    S->th = std::thread(srv_loop, S);
+    *out = S;
+    return QSG_OK;
+}
+
+int qsg_server_submit(qsg_server *S, const qsg_request *r, uint64_t *id)
+{
+    if (!S || !r || !r->psi0 || !r->V) return fail(QSG_ERR_ARG, "qsg_server_submit: null argument");
+    if ((r->dim != 1 && r->dim != 2) || (r->order != 2 && r->order != 4) || r->nx == 0 ||
+        (r->dim == 2 && r->ny == 0) || r->nsteps == 0)
+        return fail(QSG_ERR_ARG, "qsg_server_submit: bad request (dim, order, sizes or steps)");
+    if (S->ctx->budget && request_bytes(*r) > S->ctx->budget)
+        return fail(QSG_ERR_BUDGET, "qsg_server_submit: request larger than the server's HBM budget");
+    auto q = std::make_shared<SrvRequest>();
+    q->req = *r;
+    const size_t n = (size_t)r->nx * (r->dim == 2 ? r->ny : 1);
+    q->psi0.assign(r->psi0, r->psi0 + 2 * n);
+    q->V.assign(r->V, r->V + n);
+    q->req.psi0 = nullptr;
+    q->req.V = nullptr;
+    q->submit = clk::now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    q->id = S->next_id++;
+    S->all[q->id] = q;
+    S->incoming.push_back(q);
+    if (id) *id = q->id;
+    S->cv.notify_all();
+    return QSG_OK;
+}
+
+int qsg_server_poll(qsg_server *S, uint64_t id, int *state)
+{
+    if (!S || !state) return fail(QSG_ERR_ARG, "qsg_server_poll: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return fail(QSG_ERR_ARG, "qsg_server_poll: unknown request id");
+    *state = it->second->state;
+    return QSG_OK;
+}
+
+int qsg_server_wait(qsg_server *S, uint64_t id, double timeout_s, int *state)
+{
+    if (!S) return fail(QSG_ERR_ARG, "qsg_server_wait: null server");
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return fail(QSG_ERR_ARG, "qsg_server_wait: unknown request id");
+    auto q = it->second;
+    const auto until = clk::now() + std::chrono::duration_cast<clk::duration>(std::chrono::duration<double>(timeout_s));
+    while (q->state < 2) {
+        if (S->cv.wait_until(lk, until) == std::cv_status::timeout && q->state < 2) {
+            if (state) *state = q->state;
+            return fail(QSG_ERR_TIMEOUT, "qsg_server_wait: timed out");
+        }
+    }
+    if (state) *state = q->state;
+    return QSG_OK;
+}
+
+int qsg_server_take(qsg_server *S, uint64_t id, double *psi_out, double *latency_s)
+{
+    if (!S) return fail(QSG_ERR_ARG, "qsg_server_take: null server");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return fail(QSG_ERR_ARG, "qsg_server_take: unknown request id");
+    auto q = it->second;
+    if (q->state < 2) return fail(QSG_ERR_STATE, "qsg_server_take: request not finished");
+    if (latency_s) *latency_s = std::chrono::duration<double>(q->finish - q->submit).count();
+    const int err = q->error;
+    const std::string msg = q->message;
+    if (!err && psi_out) std::memcpy(psi_out, q->result.data(), q->result.size() * sizeof(double));
+    S->all.erase(it);
+    if (err) return fail(err, msg);
+    return QSG_OK;
+}
+
+int qsg_server_stats(qsg_server *S, qsg_server_info *out)
+{
+    if (!S || !out) return fail(QSG_ERR_ARG, "qsg_server_stats: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    out->completed = S->completed;
+    out->failed = S->failed;
+    out->site_steps = S->done_site_steps;
+    out->peak_device_bytes = S->peak_bytes;
+    out->budget_bytes = S->ctx->budget;
+    return QSG_OK;
+}
+
+void qsg_server_destroy(qsg_server *S)
+{
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+        S->cv.notify_all();
+    }
+    if (S->th.joinable()) S->th.join();
+    cudaSetDevice(S->ctx->dev);
+    cudaDeviceSynchronize();
+    for (auto st : S->streams) cudaStreamDestroy(st);
+    cudaFree(S->ring);
+    cudaFreeHost(S->ring_host);
+    qsg_ctx_destroy(S->ctx);
+    delete S;
 }
 
 int qsg_profile_enable(qsg_ctx *ctx, int on)

@@ -686,9 +686,12 @@ __global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatch
     // T(k) = iFFT(k * FFT(x)) = conj(FFT(conj(k * FFT(x)))): each half-substep
     // is one forward transform followed by a conjugating multiply.
     const int nsub = a.order == 2 ? 1 : 3;
+    // one count for the whole launch: instances that share a CTA synchronise
+    // with CTA-wide barriers, so every line must run the same number of steps
+    const uint64_t nsteps = a.nsteps;
 #pragma unroll
     for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], ld_c(v0 + t + e * TL));
-    for (uint64_t s = 0; s < a.nsteps; ++s) {
+    for (uint64_t s = 0; s < nsteps; ++s) {
 #pragma unroll 1
         for (int h = 0; h < 2 * nsub; ++h) {
             line_fft<C, L, E, false>(x, sm, lay, bar, t, tw);
@@ -705,7 +708,7 @@ __global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatch
                 // steps follow) the next step's opening factor
                 const bool last = u == nsub - 1;
                 const C *vt = (a.order == 4 && !last) ? v1 : v0;
-                const bool twice = last && s + 1 < a.nsteps;
+                const bool twice = last && s + 1 < nsteps;
 #pragma unroll
                 for (int e = 0; e < E; ++e) {
                     const C m = ld_c(vt + t + e * TL);

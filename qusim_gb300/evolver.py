@@ -311,6 +311,77 @@ class Batch:
             pass
 
 
+class Server:
+    """qsg_server: evolution requests served with continuous batching."""
+
+    QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, max_running: int = 64):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self.lib.qsg_server_create(device, hbm_budget, max_running, ctypes.byref(h)))
+        self.h = h
+        self._shapes = {}
+
+    def submit(self, psi0, V, dx, dt, nsteps, order=2, precision="mixed", dy=None, mass=1.0, hbar=1.0):
+        psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        if V.shape != psi0.shape or psi0.ndim not in (1, 2):
+            raise ValueError("psi0 and V: same 1D or 2D shape")
+        dt = complex(dt)
+        r = _lib.Request()
+        r.dim = psi0.ndim
+        r.order = order
+        r.precision = _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64
+        r.nx = psi0.shape[0]
+        r.ny = psi0.shape[1] if psi0.ndim == 2 else 1
+        r.dx = dx
+        r.dy = dy if dy is not None else dx
+        r.mass, r.hbar, r.dt_re, r.dt_im = mass, hbar, dt.real, dt.imag
+        r.nsteps = nsteps
+        r.psi0 = _dptr(psi0.view(np.float64))
+        r.V = _dptr(V)
+        i = ctypes.c_uint64()
+        check(self.lib.qsg_server_submit(self.h, ctypes.byref(r), ctypes.byref(i)))
+        self._shapes[i.value] = psi0.shape
+        return i.value
+
+    def poll(self, rid):
+        st = ctypes.c_int()
+        check(self.lib.qsg_server_poll(self.h, rid, ctypes.byref(st)))
+        return st.value
+
+    def wait(self, rid, timeout=600.0):
+        st = ctypes.c_int()
+        check(self.lib.qsg_server_wait(self.h, rid, timeout, ctypes.byref(st)))
+        return st.value
+
+    def take(self, rid):
+        """(psi, latency seconds); raises QsgError for a failed request."""
+        out = np.empty(self._shapes[rid], dtype=np.complex128)
+        lat = ctypes.c_double()
+        rc = self.lib.qsg_server_take(self.h, rid, _dptr(out.view(np.float64)), ctypes.byref(lat))
+        self._shapes.pop(rid, None)
+        check(rc)
+        return out, lat.value
+
+    def stats(self):
+        s = _lib.ServerInfo()
+        check(self.lib.qsg_server_stats(self.h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def close(self):
+        if self.h:
+            self.lib.qsg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _check_device(opts: Options):
     dev = opts.get("device", "CPU_SEQ")
     if dev != "GPU_GB300":
@@ -446,5 +517,5 @@ class Evolver2D(Evolver):
         return self._ny
 
 
-__all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Batch", "Evolver1D",
+__all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Batch", "Server", "Evolver1D",
            "Evolver2D", "QsgError", "default_context"]
