@@ -68,6 +68,9 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
+ * boundary: QSG_PERIOD, or QSG_INFINITE_WALL (psi_0 = psi_n = 0, kinetic step
+ * through the 2n odd extension, src/SplittingMethod1D.cpp:61-81) for
+ * n = 64 .. 4096 (QSG_MIXED) / 2048 (QSG_FP64).
  * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
  * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,

@@ -369,6 +369,11 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         a.order = in->order;
         a.renormalize = renorm;
         a.count = 1;
+        if (in->boundary == QSG_INFINITE_WALL) {
+            ProfScope ps(ctx, "evolve1d_wall", in->st);
+            QSG_CUDA(qsg::launch_wall1d(in->prec, (int)in->n, a, in->st));
+            return QSG_OK;
+        }
         ProfScope ps(ctx, "evolve1d_resident", in->st);
         QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, in->st));
         return QSG_OK;
@@ -487,7 +492,18 @@ int build_tables(qsg_inst *in)
         if ((rc = inst_alloc(in, in->n * cs, &in->vtab[k]))) return rc;
         QSG_CUDA(qsg::launch_vtable(in->prec, in->vtab[k], in->V, in->n, f.real(), f.imag(), ctx->st));
     }
-    if (in->dim == 1) {
+    if (in->dim == 1 && in->boundary == QSG_INFINITE_WALL) {
+        // ExpT wall: K_i = exp(f i^2), f = -i DT dt t / hbar, DT = Dp^2/(2m), Dp = hbar pi/(dx N),
+        // with the final -1/(2N) folded into the complex128 table (SplittingMethod1D.cpp:72-80)
+        const double dp = in->hbar * kPi / (in->dx * in->n);
+        const double DT = dp * dp / (2 * in->mass);
+        for (int k = 0; k < ntab; ++k) {
+            const cd f = -I * DT * in->dt * tc[k] / in->hbar;
+            if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
+            QSG_CUDA(qsg::launch_ktable_wall(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
+                                             -1.0 / (2.0 * (double)in->n), ctx->st));
+        }
+    } else if (in->dim == 1) {
         // ExpT periodic: f = -i DT dt t / hbar, DT = (Dk hbar)^2/(2m), Dk = 2 pi/(dx N)
         // (SplittingMethod1D.cpp:51-53)
         const double dk = 2 * kPi / (in->dx * in->n);
@@ -775,11 +791,14 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     if (!finite_pos(dx) || !finite_pos(mass) || !finite_pos(hbar) || !std::isfinite(dt_re) ||
         !std::isfinite(dt_im))
         return fail(QSG_ERR_ARG, "qsg_create_1d: dx, mass, hbar must be finite and > 0, dt finite");
-    if (boundary == QSG_INFINITE_WALL)
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall boundary is not built");
-    if (boundary != QSG_PERIOD) return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
+    if (boundary != QSG_PERIOD && boundary != QSG_INFINITE_WALL)
+        return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
+    const bool wall = boundary == QSG_INFINITE_WALL;
+    if (wall && !qsg::wall1d_supported(precision, n))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + " (supported: powers of two, 64 .. " +
+                                             (precision == QSG_MIXED ? "4096" : "2048") + ")");
     qsg::FsGeom fsg{};
-    const bool resident = qsg::evolve1d_supported(precision, n);
+    const bool resident = wall || qsg::evolve1d_supported(precision, n);
     if (!resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (supported: powers of two, 64 .. 262144)");
@@ -802,7 +821,8 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     in->fsg = fsg;
     int rc = QSG_OK;
     if (resident) {
-        rc = get_twiddles(ctx, precision, (int)n, qsg::elems_per_thread(precision), &in->tw);
+        // the wall transforms run on the 2n odd extension
+        rc = get_twiddles(ctx, precision, (int)(wall ? 2 * n : n), qsg::elems_per_thread(precision), &in->tw);
     } else {
         rc = get_twiddles(ctx, precision, fsg.n2, fsg.col_e, &in->tw_fs_col);
         if (!rc) rc = get_twiddles(ctx, precision, fsg.n1, fsg.row_e, &in->tw_fs_row);
@@ -923,7 +943,12 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102)
             const double dk = 2 * kPi / (in->dx * in->n);
             const double DT = dk * dk / (2 * in->mass);
-            if (!in->fourstep) {
+            if (in->boundary == QSG_INFINITE_WALL) {
+                // wall branch: Dk = pi/(dx N), DT = (Dk hbar)^2/(2m) (src/SplittingMethod1D.cpp:117-119)
+                const double dkw = kPi / (in->dx * in->n);
+                const double DTw = (dkw * in->hbar) * (dkw * in->hbar) / (2 * in->mass);
+                QSG_CUDA(qsg::launch_kinetic1d_wall(in->prec, (int)in->n, in->psi, in->tw, DTw, ctx->sums, ctx->st));
+            } else if (!in->fourstep) {
                 QSG_CUDA(qsg::launch_kinetic1d(in->prec, (int)in->n, in->psi, in->tw, DT, ctx->sums, ctx->st));
             } else {
                 // forward transform of a copy: column pass (natural -> k layout), then row

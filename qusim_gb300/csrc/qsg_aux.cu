@@ -63,6 +63,15 @@ __global__ void k_ktable1d(C *out, int n, double fre, double fim, double scale)
 }
 
 template <class C>
+__global__ void k_ktable_wall(C *out, int n, double fre, double fim, double scale)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double s = double(i) * double(i);
+        out[i] = phase_entry<C>(fre * s, fim * s, scale);
+    }
+}
+
+template <class C>
 __global__ void k_ktable_fs(C *out, int n1, int n2, double fre, double fim, double scale)
 {
     const long n = (long)n1 * n2;
@@ -161,6 +170,15 @@ cudaError_t launch_ktable1d(int prec, void *out, int n, double fre, double fim, 
         k_ktable1d<float2><<<blocks_for(n), kThreads, 0, st>>>((float2 *)out, n, fre, fim, scale);
     else
         k_ktable1d<double2><<<blocks_for(n), kThreads, 0, st>>>((double2 *)out, n, fre, fim, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ktable_wall(int prec, void *out, int n, double fre, double fim, double scale, cudaStream_t st)
+{
+    if (prec == 1)
+        k_ktable_wall<float2><<<blocks_for(n), kThreads, 0, st>>>((float2 *)out, n, fre, fim, scale);
+    else
+        k_ktable_wall<double2><<<blocks_for(n), kThreads, 0, st>>>((double2 *)out, n, fre, fim, scale);
     return cudaGetLastError();
 }
 

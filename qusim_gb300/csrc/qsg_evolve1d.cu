@@ -68,6 +68,67 @@ cudaError_t launch_kinetic1d(int prec, int n, const void *psi, const void *tw, d
 }
 
 // ---------------------------------------------------------------------------
+// infinite wall: a 2n line per CTA, 2n <= 8192 (complex64) / 4096 (complex128)
+// ---------------------------------------------------------------------------
+
+bool wall1d_supported(int prec, uint64_t n)
+{
+    if (n < 64 || (n & (n - 1))) return false;
+    return prec == 1 ? 2 * n <= 8192 : 2 * n <= 4096;
+}
+
+template <class T, int L2>
+static cudaError_t run_wall(const Evolve1DBatchArgs &a, cudaStream_t st)
+{
+    constexpr int E = sizeof(T) == 4 ? 16 : 8;
+    constexpr int PADS = sizeof(T) == 4 ? 4 : 3;
+    const size_t smem = sizeof(cplx_t<T>) * padded<L2, PADS>(L2);
+    auto k = k_evolve1d_wall<T, L2, E>;
+    cudaError_t e = prepare_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<a.count, L2 / E, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <class T, int L2>
+static cudaError_t run_wallkin(const void *psi, const void *tw, double dtk, double *sums, cudaStream_t st)
+{
+    constexpr int E = sizeof(T) == 4 ? 16 : 8;
+    constexpr int PADS = sizeof(T) == 4 ? 4 : 3;
+    const size_t smem = sizeof(cplx_t<T>) * padded<L2, PADS>(L2);
+    auto k = k_kinetic1d_wall<T, L2, E>;
+    cudaError_t e = prepare_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    k<<<1, L2 / E, smem, st>>>(psi, tw, dtk, sums);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wall1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st)
+{
+#define X(T, L) case L / 2: return run_wall<T, L>(a, st);
+    if (prec == 1) {
+        switch (n) { QSG_1D_CASES(X, float) X(float, 8192) default: break; }
+    } else {
+        switch (n) { QSG_1D_CASES(X, double) default: break; }
+    }
+#undef X
+    return cudaErrorNotSupported;
+}
+
+cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *tw, double dtk, double *sums,
+                                  cudaStream_t st)
+{
+#define X(T, L) case L / 2: return run_wallkin<T, L>(psi, tw, dtk, sums, st);
+    if (prec == 1) {
+        switch (n) { QSG_1D_CASES(X, float) X(float, 8192) default: break; }
+    } else {
+        switch (n) { QSG_1D_CASES(X, double) default: break; }
+    }
+#undef X
+    return cudaErrorNotSupported;
+}
+
+// ---------------------------------------------------------------------------
 // four-step geometry: n = n1 * n2 (8192 .. 262144), n1 (row, contiguous) = n2 or 2*n2
 // ---------------------------------------------------------------------------
 

@@ -76,14 +76,17 @@ template <class C> __device__ __forceinline__ double abs2d(C a)
 // block-wide sum of a double; every thread gets the result
 template <int NT> __device__ __forceinline__ double block_sum(double v, double *red)
 {
+    // a CTA narrower than a warp shuffles only among its own lanes
+    constexpr int O0 = NT < 32 ? NT / 2 : 16;
+    constexpr unsigned MASK = NT < 32 ? (1u << NT) - 1u : 0xffffffffu;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = O0; o > 0; o >>= 1) v += __shfl_xor_sync(MASK, v, o);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
     if (l == 0) red[w] = v;
     __syncthreads();
     double s = 0;
-    if (threadIdx.x < 32) {
+    if (NT >= 32 && threadIdx.x < 32) {
         s = threadIdx.x < (NT + 31) / 32 ? red[threadIdx.x] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -750,6 +753,147 @@ __global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatch
     if (active) {
 #pragma unroll
         for (int e = 0; e < E; ++e) psi[t + e * TL] = x[e];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1D infinite wall (SplittingMethod1D::ExpT, src/SplittingMethod1D.cpp:61-81):
+// psi on [0, N) with psi_0 = psi_N = 0, odd extension to 2N, inverse 2N-point
+// transform, K_i = exp(f i^2) on the first N outputs, odd extension again,
+// inverse transform, first N values times -1/(2N).  One CTA holds the 2N line
+// (slot e of thread t is element t + e*L2/E; slots e < E/2 are psi itself).
+// ---------------------------------------------------------------------------
+
+// odd extension of the first half into the second: x_0 = x_N = 0,
+// x_{2N-k} = -x_k (k = 1 .. N-1)
+template <class C, int L2, int E, class Lay>
+__device__ __forceinline__ void odd_extend(C (&x)[E], C *sm, const Lay &lay, int t)
+{
+    constexpr int TL = L2 / E;
+    __syncthreads();  // the buffer is free
+#pragma unroll
+    for (int e = 0; e < E / 2; ++e) sm[lay(t + e * TL)] = x[e];
+    __syncthreads();
+#pragma unroll
+    for (int e = E / 2; e < E; ++e) {
+        const int idx = t + e * TL;
+        x[e] = idx == L2 / 2 ? cmk<C>(0, 0) : csub(cmk<C>(0, 0), sm[lay(L2 - idx)]);
+    }
+    if (t == 0) x[0] = cmk<C>(0, 0);
+}
+
+template <class T, int L2, int E>
+__global__ void __launch_bounds__(L2 / E) k_evolve1d_wall(Evolve1DBatchArgs a)
+{
+    using C = cplx_t<T>;
+    constexpr int TL = L2 / E;
+    constexpr int H = E / 2;  // slots holding psi
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const int t = threadIdx.x;
+    const FsInst in = a.inst[blockIdx.x];
+    C *psi = static_cast<C *>(in.psi);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
+    const C *v0 = static_cast<const C *>(in.vtab[0]);
+    const C *v1 = static_cast<const C *>(in.vtab[1]);
+    const C *k0 = static_cast<const C *>(in.ktab[0]);
+    const C *k1 = static_cast<const C *>(in.ktab[1]);
+    const RowLayout<PADS> lay{0};
+    const CtaBarrier bar{};
+    constexpr T neg_inv_2n = T(-1) / T(L2);
+
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = e < H ? psi[t + e * TL] : cmk<C>(0, 0);
+
+    const int nsub = a.order == 2 ? 1 : 3;
+    const uint64_t nsteps = a.nsteps;
+#pragma unroll
+    for (int e = 0; e < H; ++e) x[e] = PhaseOps<C>::apply(x[e], ld_c(v0 + t + e * TL));
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        for (int u = 0; u < nsub; ++u) {
+            const C *kt = (a.order == 4 && u == 1) ? k1 : k0;
+            // two inverse transforms of odd extensions, K between them
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                odd_extend<C, L2, E>(x, sm, lay, t);
+#pragma unroll
+                for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+                line_fft<C, L2, E, false>(x, sm, lay, bar, t, tw);
+#pragma unroll
+                for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+                if (h == 0) {
+#pragma unroll
+                    for (int e = 0; e < H; ++e) {
+                        if constexpr (sizeof(C) == 8) x[e] = cscale(x[e], neg_inv_2n);
+                        x[e] = PhaseOps<C>::apply(x[e], ld_c(kt + t + e * TL));
+                    }
+                }
+            }
+            const bool last = u == nsub - 1;
+            const C *vt = (a.order == 4 && !last) ? v1 : v0;
+            const bool twice = last && s + 1 < nsteps;
+#pragma unroll
+            for (int e = 0; e < H; ++e) {
+                const C m = ld_c(vt + t + e * TL);
+                x[e] = PhaseOps<C>::apply(x[e], m);
+                if (twice) x[e] = PhaseOps<C>::apply(x[e], m);
+            }
+        }
+    }
+    if (a.norm_out || a.renormalize) {
+        double sum = 0;
+#pragma unroll
+        for (int e = 0; e < H; ++e) sum += abs2d(x[e]);
+        sum = block_sum<L2 / E>(sum, red);
+        if (t == 0 && a.norm_out) a.norm_out[blockIdx.x] = sum;
+        if (a.renormalize) {
+            const T sc = T(1.0 / sqrt(sum * a.dv[blockIdx.x]));
+#pragma unroll
+            for (int e = 0; e < H; ++e) x[e] = cscale(x[e], sc);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < H; ++e) psi[t + e * TL] = x[e];
+}
+
+// <T> with the wall (SplittingMethod1D::CalKinEn, :110-124): odd extension,
+// inverse 2N transform, sums[0] = sum_{i<N} |X_i|^2 i^2 dtk, sums[1] = sum_{i<N} |X_i|^2
+template <class T, int L2, int E>
+__global__ void __launch_bounds__(L2 / E) k_kinetic1d_wall(const void *psi_, const void *tw_, double dtk, double *sums)
+{
+    using C = cplx_t<T>;
+    constexpr int TL = L2 / E;
+    constexpr int H = E / 2;
+    constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C *sm = reinterpret_cast<C *>(smraw);
+    __shared__ double red[32];
+    const int t = threadIdx.x;
+    const C *psi = static_cast<const C *>(psi_);
+    const RowLayout<PADS> lay{0};
+    C x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = e < H ? psi[t + e * TL] : cmk<C>(0, 0);
+    odd_extend<C, L2, E>(x, sm, lay, t);
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+    line_fft<C, L2, E, false>(x, sm, lay, CtaBarrier{}, t, static_cast<const tw_t<C> *>(tw_));
+    double k = 0, nn = 0;
+#pragma unroll
+    for (int e = 0; e < H; ++e) {
+        const double i = double(t + e * TL);
+        const double a2 = abs2d(x[e]);
+        k += a2 * (i * i);
+        nn += a2;
+    }
+    k = block_sum<L2 / E>(k, red);
+    nn = block_sum<L2 / E>(nn, red);
+    if (t == 0) {
+        sums[0] = k * dtk;
+        sums[1] = nn;
     }
 }
 

@@ -16,6 +16,12 @@ inline int elems_per_thread(int prec) { return prec == 1 ? 16 : 8; }
 bool evolve1d_supported(int prec, uint64_t n);
 cudaError_t launch_evolve1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);
 
+// 1D infinite wall (2n line per CTA)
+bool wall1d_supported(int prec, uint64_t n);
+cudaError_t launch_wall1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);
+cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *tw, double dtk, double *sums,
+                                  cudaStream_t st);
+
 // 1D four-step geometry (n = n1 * n2, 2^13 .. 2^18) and passes over ninst instances
 struct FsGeom {
     int n, n1, n2;

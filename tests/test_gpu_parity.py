@@ -38,15 +38,16 @@ def run_1d(qsg, ctx, g, precision):
     n, x0, x1, order, wall, batch, calls, fnes = g["params"]
     n, order, batch, calls = int(n), int(order), int(batch), int(calls)
     dx = (x1 - x0) / n
+    bc = qsg.BoundaryCondition.InfiniteWall if int(wall) else qsg.BoundaryCondition.Period
     inst = qsg.Instance.create_1d(ctx, g["psi0"], g["V"], dx, complex(g["dt"]), order=order,
-                                  precision=precision)
+                                  precision=precision, boundary=bc)
     for _ in range(calls):
         inst.step(batch, renormalize=bool(fnes))
     return inst, dx
 
 
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
-             "evolve1d_n1024_o4_imag"]
+             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall"]
 GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes"]
 
 
@@ -272,3 +273,63 @@ def test_batch_matches_solo_runs(qsg, ctx, precision):
         assert np.array_equal(got, solo.get_psi()), (i, n)
         assert b.instance(i).steps_taken() == 12
     b.close()
+
+
+
+@pytest.mark.parametrize("n", [64, 256, 1024, 2048, 4096])
+@pytest.mark.parametrize("order", [2, 4])
+def test_wall_vs_oracle(qsg, ctx, oracle, n, order):
+    """InfiniteWall (odd extension to 2n) against the oracle's wall path."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    psi0, V, dx = gauss_packet_1d(n, -0.05 * n, 0.05 * n, 1.5, -0.01 * n, 0.01 * n + 1, barrier=0.7)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02, 25, order=order, wall=True)
+    cases = (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)) if n <= 2048 else (("mixed", MIXED_TOL),)
+    for precision, tol in cases:
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision, boundary=wall)
+        inst.step(25)
+        assert rel_l2(inst.get_psi(), ref) <= tol, precision
+        kin, pot = inst.energies()
+        ktol = 1e-11 if precision == "fp64" else 1e-5
+        assert abs(kin - oracle.kinen1d(ref, dx, wall=True)) <= ktol * abs(kin), precision
+        assert abs(pot - oracle.poten(ref, V, dx)) <= ktol * max(1, abs(pot)), precision
+
+
+def test_wall_imaginary_time_renormalized(qsg, ctx, oracle):
+    n = 512
+    wall = qsg.BoundaryCondition.InfiniteWall
+    psi0, V, dx = gauss_packet_1d(n, -20.0, 20.0, 1.0, -5.0, 3.0, barrier=0.5)
+    ref = oracle.evolve1d(psi0 * 2.0, V, dx, 0.01 - 0.003j, 40, order=4, wall=True, renormalize=True)
+    inst = qsg.Instance.create_1d(ctx, psi0 * 2.0, V, dx, 0.01 - 0.003j, order=4, boundary=wall)
+    inst.step(40, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_wall_box_eigenstate(qsg, ctx, precision):
+    """A sine mode of the box is stationary: psi(t) = psi(0) exp(-i E t / hbar), E = (pi hbar k / L)^2 / 2m."""
+    n, L, k, dt, steps = 1024, 30.0, 3, 0.01, 300
+    dx = L / n
+    i = np.arange(n)
+    psi0 = np.sin(np.pi * k * i / n).astype(np.complex128)
+    psi0 /= np.sqrt(np.sum(np.abs(psi0) ** 2) * dx)
+    E = (np.pi * k / L) ** 2 / 2
+    inst = qsg.Instance.create_1d(ctx, psi0, np.zeros(n), dx, dt, order=2, precision=precision,
+                                  boundary=qsg.BoundaryCondition.InfiniteWall)
+    inst.step(steps)
+    want = psi0 * np.exp(-1j * E * dt * steps)
+    tol = 1e-11 if precision == "fp64" else 5e-5
+    assert rel_l2(inst.get_psi(), want) <= tol
+    kin, _ = inst.energies()
+    assert abs(kin - E) <= tol * E
+
+
+def test_wall_limits_are_reported(qsg, ctx):
+    wall = qsg.BoundaryCondition.InfiniteWall
+    psi0, V, dx = gauss_packet_1d(4096, -50, 50, 1.0, -10, 3.0)
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
+    assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:32], V[:32], dx, 0.02, boundary=wall)
+    assert e.value.code == 5
