@@ -208,6 +208,33 @@ int qsg_profile_enable(qsg_ctx *ctx, int on);
 int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launches,
                      double *total_ms);
 
+/* Norm2 of a wavefunction the caller already holds in device memory, computed
+ * without allocating any device memory.  It has no counterpart in the
+ * reference.
+ *
+ * For callers that cannot allocate: applications whose GPU memory is reserved
+ * at start-up and handed out by another runtime's pool (a library cudaMalloc
+ * fails there, or is not allowed), and real-time loops that may not call
+ * cudaMalloc / cudaFree because those calls can stall the whole device.  It
+ * needs no context and no instance.
+ *
+ * psi: n complex values on a CUDA device (complex128 for QSG_FP64, complex64
+ * for QSG_MIXED), aligned to the element size.  *out = dv * sum |psi_i|^2,
+ * written after the work queued on `stream` (a cudaStream_t; NULL = the
+ * default stream) has finished.
+ *
+ * Its scratch is one fixed 33,024-byte device array inside libqsg.so, which
+ * every GPU that loads the library keeps until the process exits; n above
+ * QSG_NORM2_NOALLOC_MAX_SITES (2^26) is rejected with QSG_ERR_ARG.  It calls
+ * no cudaMalloc, cudaFree or other allocating routine.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture begins.  All calls on a device share
+ * the one array: calls that overlap on the GPU (different streams, or host
+ * threads not ordered with each other) race and can return wrong sums. */
+#define QSG_NORM2_NOALLOC_MAX_SITES 67108864ull
+int qsg_norm2_noalloc(const void *psi, uint64_t n, int precision, double dv, void *stream,
+                      double *out);
+
 #ifdef __cplusplus
 }
 #endif

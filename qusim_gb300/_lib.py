@@ -36,7 +36,7 @@ EXPORTS = [
     "qsg_autotune", "qsg_batch_create_1d", "qsg_batch_step", "qsg_batch_sync", "qsg_batch_size",
     "qsg_batch_instance", "qsg_batch_destroy", "qsg_server_create", "qsg_server_submit",
     "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_destroy",
-    "qsg_profile_enable", "qsg_profile_read",
+    "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc",
 ]
 
 
@@ -132,6 +132,7 @@ def _declare(lib):
     lib.qsg_server_destroy.restype = None
     lib.qsg_profile_enable.argtypes = [_vp, _i]
     lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
+    lib.qsg_norm2_noalloc.argtypes = [_vp, _u64, _i, _d, _vp, _dp]
 
 
 def load(path: str = LIB_PATH):

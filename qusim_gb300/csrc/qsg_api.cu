@@ -1808,3 +1808,5 @@ int PlanRT::tw_size() const
 }
 
 }  // namespace qsg
+
+int qsg::set_last_error(int code, const std::string &msg) { return fail(code, msg); }

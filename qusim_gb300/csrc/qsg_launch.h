@@ -2,6 +2,7 @@
 // the compiled instantiation for the runtime sizes; sizes with no
 // instantiation return cudaErrorNotSupported (surfaced as QSG_ERR_UNSUPPORTED).
 #pragma once
+#include <string>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "qsg_kernels.cuh"
@@ -70,6 +71,9 @@ cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, 
 // 1D forward transform with the kinetic-energy reduction (one CTA)
 cudaError_t launch_kinetic1d(int prec, int n, const void *psi, const void *tw, double dt_k,
                              double *sums, cudaStream_t st);
+
+// record `msg` as the calling thread's qsg_last_error(); returns code
+int set_last_error(int code, const std::string &msg);
 
 // runtime mirror of Plan<L, E>: stage-major twiddle layout
 struct PlanRT {
