@@ -105,6 +105,13 @@ class ClockSampler:
             self.t.start()
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # wait for nvidia-smi's first line, then count only the lines that arrive
+        # after this point (the timed region)
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 5.0:
+            time.sleep(0.01)
+        self.first = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -121,7 +128,7 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in self.lines[getattr(self, "first", 0):]:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -231,7 +238,7 @@ def run_reference(args, w):
         ny = w["ny"]
         per_step_budget = 150.0 / max(1, args.steps + args.warmup)
         rows = w["nx"]
-        while rows > 128 and 9.0 * rows * ny / (4096 * 4096) > per_step_budget:
+        while rows > 32 and 9.0 * rows * ny / (4096 * 4096) > per_step_budget:
             rows //= 2
         dx, dy = 2 * h / w["nx"], 2 * h / ny
         xs = -h + dx * np.arange(rows) + (w["nx"] - rows) // 2 * dx
@@ -437,7 +444,7 @@ def run_serving(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d4096", choices=sorted(WORKLOADS))

@@ -1,5 +1,6 @@
 // qsg_aux.cu -- phase tables, reductions, conversions.
 #include "qsg_aux.h"
+#include <type_traits>
 #include "qsg_kernels.cuh"
 
 namespace qsg {
@@ -112,17 +113,63 @@ __global__ void k_c64_to_c128(double2 *out, const float2 *in, size_t n)
     }
 }
 
-template <class C>
-__global__ void __launch_bounds__(kThreads) k_reduce(const C *psi, const double *V, size_t lo, size_t hi,
-                                                     int mode, double *partials)
+// Sum of |psi|^2 in FP32 with no rounding loss that matters: each square is
+// split exactly into p + e (p = x*x, e = fma(x, x, -p)) and the running sum is
+// a float pair (hi, lo) updated by two-sum (Knuth), so the per-thread result
+// carries about 48 bits before it is handed to the FP64 block sum.  FP64 runs
+// at 1/64 of the FP32 rate on this part: summing float2 values in FP64 made
+// the reduction issue-bound at a fraction of HBM bandwidth.
+struct SumF2 {
+    float hi = 0.f, lo = 0.f;
+    // explicit round-to-nearest intrinsics: the compiler may not contract
+    // or reassociate them, which the two-sum identities rely on
+    __device__ __forceinline__ void add(float v)
+    {
+        const float s = __fadd_rn(hi, v);
+        const float bv = __fsub_rn(s, hi);
+        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(v, bv)));
+        hi = s;
+    }
+    __device__ __forceinline__ void add_sq(float x)
+    {
+        const float p = __fmul_rn(x, x);
+        add(p);
+        lo = __fadd_rn(lo, fmaf(x, x, -p));
+    }
+    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
+template <class C, int MODE>
+__device__ __forceinline__ void reduce_add(double &s, SumF2 &f, C a, const double *V, size_t i, size_t lo)
+{
+    if constexpr (MODE == 0 && std::is_same<C, float2>::value) {
+        f.add_sq(a.x);
+        f.add_sq(a.y);
+    } else {
+        const double a2 = abs2d(a);
+        s += MODE == 0 ? a2 : (MODE == 1 ? a2 * V[i] : a2 * double(i - lo));
+    }
+}
+
+template <class C, int MODE>
+__global__ void __launch_bounds__(kThreads) k_reduce(const C *__restrict__ psi, const double *__restrict__ V,
+                                                     size_t lo, size_t hi, double *partials)
 {
     __shared__ double red[32];
     double s = 0;
-    for (size_t i = lo + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < hi;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const double a2 = abs2d(psi[i]);
-        s += mode == 0 ? a2 : (mode == 1 ? a2 * V[i] : a2 * double(i - lo));
+    SumF2 f;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = lo + blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    // four independent loads in flight per thread
+    for (; i + 3 * stride < hi; i += 4 * stride) {
+        const C a0 = psi[i], a1 = psi[i + stride], a2 = psi[i + 2 * stride], a3 = psi[i + 3 * stride];
+        reduce_add<C, MODE>(s, f, a0, V, i, lo);
+        reduce_add<C, MODE>(s, f, a1, V, i + stride, lo);
+        reduce_add<C, MODE>(s, f, a2, V, i + 2 * stride, lo);
+        reduce_add<C, MODE>(s, f, a3, V, i + 3 * stride, lo);
     }
+    for (; i < hi; i += stride) reduce_add<C, MODE>(s, f, psi[i], V, i, lo);
+    s += f.value();
     s = block_sum<kThreads>(s, red);
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
@@ -216,13 +263,22 @@ cudaError_t launch_c64_to_c128(void *out, const void *in, size_t n, cudaStream_t
 cudaError_t launch_reduce(int prec, const void *psi, const double *V, size_t lo, size_t hi, int mode,
                           double *partials, int max_parts, int *nparts, cudaStream_t st)
 {
-    unsigned b = blocks_for(hi > lo ? hi - lo : 1, kThreads * 8);
+    // at least 16 sites per thread, at most 8 CTAs per SM of a 152-SM part
+    unsigned b = blocks_for(hi > lo ? hi - lo : 1, kThreads * 16);
+    if (b > 1216) b = 1216;
     if ((int)b > max_parts) b = (unsigned)max_parts;
     *nparts = (int)b;
-    if (prec == 1)
-        k_reduce<float2><<<b, kThreads, 0, st>>>((const float2 *)psi, V, lo, hi, mode, partials);
-    else
-        k_reduce<double2><<<b, kThreads, 0, st>>>((const double2 *)psi, V, lo, hi, mode, partials);
+#define QSG_REDUCE(C, M) k_reduce<C, M><<<b, kThreads, 0, st>>>((const C *)psi, V, lo, hi, partials)
+    if (prec == 1) {
+        if (mode == 0) QSG_REDUCE(float2, 0);
+        else if (mode == 1) QSG_REDUCE(float2, 1);
+        else QSG_REDUCE(float2, 2);
+    } else {
+        if (mode == 0) QSG_REDUCE(double2, 0);
+        else if (mode == 1) QSG_REDUCE(double2, 1);
+        else QSG_REDUCE(double2, 2);
+    }
+#undef QSG_REDUCE
     return cudaGetLastError();
 }
 
