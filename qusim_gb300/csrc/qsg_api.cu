@@ -403,6 +403,7 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     a.m = in->geom.m;
     a.in_split = is ? 1 : 0;
     a.out_split = os ? 1 : 0;
+    a.units = in->geom.row_blocks;
     ProfScope ps(in->ctx, "row_pass", in->st);
     QSG_CUDA(qsg::launch_row_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;
@@ -420,6 +421,7 @@ int col_pass(qsg_inst *in, int d)
     a.ny = in->ny;
     a.g = in->geom.g;
     a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
+    a.tiles = (in->ny / in->geom.col_w) * in->geom.g;
     ProfScope ps(in->ctx, "col_pass", in->st);
     QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;

@@ -9,8 +9,7 @@ static cudaError_t run_col_f64(const Geom2D &g, const ColPassArgs &a, cudaStream
     auto k = k_col_pass<T, M, E, W>;
     cudaError_t e = prepare_smem(k, g.col_smem);
     if (e != cudaSuccess) return e;
-    dim3 grid(g.ny / W, g.g);
-    k<<<grid, W * (M / E), g.col_smem, st>>>(a);
+    k<<<(unsigned)a.tiles, W * (M / E), g.col_smem, st>>>(a);  // one tile per CTA
     return cudaGetLastError();
 }
 

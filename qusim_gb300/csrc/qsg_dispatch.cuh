@@ -13,6 +13,34 @@ static inline cudaError_t prepare_smem(K kernel, size_t smem)
     return cudaSuccess;
 }
 
+// Multiprocessors of the current device (cached per device).
+static inline int sm_count()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!cache[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 1;
+    }
+    return cache[dev];
+}
+
+// Grid of a persistent kernel: every resident CTA slot of the device, at most
+// one CTA per work unit.  `occ` caches the occupancy of the instantiation.
+template <class K>
+static inline unsigned persistent_grid(K kernel, int threads, size_t smem, int units, int &occ)
+{
+    if (!occ) {
+        int o = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, threads, smem) != cudaSuccess || o < 1) o = 1;
+        occ = o;
+    }
+    const long slots = (long)occ * sm_count();
+    return (unsigned)(units < slots ? units : slots);
+}
+
 // Row pass: B groups of G rows per CTA so a CTA holds >= 256 threads of line
 // work; the NT threads of a CTA (256 or 512) go over its NL = B*G lines in
 // RS = NL*(NY/E)/NT rounds (NT >= NY/E: a line is never split across rounds).

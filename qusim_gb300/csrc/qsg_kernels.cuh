@@ -58,7 +58,6 @@ __device__ __forceinline__ double2 ld_stream(const double2 *p)
     return r;
 }
 template <class C> __device__ __forceinline__ void st_stream(C *p, C v) { __stcs(p, v); }
-
 template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, -a.y); }
 
 // Every inverse transform here is computed as conj(FFT(conj(x))), which is
@@ -129,9 +128,10 @@ struct RowPassArgs {
     int vtwice;             // apply it twice (the two ExpV calls at a step boundary)
     const void *tw_row;     // stage-major twiddles for (Ny, E)
     const void *tw_nx;      // full circle exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
-    double *partials;       // per-CTA sum |psi|^2 (natural-output passes), or null
+    double *partials;       // per-unit sum |psi|^2 (natural-output passes), or null
     int nx, m;              // Nx and M = Nx / G
     int in_split, out_split;
+    int units;              // row-group units (M / B); CTAs loop over them
 };
 
 // in_split:  input is in split-k space (inverse x-split stage + row iFFT first);
@@ -139,11 +139,15 @@ struct RowPassArgs {
 // out_split: output goes back to split-k space (row FFT + forward x-split
 //            stage); otherwise natural real-space rows (+ norm partials).
 // (Runtime flags: one instantiation serves the three pass kinds of a step.)
-// One CTA handles B row groups; group b has the G rows n1 + j*M, j < G,
-// n1 = blockIdx.x*B + b, i.e. NL = B*G lines of NY.  The NT threads work on
-// NL/RS lines at a time and go over the CTA's lines in RS rounds.
-template <class T, int NY, int E, int G, int B, int RS>
-__global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
+// A unit is B row groups; group b has the G rows n1 + j*M, j < G,
+// n1 = u*B + b, i.e. NL = B*G lines of NY.  The NT threads work on NL/RS lines
+// at a time and go over the unit's lines in RS rounds.  CTAs are persistent
+// (CTA i takes units i, i + gridDim.x, ...).  When the split-k input of a unit
+// fits in 32 registers per thread, it is loaded while the previous unit's
+// forward x-split stage runs, so its HBM latency overlaps that stage.
+// The body, for a compile-time in_split (see k_row_pass).
+template <class T, int NY, int E, int G, int B, int RS, bool IN>
+__device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned char *smraw, double *red)
 {
     using C = cplx_t<T>;
     using P = Plan<NY, E>;
@@ -154,11 +158,10 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     static_assert(NL % RS == 0, "");
     constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
     constexpr int LINE = padded<NY, PADS>(NY);
-    extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C *>(smraw);
-    __shared__ double red[32];
 
-    const bool in_split = a.in_split != 0, out_split = a.out_split != 0;
+    constexpr bool in_split = IN;
+    const bool out_split = a.out_split != 0;
     const int tid = threadIdx.x;
     const int grp = tid / TL;  // line slot within a round
     const int t = tid - grp * TL;
@@ -173,17 +176,59 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
     LineBar lbar;
     if constexpr (NAMED) lbar = NamedBarrier{1 + grp, TL};
-    const bool via_smem_in = in_split && G > 1;
+    constexpr bool via_smem_in = in_split && G > 1;
     const bool via_smem_out = out_split && G > 1;
-
-    if (via_smem_in) {
-        if constexpr (G > 1) {
-            // inverse x-split stage over every column of every group of this CTA
-#pragma unroll 2
-            for (int u = 0; u < B * NY / NT; ++u) {
-                const int gc = tid + u * NT;
+    constexpr int XV = B * NY / NT;                       // x-split columns per thread
+    constexpr bool XPF = via_smem_in && XV * G <= 32;     // split-k input held in registers
+    C pf[XPF ? XV : 1][G];
+    // issue the loads of unit uu's split-k input (consumed by the next x-split
+    // stage).  Every path defines pf (zeros when !live), so the consumed values
+    // are dead during the transforms.
+    auto xs_load = [&](int uu, bool live) {
+        if constexpr (XPF) {
+#pragma unroll
+            for (int v = 0; v < XV; ++v) {
+                const int gc = tid + v * NT;
                 const int bb = gc / NY, c = gc - bb * NY;
-                const int nn1 = blockIdx.x * B + bb;
+                const int nn1 = uu * B + bb;
+#pragma unroll
+                for (int q = 0; q < G; ++q)
+                    pf[v][q] = live ? ld_stream(in + (size_t)(q * a.m + nn1) * NY + c) : cmk<C>(0, 0);
+            }
+        }
+    };
+    if constexpr (XPF) xs_load(blockIdx.x, true);
+
+#pragma unroll 1
+    for (int u = blockIdx.x; u < a.units; u += gridDim.x) {
+    const int unext = u + gridDim.x;
+    if (u != (int)blockIdx.x) cbar();  // the previous unit's readers of sm are done
+
+    if constexpr (XPF) {
+        {
+            // inverse x-split stage from the registers loaded in advance
+#pragma unroll
+            for (int v = 0; v < XV; ++v) {
+                const int gc = tid + v * NT;
+                const int bb = gc / NY, c = gc - bb * NY;
+                const int nn1 = u * B + bb;
+                C y[G];
+#pragma unroll
+                for (int q = 0; q < G; ++q) y[q] = q > 0 ? twmul<true>(pf[v][q], __ldg(twx + nn1 * q)) : pf[v][q];
+                dftg<G, true>(y);
+#pragma unroll
+                for (int q = 0; q < G; ++q) sm[(bb * G + q) * LINE + c + (c >> PADS)] = y[q];
+            }
+        }
+        cbar();
+    } else if constexpr (via_smem_in) {
+        {
+            // inverse x-split stage over every column of every group of this unit
+#pragma unroll 2
+            for (int v = 0; v < B * NY / NT; ++v) {
+                const int gc = tid + v * NT;
+                const int bb = gc / NY, c = gc - bb * NY;
+                const int nn1 = u * B + bb;
                 C y[G];
 #pragma unroll
                 for (int q = 0; q < G; ++q) {
@@ -203,7 +248,7 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     for (int r = 0; r < RS; ++r) {
         const int line = r * LPR + grp;
         const int b = line / G, j = line - b * G;
-        const int row = blockIdx.x * B + b + j * a.m;
+        const int row = u * B + b + j * a.m;
         const RowLayout<PADS> lay{line * LINE};
         C x[E];
         if (via_smem_in) {
@@ -258,14 +303,16 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
         }
     }
 
+    // the next unit's split-k input is in flight while this unit's results go out
+    if (via_smem_out) cbar();
+    if constexpr (XPF) xs_load(unext, unext < a.units);
     if (via_smem_out) {
         if constexpr (G > 1) {
-            cbar();
 #pragma unroll 2
-            for (int u = 0; u < B * NY / NT; ++u) {
-                const int gc = tid + u * NT;
+            for (int v = 0; v < B * NY / NT; ++v) {
+                const int gc = tid + v * NT;
                 const int bb = gc / NY, c = gc - bb * NY;
-                const int nn1 = blockIdx.x * B + bb;
+                const int nn1 = u * B + bb;
                 C y[G];
 #pragma unroll
                 for (int q = 0; q < G; ++q) y[q] = sm[(bb * G + q) * LINE + c + (c >> PADS)];
@@ -280,8 +327,23 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
     }
     if (!out_split && a.partials) {
         nsum = block_sum<NT>(nsum, red);
-        if (tid == 0) a.partials[blockIdx.x] = nsum;
+        if (tid == 0) a.partials[u] = nsum;
     }
+    }  // units
+}
+
+// One kernel serves the three pass kinds of a step (runtime flags); the body
+// is specialised on in_split so that the registers holding the next unit's
+// input exist only where that input is split-k.
+template <class T, int NY, int E, int G, int B, int RS>
+__global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[32];
+    if (a.in_split)
+        row_pass_units<T, NY, E, G, B, RS, true>(a, smraw, red);
+    else
+        row_pass_units<T, NY, E, G, B, RS, false>(a, smraw, red);
 }
 
 struct ColPassArgs {
@@ -292,9 +354,11 @@ struct ColPassArgs {
     const void *tw_col;     // stage-major twiddles for (M, E)
     int nx, ny, g;
     float inv_n;            // 1/(Nx Ny) (complex64 path)
+    int tiles;              // (Ny / W) * G tiles; CTAs loop over them
 };
 
-// One CTA: block q = blockIdx.y, columns [blockIdx.x*W, +W).
+// A tile is block q, columns [xt*W, +W), tile index u = q * (Ny/W) + xt;
+// CTA u handles tile u.
 template <class T, int M, int E, int W>
 __global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
 {
@@ -305,16 +369,19 @@ __global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
     C *sm = reinterpret_cast<C *>(smraw);
     const int tid = threadIdx.x;
     const int c = tid % W, t = tid / W;
-    const int q = blockIdx.y;
-    const int col = blockIdx.x * W + c;
     const int ny = a.ny;
+    const int ntx = ny / W;
     C *psi = static_cast<C *>(a.psi);
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_col);
     constexpr ColPad CP = col_pad(sizeof(C), M, W);
     const ColLayout<W, CP.sh, CP.p> lay{c};
     const CtaBarrier bar{};
-    const size_t base = ((size_t)q * M + t) * ny + col;
     const int stride = TM * ny;  // between a thread's elements
+
+    auto tile = [&](int u) {
+    const int q = u / ntx;
+    const int col = (u - q * ntx) * W + c;
+    const size_t base = ((size_t)q * M + t) * ny + col;
 
     C x[E];
     {
@@ -356,6 +423,9 @@ __global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
 #pragma unroll
         for (int e = 0; e < E; ++e) st_stream(p + (size_t)e * stride, x[e]);
     }
+    };
+    // one tile per CTA (persistent CTAs measured slower here)
+    tile(blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------

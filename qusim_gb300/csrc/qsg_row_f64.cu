@@ -12,7 +12,8 @@ static cudaError_t run_row_f64(const Geom2D &g, const RowPassArgs &a, cudaStream
     auto k = k_row_pass<double, NY, E, G, B, RS>;
     cudaError_t e = prepare_smem(k, g.row_smem);
     if (e != cudaSuccess) return e;
-    k<<<g.row_blocks, NT, g.row_smem, st>>>(a);
+    static int occ = 0;
+    k<<<persistent_grid(k, NT, g.row_smem, a.units, occ), NT, g.row_smem, st>>>(a);
     return cudaGetLastError();
 }
 
