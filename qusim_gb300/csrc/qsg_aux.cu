@@ -17,18 +17,23 @@ inline unsigned blocks_for(size_t n, int per_block = kThreads)
 
 // exp(z) and exp(z) - 1 in fp64.  The "-1" form keeps relative accuracy for
 // small |z|: re = expm1(x) - 2 e^x sin^2(y/2), im = e^x sin y.
+// A real time step (x == 0, the usual case) needs no exp / expm1, and the
+// "-1" form then needs a single sincos of y/2 (sin y = 2 sin(y/2) cos(y/2)).
+// FP64 transcendentals are the whole cost of building a table on this part.
 __device__ __forceinline__ double2 cexp_d(double x, double y)
 {
     double s, c;
     sincos(y, &s, &c);
-    const double ex = exp(x);
+    const double ex = x == 0.0 ? 1.0 : exp(x);
     return make_double2(ex * c, ex * s);
 }
 __device__ __forceinline__ float2 cexpm1_f(double x, double y)
 {
-    double s, c, sh, ch;
-    sincos(y, &s, &c);
+    double sh, ch;
     sincos(0.5 * y, &sh, &ch);
+    if (x == 0.0) return make_float2(float(-2.0 * sh * sh), float(2.0 * sh * ch));
+    double s, c;
+    sincos(y, &s, &c);
     const double ex = exp(x);
     return make_float2(float(expm1(x) - 2.0 * ex * sh * sh), float(ex * s));
 }

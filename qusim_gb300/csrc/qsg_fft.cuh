@@ -57,9 +57,17 @@ template <bool INV, class C> __device__ __forceinline__ C cmulw(C a, C w)
 // a * (1 + m) for m stored as (cos th - 1, sin th): the "phase minus one"
 // representation used by the complex64 tables, which keeps the systematic
 // rounding of a unit-modulus factor proportional to |th| instead of to 1.
+// The correction a*m is formed completely before it is added to a, so the one
+// rounding of the sum is unbiased.  Chaining a + a.x*m.x after a - a.y*m.y
+// instead drops a.x*m.x (~ -a.x th^2/2) whenever it is below half an ulp of
+// a.x, i.e. for |th| below ~2e-4: every such multiply then grows |a|^2 by
+// th^2, coherently, step after step (measured: 2.5e-5 norm drift over 1000 O4
+// steps at 1024^2, 3.0e-5 with the packet at k = 0).
 template <class C> __device__ __forceinline__ C cmul1p(C a, C m)
 {
-    return cmk<C>(fma(a.x, m.x, fma(-a.y, m.y, a.x)), fma(a.y, m.x, fma(a.x, m.y, a.y)));
+    const auto cx = fma(a.x, m.x, -(a.y * m.y));
+    const auto cy = fma(a.y, m.x, a.x * m.y);
+    return cmk<C>(a.x + cx, a.y + cy);
 }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, class C> __device__ __forceinline__ C crot(C a)
@@ -91,12 +99,10 @@ template <bool INV, class C> __device__ __forceinline__ void dft4(C &a0, C &a1, 
 // ---------------------------------------------------------------------------
 // Multiplication by the fixed roots of unity inside the radix-8/16 butterflies.
 //
-// complex128 uses the constants rounded once.  In complex64 a float rounding
-// of cos(pi/8) or 1/sqrt(2) is off the unit circle by ~3e-8, and since the
-// same constant is applied in every transform of every step, that modulus
-// error compounds coherently (~1e-4 relative error after 2000 O2 steps at
-// N=4096, measured); the complex64 rotations below avoid it (see Roots<float2>),
-// leaving random rounding, which grows like sqrt(steps).
+// complex128 uses the constants rounded once.  In complex64 the same constant
+// is applied in every transform of every step, so any error of the constant
+// itself compounds coherently; the complex64 rotations below use hi + lo
+// constants (see Roots<float2>), leaving rounding of the data.
 // ---------------------------------------------------------------------------
 
 template <class C> struct Roots;
@@ -123,38 +129,50 @@ template <> struct Roots<double2> {
     }
 };
 template <> struct Roots<float2> {
-    // complex64: each fixed rotation by phi is three shears,
-    //   x += a y;  y += b x;  x += a y,   a = -tan(phi/2), b = sin(phi),
-    // whose matrix has determinant exactly 1 for any rounded a, b, so the
-    // rounding of the constants cannot shrink or grow |psi| coherently (the
-    // modulus error is second order).  3 FMAs instead of the 4 of a complex
-    // product.  Constants for phi = -pi/8, -pi/4, -3pi/8; the inverse uses -a, -b.
-    static constexpr float A1 = 0x1.975f5ep-3f, B1 = -0x1.87de2ap-2f;  // phi = -pi/8
-    static constexpr float A2 = 0x1.a8279ap-2f, B2 = -0x1.6a09e6p-1f;  // phi = -pi/4
-    static constexpr float A3 = 0x1.561b82p-1f, B3 = -0x1.d906bcp-1f;  // phi = -3pi/8
-    template <bool INV> static __device__ __forceinline__ float2 shear(float2 v, float a, float b)
+    // complex64: every fixed rotation multiplies by (cos th, sin th) given as
+    // hi + lo float pairs (lo = float(c - hi)), as the table twiddles are.  The
+    // rotation is then unitary to ~1e-14, so the inverse transform (conjugate
+    // constants) undoes the forward one to rounding.  Both cheaper forms leave
+    // a fixed operator error that every step repeats, so it adds up linearly:
+    // - plain float constants are off the unit circle by ~3e-8;
+    // - three-shear rotations (determinant exactly 1) are not orthogonal, so
+    //   conj(FFT(conj(FFT x))) != N x by ~1e-8.
+    // Measured at 1024^2 with dt = 0 over 1000 O4 steps (pure round trips):
+    // shears gave relative L2 6.3e-5, hi + lo pairs 1.2e-5.
+    static constexpr float C1H = 0x1.d906bcp-1f, C1L = 0x1.e651a8p-26f;  // cos(pi/8)
+    static constexpr float S1H = 0x1.87de2ap-2f, S1L = 0x1.abaa58p-28f;  // sin(pi/8)
+    static constexpr float HH = 0x1.6a09e6p-1f, HL = 0x1.9fcef4p-27f;    // 1/sqrt(2)
+    // a * exp(-+ i th), th given by (cos th, sin th) = (ch + cl, sh + sl)
+    template <bool INV>
+    static __device__ __forceinline__ float2 cs(float2 a, float ch, float cl, float sh, float sl)
     {
         if (INV) {
-            a = -a;
-            b = -b;
+            const float lx = fmaf(a.x, cl, -a.y * sl), ly = fmaf(a.y, cl, a.x * sl);
+            return cmk<float2>(fmaf(a.x, ch, fmaf(-a.y, sh, lx)), fmaf(a.y, ch, fmaf(a.x, sh, ly)));
         }
-        float x = fmaf(a, v.y, v.x);
-        const float y = fmaf(b, x, v.y);
-        x = fmaf(a, y, x);
-        return cmk<float2>(x, y);
+        const float lx = fmaf(a.x, cl, a.y * sl), ly = fmaf(a.y, cl, -a.x * sl);
+        return cmk<float2>(fmaf(a.x, ch, fmaf(a.y, sh, lx)), fmaf(a.y, ch, fmaf(-a.x, sh, ly)));
     }
-    template <bool INV> static __device__ __forceinline__ float2 w16_1(float2 a) { return shear<INV>(a, A1, B1); }
-    template <bool INV> static __device__ __forceinline__ float2 w16_3(float2 a) { return shear<INV>(a, A3, B3); }
+    template <bool INV> static __device__ __forceinline__ float2 w16_1(float2 a)
+    {
+        return cs<INV>(a, C1H, C1L, S1H, S1L);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w16_3(float2 a)
+    {
+        return cs<INV>(a, S1H, S1L, C1H, C1L);
+    }
     template <bool INV> static __device__ __forceinline__ float2 w16_9(float2 a)
     {
-        return shear<INV>(cmk<float2>(-a.x, -a.y), A1, B1);
+        return cs<INV>(cmk<float2>(-a.x, -a.y), C1H, C1L, S1H, S1L);
     }
-    template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a) { return shear<INV>(a, A2, B2); }
-    // exp(-+ 3 i pi/4) = exp(-+ i pi/4) * (-+ i)
-    template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a)
+    // exp(-+ i pi/4) = (1 -+ i) / sqrt(2)
+    template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a)
     {
-        return shear<INV>(crot<INV>(a), A2, B2);
+        const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
+        return cmk<float2>(fmaf(u, HH, u * HL), fmaf(v, HH, v * HL));
     }
+    // exp(-+ 3 i pi/4) = exp(-+ i pi/4) * (-+ i)
+    template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a) { return w8_1<INV>(crot<INV>(a)); }
 };
 
 // Table twiddles: complex128 tables hold the factor; complex64 tables hold

@@ -275,11 +275,17 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
                 }
                 if (vt) {
                     const C *vr = opaque(vt) + (size_t)row * NY + t;
+                    // all loads first, then the multiplies: interleaved, the
+                    // schedule exposed the load latency (152 vs 168 us at 4096^2)
+                    C mv[E];
 #pragma unroll
-                    for (int e = 0; e < E; ++e) {
-                        const C m = ld_stream(vr + e * TL);
-                        x[e] = PhaseOps<C>::apply(x[e], m);
-                        if (a.vtwice) x[e] = PhaseOps<C>::apply(x[e], m);
+                    for (int e = 0; e < E; ++e) mv[e] = ld_stream(vr + e * TL);
+                    if (a.vtwice) {
+#pragma unroll
+                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(PhaseOps<C>::apply(x[e], mv[e]), mv[e]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], mv[e]);
                     }
                 }
             }
@@ -588,11 +594,15 @@ __global__ void __launch_bounds__(W *(N2 / E)) k_fs_col(FsColArgs a)
             const C *vt = static_cast<const C *>(in.vtab[a.vsel]);
             if (vt) {
                 const C *vr = opaque(vt) + base;
+                C mv[E];
 #pragma unroll
-                for (int e = 0; e < E; ++e) {
-                    const C m = ld_stream(vr + e * stride);
-                    x[e] = PhaseOps<C>::apply(x[e], m);
-                    if (a.vtwice) x[e] = PhaseOps<C>::apply(x[e], m);
+                for (int e = 0; e < E; ++e) mv[e] = ld_stream(vr + e * stride);
+                if (a.vtwice) {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(PhaseOps<C>::apply(x[e], mv[e]), mv[e]);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], mv[e]);
                 }
             }
         }
