@@ -93,7 +93,7 @@ bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
     g->col_w = p.col_w;
     if (ny % p.col_w) return false;
     g->col_threads = p.col_w * (g->m / p.col_e);
-    g->col_smem = (size_t)csz * col_tile_elems(csz, g->m, p.col_w);
+    g->col_smem = (size_t)csz * col_tile_elems(csz, g->m, p.col_w, p.col_e);
     g->kin_e = kin_e_for(prec);
     g->kin_w = kin_w_for(prec, g->m);
     if (ny % g->kin_w) return false;
@@ -109,12 +109,13 @@ int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap)
 {
     int n = 0;
     const int es[2] = {16, 8};
+    const int ces[3] = {16, 8, 32};
     const int ws[5] = {4, 8, 16, 32, 2};
     const int nts[2] = {512, 256};
     for (int g = 1; g <= 4; g *= 2)
         for (int re : es)
             for (int nt : nts)
-                for (int ce : es)
+                for (int ce : ces)
                     for (int w : ws) {
                         Plan2D p{g, re, nt, ce, w};
                         Geom2D gm;

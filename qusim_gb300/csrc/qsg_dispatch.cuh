@@ -81,8 +81,8 @@ constexpr size_t row_smem_for(int csz, int ny, int e, int g)
 #define QSG_COL_VARIANTS_F32(C) \
     C(float, 128, 16, 16) C(float, 128, 16, 32) \
     C(float, 256, 16, 8) C(float, 256, 16, 16) C(float, 256, 16, 32) \
-    C(float, 512, 16, 4) C(float, 512, 16, 8) C(float, 512, 16, 16) \
-    C(float, 1024, 16, 4) C(float, 1024, 16, 8) \
+    C(float, 512, 16, 4) C(float, 512, 16, 8) C(float, 512, 16, 16) C(float, 512, 32, 16) \
+    C(float, 1024, 16, 4) C(float, 1024, 16, 8) C(float, 1024, 32, 8) \
     C(float, 2048, 16, 4) \
     C(float, 128, 8, 8) C(float, 128, 8, 16) C(float, 128, 8, 32) \
     C(float, 256, 8, 4) C(float, 256, 8, 8) C(float, 256, 8, 16) \

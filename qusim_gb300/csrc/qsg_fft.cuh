@@ -127,6 +127,13 @@ template <> struct Roots<double2> {
     {
         return INV ? cmk<double2>(-(a.x + a.y) * H, (a.x - a.y) * H) : cmk<double2>((a.y - a.x) * H, -(a.x + a.y) * H);
     }
+    // exp(-+ i r pi/16), r = 1, 3, 5, 7 (radix 32)
+    static constexpr double C16 = 0.98078528040323044913, S16 = 0.19509032201612826785;
+    static constexpr double C316 = 0.83146961230254523708, S316 = 0.55557023301960222474;
+    template <bool INV> static __device__ __forceinline__ double2 w32_1(double2 a) { return cs<INV>(a, C16, S16); }
+    template <bool INV> static __device__ __forceinline__ double2 w32_3(double2 a) { return cs<INV>(a, C316, S316); }
+    template <bool INV> static __device__ __forceinline__ double2 w32_5(double2 a) { return cs<INV>(a, S316, C316); }
+    template <bool INV> static __device__ __forceinline__ double2 w32_7(double2 a) { return cs<INV>(a, S16, C16); }
 };
 template <> struct Roots<float2> {
     // complex64: every fixed rotation multiplies by (cos th, sin th) given as
@@ -173,7 +180,47 @@ template <> struct Roots<float2> {
     }
     // exp(-+ 3 i pi/4) = exp(-+ i pi/4) * (-+ i)
     template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a) { return w8_1<INV>(crot<INV>(a)); }
+    // exp(-+ i r pi/16), r = 1, 3, 5, 7 (radix 32)
+    static constexpr float C16H = 0x1.f6297cp-1f, C16L = 0x1.feeb96p-26f;    // cos(pi/16)
+    static constexpr float S16H = 0x1.8f8b84p-3f, S16L = -0x1.cb2cfcp-30f;   // sin(pi/16)
+    static constexpr float C316H = 0x1.a9b662p-1f, C316L = 0x1.21d434p-26f;  // cos(3pi/16)
+    static constexpr float S316H = 0x1.1c73b4p-1f, S316L = -0x1.9465cep-27f; // sin(3pi/16)
+    template <bool INV> static __device__ __forceinline__ float2 w32_1(float2 a)
+    {
+        return cs<INV>(a, C16H, C16L, S16H, S16L);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w32_3(float2 a)
+    {
+        return cs<INV>(a, C316H, C316L, S316H, S316L);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w32_5(float2 a)
+    {
+        return cs<INV>(a, S316H, S316L, C316H, C316L);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w32_7(float2 a)
+    {
+        return cs<INV>(a, S16H, S16L, C16H, C16L);
+    }
 };
+
+// a * exp(-+ 2 pi i M / 32) for a compile-time M: the r pi/16 rotation of
+// M mod 8, then (M / 8) quarter turns
+template <int M, bool INV, class C> __device__ __forceinline__ C rot32(C a)
+{
+    using RT = Roots<C>;
+    constexpr int r = M % 8, q = (M / 8) % 4;
+    if constexpr (r == 1) a = RT::template w32_1<INV>(a);
+    if constexpr (r == 2) a = RT::template w16_1<INV>(a);
+    if constexpr (r == 3) a = RT::template w32_3<INV>(a);
+    if constexpr (r == 4) a = RT::template w8_1<INV>(a);
+    if constexpr (r == 5) a = RT::template w32_5<INV>(a);
+    if constexpr (r == 6) a = RT::template w16_3<INV>(a);
+    if constexpr (r == 7) a = RT::template w32_7<INV>(a);
+    if constexpr (q >= 1) a = crot<INV>(a);
+    if constexpr (q >= 2) a = crot<INV>(a);
+    if constexpr (q >= 3) a = crot<INV>(a);
+    return a;
+}
 
 // Table twiddles: complex128 tables hold the factor; complex64 tables hold
 // float4 {hi.x, hi.y, lo.x, lo.y}, the factor as an unevaluated sum of two
@@ -243,6 +290,47 @@ template <bool INV, class C> __device__ __forceinline__ void dft16(C (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = r[i];
 }
 
+// n = 8 n1 + n2: DFT4 over n1, twiddle w32^(n2 k1), DFT8 over n2; output k = k1 + 4 k2
+template <bool INV, class C> __device__ __forceinline__ void dft32(C (&v)[32])
+{
+#pragma unroll
+    for (int n2 = 0; n2 < 8; ++n2) dft4<INV>(v[n2], v[8 + n2], v[16 + n2], v[24 + n2]);
+    // v[8 k1 + n2] = z[n2][k1]
+    v[9] = rot32<1, INV>(v[9]);
+    v[10] = rot32<2, INV>(v[10]);
+    v[11] = rot32<3, INV>(v[11]);
+    v[12] = rot32<4, INV>(v[12]);
+    v[13] = rot32<5, INV>(v[13]);
+    v[14] = rot32<6, INV>(v[14]);
+    v[15] = rot32<7, INV>(v[15]);
+    v[17] = rot32<2, INV>(v[17]);
+    v[18] = rot32<4, INV>(v[18]);
+    v[19] = rot32<6, INV>(v[19]);
+    v[20] = rot32<8, INV>(v[20]);
+    v[21] = rot32<10, INV>(v[21]);
+    v[22] = rot32<12, INV>(v[22]);
+    v[23] = rot32<14, INV>(v[23]);
+    v[25] = rot32<3, INV>(v[25]);
+    v[26] = rot32<6, INV>(v[26]);
+    v[27] = rot32<9, INV>(v[27]);
+    v[28] = rot32<12, INV>(v[28]);
+    v[29] = rot32<15, INV>(v[29]);
+    v[30] = rot32<18, INV>(v[30]);
+    v[31] = rot32<21, INV>(v[31]);
+    C r[32];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        C u[8];
+#pragma unroll
+        for (int n2 = 0; n2 < 8; ++n2) u[n2] = v[8 * k1 + n2];
+        dft8<INV>(u);
+#pragma unroll
+        for (int k2 = 0; k2 < 8; ++k2) r[k1 + 4 * k2] = u[k2];
+    }
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = r[i];
+}
+
 template <int R, bool INV, class C> __device__ __forceinline__ void dft(C (&v)[R])
 {
     if constexpr (R == 2) {
@@ -253,8 +341,10 @@ template <int R, bool INV, class C> __device__ __forceinline__ void dft(C (&v)[R
         dft8<INV>(v);
     } else if constexpr (R == 16) {
         dft16<INV>(v);
+    } else if constexpr (R == 32) {
+        dft32<INV>(v);
     } else {
-        static_assert(R == 1, "radix must be 1, 2, 4, 8 or 16");
+        static_assert(R == 1, "radix must be 1, 2, 4, 8, 16 or 32");
     }
 }
 
@@ -268,7 +358,7 @@ __host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v
 
 template <int L, int E> struct Plan {
     static_assert((L & (L - 1)) == 0 && (E & (E - 1)) == 0, "powers of two only");
-    static_assert(E >= 2 && E <= 16 && E <= L, "2 <= E <= 16, E <= L");
+    static_assert(E >= 2 && E <= 32 && E <= L, "2 <= E <= 32, E <= L");
     static constexpr int LOGL = ilog2(L);
     static constexpr int LOGE = ilog2(E);
     static constexpr int NST = (LOGL + LOGE - 1) / LOGE;
@@ -381,8 +471,11 @@ template <int W, int SH, int P> struct ColLayout {
 struct ColPad {
     int sh, p;
 };
-__host__ __device__ constexpr ColPad col_pad(int esize, int m, int w)
+__host__ __device__ constexpr ColPad col_pad(int esize, int m, int w, int e = 16)
 {
+    // radix 32 (one exchange): thread t writes rows 32t + q, so rows 32 apart
+    // must land in different halves of the banks
+    if (e == 32) return ColPad{5, 8};
     if (esize == 8) {
         if (w >= 16) return ColPad{0, 1};
         if (m <= 128) return ColPad{1, 2};
@@ -394,9 +487,9 @@ __host__ __device__ constexpr ColPad col_pad(int esize, int m, int w)
     return (m == 256 || m >= 2048) ? ColPad{2, 2} : ColPad{2, 1};
 }
 // elements of shared memory a column tile needs
-__host__ __device__ constexpr int col_tile_elems(int esize, int m, int w)
+__host__ __device__ constexpr int col_tile_elems(int esize, int m, int w, int e = 16)
 {
-    return m * w + (m >> col_pad(esize, m, w).sh) * col_pad(esize, m, w).p;
+    return m * w + (m >> col_pad(esize, m, w, e).sh) * col_pad(esize, m, w, e).p;
 }
 
 template <int L, int PADSHIFT> __host__ __device__ constexpr int padded(int n) { return n + (n >> PADSHIFT); }

@@ -365,8 +365,10 @@ struct ColPassArgs {
 
 // A tile is block q, columns [xt*W, +W), tile index u = q * (Ny/W) + xt;
 // CTA u handles tile u.
+// Radix-32 variants (256 threads) are held to 128 registers so that two CTAs
+// share an SM.
 template <class T, int M, int E, int W>
-__global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
+__global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPassArgs a)
 {
     using C = cplx_t<T>;
     using P = Plan<M, E>;
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(W *(M / E)) k_col_pass(ColPassArgs a)
     const int ntx = ny / W;
     C *psi = static_cast<C *>(a.psi);
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_col);
-    constexpr ColPad CP = col_pad(sizeof(C), M, W);
+    constexpr ColPad CP = col_pad(sizeof(C), M, W, E);
     const ColLayout<W, CP.sh, CP.p> lay{c};
     const CtaBarrier bar{};
     const int stride = TM * ny;  // between a thread's elements

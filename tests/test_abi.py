@@ -76,6 +76,6 @@ def test_candidate_plans_host_only(lib):
     assert gs <= {1, 2, 4} and 4 in gs
     for p in arr:
         assert 4096 // p.g <= 2048
-        assert p.row_e in (8, 16) and p.col_e in (8, 16)
+        assert p.row_e in (8, 16) and p.col_e in (8, 16, 32)
     assert lib.qsg_candidate_plans(1, 1000, 1024, None, 0) == 0
     assert lib.qsg_candidate_plans(0, 1024, 1024, None, 0) >= 1
