@@ -138,6 +138,12 @@ bool default_plan(int prec, int nx, int ny, Plan2D *p)
         c.col_e = 16;
         const int m = nx / c.g;
         c.col_w = m >= 512 ? 8 : (m == 256 ? 16 : 32);
+        // radix 32: two stages (one exchange) for 512- and 1024-point columns
+        if (m == 1024) c.col_e = 32;
+        if (m == 512) {
+            c.col_e = 32;
+            c.col_w = 16;
+        }
     } else {
         c.g = nx > 2048 ? nx / 2048 : 1;
         c.row_e = 8;
