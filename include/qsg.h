@@ -200,10 +200,12 @@ int qsg_server_take(qsg_server *server, uint64_t id, double *psi_out, double *la
 int qsg_server_stats(qsg_server *server, qsg_server_info *out);
 void qsg_server_destroy(qsg_server *server);
 
-/* Per-kernel timing of this context's launches (CUDA events around every
- * launch on the context stream), for roofline reporting.  Enabling resets the
- * counters.  qsg_profile_read fills up to cap entries of name / launches /
- * total milliseconds and returns the number of kernel kinds seen. */
+/* Per-kernel timing of this context's launches, for roofline reporting.
+ * on = 1: CUDA events around every launch (they add a little time between
+ * launches); on = 2: launch counts only, no events (total_ms stays 0); 0: off.
+ * Enabling resets the counters.  qsg_profile_read fills up to cap entries of
+ * name / launches / total milliseconds and returns the number of kernel kinds
+ * seen. */
 int qsg_profile_enable(qsg_ctx *ctx, int on);
 int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launches,
                      double *total_ms);

@@ -91,7 +91,7 @@ struct qsg_ctx {
     int max_partials = 0;
     double *sums = nullptr;      // small device result buffer
     double *host_sums = nullptr; // pinned mirror
-    bool prof = false;
+    int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
     std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> prof_pending;
     std::vector<cudaEvent_t> event_pool;
     std::map<std::string, ProfStat> prof_stats;
@@ -269,9 +269,11 @@ struct ProfScope {
     cudaEvent_t e0 = nullptr;
     ProfScope(qsg_ctx *c, const char *n, cudaStream_t s = nullptr) : ctx(c), name(n), st(s ? s : c->st)
     {
-        if (ctx->prof) {
+        if (ctx->prof == 1) {
             e0 = take_event(ctx);
             cudaEventRecord(e0, st);
+        } else if (ctx->prof == 2) {
+            ctx->prof_stats[name].launches += 1;
         }
     }
     ~ProfScope()
@@ -1125,8 +1127,8 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     if (rc) return rc;
     QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     const Plan2D keep = in->plan;
-    const bool prof = ctx->prof;
-    ctx->prof = false;
+    const int prof = ctx->prof;
+    ctx->prof = 0;
     cudaEvent_t e0, e1;
     QSG_CUDA(cudaEventCreate(&e0));
     QSG_CUDA(cudaEventCreate(&e1));
@@ -1762,7 +1764,7 @@ int qsg_profile_enable(qsg_ctx *ctx, int on)
     std::lock_guard<std::mutex> lk(ctx->mu);
     prof_drain(ctx);
     ctx->prof_stats.clear();
-    ctx->prof = on != 0;
+    ctx->prof = on == 2 ? 2 : (on != 0 ? 1 : 0);
     return QSG_OK;
 }
 

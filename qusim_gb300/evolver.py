@@ -108,7 +108,8 @@ class Context:
     def bytes_in_use(self) -> int:
         return self.lib.qsg_ctx_bytes_in_use(self.h)
 
-    def profile(self, on: bool):
+    def profile(self, on):
+        """on: True / 1 times every launch with CUDA events; 2 counts launches only; False / 0 off."""
         check(self.lib.qsg_profile_enable(self.h, int(on)))
 
     def profile_read(self):
