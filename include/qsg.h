@@ -121,8 +121,10 @@ void qsg_destroy(qsg_inst *inst);
 
 /* 2D execution plan: the x split (Nx = g * m, column transforms of length m,
  * a radix-g stage folded into the row pass), the elements per thread (radix)
- * of the row and column transforms, the threads per row-pass CTA, and the
- * columns per column-pass CTA.
+ * of the row and column transforms, the threads per row-pass CTA, the
+ * columns per column-pass CTA, and the row-pass kind (0: the unit of g rows
+ * staged in shared memory; 1: one row per thread group in flight, the others
+ * parked in the SM's tensor memory; complex64, g = 4, ny = 2048 or 4096).
  * Every plan computes the same result to rounding; they differ in speed.
  * New to this engine (the reference has one fixed cuFFT / KISS path). */
 typedef struct {
@@ -131,6 +133,7 @@ typedef struct {
     int32_t row_nt;
     int32_t col_e;
     int32_t col_w;
+    int32_t row_kind;
 } qsg_plan2d;
 
 /* Plans compiled for an nx x ny grid at `precision`; fills up to cap, returns

@@ -56,16 +56,16 @@ class ServerInfo(ctypes.Structure):
 
 
 class Plan2D(ctypes.Structure):
-    """qsg_plan2d: x split g, row radix and CTA threads, column radix and tile width."""
+    """qsg_plan2d: x split g, row radix and CTA threads, column radix and tile width, row-pass kind."""
     _fields_ = [("g", ctypes.c_int32), ("row_e", ctypes.c_int32), ("row_nt", ctypes.c_int32),
-                ("col_e", ctypes.c_int32), ("col_w", ctypes.c_int32)]
+                ("col_e", ctypes.c_int32), ("col_w", ctypes.c_int32), ("row_kind", ctypes.c_int32)]
 
     def as_tuple(self):
-        return (self.g, self.row_e, self.row_nt, self.col_e, self.col_w)
+        return (self.g, self.row_e, self.row_nt, self.col_e, self.col_w, self.row_kind)
 
     def __repr__(self):
         return (f"Plan2D(g={self.g}, row_e={self.row_e}, row_nt={self.row_nt}, col_e={self.col_e}, "
-                f"col_w={self.col_w})")
+                f"col_w={self.col_w}, row_kind={self.row_kind})")
 
 
 class QsgError(RuntimeError):

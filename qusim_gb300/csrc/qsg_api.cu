@@ -616,7 +616,7 @@ std::string plan_cache_path()
     return std::string(home ? home : ".") + "/.cache/qusim_gb300/plans.tsv";
 }
 
-// lines: device \t prec \t nx \t ny \t g \t row_e \t row_nt \t col_e \t col_w \t ms_per_step
+// lines: device \t prec \t nx \t ny \t g \t row_e \t row_nt \t col_e \t col_w \t ms_per_step [\t row_kind]
 void load_plans(qsg_ctx *ctx)
 {
     if (ctx->plans_loaded) return;
@@ -631,6 +631,8 @@ void load_plans(qsg_ctx *ctx)
         double ms;
         if (!std::getline(is, dev, '\t')) continue;
         if (!(is >> prec >> nx >> ny >> p.g >> p.row_e >> p.row_nt >> p.col_e >> p.col_w >> ms)) continue;
+        int kind = 0;
+        if (is >> kind) p.row_kind = kind;
         Geom2D g;
         if (dev == ctx->device_name && qsg::geom2d(prec, nx, ny, p, &g)) ctx->plans[std::make_tuple(prec, nx, ny)] = p;
     }
@@ -652,7 +654,7 @@ void save_plan(qsg_ctx *ctx, int prec, int nx, int ny, const Plan2D &p, double m
     std::ofstream f(path, std::ios::app);
     if (!f) return;
     f << ctx->device_name << '\t' << prec << '\t' << nx << '\t' << ny << '\t' << p.g << '\t' << p.row_e << '\t'
-      << p.row_nt << '\t' << p.col_e << '\t' << p.col_w << '\t' << ms << '\n';
+      << p.row_nt << '\t' << p.col_e << '\t' << p.col_w << '\t' << ms << '\t' << p.row_kind << '\n';
 }
 
 // point the instance at a plan: geometry + the twiddle tables it needs
@@ -1087,7 +1089,8 @@ int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out
     if (nx > 8192 || ny > 8192) return 0;
     std::vector<Plan2D> v(256);
     const int n = qsg::candidate_plans(precision, (int)nx, (int)ny, v.data(), (int)v.size());
-    for (int i = 0; i < n && i < cap && out; ++i) out[i] = qsg_plan2d{v[i].g, v[i].row_e, v[i].row_nt, v[i].col_e, v[i].col_w};
+    for (int i = 0; i < n && i < cap && out; ++i)
+        out[i] = qsg_plan2d{v[i].g, v[i].row_e, v[i].row_nt, v[i].col_e, v[i].col_w, v[i].row_kind};
     return n;
 }
 
@@ -1095,7 +1098,7 @@ int qsg_get_plan(qsg_inst *in, qsg_plan2d *out)
 {
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_plan: null argument");
     if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_get_plan: 2D instances only");
-    *out = qsg_plan2d{in->plan.g, in->plan.row_e, in->plan.row_nt, in->plan.col_e, in->plan.col_w};
+    *out = qsg_plan2d{in->plan.g, in->plan.row_e, in->plan.row_nt, in->plan.col_e, in->plan.col_w, in->plan.row_kind};
     return QSG_OK;
 }
 
@@ -1106,7 +1109,7 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
-    return apply_plan(in, Plan2D{p->g, p->row_e, p->row_nt, p->col_e, p->col_w});
+    return apply_plan(in, Plan2D{p->g, p->row_e, p->row_nt, p->col_e, p->col_w, p->row_kind});
 }
 
 int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, double *best_ms_per_step)
@@ -1159,7 +1162,7 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     if ((rc = apply_plan(in, best_p))) return rc;
     ctx->plans[std::make_tuple(in->prec, in->nx, in->ny)] = best_p;
     if (persist) save_plan(ctx, in->prec, in->nx, in->ny, best_p, best_ms);
-    if (best) *best = qsg_plan2d{best_p.g, best_p.row_e, best_p.row_nt, best_p.col_e, best_p.col_w};
+    if (best) *best = qsg_plan2d{best_p.g, best_p.row_e, best_p.row_nt, best_p.col_e, best_p.col_w, best_p.row_kind};
     if (best_ms_per_step) *best_ms_per_step = best_ms;
     return QSG_OK;
 }

@@ -63,6 +63,7 @@ bool row_variant_exists_f64(int ny, int e, int g, int nt);
 
 cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
 {
+    if (g.row_kind == 1) return launch_row_pass_tm(g, a, st);
     if (prec == 0) return launch_row_pass_f64(g, a, st);
     return g.row_e == 16 ? launch_row_pass_f32a(g, a, st) : launch_row_pass_f32b(g, a, st);
 }
@@ -73,22 +74,27 @@ bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
     if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 4096 || nx < 128 || nx > 8192) return false;
     if (!pow2(p.g) || p.g > 4 || nx % p.g) return false;
     const int csz = prec == 1 ? 8 : 16;
-    const bool row_ok = prec == 1 ? (row_variant_exists_f32a(ny, p.row_e, p.g, p.row_nt) ||
+    if (p.row_kind != 0 && p.row_kind != 1) return false;
+    const bool tm = p.row_kind == 1;
+    const bool row_ok = tm ? (prec == 1 && row_tm_supported(ny, p.g) && p.row_e == 16 && p.row_nt == 512)
+                      : prec == 1 ? (row_variant_exists_f32a(ny, p.row_e, p.g, p.row_nt) ||
                                      row_variant_exists_f32b(ny, p.row_e, p.g, p.row_nt))
-                                   : row_variant_exists_f64(ny, p.row_e, p.g, p.row_nt);
+                                  : row_variant_exists_f64(ny, p.row_e, p.g, p.row_nt);
     if (!row_ok) return false;
+    g->row_kind = p.row_kind;
     g->nx = nx;
     g->ny = ny;
     g->g = p.g;
     g->m = nx / p.g;
     if (!col_variant_exists(prec, g->m, p.col_e, p.col_w)) return false;
     g->row_e = p.row_e;
-    g->row_b = row_b_for(ny, p.row_e, p.g);
+    g->row_b = tm ? 1 : row_b_for(ny, p.row_e, p.g);
     g->row_threads = p.row_nt;
-    g->row_rs = row_work_for(ny, p.row_e, p.g) / p.row_nt;
+    g->row_rs = tm ? p.g : row_work_for(ny, p.row_e, p.g) / p.row_nt;
     if (g->m % g->row_b) return false;
     g->row_blocks = g->m / g->row_b;
-    g->row_smem = row_smem_for(csz, ny, p.row_e, p.g);
+    // the TMEM pass sizes its own shared memory (one line per thread group)
+    g->row_smem = tm ? 0 : row_smem_for(csz, ny, p.row_e, p.g);
     g->col_e = p.col_e;
     g->col_w = p.col_w;
     if (ny % p.col_w) return false;
@@ -123,6 +129,15 @@ int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap)
                         if (n < cap) out[n] = p;
                         ++n;
                     }
+    // TMEM row pass (one row per thread group in flight, the others parked in tensor memory)
+    for (int ce : ces)
+        for (int w : ws) {
+            Plan2D p{4, 16, 512, ce, w, 1};
+            Geom2D gm;
+            if (!geom2d(prec, nx, ny, p, &gm)) continue;
+            if (n < cap) out[n] = p;
+            ++n;
+        }
     return n;
 }
 
@@ -143,6 +158,11 @@ bool default_plan(int prec, int nx, int ny, Plan2D *p)
         if (m == 512) {
             c.col_e = 32;
             c.col_w = 16;
+        }
+        // rows of 2048 / 4096 points in 4-row units: waiting rows parked in TMEM
+        if (c.g == 4 && row_tm_supported(ny, c.g)) {
+            c.row_nt = 512;
+            c.row_kind = 1;
         }
     } else {
         c.g = nx > 2048 ? nx / 2048 : 1;

@@ -44,11 +44,13 @@ struct Plan2D {
     int row_nt;     // threads per row-pass CTA (256 or 512)
     int col_e;      // elements per thread of the column transforms
     int col_w;      // adjacent columns per column-pass CTA
+    int row_kind = 0;  // 0: k_row_pass (unit staged in shared memory); 1: k_row_pass_tm (lines parked in TMEM)
 };
 
 // Launch geometry of a plan for a grid
 struct Geom2D {
     int nx, ny, g, m;
+    int row_kind;
     int row_e, row_b, row_rs, row_threads, row_blocks;
     size_t row_smem;
     int col_e, col_w, col_threads;
@@ -64,6 +66,9 @@ int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap);
 bool default_plan(int prec, int nx, int ny, Plan2D *p);
 
 cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cudaStream_t st);
+// TMEM row pass (complex64, g = 4, ny = 2048 / 4096)
+bool row_tm_supported(int ny, int g);
+cudaError_t launch_row_pass_tm(const Geom2D &g, const RowPassArgs &a, cudaStream_t st);
 cudaError_t launch_col_pass(int prec, const Geom2D &g, const ColPassArgs &a, cudaStream_t st);
 // forward column transform with the kinetic-energy reduction (uses kin_* geometry)
 cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, double dtx,

@@ -1,0 +1,35 @@
+// 2D row pass with the waiting rows parked in tensor memory: instantiations + launcher.
+#include "qsg_dispatch.cuh"
+#include "qsg_row_tm.cuh"
+
+namespace qsg {
+
+bool row_tm_supported(int ny, int g) { return g == 4 && (ny == 2048 || ny == 4096); }
+
+template <int NY>
+static cudaError_t run_row_tm(const RowPassArgs &a, cudaStream_t st)
+{
+    constexpr int NG = 512 / (NY / 16);  // independent row groups per CTA
+    auto k = k_row_pass_tm<NY>;
+    const size_t smem = sizeof(float2) * NG * padded<NY, 4>(NY);  // one line buffer per group
+    static bool ready = false;
+    if (!ready) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        ready = true;
+    }
+    // one CTA per SM: each takes all 512 TMEM columns of its SM
+    const int ctas = (a.units + NG - 1) / NG;
+    const int sms = sm_count();
+    k<<<(unsigned)(ctas < sms ? ctas : sms), 512, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_pass_tm(const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
+{
+    if (g.ny == 4096) return run_row_tm<4096>(a, st);
+    if (g.ny == 2048) return run_row_tm<2048>(a, st);
+    return cudaErrorNotSupported;
+}
+
+}  // namespace qsg

@@ -189,7 +189,7 @@ def test_evolver_api_mirror(qsg):
                          BoundaryCondition.Period, SolverMethod.SplittingMethodO2, 1, 1, Options())
 
 
-@pytest.mark.parametrize("nx,ny", [(4096, 128), (2048, 256), (256, 1024)])
+@pytest.mark.parametrize("nx,ny", [(4096, 128), (2048, 256), (256, 1024), (512, 2048)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_every_plan_matches_oracle(qsg, ctx, oracle, nx, ny, precision):
     hx, hy = 0.05 * nx, 0.05 * ny
@@ -333,3 +333,30 @@ def test_wall_limits_are_reported(qsg, ctx):
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:32], V[:32], dx, 0.02, boundary=wall)
     assert e.value.code == 5
+
+
+@pytest.mark.parametrize("nx,ny", [(512, 4096), (1024, 2048)])
+def test_tmem_row_pass_equals_shared_memory_row_pass(qsg, ctx, nx, ny):
+    """The row pass that parks waiting rows in tensor memory does the same
+    arithmetic in the same order as the shared-memory one: bitwise equal."""
+    hx, hy = 0.05 * nx, 0.05 * ny
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=0.08 * min(hx, hy))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=8, seed=4, spread=0.5 * min(hx, hy))
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    plans = {p.as_tuple(): p for p in inst.candidate_plans()}
+    tm = [p for t, p in plans.items() if t[5] == 1]
+    assert tm, "no tensor-memory row plan for this grid"
+    key = tm[0].as_tuple()
+    shared = [p for t, p in plans.items() if t[5] == 0 and (t[0], t[1], t[3], t[4]) == (key[0], key[1], key[3], key[4])]
+    assert shared
+    out = []
+    for p in (tm[0], shared[0]):
+        inst.set_psi(psi0)
+        inst.set_plan(p)
+        inst.step(3)
+        inst.step(2, renormalize=True)
+        out.append((inst.get_psi(), inst.norm2(), inst.energies()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+    assert out[0][2] == out[1][2]
