@@ -469,6 +469,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="steps of the mixed-vs-fp64 accuracy run (default: the configuration's own count)")
     ap.add_argument("--no-tune", action="store_true", help="use the default plan instead of autotuning")
+    ap.add_argument("--plan", default=None,
+                    help="2D plan g,row_e,row_nt,col_e,col_w[,row_kind] for the timed precision (no autotuning)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: requests per second")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving: length of the arrival stream")
     args = ap.parse_args()
@@ -504,7 +506,11 @@ def main():
 
     def tuned_instance(precision):
         i = create(precision)
-        if w["dim"] == 2 and not args.no_tune:
+        if w["dim"] == 2 and args.plan and precision == args.precision:
+            p = [int(v) for v in args.plan.split(",")]
+            i.set_plan(p)
+            tuned[precision] = {"plan": list(i.plan().as_tuple()), "trial_ms_per_step": None}
+        elif w["dim"] == 2 and not args.no_tune:
             if precision not in tuned:
                 p, ms_tr = i.autotune(trial_steps=3, persist=True)
                 tuned[precision] = {"plan": list(p.as_tuple()), "trial_ms_per_step": ms_tr}
