@@ -324,6 +324,30 @@ def run_batch(args, w):
             errs.append(float(np.linalg.norm(a - r) / np.linalg.norm(r)))
         acc = {"steps": nacc, "instances": len(sub), "rel_l2_vs_fp64_max": max(errs),
                "rel_l2_vs_fp64_median": float(np.median(errs))}
+    # the complex128 path instance by instance (one qsg_step per instance), on
+    # the first 256 instances of the batch
+    plain = None
+    if not args.no_plain and args.precision == "mixed":
+        sub = list(range(min(256, len(psis))))
+        solo = [q.Instance.create_1d(ctx, psis[i], Vs[i], dxs[i], w["dt"], order=w["order"], precision="fp64")
+                for i in sub]
+        for s_ in solo:
+            s_.step(2)
+        solo[0].sync()
+        torch.cuda.synchronize()
+        psteps = 10
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for s_ in solo:
+            s_.step(psteps)
+        f1.record(stream)
+        f1.synchronize()
+        pms = f0.elapsed_time(f1)
+        psites = sum(psis[i].size for i in sub)
+        plain = {"value": psites * psteps / (pms / 1e3), "unit": "site-steps/s", "steps": psteps,
+                 "instances": len(sub), "dtype": "c128", "launch": "one qsg_step per instance"}
+        for s_ in solo:
+            s_.close()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as orc
@@ -350,7 +374,7 @@ def run_batch(args, w):
                            "l2": "2.2 GB of state and tables, larger than L2"},
                 "roofline": {"bound": "on-chip", "note": "resident sizes keep psi in shared memory for all "
                              "K steps; four-step sizes make 2 HBM passes per step"},
-                "step_roofline": fs_roof,
+                "step_roofline": fs_roof, "plain_fp64": plain,
                 "accuracy": acc, "gpu_launches": int(sum(v[0] for v in counts.values())),
                 "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
                 "cpu_baseline": cpu, "clocks": clk}
