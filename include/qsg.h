@@ -84,6 +84,38 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
                   double hbar, double dt_re, double dt_im, int order, int precision,
                   const double *psi0, const double *V, qsg_inst **out);
 
+/* Initial state and potential given as a formula instead of arrays, sampled on
+ * the device in FP64 at x_i = x0 + i*dx, y_j = y0 + j*dy (the points at which
+ * the reference samples its psi / V functors, src/EvolverImpl1D.cpp:33-81,
+ * src/EvolverImpl2D.cpp:39-98), so no host array is built or copied:
+ *   psi0(r) = exp(i k.r) exp(-|r - c|^2 / (4 s^2)), scaled to
+ *             sum |psi0|^2 dv = 1 when normalize (the reference's
+ *             force_normalization);
+ *   V(r)    = v0 + sum_b h_b exp(-|r - b_b|^2 / (2 w_b^2)), bumps[b] = {h, bx, by, w}.
+ * In 1D the y terms (ky, cy, by) are unused.  This is the packet-plus-bumps
+ * family of the benchmark and serving inputs; a general expression (the
+ * reference's Cal.cpp calculator) is not parsed. */
+#define QSG_SPEC_MAX_BUMPS 32
+typedef struct {
+    double x0, y0;
+    double kx, ky;
+    double cx, cy;
+    double s;
+    double v0;
+    int32_t normalize;
+    int32_t nbumps; /* 0 .. QSG_SPEC_MAX_BUMPS */
+    double bumps[QSG_SPEC_MAX_BUMPS][4];
+} qsg_spec;
+/* qsg_create_1d / qsg_create_2d with psi0 and V from a spec (sampled into a
+ * temporary device buffer of 24 bytes per site, counted against the HBM budget
+ * while it lives). */
+int qsg_create_1d_spec(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
+                       double dt_im, int order, int precision, int boundary, const qsg_spec *spec,
+                       qsg_inst **out);
+int qsg_create_2d_spec(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
+                       double hbar, double dt_re, double dt_im, int order, int precision,
+                       const qsg_spec *spec, qsg_inst **out);
+
 /* Advance by nsteps steps (O2: V/2 T V/2; O4: the 7-factor Forest-Ruth
  * sequence), then, if renormalize, scale psi to Norm2 == 1.  Asynchronous:
  * returns once the launches are queued.
@@ -188,6 +220,7 @@ typedef struct {
     uint64_t nsteps;
     const double *psi0; /* nx*ny complex */
     const double *V;    /* nx*ny real */
+    const qsg_spec *spec; /* if not null, psi0 / V come from it (sampled on the device); copied at submit */
 } qsg_request;
 typedef struct {
     uint64_t completed, failed, site_steps;

@@ -5,6 +5,6 @@ The engine is libqsg.so (C ABI, include/qsg.h); this package holds its
 sources (csrc/), its build (build.py) and a Python mirror of the reference's
 Evolver/Options API (evolver.py).
 """
-from ._lib import QsgError, load  # noqa: F401
+from ._lib import QsgError, Spec, load  # noqa: F401
 from .evolver import (Batch, BoundaryCondition, Context, Evolver1D, Evolver2D, Instance,  # noqa: F401
                       Options, Server, SolverMethod, default_context)

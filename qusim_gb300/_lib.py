@@ -36,8 +36,35 @@ EXPORTS = [
     "qsg_autotune", "qsg_batch_create_1d", "qsg_batch_step", "qsg_batch_sync", "qsg_batch_size",
     "qsg_batch_instance", "qsg_batch_destroy", "qsg_server_create", "qsg_server_submit",
     "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_destroy",
-    "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc",
+    "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc", "qsg_create_1d_spec", "qsg_create_2d_spec",
 ]
+
+
+SPEC_MAX_BUMPS = 32
+
+
+class Spec(ctypes.Structure):
+    """qsg_spec: psi0 = exp(i k.r) exp(-|r-c|^2/(4 s^2)) (normalised if asked),
+    V = v0 + sum_b h exp(-|r-b|^2/(2 w^2)), sampled on the device at x0 + i*dx (, y0 + j*dy)."""
+    _fields_ = [("x0", ctypes.c_double), ("y0", ctypes.c_double), ("kx", ctypes.c_double), ("ky", ctypes.c_double),
+                ("cx", ctypes.c_double), ("cy", ctypes.c_double), ("s", ctypes.c_double), ("v0", ctypes.c_double),
+                ("normalize", ctypes.c_int32), ("nbumps", ctypes.c_int32),
+                ("bumps", (ctypes.c_double * 4) * SPEC_MAX_BUMPS)]
+
+    @classmethod
+    def make(cls, x0, s, kx=0.0, cx=0.0, y0=0.0, ky=0.0, cy=0.0, bumps=(), v0=0.0, normalize=True):
+        """bumps: rows (h, bx, by, w) (by unused in 1D)."""
+        sp = cls()
+        sp.x0, sp.y0, sp.kx, sp.ky, sp.cx, sp.cy, sp.s, sp.v0 = x0, y0, kx, ky, cx, cy, s, v0
+        sp.normalize = 1 if normalize else 0
+        bumps = [tuple(float(v) for v in b) for b in bumps]
+        if len(bumps) > SPEC_MAX_BUMPS:
+            raise ValueError(f"at most {SPEC_MAX_BUMPS} bumps")
+        sp.nbumps = len(bumps)
+        for i, b in enumerate(bumps):
+            for k in range(4):
+                sp.bumps[i][k] = b[k]
+        return sp
 
 
 class Request(ctypes.Structure):
@@ -47,7 +74,7 @@ class Request(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("mass", ctypes.c_double),
                 ("hbar", ctypes.c_double), ("dt_re", ctypes.c_double), ("dt_im", ctypes.c_double),
                 ("nsteps", ctypes.c_uint64), ("psi0", ctypes.POINTER(ctypes.c_double)),
-                ("V", ctypes.POINTER(ctypes.c_double))]
+                ("V", ctypes.POINTER(ctypes.c_double)), ("spec", ctypes.POINTER(Spec))]
 
 
 class ServerInfo(ctypes.Structure):
@@ -96,6 +123,10 @@ def _declare(lib):
     lib.qsg_ctx_bytes_in_use.argtypes = [_vp]
     lib.qsg_ctx_bytes_in_use.restype = _sz
     lib.qsg_create_1d.argtypes = [_vp, _u64, _d, _d, _d, _d, _d, _i, _i, _i, _dp, _dp, ctypes.POINTER(_vp)]
+    lib.qsg_create_1d_spec.argtypes = [_vp, _u64, _d, _d, _d, _d, _d, _i, _i, _i, ctypes.POINTER(Spec),
+                                       ctypes.POINTER(_vp)]
+    lib.qsg_create_2d_spec.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _i, _i, ctypes.POINTER(Spec),
+                                       ctypes.POINTER(_vp)]
     lib.qsg_create_2d.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp,
                                   ctypes.POINTER(_vp)]
     lib.qsg_step.argtypes = [_vp, _u64, _i]

@@ -551,12 +551,12 @@ int upload_psi(qsg_inst *in, const double *psi)
 {
     qsg_ctx *ctx = in->ctx;
     if (in->prec == 0) {
-        QSG_CUDA(cudaMemcpyAsync(in->psi, psi, in->n * 16, cudaMemcpyHostToDevice, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(in->psi, psi, in->n * 16, cudaMemcpyDefault, ctx->st));  // host or device source
         return QSG_OK;
     }
     int rc = ensure_scratch(ctx, in->n * 16);
     if (rc) return rc;
-    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, psi, in->n * 16, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, psi, in->n * 16, cudaMemcpyDefault, ctx->st));
     QSG_CUDA(qsg::launch_c128_to_c64(in->psi, ctx->scratch, in->n, ctx->st));
     return QSG_OK;
 }
@@ -581,7 +581,7 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     void *v = nullptr;
     if ((rc = inst_alloc(in, in->n * 8, &v))) return rc;
     in->V = (double *)v;
-    QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyDefault, ctx->st));  // host or device source
     if ((rc = upload_psi(in, psi0))) return rc;
     if ((rc = build_tables(in))) return rc;
     if (in->dim == 1) {
@@ -843,6 +843,120 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     }
     *out = in;
     return QSG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int check_spec(const qsg_spec *sp, const char *who)
+{
+    if (!sp) return fail(QSG_ERR_ARG, std::string(who) + ": null spec");
+    if (!(sp->s > 0) || !std::isfinite(sp->s) || sp->nbumps < 0 || sp->nbumps > QSG_SPEC_MAX_BUMPS)
+        return fail(QSG_ERR_ARG, std::string(who) + ": spec needs s > 0 and 0 <= nbumps <= " +
+                                     std::to_string(QSG_SPEC_MAX_BUMPS));
+    for (int b = 0; b < sp->nbumps; ++b)
+        if (!(sp->bumps[b][3] > 0)) return fail(QSG_ERR_ARG, std::string(who) + ": bump widths must be > 0");
+    return QSG_OK;
+}
+
+// psi0 (complex128, normalised if asked) and V sampled from the spec into one
+// temporary device buffer of 24 bytes per site on the context stream; the
+// buffer counts against the budget until the caller releases it
+int sample_spec(qsg_ctx *ctx, int dim, uint64_t nx, uint64_t ny, double dx, double dy, const qsg_spec &sp,
+                void **buf)
+{
+    const size_t n = (size_t)nx * ny;
+    const size_t bytes = n * 24;
+    if (ctx->budget && ctx->in_use + bytes > ctx->budget)
+        return fail(QSG_ERR_BUDGET, "spec sampling needs " + std::to_string(bytes) + " bytes of the HBM budget");
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    QSG_CUDA(cudaMallocAsync(buf, bytes, ctx->st));
+    ctx->in_use += bytes;
+    qsg::SpecArgs a{};
+    a.x0 = sp.x0;
+    a.y0 = sp.y0;
+    a.dx = dx;
+    a.dy = dy;
+    a.kx = sp.kx;
+    a.ky = sp.ky;
+    a.cx = sp.cx;
+    a.cy = sp.cy;
+    a.s = sp.s;
+    a.v0 = sp.v0;
+    a.dim = dim;
+    a.nbumps = sp.nbumps;
+    for (int b = 0; b < sp.nbumps; ++b)
+        for (int k = 0; k < 4; ++k) a.bumps[b][k] = sp.bumps[b][k];
+    double *psi = static_cast<double *>(*buf);
+    cudaError_t e = qsg::launch_sample_spec(a, (int)nx, (int)ny, psi, psi + 2 * n, ctx->st);
+    if (e == cudaSuccess && sp.normalize) {
+        // psi *= 1 / sqrt(sum |psi|^2 dv), the reference's host normalisation
+        int np = 0;
+        e = qsg::launch_reduce(0, psi, nullptr, 0, n, 0, ctx->partials, ctx->max_partials, &np, ctx->st);
+        if (e == cudaSuccess) e = qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st);
+        if (e == cudaSuccess) e = qsg::launch_renorm(0, psi, n, ctx->sums, dim == 2 ? dx * dy : dx, ctx->st);
+    }
+    if (e != cudaSuccess) {
+        cudaFreeAsync(*buf, ctx->st);
+        ctx->in_use -= bytes;
+        *buf = nullptr;
+        return fail(QSG_ERR_CUDA, std::string("spec sampling: ") + cudaGetErrorString(e));
+    }
+    return QSG_OK;
+}
+
+void release_spec(qsg_ctx *ctx, void *buf, size_t n)
+{
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaFreeAsync(buf, ctx->st);
+    ctx->in_use -= n * 24;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsg_create_1d_spec(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
+                       double dt_im, int order, int precision, int boundary, const qsg_spec *spec,
+                       qsg_inst **out)
+{
+    if (!ctx || !out) return fail(QSG_ERR_ARG, "qsg_create_1d_spec: null argument");
+    int rc = check_spec(spec, "qsg_create_1d_spec");
+    if (rc) return rc;
+    if (n == 0 || n > 262144 || !(dx > 0)) return fail(QSG_ERR_ARG, "qsg_create_1d_spec: bad n or dx");
+    void *buf = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if ((rc = sample_spec(ctx, 1, n, 1, dx, 0.0, *spec, &buf))) return rc;
+    }
+    const double *psi = static_cast<const double *>(buf);
+    rc = qsg_create_1d(ctx, n, dx, mass, hbar, dt_re, dt_im, order, precision, boundary, psi, psi + 2 * n, out);
+    const std::string msg = rc ? std::string(g_last_error) : std::string();
+    release_spec(ctx, buf, n);
+    return rc ? fail(rc, msg) : QSG_OK;
+}
+
+int qsg_create_2d_spec(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
+                       double hbar, double dt_re, double dt_im, int order, int precision,
+                       const qsg_spec *spec, qsg_inst **out)
+{
+    if (!ctx || !out) return fail(QSG_ERR_ARG, "qsg_create_2d_spec: null argument");
+    int rc = check_spec(spec, "qsg_create_2d_spec");
+    if (rc) return rc;
+    if (nx == 0 || ny == 0 || nx > 8192 || ny > 8192 || !(dx > 0) || !(dy > 0))
+        return fail(QSG_ERR_ARG, "qsg_create_2d_spec: bad sizes or spacing");
+    void *buf = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        if ((rc = sample_spec(ctx, 2, nx, ny, dx, dy, *spec, &buf))) return rc;
+    }
+    const size_t n = (size_t)nx * ny;
+    const double *psi = static_cast<const double *>(buf);
+    rc = qsg_create_2d(ctx, nx, ny, dx, dy, mass, hbar, dt_re, dt_im, order, precision, psi, psi + 2 * n, out);
+    const std::string msg = rc ? std::string(g_last_error) : std::string();
+    release_spec(ctx, buf, n);
+    return rc ? fail(rc, msg) : QSG_OK;
 }
 
 int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
@@ -1387,6 +1501,8 @@ struct SrvRequest {
     uint64_t id = 0;
     qsg_request req{};
     std::vector<double> psi0, V, result;
+    qsg_spec spec{};
+    bool has_spec = false;  // psi0 / V from spec
     int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
     int error = 0;
     std::string message;
@@ -1426,13 +1542,23 @@ size_t request_bytes(const qsg_request &r)
     const size_t n = (size_t)r.nx * (r.dim == 2 ? r.ny : 1);
     const size_t cs = r.precision == QSG_MIXED ? 8 : 16;
     const int ntab = r.order == 2 ? 1 : 2;
-    return n * (cs + 8 + ntab * cs * 2) + n * 16;  // psi, V, V and K tables, import staging
+    return n * (cs + 8 + ntab * cs * 2) + n * 16 + (r.spec ? n * 24 : 0);  // psi, V, tables, staging, spec buffer
 }
 
 int srv_create(qsg_server *S, SrvRequest &q)
 {
     const qsg_request &r = q.req;
     qsg_ctx *ctx = S->ctx;
+    if (q.has_spec) {
+        // the spec entry points take the context lock themselves
+        ctx->mu.unlock();
+        int rc = r.dim == 1 ? qsg_create_1d_spec(ctx, r.nx, r.dx, r.mass, r.hbar, r.dt_re, r.dt_im, r.order,
+                                                 r.precision, QSG_PERIOD, &q.spec, &q.inst)
+                            : qsg_create_2d_spec(ctx, r.nx, r.ny, r.dx, r.dy, r.mass, r.hbar, r.dt_re, r.dt_im,
+                                                 r.order, r.precision, &q.spec, &q.inst);
+        ctx->mu.lock();
+        return rc;
+    }
     if (r.dim == 1)
         return create_1d_locked(ctx, r.nx, r.dx, r.mass, r.hbar, r.dt_re, r.dt_im, r.order, r.precision, QSG_PERIOD,
                                 q.psi0.data(), q.V.data(), &q.inst);
@@ -1663,7 +1789,11 @@ int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_runni
 
 int qsg_server_submit(qsg_server *S, const qsg_request *r, uint64_t *id)
 {
-    if (!S || !r || !r->psi0 || !r->V) return fail(QSG_ERR_ARG, "qsg_server_submit: null argument");
+    if (!S || !r || (!r->spec && (!r->psi0 || !r->V))) return fail(QSG_ERR_ARG, "qsg_server_submit: null argument");
+    if (r->spec) {
+        const int rc = check_spec(r->spec, "qsg_server_submit");
+        if (rc) return rc;
+    }
     if ((r->dim != 1 && r->dim != 2) || (r->order != 2 && r->order != 4) || r->nx == 0 ||
         (r->dim == 2 && r->ny == 0) || r->nsteps == 0)
         return fail(QSG_ERR_ARG, "qsg_server_submit: bad request (dim, order, sizes or steps)");
@@ -1672,10 +1802,16 @@ int qsg_server_submit(qsg_server *S, const qsg_request *r, uint64_t *id)
     auto q = std::make_shared<SrvRequest>();
     q->req = *r;
     const size_t n = (size_t)r->nx * (r->dim == 2 ? r->ny : 1);
-    q->psi0.assign(r->psi0, r->psi0 + 2 * n);
-    q->V.assign(r->V, r->V + n);
+    if (r->spec) {
+        q->spec = *r->spec;
+        q->has_spec = true;
+    } else {
+        q->psi0.assign(r->psi0, r->psi0 + 2 * n);
+        q->V.assign(r->V, r->V + n);
+    }
     q->req.psi0 = nullptr;
     q->req.V = nullptr;
+    q->req.spec = nullptr;
     q->submit = clk::now();
     std::lock_guard<std::mutex> lk(S->mu);
     q->id = S->next_id++;

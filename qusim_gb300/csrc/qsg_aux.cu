@@ -225,6 +225,34 @@ cudaError_t launch_ktable1d(int prec, void *out, int n, double fre, double fim, 
     return cudaGetLastError();
 }
 
+__global__ void k_sample_spec(SpecArgs a, int nx, int ny, double2 *psi, double *V)
+{
+    const size_t n = (size_t)nx * ny;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / ny), j = (int)(idx - (size_t)i * ny);
+        const double x = a.x0 + i * a.dx;
+        const double y = a.dim == 2 ? a.y0 + j * a.dy : 0.0;
+        const double rx = x - a.cx, ry = a.dim == 2 ? y - a.cy : 0.0;
+        const double env = exp(-(rx * rx + ry * ry) / (4.0 * a.s * a.s));
+        double sp, cp;
+        sincos(a.kx * x + (a.dim == 2 ? a.ky * y : 0.0), &sp, &cp);
+        psi[idx] = make_double2(env * cp, env * sp);
+        double v = a.v0;
+        for (int b = 0; b < a.nbumps; ++b) {
+            const double bx = x - a.bumps[b][1], by = a.dim == 2 ? y - a.bumps[b][2] : 0.0;
+            const double w = a.bumps[b][3];
+            v += a.bumps[b][0] * exp(-(bx * bx + by * by) / (2.0 * w * w));
+        }
+        V[idx] = v;
+    }
+}
+
+cudaError_t launch_sample_spec(const SpecArgs &a, int nx, int ny, void *psi, double *V, cudaStream_t st)
+{
+    k_sample_spec<<<blocks_for((size_t)nx * ny), kThreads, 0, st>>>(a, nx, ny, (double2 *)psi, V);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ktable_wall(int prec, void *out, int n, double fre, double fim, double scale, cudaStream_t st)
 {
     if (prec == 1)

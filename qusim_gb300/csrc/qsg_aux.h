@@ -25,6 +25,17 @@ cudaError_t launch_ktable_fs(int prec, void *out, int n1, int n2, double fre, do
 cudaError_t launch_ktable2d(void *out, int nx, int ny, double are, double aim, double dtx,
                             double dty, double scale, cudaStream_t st);
 
+// psi0 (complex128) and V sampled on the device from a packet-plus-bumps
+// formula (qsg_spec), point (i, j) at x0 + i*dx, y0 + j*dy, index j + i*ny
+// (ny = 1 and the y terms unused in 1D)
+struct SpecArgs {
+    double x0, y0, dx, dy;
+    double kx, ky, cx, cy, s, v0;
+    int dim, nbumps;
+    double bumps[32][4];
+};
+cudaError_t launch_sample_spec(const SpecArgs &a, int nx, int ny, void *psi, double *V, cudaStream_t st);
+
 // host complex128 staging <-> device state
 cudaError_t launch_c128_to_c64(void *out, const void *in, size_t n, cudaStream_t st);
 cudaError_t launch_c64_to_c128(void *out, const void *in, size_t n, cudaStream_t st);

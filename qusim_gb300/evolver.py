@@ -160,6 +160,26 @@ class Instance:
         return cls(ctx, h, psi0.shape, dx, 1 if precision == "mixed" else 0)
 
     @classmethod
+    def create_1d_spec(cls, ctx, spec, n, dx, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
+                       boundary=BoundaryCondition.Period):
+        """psi0 and V sampled on the device from a _lib.Spec (no host arrays)."""
+        dt = complex(dt)
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_1d_spec(ctx.h, n, dx, mass, hbar, dt.real, dt.imag, order,
+                                         _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                         boundary.value, ctypes.byref(spec), ctypes.byref(h)))
+        return cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+
+    @classmethod
+    def create_2d_spec(cls, ctx, spec, nx, ny, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
+        dt = complex(dt)
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_2d_spec(ctx.h, nx, ny, dx, dy, mass, hbar, dt.real, dt.imag, order,
+                                         _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                         ctypes.byref(spec), ctypes.byref(h)))
+        return cls(ctx, h, (nx, ny), dx * dy, 1 if precision == "mixed" else 0)
+
+    @classmethod
     def create_2d(cls, ctx, psi0, V, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
         psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
         V = np.ascontiguousarray(V, dtype=np.float64)
@@ -323,6 +343,28 @@ class Server:
         check(self.lib.qsg_server_create(device, hbm_budget, max_running, ctypes.byref(h)))
         self.h = h
         self._shapes = {}
+
+    def submit_spec(self, spec, shape, dx, dt, nsteps, order=2, precision="mixed", dy=None, mass=1.0, hbar=1.0):
+        """A request whose psi0 and V are sampled on the device from a _lib.Spec."""
+        shape = tuple(int(v) for v in shape)
+        if len(shape) not in (1, 2):
+            raise ValueError("shape: (n,) or (nx, ny)")
+        dt = complex(dt)
+        r = _lib.Request()
+        r.dim = len(shape)
+        r.order = order
+        r.precision = _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64
+        r.nx = shape[0]
+        r.ny = shape[1] if len(shape) == 2 else 1
+        r.dx = dx
+        r.dy = dy if dy is not None else dx
+        r.mass, r.hbar, r.dt_re, r.dt_im = mass, hbar, dt.real, dt.imag
+        r.nsteps = nsteps
+        r.spec = ctypes.pointer(spec)
+        i = ctypes.c_uint64()
+        check(self.lib.qsg_server_submit(self.h, ctypes.byref(r), ctypes.byref(i)))
+        self._shapes[i.value] = shape
+        return i.value
 
     def submit(self, psi0, V, dx, dt, nsteps, order=2, precision="mixed", dy=None, mass=1.0, hbar=1.0):
         psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
