@@ -420,7 +420,8 @@ def run_serving(args, w):
     import torch
     torch.cuda.set_device(local)
     import qusim_gb300 as q
-    pool = serving_inputs(seed=rank)
+    from tests.workloads import grid
+    pool = serving_inputs(seed=rank) if args.serve_inputs == "arrays" else None
     rng = np.random.default_rng(1000 + rank)
     nreq = int(args.serve_rate * args.serve_seconds)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=nreq))
@@ -435,10 +436,34 @@ def run_serving(args, w):
         reqs.append((key, int(rng.integers(0, len(pool[key]))), int(rng.integers(100, 5001)),
                      2 if rng.uniform() < 0.5 else 4))
     srv = q.Server(local, hbm_budget=120 << 30, max_running=256)
+
+    def spec_for(key):
+        # a fresh seeded packet and 8 bumps per request, sampled on the device
+        dim, n = key
+        half = 0.05 * n
+        _, dx = grid(n, -half, half)
+        if dim == 1:
+            bumps = [(rng.uniform(-1, 1), rng.uniform(-half, half), 0.0, rng.uniform(1, 5)) for _ in range(8)]
+            sp = q.Spec.make(x0=-half, s=rng.uniform(2, 20), kx=rng.uniform(0.5, 3), cx=-0.25 * half, bumps=bumps)
+        else:
+            bumps = [(rng.uniform(-1, 1), rng.uniform(-0.8 * half, 0.8 * half), rng.uniform(-0.8 * half, 0.8 * half),
+                      rng.uniform(1, 5)) for _ in range(8)]
+            sp = q.Spec.make(x0=-half, y0=-half, s=rng.uniform(2, 20), kx=rng.uniform(0.5, 3), cx=-0.25 * half,
+                             bumps=bumps)
+        return sp, dx
+
+    def submit(key, var, steps, order):
+        dim, n = key
+        shape = (n,) if dim == 1 else (n, n)
+        if args.serve_inputs == "spec":
+            sp, dx = spec_for(key)
+            return srv.submit_spec(sp, shape, dx, 0.01, steps, order=order, precision="mixed", dy=dx)
+        p, V, dx = pool[key][var]
+        return srv.submit(p, V, dx, 0.01, steps, order=order, precision="mixed", dy=dx)
+
     # warm-up: one small request of each kind, so module loading is not in the latencies
     for key in [(1, 1024), (1, 65536), (2, 256)]:
-        p, V, dx = pool[key][0]
-        rid = srv.submit(p, V, dx, 0.01, 10, precision="mixed", dy=dx)
+        rid = submit(key, 0, 10, 2)
         srv.wait(rid, 120)
         srv.take(rid)
     clocks = ClockSampler(local)
@@ -450,9 +475,8 @@ def run_serving(args, w):
         now = time.perf_counter() - t0
         if arrivals[i] > now:
             time.sleep(arrivals[i] - now)
-        p, V, dx = pool[key][var]
-        ids.append(srv.submit(p, V, dx, 0.01, steps, order=order, precision="mixed", dy=dx))
-        site_steps += p.size * steps
+        ids.append(submit(key, var, steps, order))
+        site_steps += (key[1] if key[0] == 1 else key[1] * key[1]) * steps
     lats = []
     for rid in ids:
         srv.wait(rid, 3600)
@@ -470,6 +494,8 @@ def run_serving(args, w):
                 "data": "synthetic",
                 "config": {"workload": w["desc"], "rate_per_s": args.serve_rate, "seconds": args.serve_seconds,
                            "requests": nreq, "budget_bytes": 120 << 30, "parallelism": f"replicas x{world}",
+                           "inputs": ("packet-plus-bumps specs sampled on the device, one seeded spec per request"
+                                      if args.serve_inputs == "spec" else "host arrays from a seeded pool"),
                            "l2": "requests' state far larger than L2"},
                 "latency_s": {"p50": float(np.percentile(lats, 50)), "p90": float(np.percentile(lats, 90)),
                               "p99": float(np.percentile(lats, 99)), "max": float(lats.max())},
@@ -497,6 +523,8 @@ def main():
                     help="2D plan g,row_e,row_nt,col_e,col_w[,row_kind] for the timed precision (no autotuning)")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: requests per second")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving: length of the arrival stream")
+    ap.add_argument("--serve-inputs", default="spec", choices=["spec", "arrays"],
+                    help="serving: psi0 / V as device-sampled specs or as host arrays")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.warmup < 3:
