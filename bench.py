@@ -433,7 +433,7 @@ def run_serving(args, w):
         else:
             side = 1 << int(np.clip(np.round(rng.uniform(8, 11)), 8, 11))
             key = (2, side)
-        reqs.append((key, int(rng.integers(0, len(pool[key]))), int(rng.integers(100, 5001)),
+        reqs.append((key, int(rng.integers(0, len(pool[key]))) if pool else 0, int(rng.integers(100, 5001)),
                      2 if rng.uniform() < 0.5 else 4))
     srv = q.Server(local, hbm_budget=120 << 30, max_running=256)
 
