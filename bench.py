@@ -208,6 +208,21 @@ def cpu_sample(w, budget_s=15.0):
                 sample=f"{n} O4 step(s) of a {rows}x{ny} slab of the workload (full-length rows), single thread")
 
 
+def world_max(x: float, world: int, device: str = "cuda") -> float:
+    """The maximum of x over the ranks (the slowest rank's time), or x alone."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all ranks processed per second of the slowest rank (weak scaling)."""
+    return units_per_rank * world / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -604,11 +619,8 @@ def main():
     inst.sync()
     prof = ctx.profile_read()
     ctx.profile(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = sites * args.steps * world / (ms / 1e3)
+    ms = world_max(ms, world)
+    value = whole_job_rate(sites * args.steps, world, ms / 1e3)
 
     # dominant kernel and its roofline
     peak, peak_kind = measured_peaks()
@@ -701,11 +713,8 @@ def main():
     e2.get_psi(out.numpy().view(np.complex128).reshape(psi0.shape))
     e2.close()
     el = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([el], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        el = float(t.item())
-    e2e = {"value": sites * args.steps * world / el, "unit": "site-steps/s",
+    el = world_max(el, world)
+    e2e = {"value": whole_job_rate(sites * args.steps, world, el), "unit": "site-steps/s",
            "h2d_bytes_per_step": (psi0.nbytes + V.nbytes) / args.steps,
            "d2h_bytes_per_step": psi0.nbytes / args.steps + 8,
            "includes": "instance creation (H2D psi0+V, phase tables), K x (step + Norm2 read back), "
