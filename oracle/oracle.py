@@ -79,6 +79,15 @@ class Oracle:
         lib.orc_ev2d_new.restype = ctypes.c_void_p
         lib.orc_ev2d_step.argtypes = [ctypes.c_void_p, _dp, _u64]
         lib.orc_ev2d_free.argtypes = [ctypes.c_void_p]
+        lib.orc_born_init1d.argtypes = [_sz, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp, _dp]
+        lib.orc_born_init2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _d, _d, _d, _i, _i, _dp,
+                                        _dp, _dp]
+        lib.orc_born_iter1d.argtypes = [_sz, _d, _d, _d, _d, _d, _i, _i, _i, _d, _dp, _dp, _dp]
+        lib.orc_born_rt1d.argtypes = [_sz, _d, _d, _d, _d, _d, _d, _dp, _dp, _dp, _dp, _dp]
+        lib.orc_born_iter2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _i, _i, _i, _d, _dp, _dp,
+                                        _dp, _dp]
+        lib.orc_born_xsec2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _d, _dp, _dp, _dp, _d, _d]
+        lib.orc_born_xsec2d.restype = _d
         self.lib = lib
 
     def fft1d(self, x, inverse=False):
@@ -145,6 +154,63 @@ class Oracle:
         psi = _c128(psi)
         return self.lib.orc_norm2_range(psi.size, x0, dx, xa, xb, _ptr(psi))
 
+    def born1d(self, V, x0, x1, en, epsilon, direction=1.0, mass=1.0, hbar=1.0, order=1,
+               preconditional=False, preconditioner=1, slow=1.0, computes=1):
+        """QuPerturbation1D: init + ``computes`` Compute() calls.  Returns a dict
+        with dpsi, psi0, v, epsilon, R, T.  preconditioner: 0 identity,
+        1 Vellekoop, 2 Hao1, 3 Hao2."""
+        v = _c128(V).copy()
+        n = v.size
+        dx = (x1 - x0) / n
+        psi0 = np.empty(n, np.complex128)
+        eps = ctypes.c_double(epsilon)
+        rc = self.lib.orc_born_init1d(n, x0, dx, en, direction, mass, hbar, int(preconditional),
+                                      preconditioner, ctypes.byref(eps), _ptr(v), _ptr(psi0))
+        if rc != 0:
+            raise ValueError("world too small for the absorbing layer")
+        dpsi = np.zeros(n, np.complex128)
+        R, T = ctypes.c_double(), ctypes.c_double()
+        for _ in range(computes):
+            assert self.lib.orc_born_iter1d(n, dx, en, eps.value, mass, hbar, order,
+                                            int(preconditional), preconditioner, slow, _ptr(psi0),
+                                            _ptr(v), _ptr(dpsi)) == 0
+            self.lib.orc_born_rt1d(n, x0, dx, en, direction, mass, hbar, _ptr(psi0), _ptr(dpsi),
+                                   _ptr(v), ctypes.byref(R), ctypes.byref(T))
+        return dict(dpsi=dpsi, psi0=psi0, v=v, epsilon=eps.value, R=R.value, T=T.value)
+
+    def born2d(self, V, x0, x1, y0, y1, en, epsilon, dirx=1.0, diry=0.0, mass=1.0, hbar=1.0,
+               order=1, preconditional=False, preconditioner=1, slow=1.0, computes=1,
+               cosxy=(), ntot=0):
+        """QuPerturbation2D: init + ``computes`` Compute() calls; then
+        ComputeXSection for each (cosx, cosy) and ComputeTotalXSection(ntot)."""
+        v = _c128(V).copy()
+        nx, ny = v.shape
+        dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+        psi0 = np.empty((nx, ny), np.complex128)
+        eps = ctypes.c_double(epsilon)
+        rc = self.lib.orc_born_init2d(nx, ny, x0, dx, y0, dy, en, dirx, diry, mass, hbar,
+                                      int(preconditional), preconditioner, ctypes.byref(eps),
+                                      _ptr(v), _ptr(psi0))
+        if rc != 0:
+            raise ValueError("world too small for the absorbing layer")
+        dpsi = np.zeros((nx, ny), np.complex128)
+        dn = ctypes.c_double(0.0)
+        for _ in range(computes):
+            assert self.lib.orc_born_iter2d(nx, ny, dx, dy, en, eps.value, mass, hbar, order,
+                                            int(preconditional), preconditioner, slow, _ptr(psi0),
+                                            _ptr(v), _ptr(dpsi), ctypes.byref(dn)) == 0
+
+        def xs(cx, cy):
+            return self.lib.orc_born_xsec2d(nx, ny, x0, dx, y0, dy, en, mass, hbar, _ptr(psi0),
+                                            _ptr(dpsi), _ptr(v), cx, cy)
+        xsec = [xs(cx, cy) for cx, cy in cosxy]
+        tot = None
+        if ntot > 0:
+            tot = sum(xs(np.cos(i * 2 * np.pi / ntot), np.sin(i * 2 * np.pi / ntot))
+                      for i in range(ntot)) * (2 * np.pi / ntot)
+        return dict(dpsi=dpsi, psi0=psi0, v=v, epsilon=eps.value, delta_norm=dn.value,
+                    xsec=xsec, total=tot)
+
     def splitting_constants(self):
         v = [ctypes.c_double() for _ in range(4)]
         self.lib.orc_splitting_constants(*[ctypes.byref(c) for c in v])
@@ -201,6 +267,11 @@ class Reference:
                                      _dp, _u64, _u64, _dp, _dp, _dp]
         lib.ref_fft1d.argtypes = [_sz, _i, _dp, _dp]
         lib.ref_fft2d.argtypes = [_sz, _sz, _i, _dp, _dp]
+        lib.ref_born1d.argtypes = [_sz, _d, _d, _dp, _d, _d, _d, _d, _d, _i, _i, ctypes.c_char_p,
+                                   _d, _i, _dp, _dp, _dp, _dp]
+        lib.ref_born2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _dp, _d, _d, _d, _d, _d, _d, _i, _i,
+                                   ctypes.c_char_p, _d, _i, _dp, _dp, _dp, _dp, _dp, _i, _dp, _i,
+                                   _dp]
         self.lib = lib
 
     @staticmethod
@@ -245,6 +316,44 @@ class Reference:
                                    *[ctypes.pointer(o) for o in outs])
         assert rc == 0
         return (psi,) + tuple(o.value for o in outs)
+
+    PRECONDITIONERS = (b"BornIndentity", b"Vellekoop", b"Hao1", b"Hao2")
+
+    def born1d(self, V, x0, x1, en, epsilon, direction=1.0, mass=1.0, hbar=1.0, order=1,
+               preconditional=False, preconditioner=1, slow=1.0, computes=1):
+        """The reference's QuPerturbation1DImpl (same arguments and result as
+        Oracle.born1d)."""
+        V = _c128(V)
+        n = V.size
+        dpsi, psi0, v = (np.zeros(n, np.complex128) for _ in range(3))
+        sc = np.zeros(3)
+        prec = self.PRECONDITIONERS[preconditioner] if preconditional else None
+        rc = self.lib.ref_born1d(n, x0, x1, _ptr(V), en, epsilon, direction, mass, hbar, order,
+                                 int(preconditional), prec, slow, computes, _ptr(dpsi), _ptr(psi0),
+                                 _ptr(v), _ptr(sc))
+        if rc != 0:
+            raise ValueError("reference init failed")
+        return dict(dpsi=dpsi, psi0=psi0, v=v, epsilon=sc[2], R=sc[0], T=sc[1])
+
+    def born2d(self, V, x0, x1, y0, y1, en, epsilon, dirx=1.0, diry=0.0, mass=1.0, hbar=1.0,
+               order=1, preconditional=False, preconditioner=1, slow=1.0, computes=1,
+               cosxy=(), ntot=0):
+        V = _c128(V)
+        nx, ny = V.shape
+        dpsi, psi0, v = (np.zeros((nx, ny), np.complex128) for _ in range(3))
+        sc = np.zeros(2)
+        cs = np.ascontiguousarray(np.asarray(cosxy, dtype=np.float64).reshape(-1, 2))
+        xsec = np.zeros(max(len(cs), 1))
+        tot = ctypes.c_double(0.0)
+        prec = self.PRECONDITIONERS[preconditioner] if preconditional else None
+        rc = self.lib.ref_born2d(nx, ny, x0, x1, y0, y1, _ptr(V), en, epsilon, dirx, diry, mass,
+                                 hbar, order, int(preconditional), prec, slow, computes,
+                                 _ptr(dpsi), _ptr(psi0), _ptr(v), _ptr(sc), _ptr(cs), len(cs),
+                                 _ptr(xsec), ntot, ctypes.byref(tot))
+        if rc != 0:
+            raise ValueError("reference init failed")
+        return dict(dpsi=dpsi, psi0=psi0, v=v, epsilon=sc[1], delta_norm=sc[0],
+                    xsec=list(xsec[:len(cs)]), total=tot.value if ntot > 0 else None)
 
 
 def rel_l2(a, b) -> float:

@@ -1,5 +1,6 @@
 /*
- * qusim_oracle.c -- CPU restatement of QuSim's split-operator time evolution.
+ * qusim_oracle.c -- CPU restatement of QuSim's split-operator time evolution
+ * and of its Born-series scattering solvers.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GB300
  * engine: only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline /
@@ -30,6 +31,11 @@
  *   - Norm2 / PotEn / Xavg / Norm2(x0,x1) / Step renormalisation:
  *     src/EvolverImpl.cpp:45-68, src/EvolverImpl1D.cpp:83-102
  *   - k index fold i > N/2 ? N - i : i: src/DeviceTemplate.h:544-547
+ *   - Born-series scattering solvers QuPerturbation1D/2D (naive and
+ *     preconditioned series, absorbing layer, epsilon, R/T, delta-psi norm,
+ *     cross sections): src/Perturbation1DImpl.cpp, src/Perturbation2DImpl.cpp,
+ *     src/Perburbation.h, src/ScatteringSolverImpl.cpp (cited per function
+ *     in the last section of this file)
  */
 #include <complex.h>
 #include <math.h>
@@ -655,4 +661,268 @@ void orc_ev2d_free(void *h)
     if (!h) return;
     ev2d_free((ev2d *)h);
     free(h);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Born-series scattering solvers (QuPerturbation1D / QuPerturbation2D)      */
+/*                                                                          */
+/*   init:   src/Perturbation1DImpl.cpp:7-42, src/Perturbation2DImpl.cpp:4-47, */
+/*           src/ScatteringSolverImpl.cpp:20-38, 68-83, 87-172               */
+/*   layer:  GaussMAsbLayer1D/2D and cal_v15, src/Perburbation.h:47-57,      */
+/*           80-95, 131-148                                                  */
+/*   eps:    PreconditionalBornSeries::GetEpsilon, src/Perburbation.h:326-341 */
+/*   naive:  BornSeries::Update1D/2D, src/Perburbation.h:238-287             */
+/*   precon: PreconditionalBornSeries::Update, src/Perburbation.h:349-417,   */
+/*           ops src/DeviceTemplate.h:1004-1093 (AddMul, Vellekoop, Hao1,    */
+/*           Hao2, Add3), G01D/G02D :881-931, LinearUpdate :532-541          */
+/*   R, T:   ScatteringSolver1DImpl::ComputeRT, ScatteringSolverImpl.cpp:40-55 */
+/*   2D:     Compute's delta-psi norm, src/Perturbation2DImpl.cpp:49-83;     */
+/*           ComputeXSection / ComputeTotalXSection,                         */
+/*           src/ScatteringSolverImpl.cpp:218-266                            */
+/* preconditioner: 0 identity ("BornIndentity"), 1 Vellekoop, 2 Hao1, 3 Hao2 */
+/* ------------------------------------------------------------------------ */
+
+static size_t fold_half_pb(size_t i, size_t n) { return i < n / 2 ? i : n - i; }  /* Perburbation.h:30-33 */
+
+static double cal_v15(double x, double k0, double e0)  /* Perburbation.h:47-57 */
+{
+    x *= k0;
+    const double u = 1 - x * x / (15. * 15);
+    return (-0.8 * e0) * (u > 0 ? exp(-0.015 * x * x * 1. / sqrt(1 - x * x / (15. * 15))) : 0);
+}
+
+/* The reference's CPU reductions are std::transform_reduce with the sequential
+ * policy (src/DeviceTemplate.h:404-407), which libstdc++ evaluates four
+ * elements at a time: init + ((f0 + f1) + (f2 + f3)), then the tail one by
+ * one.  Restated with that pairing so the sums agree to the last bit. */
+#define TR_SUM(n, F)                                                           \
+    ({                                                                         \
+        double acc_ = 0;                                                       \
+        size_t i_ = 0;                                                         \
+        for (; (n) - i_ >= 4; i_ += 4) {                                       \
+            size_t i = i_;                                                     \
+            const double f0_ = (F);                                            \
+            i = i_ + 1;                                                        \
+            const double f1_ = (F);                                            \
+            i = i_ + 2;                                                        \
+            const double f2_ = (F);                                            \
+            i = i_ + 3;                                                        \
+            const double f3_ = (F);                                            \
+            acc_ = acc_ + ((f0_ + f1_) + (f2_ + f3_));                         \
+        }                                                                      \
+        for (; i_ < (n); ++i_) {                                               \
+            size_t i = i_;                                                     \
+            acc_ = acc_ + (F);                                                 \
+        }                                                                      \
+        acc_;                                                                  \
+    })
+
+static double abs2c(cplx z) { return cimag(z) * cimag(z) + creal(z) * creal(z); }  /* op_Abs2 */
+
+/* epsilon actually used by the preconditioned series (GetEpsilon) */
+static double born_min_epsilon(const cplx *v, size_t n, int precer)
+{
+    if (precer == 0) {
+        const double a = TR_SUM(n, cimag(v[i]));
+        const double a2 = TR_SUM(n, abs2c(v[i]));
+        return 0.5 * a2 / (-a);
+    }
+    double m = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const double s = abs2c(v[i]);
+        m = m >= s ? m : s;
+    }
+    return sqrt(m);
+}
+
+/* 1D set-up: psi0 = exp(i dir k0 x_i), absorbing layer and epsilon when
+ * preconditioned.  v_io: n complex in (the sampled potential), out (with the
+ * layer).  Returns 0, or -1 for a world too small for the layer. */
+int orc_born_init1d(size_t n, double x0, double dx, double en, double direction, double mass,
+                    double hbar, int preconditional, int precer, double *eps_io, double *v_io,
+                    double *psi0_out)
+{
+    cplx *v = (cplx *)v_io, *psi0 = (cplx *)psi0_out;
+    const double k0 = sqrt(2 * en * mass) / hbar;
+    const double dir = direction > 0 ? 1 : -1;
+    for (size_t i = 0; i < n; ++i) psi0[i] = cexp(dir * k0 * (x0 + dx * i) * I);
+    if (preconditional) {
+        const double lambda = 2 * kPi / (sqrt(2 * mass * en) / hbar);
+        if (n * dx < 24 * lambda) return -1;
+        const double kk = sqrt(2 * mass * en) / hbar;
+        if (kk * dx * n < 30) return -1;
+        for (size_t i = 0; i < n; ++i)
+            v[i] = CMPLX(creal(v[i]), cimag(v[i]) + cal_v15(fold_half_pb(i, n) * dx, kk, en));
+        const double me = born_min_epsilon(v, n, precer);
+        if (*eps_io < me) *eps_io = me;
+    }
+    return 0;
+}
+
+int orc_born_init2d(size_t nx, size_t ny, double x0, double dx, double y0, double dy, double en,
+                    double dirx, double diry, double mass, double hbar, int preconditional,
+                    int precer, double *eps_io, double *v_io, double *psi0_out)
+{
+    cplx *v = (cplx *)v_io, *psi0 = (cplx *)psi0_out;
+    const double k0 = sqrt(2 * en * mass) / hbar;
+    const double nm = 1 / sqrt(dirx * dirx + diry * diry);
+    const double kx = k0 * (dirx * nm), ky = k0 * (diry * nm);
+    for (size_t i = 0; i < nx; ++i)
+        for (size_t j = 0; j < ny; ++j)
+            psi0[i * ny + j] = cexp((kx * (x0 + dx * i) + ky * (y0 + dy * j)) * I);
+    if (preconditional) {
+        const double lambda = 2 * kPi / (sqrt(2 * mass * en) / hbar);
+        if (nx * dx < 24 * lambda || ny * dy < 24 * lambda) return -1;
+        const double kk = sqrt(2 * mass * en) / hbar;
+        for (size_t i = 0; i < nx; ++i)
+            for (size_t j = 0; j < ny; ++j) {
+                const size_t k = i * ny + j;
+                v[k] = CMPLX(creal(v[k]), cimag(v[k]) + (cal_v15(fold_half_pb(i, nx) * dx, kk, en) +
+                                                         cal_v15(fold_half_pb(j, ny) * dy, kk, en)));
+            }
+        const double me = born_min_epsilon(v, nx * ny, precer);
+        if (*eps_io < me) *eps_io = me;
+    }
+    return 0;
+}
+
+/* tmp <- (Re v + i (Im v + eps)) dpsi + Re v psi0 (op_Add3) or
+ * dpsi <- (dpsi + psi0) v (op_AddMul) */
+static void born_pre(size_t n, int preconditional, double eps, const cplx *psi0, const cplx *v,
+                     const cplx *dpsi, cplx *out)
+{
+    for (size_t i = 0; i < n; ++i) {
+        if (preconditional)
+            out[i] = CMPLX(creal(v[i]), cimag(v[i]) + eps) * dpsi[i] + creal(v[i]) * psi0[i];
+        else
+            out[i] = (dpsi[i] + psi0[i]) * v[i];
+    }
+}
+
+/* the update after the transform pair; tmp already carries 1/N */
+static void born_post(size_t n, int precer, double slow, double eps, const cplx *v, const cplx *tmp,
+                      cplx *dpsi)
+{
+    for (size_t i = 0; i < n; ++i) {
+        if (precer == 0) {
+            dpsi[i] = slow == 1. ? tmp[i] : dpsi[i] * (1 - slow) + tmp[i] * slow;
+            continue;
+        }
+        cplx g;
+        const cplx iv = CMPLX(-cimag(v[i]), creal(v[i]));          /* i v */
+        const cplx ivc = CMPLX(cimag(v[i]), creal(v[i]));          /* i conj(v) */
+        if (precer == 1) g = 1. - iv / eps;
+        else if (precer == 2) g = 1. - ivc / eps;
+        else g = CMPLX(2., 0.) / (1. + iv / eps);
+        g *= slow;
+        dpsi[i] = (1. - g) * dpsi[i] + g * tmp[i];
+    }
+}
+
+/* `order` iterations of the naive or the preconditioned series on dpsi_io */
+int orc_born_iter1d(size_t n, double dx, double en, double eps, double mass, double hbar, int order,
+                    int preconditional, int precer, double slow, const double *psi0_in,
+                    const double *v_in, double *dpsi_io)
+{
+    const cplx *psi0 = (const cplx *)psi0_in, *v = (const cplx *)v_in;
+    cplx *dpsi = (cplx *)dpsi_io;
+    fft_plan fwd, inv;
+    if (plan_init(&fwd, n, 0)) return -1;
+    if (plan_init(&inv, n, 1)) { plan_free(&fwd); return -1; }
+    cplx *a = (cplx *)malloc(sizeof(cplx) * n), *k = (cplx *)malloc(sizeof(cplx) * n);
+    const double dp = 2 * kPi / (dx * n) * hbar, d = dp * dp / (2 * mass);
+    for (int it = 0; it < order; ++it) {
+        born_pre(n, preconditional, eps, psi0, v, dpsi, a);
+        plan_exec(&fwd, a, k);
+        for (size_t i = 0; i < n; ++i) {
+            const double f = (double)fold_half(i, n);
+            k[i] = k[i] / CMPLX(en - f * f * d, eps);
+            k[i] = CMPLX(creal(k[i]) * (1. / n), cimag(k[i]) * (1. / n));
+        }
+        plan_exec(&inv, k, a);
+        if (preconditional) born_post(n, precer, slow, eps, v, a, dpsi);
+        else memcpy(dpsi, a, sizeof(cplx) * n);
+    }
+    free(a); free(k);
+    plan_free(&fwd); plan_free(&inv);
+    return 0;
+}
+
+/* R and T (ComputeRT) */
+void orc_born_rt1d(size_t n, double x0, double dx, double en, double direction, double mass, double hbar,
+                   const double *psi0_in, const double *dpsi_in, const double *v_in, double *R, double *T)
+{
+    const cplx *psi0 = (const cplx *)psi0_in, *dpsi = (const cplx *)dpsi_in, *v = (const cplx *)v_in;
+    const double k0 = sqrt(2 * en * mass) / hbar;
+    const double dir = direction > 0 ? 1 : -1;
+    cplx r = 0, t = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const double x = x0 + dx * i;
+        r += (psi0[i] + dpsi[i]) * creal(v[i]) * cexp(I * (-dir * k0) * (-x));
+        t += (psi0[i] + dpsi[i]) * creal(v[i]) * cexp(I * (+dir * k0) * (-x));
+    }
+    const cplx f = dx * mass / (hbar * hbar * fabs(k0) * I);
+    const cplx rr = r * f, tt = t * f + 1;
+    *R = creal(rr) * creal(rr) + cimag(rr) * cimag(rr);
+    *T = creal(tt) * creal(tt) + cimag(tt) * cimag(tt);
+}
+
+/* 2D: `order` iterations (2D transforms as orc_fft2d) and the delta-psi norm
+ * sqrt(sum |psi - psi_start|^2 / sum |psi|^2) */
+int orc_born_iter2d(size_t nx, size_t ny, double dx, double dy, double en, double eps, double mass,
+                    double hbar, int order, int preconditional, int precer, double slow,
+                    const double *psi0_in, const double *v_in, double *dpsi_io, double *delta_norm)
+{
+    const size_t n = nx * ny;
+    const cplx *psi0 = (const cplx *)psi0_in, *v = (const cplx *)v_in;
+    cplx *dpsi = (cplx *)dpsi_io;
+    fft_plan fx, fy, ix, iy;
+    if (plan_init(&fx, nx, 0) || plan_init(&fy, ny, 0) || plan_init(&ix, nx, 1) || plan_init(&iy, ny, 1))
+        return -1;
+    cplx *a = (cplx *)malloc(sizeof(cplx) * n), *k = (cplx *)malloc(sizeof(cplx) * n);
+    cplx *last = (cplx *)malloc(sizeof(cplx) * n);
+    cplx *ci = (cplx *)malloc(sizeof(cplx) * nx), *co = (cplx *)malloc(sizeof(cplx) * nx);
+    memcpy(last, dpsi, sizeof(cplx) * n);
+    const double dpx = 2 * kPi / (dx * nx) * hbar, ddx = dpx * dpx / (2 * mass);
+    const double dpy = 2 * kPi / (dy * ny) * hbar, ddy = dpy * dpy / (2 * mass);
+    for (int it = 0; it < order; ++it) {
+        born_pre(n, preconditional, eps, psi0, v, dpsi, a);
+        fft2d_exec(&fx, &fy, nx, ny, a, k, ci, co);
+        for (size_t i = 0; i < nx; ++i)
+            for (size_t j = 0; j < ny; ++j) {
+                const double fi = (double)fold_half(i, nx), fj = (double)fold_half(j, ny);
+                const double t = fi * fi * ddx + fj * fj * ddy;
+                cplx *p = &k[i * ny + j];
+                *p = *p / CMPLX(en - t, eps);
+                *p = CMPLX(creal(*p) * (1. / n), cimag(*p) * (1. / n));
+            }
+        fft2d_exec(&ix, &iy, nx, ny, k, a, ci, co);
+        if (preconditional) born_post(n, precer, slow, eps, v, a, dpsi);
+        else memcpy(dpsi, a, sizeof(cplx) * n);
+    }
+    const double num = TR_SUM(n, abs2c(dpsi[i] - last[i]));  /* MinusNorm2 */
+    const double den = TR_SUM(n, abs2c(dpsi[i]));
+    *delta_norm = sqrt(num / den);
+    free(a); free(k); free(last); free(ci); free(co);
+    plan_free(&fx); plan_free(&fy); plan_free(&ix); plan_free(&iy);
+    return 0;
+}
+
+double orc_born_xsec2d(size_t nx, size_t ny, double x0, double dx, double y0, double dy, double en,
+                       double mass, double hbar, const double *psi0_in, const double *dpsi_in,
+                       const double *v_in, double cosx, double cosy)
+{
+    const cplx *psi0 = (const cplx *)psi0_in, *dpsi = (const cplx *)dpsi_in, *v = (const cplx *)v_in;
+    const double k0 = sqrt(2 * en * mass) / hbar;
+    const double nm = 1 / sqrt(cosx * cosx + cosy * cosy);
+    const double kx = k0 * (cosx * nm), ky = k0 * (cosy * nm);
+    cplx r = 0;
+    for (size_t i = 0; i < nx; ++i)
+        for (size_t j = 0; j < ny; ++j) {
+            const size_t idx = i * ny + j;
+            const double x = x0 + dx * i, y = y0 + dy * j;
+            r += (psi0[idx] + dpsi[idx]) * creal(v[idx]) * cexp(-I * (kx * x + ky * y));
+        }
+    const cplx s = r * (2 * mass) / (hbar * hbar) * dx * dy * (1. / 4);
+    return (creal(s) * creal(s) + cimag(s) * cimag(s)) * (2 / (kPi * k0));
 }

@@ -1,5 +1,5 @@
-// Thin extern "C" driver over the reference's own SplittingMethod1D/2D,
-// compiled from the reference sources in place (oracle/Makefile).  It is the
+// Thin extern "C" driver over the reference's own SplittingMethod1D/2D and
+// Born-series solvers QuPerturbation1DImpl/2DImpl, compiled from the reference sources in place (oracle/Makefile).  It is the
 // "reference" leg of the oracle: it validates the C restatement
 // (oracle/qusim_oracle.c) and times the reference's CPU path.  Test
 // infrastructure only.
@@ -10,6 +10,8 @@
 // "batch" = the number of steps requested.
 #include "SplittingMethod1D.h"
 #include "SplittingMethod2D.h"
+#include "Perturbation1DImpl.h"
+#include "Perturbation2DImpl.h"
 #include "OptionsImpl.h"
 #include <cmath>
 #include <cstdint>
@@ -122,6 +124,86 @@ int ref_fft2d(size_t nx, size_t ny, int inverse, const double *in, double *out)
     try {
         std::unique_ptr<FourierTransform2D> f(FourierTransform2D::Create(nx, ny, inverse != 0, FourierTransformLibrary::KISS));
         f->Transform((const Complex *)in, (Complex *)out);
+        return 0;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
+// Born-series scattering solvers, driven as QuPerturbation1D/2D::init and
+// Compute() drive them (src/QuSim.cpp:499-505, 620-630): the impl's
+// InitPerturbation1D/2D (src/Perturbation1DImpl.cpp:7-42,
+// src/Perturbation2DImpl.cpp:4-47) then `computes` Compute() calls.
+// V: n complex (re,im) sampled at the grid points.  Outputs (each may be
+// null): dpsi (the scattered part fPsiX), psi0, v (after the absorbing layer
+// the preconditioned series adds), scal[0..2] = R, T, epsilon in use (1D) or
+// delta-psi norm, epsilon in use (2D).  prec: null = the options' default.
+static void born_opts(OptionsImpl &opts, int order, int preconditional, const char *prec, double slow)
+{
+    opts.SetInt("order", (Int)order);
+    opts.SetReal("slow", slow);
+    // OptionsImpl::GetBool(key, default) (src/OptionsImpl.cpp:88-91) returns
+    // whether the key is present, not its value, so the key is set only when
+    // the preconditioned series is wanted
+    if (preconditional) opts.SetBool("preconditional", true);
+    if (prec) opts.SetString("preconditioner", prec);
+}
+
+int ref_born1d(size_t n, double x0, double x1, const double *V, double en, double epsilon,
+               double direction, double mass, double hbar, int order, int preconditional,
+               const char *prec, double slow, int computes, double *dpsi, double *psi0,
+               double *v, double *scal)
+{
+    try {
+        OptionsImpl opts;
+        born_opts(opts, order, preconditional, prec, slow);
+        QuPerturbation1DImpl impl;
+        const double dx = (x1 - x0) / n;
+        Grid1 gv{x0, dx, n, V, nullptr};
+        impl.InitPerturbation1D(gv, x0, x1, n, en, epsilon, direction, SolverMethod::BornSerise,
+                                mass, hbar, opts);
+        for (int c = 0; c < computes; ++c) impl.Compute();
+        if (dpsi) std::memcpy(dpsi, impl.fPsiX, sizeof(double) * 2 * n);
+        if (psi0) std::memcpy(psi0, impl.fPsi0X, sizeof(double) * 2 * n);
+        if (v) std::memcpy(v, impl.fV, sizeof(double) * 2 * n);
+        if (scal) {
+            scal[0] = impl.fR;
+            scal[1] = impl.fT;
+            scal[2] = impl.fEpsilon;
+        }
+        return 0;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
+// xsec: ncos (cosx, cosy) pairs in, ComputeXSection of each out (after the
+// last Compute); tot: ComputeTotalXSection(ntot) when ntot > 0.
+int ref_born2d(size_t nx, size_t ny, double x0, double x1, double y0, double y1, const double *V,
+               double en, double epsilon, double dirx, double diry, double mass, double hbar,
+               int order, int preconditional, const char *prec, double slow, int computes,
+               double *dpsi, double *psi0, double *v, double *scal, const double *cosxy,
+               int ncos, double *xsec, int ntot, double *tot)
+{
+    try {
+        OptionsImpl opts;
+        born_opts(opts, order, preconditional, prec, slow);
+        QuPerturbation2DImpl impl;
+        const double dx = (x1 - x0) / nx, dy = (y1 - y0) / ny;
+        Grid2 gv{x0, dx, y0, dy, nx, ny, V, nullptr};
+        impl.InitPerturbation2D(gv, x0, x1, nx, y0, y1, ny, en, epsilon, dirx, diry,
+                                SolverMethod::BornSerise, mass, hbar, opts);
+        for (int c = 0; c < computes; ++c) impl.Compute();
+        const size_t n = nx * ny;
+        if (dpsi) std::memcpy(dpsi, impl.fPsiX, sizeof(double) * 2 * n);
+        if (psi0) std::memcpy(psi0, impl.fPsi0X, sizeof(double) * 2 * n);
+        if (v) std::memcpy(v, impl.fV, sizeof(double) * 2 * n);
+        if (scal) {
+            scal[0] = impl.fNormDeltaPsi;
+            scal[1] = impl.fEpsilon;
+        }
+        for (int i = 0; i < ncos; ++i) xsec[i] = impl.ComputeXSection(cosxy[2 * i], cosxy[2 * i + 1]);
+        if (ntot > 0 && tot) *tot = impl.ComputeTotalXSection(ntot);
         return 0;
     } catch (std::exception &) {
         return -1;

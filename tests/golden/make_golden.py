@@ -1,6 +1,7 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Runs the reference's own SplittingMethod1D/2D and KISS FourierTransform,
+Runs the reference's own SplittingMethod1D/2D, KISS FourierTransform and
+Born-series solvers (QuPerturbation1DImpl/2DImpl),
 compiled from its sources by ``make -C oracle ref`` (oracle/_ref), on seeded
 inputs and stores inputs + outputs as .npz.  The reference tree is needed
 only here; the committed fixtures travel without it.
@@ -19,7 +20,9 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as orc  # noqa: E402
-from tests.workloads import gauss_packet_1d, gauss_packet_2d, gaussian_bumps_2d  # noqa: E402
+from tests.workloads import (BORN_1D_CASES, BORN_2D_CASES, BORN_XSEC_TOTAL,  # noqa: E402
+                             born_potential_1d, born_potential_2d, gauss_packet_1d,
+                             gauss_packet_2d, gaussian_bumps_2d, xsec_cosines)
 
 
 def save(name, **arrays):
@@ -74,6 +77,26 @@ def main():
         save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
              params=np.array([nx, ny, x0, x1, y0, y1, order, batch, calls, int(fnes)], dtype=np.float64),
              dt=np.complex128(dt))
+
+    # Born-series scattering, 1D and 2D (tests/workloads.py BORN_*_CASES)
+    for (name, n, x0, x1, v0, en, eps, direction, order, pre, precer, slow,
+         computes) in BORN_1D_CASES:
+        V, _ = born_potential_1d(n, x0, x1, v0)
+        r = ref.born1d(V, x0, x1, en, eps, direction=direction, order=order, preconditional=pre,
+                       preconditioner=precer, slow=slow, computes=computes)
+        save(name, dpsi=r["dpsi"], psi0=r["psi0"], v=r["v"], epsilon=r["epsilon"],
+             R=r["R"], T=r["T"])
+    cs = xsec_cosines()
+    for (name, nx, ny, hx, hy, en, eps, dirx, diry, order, pre, precer, slow,
+         computes) in BORN_2D_CASES:
+        V, _, _ = born_potential_2d(nx, ny, -hx, hx, -hy, hy)
+        r = ref.born2d(V, -hx, hx, -hy, hy, en, eps, dirx=dirx, diry=diry, order=order,
+                       preconditional=pre, preconditioner=precer, slow=slow, computes=computes,
+                       cosxy=cs, ntot=BORN_XSEC_TOTAL)
+        # psi0 and v by their sums (V is regenerated from the workload)
+        save(name, dpsi=r["dpsi"], psi0_sum=r["psi0"].sum(), v_sum=r["v"].sum(),
+             epsilon=r["epsilon"], delta_norm=r["delta_norm"], xsec=np.array(r["xsec"]),
+             total=r["total"])
 
 
 if __name__ == "__main__":

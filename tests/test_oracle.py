@@ -104,3 +104,50 @@ def test_group_velocity(oracle):
     xa = oracle.xavg(psi, x0, dx)
     p = oracle.evolve1d(psi, np.zeros(n), dx, dt, 11, order=2)
     assert abs((oracle.xavg(p, x0, dx) - xa) / (11 * dt) - 1) < 1e-10
+
+
+# --- Born-series scattering solvers -------------------------------------------
+
+from tests.workloads import (BORN_1D_CASES, BORN_2D_CASES, BORN_XSEC_TOTAL,  # noqa: E402
+                             born_potential_1d, born_potential_2d, xsec_cosines)
+
+
+@pytest.mark.parametrize("case", BORN_1D_CASES, ids=[c[0] for c in BORN_1D_CASES])
+def test_born1d_matches_reference(oracle, case):
+    """QuPerturbation1D: naive and preconditioned series (each preconditioner),
+    several Compute() calls, a left-going wave and a grid that is not a power
+    of two."""
+    name, n, x0, x1, v0, en, eps, direction, order, pre, precer, slow, computes = case
+    g = load_golden(name)
+    V, _ = born_potential_1d(n, x0, x1, v0)
+    r = oracle.born1d(V, x0, x1, en, eps, direction=direction, order=order, preconditional=pre,
+                      preconditioner=precer, slow=slow, computes=computes)
+    assert np.array_equal(r["psi0"], g["psi0"])
+    assert np.array_equal(r["v"], g["v"])
+    assert abs(r["epsilon"] - g["epsilon"]) <= 1e-15 * abs(g["epsilon"])
+    assert rel_l2(r["dpsi"], g["dpsi"]) <= 1e-14
+    assert abs(r["R"] - g["R"]) <= 1e-14 and abs(r["T"] - g["T"]) <= 1e-14
+
+
+@pytest.mark.parametrize("case", BORN_2D_CASES, ids=[c[0] for c in BORN_2D_CASES])
+def test_born2d_matches_reference(oracle, case):
+    name, nx, ny, hx, hy, en, eps, dirx, diry, order, pre, precer, slow, computes = case
+    g = load_golden(name)
+    V, _, _ = born_potential_2d(nx, ny, -hx, hx, -hy, hy)
+    r = oracle.born2d(V, -hx, hx, -hy, hy, en, eps, dirx=dirx, diry=diry, order=order,
+                      preconditional=pre, preconditioner=precer, slow=slow, computes=computes,
+                      cosxy=xsec_cosines(), ntot=BORN_XSEC_TOTAL)
+    assert r["psi0"].sum() == g["psi0_sum"] and r["v"].sum() == g["v_sum"]
+    assert abs(r["epsilon"] - g["epsilon"]) <= 1e-15 * abs(g["epsilon"])
+    assert rel_l2(r["dpsi"], g["dpsi"]) <= 1e-14
+    assert abs(r["delta_norm"] - g["delta_norm"]) <= 1e-13 * g["delta_norm"]
+    assert np.allclose(r["xsec"], g["xsec"], rtol=1e-13, atol=0)
+    assert abs(r["total"] - g["total"]) <= 1e-13 * g["total"]
+
+
+def test_born_layer_refuses_small_world(oracle):
+    """The preconditioned series needs a box of at least 24 wavelengths
+    (src/Perturbation1DImpl.cpp:24-27, src/Perturbation2DImpl.cpp:25-31)."""
+    V, _ = born_potential_1d(256, -10.0, 10.0, 0.5)
+    with pytest.raises(ValueError):
+        oracle.born1d(V, -10.0, 10.0, 0.5, 0.0, order=1, preconditional=True)

@@ -111,3 +111,55 @@ def batch_1d(count=2048, emin=10, emax=17, seed=0):
         Vs.append(gaussian_bumps_1d(xs, 8, rng, -half, half))
         dxs.append(dx)
     return psis, Vs, dxs
+
+
+# --- Born-series scattering ---------------------------------------------------
+
+# (name, n, x0, x1, v0, en, epsilon, direction, order, preconditional,
+#  preconditioner (0 identity, 1 Vellekoop, 2 Hao1, 3 Hao2), slow, computes);
+# potential v0 exp(-x^2), the one of applications/QuScattering1DPrecision
+# (QuScattering1DPrecision.cpp:180-221), on power-of-two grids
+BORN_1D_CASES = [
+    ("born1d_n2048_naive_o3_c2", 2048, -100.0, 100.0, 0.5, 0.5, 0.01, 1.0, 3, False, 1, 1.0, 2),
+    ("born1d_n2048_vellekoop_o5", 2048, -100.0, 100.0, 0.5, 0.5, 0.51, 1.0, 5, True, 1, 1.0, 1),
+    ("born1d_n2048_hao1_o10_s05", 2048, -100.0, 100.0, 0.5, 0.5, 0.0, 1.0, 10, True, 2, 0.5, 1),
+    ("born1d_n2048_hao2_o10_s07_left", 2048, -100.0, 100.0, 0.5, 0.5, 0.0, -1.0, 10, True, 3, 0.7, 1),
+    ("born1d_n2048_identity_o10_s05", 2048, -100.0, 100.0, 0.5, 0.5, 0.0, 1.0, 10, True, 0, 0.5, 1),
+    ("born1d_n2048_identity_o10_s1", 2048, -100.0, 100.0, 0.5, 0.5, 0.0, 1.0, 10, True, 0, 1.0, 1),
+    ("born1d_n1000_vellekoop_o5", 1000, -100.0, 100.0, 1.0, 0.5, 0.0, 1.0, 5, True, 1, 1.0, 1),
+]
+
+# (name, nx, ny, hx, hy, en, epsilon, dirx, diry, order, preconditional,
+#  preconditioner, slow, computes)
+BORN_2D_CASES = [
+    ("born2d_128x64_naive_o2", 128, 64, 60.0, 45.0, 0.5, 0.1, 1.0, 0.0, 2, False, 1, 1.0, 1),
+    ("born2d_128x128_vellekoop_o4_c2", 128, 128, 60.0, 45.0, 2.0, 0.0, 1.0, 0.5, 4, True, 1, 1.0, 2),
+    ("born2d_64x128_hao2_o3_s05", 64, 128, 45.0, 60.0, 2.0, 0.0, 0.0, 1.0, 3, True, 3, 0.5, 1),
+    ("born2d_128x128_identity_o3", 128, 128, 40.0, 40.0, 2.0, 0.0, 1.0, 1.0, 3, True, 0, 1.0, 1),
+]
+
+BORN_XSEC_ANGLES = 8      # ComputeXSection at theta = 2 pi i / 8
+BORN_XSEC_TOTAL = 16      # ComputeTotalXSection(16)
+
+
+def born_potential_1d(n, x0, x1, v0):
+    """v0 exp(-x^2) sampled at x_i = x0 + i dx (complex, as the functor returns)."""
+    xs, dx = grid(n, x0, x1)
+    return (v0 * np.exp(-xs * xs)).astype(np.complex128), dx
+
+
+def born_potential_2d(nx, ny, x0, x1, y0, y1, v0=0.3, seed=0):
+    """A Gaussian well v0 exp(-(x^2+y^2)/4) plus a weak seeded absorbing
+    imaginary part (complex, as the functor returns)."""
+    xs, dx = grid(nx, x0, x1)
+    ys, dy = grid(ny, y0, y1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-5, 5, size=2)
+    V = v0 * np.exp(-(X * X + Y * Y) / 4) - 0.02j * np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2) / 8)
+    return V.astype(np.complex128), dx, dy
+
+
+def xsec_cosines(count=BORN_XSEC_ANGLES):
+    th = 2 * np.pi * np.arange(count) / count
+    return np.stack([np.cos(th), np.sin(th)], axis=1)
