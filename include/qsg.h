@@ -273,6 +273,73 @@ int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launch
 int qsg_norm2_noalloc(const void *psi, uint64_t n, int precision, double dv, void *stream,
                       double *out);
 
+/* ------------------------------------------------------------------------
+ * Born-series scattering solvers: QuPerturbation1D / QuPerturbation2D
+ * (include/QuSim.h:689-806; src/Perturbation1DImpl.cpp, src/Perturbation2DImpl.cpp,
+ * src/Perburbation.h, src/ScatteringSolverImpl.cpp).  A solver holds the
+ * incident wave psi0 = exp(i k0 d.r) (k0 = sqrt(2 m E) / hbar, d the unit
+ * direction), the potential V (complex, as the reference's functor returns
+ * it) and the scattered part psi of the wave function; each qsg_born_compute
+ * runs `order` updates of the naive or the preconditioned series on psi.
+ * Grids: 1D n a power of two, 128 .. 2^22; 2D nx, ny powers of two,
+ * 64 .. 4096 (other sizes: QSG_ERR_UNSUPPORTED).
+ * ------------------------------------------------------------------------ */
+typedef struct qsg_born qsg_born;
+
+/* the "preconditioner" option values (src/PerturbationOptions.cpp:15-31);
+ * QSG_BORN_IDENTITY is the reference's "BornIndentity" */
+typedef enum {
+    QSG_BORN_IDENTITY = 0,
+    QSG_BORN_VELLEKOOP = 1,
+    QSG_BORN_HAO1 = 2,
+    QSG_BORN_HAO2 = 3
+} qsg_born_preconditioner;
+
+/* the reference's Options keys for these solvers (PerturbationCommon,
+ * src/PerturbationOptions.cpp:8-43); qsg_born_default_opts gives its defaults */
+typedef struct {
+    int order;           /* "order": updates per compute (default 1; >= 1 here)          */
+    int preconditional;  /* "preconditional": 0 naive series, 1 preconditioned          */
+    int preconditioner;  /* "preconditioner" (default QSG_BORN_VELLEKOOP)                */
+    double slow;         /* "slow" (default 1)                                           */
+} qsg_born_opts;
+void qsg_born_default_opts(qsg_born_opts *opts);
+
+/* QuPerturbation1D::init (src/Perturbation1DImpl.cpp:7-42): grid x_i = x0 + i dx,
+ * dx = (x1 - x0) / n; V: n complex (re, im) sampled there; en the energy;
+ * epsilon the i eps of the Green's function (raised to the preconditioner's
+ * minimum when preconditioned); direction > 0 right-going, else left-going.
+ * The preconditioned series adds the reference's absorbing layer to Im V and
+ * needs a box of at least 24 wavelengths (QSG_ERR_ARG otherwise). */
+int qsg_born_create_1d(qsg_ctx *ctx, uint64_t n, double x0, double x1, const double *V, double en,
+                       double epsilon, double direction, double mass, double hbar,
+                       const qsg_born_opts *opts, int precision, qsg_born **out);
+/* QuPerturbation2D::init (src/Perturbation2DImpl.cpp:4-47): V nx*ny complex,
+ * index iy + ix*ny; (dirx, diry) the incident direction (normalised here). */
+int qsg_born_create_2d(qsg_ctx *ctx, int nx, int ny, double x0, double x1, double y0, double y1,
+                       const double *V, double en, double epsilon, double dirx, double diry,
+                       double mass, double hbar, const qsg_born_opts *opts, int precision,
+                       qsg_born **out);
+/* Compute(): `order` updates; then (1D) R and T, (2D) the delta-psi norm.
+ * Queued on the context's stream; the results below wait for it. */
+int qsg_born_compute(qsg_born *b);
+/* GetPsi / GetPsi0 / GetV: what = QSG_BORN_PSI (the scattered part), QSG_BORN_PSI0
+ * or QSG_BORN_V (with the absorbing layer); out: n complex (re, im). */
+typedef enum { QSG_BORN_PSI = 0, QSG_BORN_PSI0 = 1, QSG_BORN_V = 2 } qsg_born_field;
+int qsg_born_get(qsg_born *b, int what, double *out);
+/* GetR / GetT (1D), after a compute (ScatteringSolver1DImpl::ComputeRT) */
+int qsg_born_rt(qsg_born *b, double *R, double *T);
+/* GetDeltaPsiNorm (2D): sqrt(sum |psi - psi_before|^2 / sum |psi|^2) of the last compute */
+int qsg_born_delta_norm(qsg_born *b, double *out);
+/* GetEpsilon: the epsilon in use */
+int qsg_born_epsilon(qsg_born *b, double *out);
+/* ComputeXSection (2D) for `count` directions cosxy[2*i], cosxy[2*i+1]: out[i] */
+int qsg_born_xsection(qsg_born *b, int count, const double *cosxy, double *out);
+/* ComputeTotalXSection(n) (2D): sum over theta_i = 2 pi i / n of the
+ * cross section, times 2 pi / n */
+int qsg_born_total_xsection(qsg_born *b, int n, double *out);
+void qsg_born_destroy(qsg_born *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,8 +3,10 @@ GPU_GB300 device for QuSim's SplittingMethod1D/2D (O2, O4).
 
 The engine is libqsg.so (C ABI, include/qsg.h); this package holds its
 sources (csrc/), its build (build.py) and a Python mirror of the reference's
-Evolver/Options API (evolver.py).
+Evolver/Options API (evolver.py) and of its Born-series scattering solvers
+QuPerturbation1D/2D (born.py).
 """
 from ._lib import QsgError, Spec, load  # noqa: F401
 from .evolver import (Batch, BoundaryCondition, Context, Evolver1D, Evolver2D, Instance,  # noqa: F401
                       Options, Server, SolverMethod, default_context)
+from .born import QuPerturbation1D, QuPerturbation2D  # noqa: F401

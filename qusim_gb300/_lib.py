@@ -37,7 +37,14 @@ EXPORTS = [
     "qsg_batch_instance", "qsg_batch_destroy", "qsg_server_create", "qsg_server_submit",
     "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_destroy",
     "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc", "qsg_create_1d_spec", "qsg_create_2d_spec",
+    "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
+    "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
+    "qsg_born_destroy",
 ]
+
+# qsg_born_preconditioner / qsg_born_field
+QSG_BORN_IDENTITY, QSG_BORN_VELLEKOOP, QSG_BORN_HAO1, QSG_BORN_HAO2 = 0, 1, 2, 3
+QSG_BORN_PSI, QSG_BORN_PSI0, QSG_BORN_V = 0, 1, 2
 
 
 SPEC_MAX_BUMPS = 32
@@ -93,6 +100,12 @@ class Plan2D(ctypes.Structure):
     def __repr__(self):
         return (f"Plan2D(g={self.g}, row_e={self.row_e}, row_nt={self.row_nt}, col_e={self.col_e}, "
                 f"col_w={self.col_w}, row_kind={self.row_kind})")
+
+
+class BornOpts(ctypes.Structure):
+    """qsg_born_opts: the order / preconditional / preconditioner / slow options."""
+    _fields_ = [("order", ctypes.c_int), ("preconditional", ctypes.c_int), ("preconditioner", ctypes.c_int),
+                ("slow", ctypes.c_double)]
 
 
 class QsgError(RuntimeError):
@@ -164,6 +177,21 @@ def _declare(lib):
     lib.qsg_profile_enable.argtypes = [_vp, _i]
     lib.qsg_profile_read.argtypes = [_vp, _i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_u64), _dp]
     lib.qsg_norm2_noalloc.argtypes = [_vp, _u64, _i, _d, _vp, _dp]
+    lib.qsg_born_default_opts.argtypes = [ctypes.POINTER(BornOpts)]
+    lib.qsg_born_default_opts.restype = None
+    lib.qsg_born_create_1d.argtypes = [_vp, _u64, _d, _d, _dp, _d, _d, _d, _d, _d, ctypes.POINTER(BornOpts), _i,
+                                       ctypes.POINTER(_vp)]
+    lib.qsg_born_create_2d.argtypes = [_vp, _i, _i, _d, _d, _d, _d, _dp, _d, _d, _d, _d, _d, _d,
+                                       ctypes.POINTER(BornOpts), _i, ctypes.POINTER(_vp)]
+    lib.qsg_born_compute.argtypes = [_vp]
+    lib.qsg_born_get.argtypes = [_vp, _i, _dp]
+    lib.qsg_born_rt.argtypes = [_vp, _dp, _dp]
+    lib.qsg_born_delta_norm.argtypes = [_vp, _dp]
+    lib.qsg_born_epsilon.argtypes = [_vp, _dp]
+    lib.qsg_born_xsection.argtypes = [_vp, _i, _dp, _dp]
+    lib.qsg_born_total_xsection.argtypes = [_vp, _i, _dp]
+    lib.qsg_born_destroy.argtypes = [_vp]
+    lib.qsg_born_destroy.restype = None
 
 
 def load(path: str = LIB_PATH):

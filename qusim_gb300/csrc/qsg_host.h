@@ -1,0 +1,208 @@
+// qsg_host.h -- host-side context and helpers shared by the C-ABI units
+// (qsg_api.cu: evolvers and serving; qsg_born_api.cu: Born-series solvers):
+// the context struct, error reporting, budgeted device allocation, twiddle
+// tables and launch profiling.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/qsg.h"
+#include "qsg_launch.h"
+
+namespace qsg_host {
+
+using qsg::Plan2D;
+
+inline thread_local std::string g_last_error;
+
+inline int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define QSG_CUDA(call)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ == cudaErrorNotSupported)                                                   \
+            return fail(QSG_ERR_UNSUPPORTED, std::string("unsupported size: ") + #call);   \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(QSG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+inline constexpr double kPi = 3.141592653589793238462643383279502884197169399375;
+
+struct ProfStat {
+    uint64_t launches = 0;
+    double total_ms = 0;
+};
+
+}  // namespace qsg_host
+
+struct qsg_ctx {
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    size_t budget = 0, in_use = 0;
+    std::mutex mu;
+    std::map<std::tuple<int, int, int>, void *> tw_cache;  // (prec, L, E) -> stage-major twiddles
+    std::map<std::pair<int, int>, void *> circle_cache;    // (prec, n) -> exp(-2 pi i m/n)
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    double *partials = nullptr;  // reduction partials
+    int max_partials = 0;
+    double *sums = nullptr;      // small device result buffer
+    double *host_sums = nullptr; // pinned mirror
+    int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
+    std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> prof_pending;
+    std::vector<cudaEvent_t> event_pool;
+    std::map<std::string, qsg_host::ProfStat> prof_stats;
+    std::vector<std::string> prof_names;  // stable storage for returned names
+    std::string device_name;
+    std::map<std::tuple<int, int, int>, qsg::Plan2D> plans;  // tuned plans: (prec, nx, ny) -> plan
+    bool plans_loaded = false;
+};
+
+namespace qsg_host {
+
+inline size_t csize(int prec) { return prec == 1 ? 8 : 16; }
+
+// Allocate device memory.  Instance memory, twiddle tables and scratch count
+// against the context's HBM budget; the context's own fixed buffers (budgeted
+// = false) do not.
+inline int dev_alloc(qsg_ctx *ctx, size_t bytes, void **p, size_t *acct, bool budgeted = true)
+{
+    if (budgeted && ctx->budget && ctx->in_use + bytes > ctx->budget)
+        return fail(QSG_ERR_BUDGET, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
+                                        std::to_string(ctx->budget - ctx->in_use) + " left");
+    // stream-ordered: a free does not stall other streams (cudaFree synchronises the device)
+    cudaError_t e = cudaMallocAsync(p, bytes, ctx->st);
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+    if (budgeted) ctx->in_use += bytes;
+    if (acct) *acct += bytes;
+    return QSG_OK;
+}
+
+// twiddle table entry: complex128 {re, im}; complex64 {hi.re, hi.im, lo.re, lo.im}
+// with hi = float(v), lo = float(v - hi)
+inline size_t twsize(int) { return 16; }
+
+inline void put_twiddle(int prec, unsigned char *dst, long double re, long double im)
+{
+    if (prec == 1) {
+        const float hr = (float)re, hi = (float)im;
+        float v[4] = {hr, hi, (float)(re - (long double)hr), (float)(im - (long double)hi)};
+        std::memcpy(dst, v, 16);
+    } else {
+        double v[2] = {(double)re, (double)im};
+        std::memcpy(dst, v, 16);
+    }
+}
+
+// stage-major twiddles of qsg::Plan<L, E>, from long double
+inline int get_twiddles(qsg_ctx *ctx, int prec, int L, int E, const void **out)
+{
+    auto key = std::make_tuple(prec, L, E);
+    auto it = ctx->tw_cache.find(key);
+    if (it != ctx->tw_cache.end()) {
+        *out = it->second;
+        return QSG_OK;
+    }
+    qsg::PlanRT p(L, E);
+    const int size = p.tw_size() > 0 ? p.tw_size() : 1;
+    std::vector<long double> re(size, 1.0L), im(size, 0.0L);
+    int off = 0;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int s = 1; s < p.nst; ++s) {
+        const int R = 1 << p.radix_log(s), P = 1 << p.p_log(s);
+        for (int q = 1; q < R; ++q)
+            for (int k = 0; k < P; ++k) {
+                const long double ang = two_pi * (long double)(q * k) / (long double)(P * R);
+                re[off + (q - 1) * P + k] = cosl(ang);
+                im[off + (q - 1) * P + k] = -sinl(ang);
+            }
+        off += (R - 1) * P;
+    }
+    std::vector<unsigned char> host(size * twsize(prec));
+    for (int i = 0; i < size; ++i) put_twiddle(prec, &host[i * twsize(prec)], re[i], im[i]);
+    void *d = nullptr;
+    int rc = dev_alloc(ctx, host.size(), &d, nullptr);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->tw_cache[key] = d;
+    *out = d;
+    return QSG_OK;
+}
+
+// exp(-2 pi i m / n), m < n
+inline int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
+{
+    auto key = std::make_pair(prec, n);
+    auto it = ctx->circle_cache.find(key);
+    if (it != ctx->circle_cache.end()) {
+        *out = it->second;
+        return QSG_OK;
+    }
+    std::vector<unsigned char> host((size_t)n * twsize(prec));
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int m = 0; m < n; ++m) {
+        const long double ang = two_pi * (long double)m / (long double)n;
+        put_twiddle(prec, &host[(size_t)m * twsize(prec)], cosl(ang), -sinl(ang));
+    }
+    void *d = nullptr;
+    int rc = dev_alloc(ctx, host.size(), &d, nullptr);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->circle_cache[key] = d;
+    *out = d;
+    return QSG_OK;
+}
+
+// --- profiling -------------------------------------------------------------
+
+inline cudaEvent_t take_event(qsg_ctx *ctx)
+{
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct ProfScope {
+    qsg_ctx *ctx;
+    const char *name;
+    cudaStream_t st;
+    cudaEvent_t e0 = nullptr;
+    ProfScope(qsg_ctx *c, const char *n, cudaStream_t s = nullptr) : ctx(c), name(n), st(s ? s : c->st)
+    {
+        if (ctx->prof == 1) {
+            e0 = take_event(ctx);
+            cudaEventRecord(e0, st);
+        } else if (ctx->prof == 2) {
+            ctx->prof_stats[name].launches += 1;
+        }
+    }
+    ~ProfScope()
+    {
+        if (e0) {
+            cudaEvent_t e1 = take_event(ctx);
+            cudaEventRecord(e1, st);
+            ctx->prof_pending.emplace_back(name, e0, e1);
+        }
+    }
+};
+
+}  // namespace qsg_host

@@ -34,6 +34,7 @@ class SolverMethod(enum.Enum):
     Unknown = 0
     SplittingMethodO2 = 1
     SplittingMethodO4 = 2
+    BornSerise = 3  # the reference's spelling (include/QuSim.h:492)
 
 
 class Options:
@@ -62,6 +63,35 @@ class Options:
 
     def DeviceOrdinal(self, i: int):
         self._kv["device_ordinal"] = int(i)
+        return self
+
+    # Born-series options (include/QuSim.h:288-333)
+    def Order(self, n: int):
+        self._kv["order"] = int(n)
+        return self
+
+    def Preconditional(self, v: bool):
+        self._kv["preconditional"] = bool(v)
+        return self
+
+    def Slow(self, v: float):
+        self._kv["slow"] = float(v)
+        return self
+
+    def VellekoopPreconditioner(self):
+        self._kv["preconditioner"] = "Vellekoop"
+        return self
+
+    def Hao1Preconditioner(self):
+        self._kv["preconditioner"] = "Hao1"
+        return self
+
+    def Hao2Preconditioner(self):
+        self._kv["preconditioner"] = "Hao2"
+        return self
+
+    def BornIdentityPreconditioner(self):
+        self._kv["preconditioner"] = "BornIndentity"
         return self
 
     def SetInt(self, k, v):
