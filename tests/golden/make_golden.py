@@ -84,7 +84,8 @@ def main():
         V, _ = born_potential_1d(n, x0, x1, v0)
         r = ref.born1d(V, x0, x1, en, eps, direction=direction, order=order, preconditional=pre,
                        preconditioner=precer, slow=slow, computes=computes)
-        save(name, dpsi=r["dpsi"], psi0=r["psi0"], v=r["v"], epsilon=r["epsilon"],
+        # V (the input) is stored: numpy's exp differs in the last bit between platforms
+        save(name, V=V, dpsi=r["dpsi"], psi0=r["psi0"], v=r["v"], epsilon=r["epsilon"],
              R=r["R"], T=r["T"])
     cs = xsec_cosines()
     for (name, nx, ny, hx, hy, en, eps, dirx, diry, order, pre, precer, slow,

@@ -119,7 +119,7 @@ def test_born1d_matches_reference(oracle, case):
     of two."""
     name, n, x0, x1, v0, en, eps, direction, order, pre, precer, slow, computes = case
     g = load_golden(name)
-    V, _ = born_potential_1d(n, x0, x1, v0)
+    V = g["V"]
     r = oracle.born1d(V, x0, x1, en, eps, direction=direction, order=order, preconditional=pre,
                       preconditioner=precer, slow=slow, computes=computes)
     assert np.array_equal(r["psi0"], g["psi0"])
