@@ -1,7 +1,8 @@
 """Benchmark of the split-operator step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload 2d4096|2d1024|1d4096] [--precision mixed|fp64]
+                    [--workload 2d4096|2d1024|1d4096|batch1d|serving|born2d]
+                    [--precision mixed|fp64]
 
 Default workload: the large 2D configuration -- 4096x4096 periodic grid on
 [-200,200)^2, double-slit wall (V=10 on |x|<1 except openings of width 2 at
@@ -49,6 +50,10 @@ WORKLOADS = {
                    full_steps=2000),
     "batch1d": dict(desc="batched 1D: 2048 instances, N=2^e e~U{10..17} (seed 0), 8 bumps, O2, dt=0.01",
                     dim=0, count=2048, dt=0.01, order=2, full_steps=500),
+    "born2d": dict(desc="Born series 2D: 2048x2048 on [-150,150)^2, E=2 (21 points per wavelength), Gaussian "
+                        "well 0.3 exp(-r^2/4) with a weak absorbing spot, preconditioned (Vellekoop), order 20 "
+                        "updates per Compute, incident along x", dim=-2, nx=2048, ny=2048, half=150.0, en=2.0,
+                   order=20, preconditioner=1),
     "serving": dict(desc="serving: seeded Poisson arrivals; 70% 1D N log-uniform 2^10..2^18, 30% 2D side "
                          "log-uniform 256..2048 (both rounded to powers of two); steps U{100..5000}; O2/O4 50/50; "
                          "complex64; 120 GB budget", dim=-1),
@@ -230,9 +235,49 @@ def dist_env():
     return rank, world, local
 
 
+def born_inputs(w):
+    from tests.workloads import born_potential_2d
+    h = w["half"]
+    V, _, _ = born_potential_2d(w["nx"], w["ny"], -h, h, -h, h)
+    return V
+
+
+def born_cpu_sample(budget_s, order):
+    """The oracle's preconditioned Born series (1 core) on a 640x640 grid of the
+    workload's wavelength and potential: site-updates/s."""
+    from oracle import oracle as orc
+    from tests.workloads import born_potential_2d
+    if not os.path.exists(orc.ORACLE_SO):
+        orc.build()
+    o = orc.Oracle()
+    n = 640  # the smallest box of >= 24 wavelengths at this grid spacing, 5 x 2^7 points
+    h = 150.0 * n / 2048
+    V, _, _ = born_potential_2d(n, n, -h, h, -h, h)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        o.born2d(V, -h, h, -h, h, 2.0, 0.0, order=order, preconditional=True, preconditioner=1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return dict(value=n * n * order * done / el, unit="site-updates/s", cores=1, kind="port",
+                sample=f"{done} x (init + one Compute of {order} preconditioned updates) on a {n}x{n} grid with "
+                       "the workload's grid spacing and potential, single thread")
+
+
 def run_reference(args, w):
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if w["dim"] == -2:
+        cpu = born_cpu_sample(120.0 / max(1, args.steps + args.warmup) * args.steps, 2)
+        v = cpu["value"]
+        line = {"metric": "site-updates/s", "value": v, "unit": "site-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "impl": "reference",
+                "config": {"workload": w["desc"], "precision": "fp64"}, "cpu_baseline": cpu,
+                "e2e": {"value": v, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     from oracle import oracle as orc
     if not os.path.exists(orc.ORACLE_SO):
@@ -396,6 +441,153 @@ def run_batch(args, w):
         print(json.dumps(line), flush=True)
 
 
+def born_bytes_per_site(order, precision, needs_old=True):
+    """Algorithmic HBM bytes per site of one Compute of `order` updates: the
+    first row pass reads dpsi and V and writes the scratch (3 elements); each
+    later one reads the scratch, V and (post-updates that need it) dpsi, and
+    writes dpsi and the scratch (5); the last reads the scratch, V, dpsi and
+    dpsi at the start of the Compute and writes dpsi (5); each column pass
+    reads and writes the scratch (2)."""
+    cs = 8 if precision == "mixed" else 16
+    mid = 5 if needs_old else 3
+    row = 3 + (order - 1) * mid + 5
+    return cs * (row + 2 * order), cs * row, cs * 2 * order
+
+
+def run_born(args, w):
+    """The Born-series 2D workload: a step is one Compute (``order`` updates)."""
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import qusim_gb300 as q
+    V = born_inputs(w)
+    nx, ny, h, K = w["nx"], w["ny"], w["half"], w["order"]
+    sites = nx * ny
+    ctx = q.default_context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def solver(precision):
+        per = q.QuPerturbation2D()
+        per.init(V, -h, h, nx, -h, h, ny, w["en"], 0.0, 1.0, 0.0, q.SolverMethod.BornSerise, 1.0, 1.0,
+                 q.Options().Gb300().Order(K).Preconditional(True).VellekoopPreconditioner().Precision(precision))
+        return per
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    per = solver(args.precision)
+    for _ in range(args.warmup):
+        per.Compute()
+    per.GetDeltaPsiNorm()
+    torch.cuda.synchronize()
+    ctx.profile(2)
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        per.Compute()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    ms = world_max(e0.elapsed_time(e1), world)
+    counts = ctx.profile_read()
+    ctx.profile(False)
+    ctx.profile(True)
+    for _ in range(args.steps):
+        per.Compute()
+    per.GetDeltaPsiNorm()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    value = whole_job_rate(sites * K * args.steps, world, ms / 1e3)
+    peak, peak_kind = measured_peaks()
+    total_b, row_b, col_b = born_bytes_per_site(K, args.precision)
+    roof = None
+    if "born_row_pass" in prof:
+        nl, tot = prof["born_row_pass"]
+        avg = tot / nl
+        per_launch = row_b / (K + 1) * sites
+        ach = per_launch / (avg / 1e3) / 1e9
+        tr = profile_traffic(f"born_row_pass_{args.precision}")
+        roof = {"bound": "hbm", "kernel": "born_row_pass", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_source": peak_kind, "avg_launch_ms": avg,
+                "algorithmic_bytes_per_launch": per_launch, "traffic": (tr * sites) if tr else None,
+                "share": tot / sum(v[1] for v in prof.values())}
+    step_roof = {"algorithmic_bytes_per_site_update": total_b / K,
+                 "achieved_gbs": total_b / K * value / world / 1e9,
+                 "frac": total_b / K * value / world / 1e9 / peak}
+    # accuracy of the mixed form against the complex128 path, and its speed
+    acc = plain = None
+    if not args.no_plain and args.precision == "mixed":
+        p64 = solver("fp64")
+        p64.Compute()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        p64.Compute()
+        f1.record(stream)
+        f1.synchronize()
+        plain = {"value": sites * K / (f0.elapsed_time(f1) / 1e3), "unit": "site-updates/s", "dtype": "c128"}
+        m = solver("mixed")
+        m.Compute()
+        m.Compute()
+        a, b = m.GetPsi(), p64.GetPsi()
+        cs = [(np.cos(t), np.sin(t)) for t in np.linspace(0, 2 * np.pi, 16, endpoint=False)]
+        xa, xb = m.ComputeXSections(cs), p64.ComputeXSections(cs)
+        acc = {"computes": 2, "updates": 2 * K, "rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+               "xsection_max_rel_vs_fp64": float(np.max(np.abs(xa - xb) / np.abs(xb))),
+               "delta_norm_mixed": m.GetDeltaPsiNorm(), "delta_norm_fp64": p64.GetDeltaPsiNorm()}
+        m.close()
+        p64.close()
+    # end to end through the public API: init (H2D of V from pinned memory),
+    # K x (Compute + GetDeltaPsiNorm read back), GetPsi and 16 cross sections
+    import torch as _t
+    pin_V = _t.from_numpy(np.ascontiguousarray(V).view(np.float64).copy()).pin_memory()
+    V_pinned = pin_V.numpy().view(np.complex128).reshape(V.shape)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e2 = q.QuPerturbation2D()
+    e2.init(V_pinned, -h, h, nx, -h, h, ny, w["en"], 0.0, 1.0, 0.0, q.SolverMethod.BornSerise, 1.0, 1.0,
+            q.Options().Gb300().Order(K).Preconditional(True).VellekoopPreconditioner().Precision(args.precision))
+    for _ in range(args.steps):
+        e2.Compute()
+        e2.GetDeltaPsiNorm()
+    e2.GetPsi()
+    xs16 = e2.ComputeXSections([(np.cos(t), np.sin(t)) for t in np.linspace(0, 2 * np.pi, 16, endpoint=False)])
+    e2.close()
+    el = world_max(time.perf_counter() - t0, world)
+    e2e = {"value": whole_job_rate(sites * K * args.steps, world, el), "unit": "site-updates/s",
+           "h2d_bytes_per_step": V.nbytes / args.steps, "d2h_bytes_per_step": V.nbytes / args.steps + 16,
+           "includes": "init (V upload, tables), K x (Compute + delta-psi norm read back), GetPsi, 16 cross sections",
+           "xsection_theta0": float(xs16[0])}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = born_cpu_sample(15.0, 2)
+    per.close()
+    if rank == 0:
+        line = {"metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                           "updates_per_step": K, "parallelism": f"replicas x{world}",
+                           "l2": "dpsi x2, V and the scratch (128 MiB in complex64) exceed L2"},
+                "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
+                "gpu_launches": int(sum(v[0] for v in counts.values())),
+                "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def serving_inputs(seed=0):
     """A pool of seeded inputs per power-of-two size (4 variants each): a packet
     and an 8-bump potential as in the batched configuration."""
@@ -550,6 +742,8 @@ def main():
         return run_batch(args, w)
     if w["dim"] == -1:
         return run_serving(args, w)
+    if w["dim"] == -2:
+        return run_born(args, w)
 
     rank, world, local = dist_env()
     import torch
