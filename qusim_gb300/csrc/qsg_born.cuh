@@ -83,7 +83,48 @@ template <class C> __device__ __forceinline__ C born_g0(C x, double dr, double e
     }
 }
 
+// complex64 form from float hi + lo tables: E - T = (gx - gy), gx = E - Tx(kx),
+// gy = Ty(ky).  The hi difference is exact wherever gx and gy are close
+// (Sterbenz), i.e. near the resonance E = T where G0 is large, so the
+// denominator keeps its float precision there without FP64 arithmetic.
+__device__ __forceinline__ float2 born_g0f(float2 x, float2 gx, float2 gy, float eps, float inv_n)
+{
+    const float d = __fsub_rn(gx.x, gy.x) + __fsub_rn(gx.y, gy.y);
+    const float q = inv_n * __frcp_rn(__fmaf_rn(d, d, eps * eps));
+    return cmul(x, make_float2(d * q, -eps * q));
+}
+
 __device__ __forceinline__ int born_fold(int i, int n) { return i > n / 2 ? n - i : i; }
+
+// 1D G0 / N at k index fold f, complex64 form: E - f^2 D with E = (eh, el),
+// D = (dh, dl) given as float hi + lo pairs and f^2 split exactly into two
+// floats, the product formed with an FMA error term (Dekker's two-product),
+// so E - T keeps ~1e-14 relative accuracy (of E) in FP32 arithmetic.
+__device__ __forceinline__ float2 born_g0_1d(float2 x, int f, float2 en, float2 dk, float eps, float inv_n)
+{
+    const long long f2 = (long long)f * f;
+    const float ah = __ll2float_rz(f2);
+    const float al = (float)(f2 - (long long)ah);
+    const float p = ah * dk.x;
+    const float pe = __fmaf_rn(ah, dk.x, -p);
+    const float tl = pe + __fmaf_rn(ah, dk.y, al * dk.x);
+    const float d = __fsub_rn(en.x, p) + __fsub_rn(en.y, tl);
+    const float q = inv_n * __frcp_rn(__fmaf_rn(d, d, eps * eps));
+    return cmul(x, make_float2(d * q, -eps * q));
+}
+template <class C> __device__ __forceinline__ C born_g0_k(C x, int f, double en, double dk2, float2 enf, float2 dkf,
+                                                          double eps, double inv_n)
+{
+    if constexpr (sizeof(C) == 8) {
+        return born_g0_1d(x, f, enf, dkf, (float)eps, (float)inv_n);
+    } else {
+        const double fd = (double)f;
+        return born_g0(x, en - fd * fd * dk2, eps, inv_n);
+    }
+}
+
+// two CTAs per SM where a CTA has at most 256 threads (registers capped at 128)
+constexpr int born_min_blocks(int threads) { return threads <= 256 ? 2 : 1; }
 
 // ---------------------------------------------------------------------------
 // 2D real-space pass: B rows of NY per CTA
@@ -91,7 +132,7 @@ __device__ __forceinline__ int born_fold(int i, int n) { return i > n / 2 ? n - 
 
 
 template <class T, int NY, int E, int B>
-__global__ void __launch_bounds__(B *(NY / E)) k_born_row(BornRowArgs a)
+__global__ void __launch_bounds__(B *(NY / E), born_min_blocks(B *(NY / E))) k_born_row(BornRowArgs a)
 {
     using C = cplx_t<T>;
     constexpr int TL = Plan<NY, E>::TL;
@@ -182,7 +223,7 @@ __global__ void __launch_bounds__(B *(NY / E)) k_born_row(BornRowArgs a)
 
 
 template <class T, int M, int E, int W>
-__global__ void __launch_bounds__(W *(M / E)) k_born_col(BornColArgs a)
+__global__ void __launch_bounds__(W *(M / E), born_min_blocks(W *(M / E))) k_born_col(BornColArgs a)
 {
     using C = cplx_t<T>;
     constexpr int TM = Plan<M, E>::TL;
@@ -202,14 +243,20 @@ __global__ void __launch_bounds__(W *(M / E)) k_born_col(BornColArgs a)
     C x[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) x[e] = ld_stream(p + e * stride);
-    const double gy = __ldg(a.gy + col);
 #pragma unroll 1
     for (int q = 0; q < 2; ++q) {
         line_fft<C, M, E, false>(x, sm, lay, bar, t, tw);
         if (q == 1) continue;
+        if constexpr (sizeof(T) == 4) {
+            const float2 gy = __ldg(a.gy2 + col);
+            const float ef = (float)a.eps, inf = (float)a.inv_n;
 #pragma unroll
-        for (int e = 0; e < E; ++e)
-            x[e] = cconj(born_g0(x[e], __ldg(a.gx + t + e * TM) - gy, a.eps, a.inv_n));
+            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0f(x[e], __ldg(a.gx2 + t + e * TM), gy, ef, inf));
+        } else {
+            const double gy = __ldg(a.gy + col);
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0(x[e], __ldg(a.gx + t + e * TM) - gy, a.eps, a.inv_n));
+        }
     }
     C *o = const_cast<C *>(opaque(p));
 #pragma unroll
@@ -252,10 +299,8 @@ __global__ void __launch_bounds__(L / E) k_born1d(Born1DArgs a)
             line_fft<C, L, E, false>(x, sm, lay, bar, t, opaque(tw));
             if (q == 1) continue;
 #pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const double f = (double)born_fold(t + e * TL, L);
-                x[e] = cconj(born_g0(x[e], a.en - f * f * a.dk2, a.ops.eps, a.inv_n));
-            }
+            for (int e = 0; e < E; ++e)
+                x[e] = cconj(born_g0_k(x[e], born_fold(t + e * TL, L), a.en, a.dk2, a.enf, a.dkf, a.ops.eps, a.inv_n));
         }
 #pragma unroll
         for (int e = 0; e < E; ++e) dp[e * TL] = born_post(a.ops, cconj(x[e]), dp[e * TL], __ldg(opaque(V) + e * TL));
@@ -412,10 +457,9 @@ __global__ void __launch_bounds__(B *(N1 / E)) k_born_fs_row(BornFsRowArgs a)
         line_fft<C, N1, E, false>(x, sm, lay, lbar, t, tw);
         if (q == 1) continue;
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const double f = (double)born_fold(row + a.n2 * (t + e * TL), a.n);
-            x[e] = cconj(born_g0(x[e], a.en - f * f * a.dk2, a.eps, a.inv_n));
-        }
+        for (int e = 0; e < E; ++e)
+            x[e] = cconj(born_g0_k(x[e], born_fold(row + a.n2 * (t + e * TL), a.n), a.en, a.dk2, a.enf, a.dkf,
+                                   a.eps, a.inv_n));
     }
     C *o = const_cast<C *>(opaque(p));
 #pragma unroll

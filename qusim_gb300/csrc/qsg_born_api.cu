@@ -49,6 +49,7 @@ struct qsg_born {
     int cur = 0;
     void *tmp = nullptr, *psi0 = nullptr, *V = nullptr, *ex = nullptr, *ey = nullptr;
     double *gx = nullptr, *gy = nullptr;
+    float2 *gx2 = nullptr, *gy2 = nullptr;  // hi + lo float forms
     const void *tw_a = nullptr, *tw_b = nullptr, *tw_n = nullptr;
     double *parts = nullptr;   // device partials of the last pass
     double *hparts = nullptr;  // pinned mirror
@@ -123,6 +124,12 @@ double min_epsilon(const std::vector<cd> &v, int precer)
     double m = 0;
     for (size_t i = 0; i < v.size(); ++i) m = m >= abs2(i) ? m : abs2(i);
     return std::sqrt(m);
+}
+
+float2 hilo(double v)
+{
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
 }
 
 // (2 pi hbar / (d n))^2 / 2m: PerburbationUtility::CalDp2Div2M (src/Perburbation.h:17-23)
@@ -287,6 +294,15 @@ int create_2d(qsg_born *b, const double *V)
     b->gy = (double *)p;
     QSG_CUDA(cudaMemcpyAsync(b->gx, gx.data(), nx * 8, cudaMemcpyHostToDevice, b->ctx->st));
     QSG_CUDA(cudaMemcpyAsync(b->gy, gy.data(), ny * 8, cudaMemcpyHostToDevice, b->ctx->st));
+    std::vector<float2> gx2(nx), gy2(ny);
+    for (int i = 0; i < nx; ++i) gx2[i] = hilo(gx[i]);
+    for (int j = 0; j < ny; ++j) gy2[j] = hilo(gy[j]);
+    if ((rc = born_alloc(b, nx * 8, &p))) return rc;
+    b->gx2 = (float2 *)p;
+    if ((rc = born_alloc(b, ny * 8, &p))) return rc;
+    b->gy2 = (float2 *)p;
+    QSG_CUDA(cudaMemcpyAsync(b->gx2, gx2.data(), nx * 8, cudaMemcpyHostToDevice, b->ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(b->gy2, gy2.data(), ny * 8, cudaMemcpyHostToDevice, b->ctx->st));
     QSG_CUDA(cudaStreamSynchronize(b->ctx->st));
     if ((rc = get_twiddles(b->ctx, b->prec, ny, qsg::born_e(b->prec), &b->tw_a))) return rc;
     if ((rc = get_twiddles(b->ctx, b->prec, nx, qsg::born_col_e(b->prec, nx), &b->tw_b))) return rc;
@@ -316,6 +332,8 @@ template <class T> int compute_2d(qsg_born *b)
     c.tmp = b->tmp;
     c.gx = b->gx;
     c.gy = b->gy;
+    c.gx2 = b->gx2;
+    c.gy2 = b->gy2;
     c.tw = b->tw_b;
     c.eps = b->eps;
     c.inv_n = 1.0 / (double)b->n;
@@ -356,6 +374,8 @@ template <class T> int compute_1d(qsg_born *b)
         a.tw = b->tw_a;
         a.en = b->en;
         a.dk2 = dk2;
+        a.enf = hilo(b->en);
+        a.dkf = hilo(dk2);
         a.inv_n = 1.0 / (double)b->n;
         a.sums = b->parts;
         a.ops = b->ops;
@@ -385,6 +405,8 @@ template <class T> int compute_1d(qsg_born *b)
     rr.tw = b->tw_b;
     rr.en = b->en;
     rr.dk2 = dk2;
+    rr.enf = hilo(b->en);
+    rr.dkf = hilo(dk2);
     rr.eps = b->eps;
     rr.inv_n = 1.0 / (double)b->n;
     rr.n = (int)b->n;

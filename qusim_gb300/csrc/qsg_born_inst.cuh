@@ -17,7 +17,7 @@ constexpr int born_row_b(int prec, int ny)
 // 2D column pass: W adjacent columns of M rows, W * M / E <= 512 threads
 constexpr int born_col_w(int prec, int m)
 {
-    return prec == 1 ? (m <= 512 ? 16 : (m <= 2048 ? 8 : 4))
+    return prec == 1 ? (m <= 512 ? 16 : (m <= 1024 ? 8 : 4))
                      : (m <= 256 ? 16 : (m == 512 ? 8 : (m <= 2048 ? 4 : 2)));
 }
 // four-step column pass: W * N2 / E = 512 threads

@@ -44,6 +44,8 @@ struct BornColArgs {
     void *tmp;           // in/out, natural k layout (kx row, ky column)
     const double *gx;    // E - fold(kx)^2 DPx^2/2m, Nx entries
     const double *gy;    // fold(ky)^2 DPy^2/2m, Ny entries
+    const float2 *gx2;   // the same tables as float hi + lo pairs (complex64 path)
+    const float2 *gy2;
     const void *tw;      // stage twiddles (Nx, E)
     double eps, inv_n;
     int ny;
@@ -56,6 +58,7 @@ struct Born1DArgs {
     const void *V;
     const void *tw;       // stage twiddles (L, E)
     double en, dk2;       // E and (2 pi hbar / (dx n))^2 / 2m
+    float2 enf, dkf;      // the same as float hi + lo pairs (complex64 path)
     double inv_n;
     double *sums;         // 4 doubles: r (re, im), t (re, im) before the prefactor
     BornOps ops;
@@ -81,6 +84,7 @@ struct BornFsRowArgs {
     void *tmp;            // in/out, k layout
     const void *tw;       // stage twiddles (N1, E)
     double en, dk2, eps, inv_n;
+    float2 enf, dkf;      // en, dk2 as float hi + lo pairs (complex64 path)
     int n, n2;
 };
 
