@@ -131,12 +131,19 @@ constexpr int born_min_blocks(int threads) { return threads <= 256 ? 2 : 1; }
 // ---------------------------------------------------------------------------
 
 
-template <class T, int NY, int E, int B>
-__global__ void __launch_bounds__(B *(NY / E), born_min_blocks(B *(NY / E))) k_born_row(BornRowArgs a)
+// The x split (as in the split-operator passes): a column transform of
+// length Nx = G*M is a radix-G decimation-in-frequency stage across the G rows
+// n1 + j*M, twiddled by exp(-2 pi i n1 q / Nx), then M-point transforms over
+// each block q of M consecutive rows (the k-space pass), where kx = G*k2 + q.
+// A CTA holds B groups of those G rows; the stage runs here through shared
+// memory, so the column pass reads W-column tiles of length M instead of Nx.
+template <class T, int NY, int E, int G, int B>
+__global__ void __launch_bounds__(B *G *(NY / E), born_min_blocks(B *G *(NY / E))) k_born_row(BornRowArgs a)
 {
     using C = cplx_t<T>;
     constexpr int TL = Plan<NY, E>::TL;
-    constexpr int NT = B * TL;
+    constexpr int NL = B * G;
+    constexpr int NT = NL * TL;
     constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
     constexpr int LINE = padded<NY, PADS>(NY);
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -144,18 +151,42 @@ __global__ void __launch_bounds__(B *(NY / E), born_min_blocks(B *(NY / E))) k_b
     C *sm = reinterpret_cast<C *>(smraw);
     const int tid = threadIdx.x;
     const int line = tid / TL, t = tid - line * TL;
-    const int row = blockIdx.x * B + line;
+    const int b = line / G, j = line - b * G;
+    const int m = a.m;
+    const int row = blockIdx.x * B + b + j * m;
     const RowLayout<PADS> lay{line * LINE};
-    constexpr bool NAMED = (TL % 32 == 0) && (B <= 15) && (B > 1);
+    constexpr bool NAMED = (TL % 32 == 0) && (NL <= 15) && (NL > 1);
     using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
     LineBar lbar;
     if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    const CtaBarrier cbar{};
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
+    const tw_t<C> *twx = static_cast<const tw_t<C> *>(a.tw_nx);
     const size_t base = (size_t)row * NY + t;
     const C *V = static_cast<const C *>(a.V) + base;
 
     C x[E];
-    {
+    if (a.in_k && G > 1) {
+        // inverse x-split stage over every column of the CTA's groups
+#pragma unroll 2
+        for (int v = 0; v < B * NY / NT; ++v) {
+            const int gc = tid + v * NT;
+            const int bb = gc / NY, c = gc - bb * NY;
+            const int nn1 = blockIdx.x * B + bb;
+            C y[G];
+#pragma unroll
+            for (int q = 0; q < G; ++q) {
+                y[q] = ld_stream(static_cast<const C *>(a.in) + (size_t)(q * m + nn1) * NY + c);
+                if (q > 0) y[q] = twmul<true>(y[q], __ldg(twx + nn1 * q));
+            }
+            dftg<G, true>(y);
+#pragma unroll
+            for (int q = 0; q < G; ++q) sm[(bb * G + q) * LINE + c + (c >> PADS)] = y[q];
+        }
+        cbar();
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = sm[lay(t + e * TL)];
+    } else {
         const C *p = static_cast<const C *>(a.in) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) x[e] = ld_stream(p + e * TL);
@@ -203,9 +234,32 @@ __global__ void __launch_bounds__(B *(NY / E), born_min_blocks(B *(NY / E))) k_b
             x[e] = born_pre(a.ops, x[e], cmul(ex, __ldg(ey + e * TL)), v);
         }
         line_fft<C, NY, E, false>(x, sm, lay, lbar, t, opaque(tw));
-        C *p = static_cast<C *>(a.tmp) + base;
+        if constexpr (G > 1) {
+            lbar();  // this line's readers of the last exchange are done
 #pragma unroll
-        for (int e = 0; e < E; ++e) st_stream(p + e * TL, x[e]);
+            for (int e = 0; e < E; ++e) sm[lay(t + e * TL)] = x[e];
+            cbar();
+            // forward x-split stage
+#pragma unroll 2
+            for (int v = 0; v < B * NY / NT; ++v) {
+                const int gc = tid + v * NT;
+                const int bb = gc / NY, c = gc - bb * NY;
+                const int nn1 = blockIdx.x * B + bb;
+                C y[G];
+#pragma unroll
+                for (int q = 0; q < G; ++q) y[q] = sm[(bb * G + q) * LINE + c + (c >> PADS)];
+                dftg<G, false>(y);
+#pragma unroll
+                for (int q = 0; q < G; ++q) {
+                    if (q > 0) y[q] = twmul<false>(y[q], __ldg(twx + nn1 * q));
+                    st_stream(static_cast<C *>(a.tmp) + (size_t)(q * m + nn1) * NY + c, y[q]);
+                }
+            }
+        } else {
+            C *p = static_cast<C *>(a.tmp) + base;
+#pragma unroll
+            for (int e = 0; e < E; ++e) st_stream(p + e * TL, x[e]);
+        }
     }
     if (a.partials) {
         s0 = block_sum<NT>(s0, red);
@@ -218,7 +272,8 @@ __global__ void __launch_bounds__(B *(NY / E), born_min_blocks(B *(NY / E))) k_b
 }
 
 // ---------------------------------------------------------------------------
-// 2D k-space pass: W columns of M = Nx per CTA, column FFT -> G0/N -> column iFFT
+// 2D k-space pass: W columns of one x-split block (M = Nx / G rows) per CTA,
+// column FFT -> G0/N -> column iFFT
 // ---------------------------------------------------------------------------
 
 
@@ -232,8 +287,10 @@ __global__ void __launch_bounds__(W *(M / E), born_min_blocks(W *(M / E))) k_bor
     const int tid = threadIdx.x;
     const int c = tid % W, t = tid / W;
     const int ny = a.ny;
-    const int col = blockIdx.x * W + c;
-    C *p = static_cast<C *>(a.tmp) + (size_t)t * ny + col;
+    const int ntx = ny / W;
+    const int qb = blockIdx.x / ntx;  // x-split block: rows qb*M .. qb*M + M - 1, kx = G*k2 + qb
+    const int col = (blockIdx.x - qb * ntx) * W + c;
+    C *p = static_cast<C *>(a.tmp) + ((size_t)qb * M + t) * ny + col;
     const size_t stride = (size_t)TM * ny;
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
     constexpr ColPad CP = col_pad(sizeof(C), M, W, E);
@@ -251,11 +308,11 @@ __global__ void __launch_bounds__(W *(M / E), born_min_blocks(W *(M / E))) k_bor
             const float2 gy = __ldg(a.gy2 + col);
             const float ef = (float)a.eps, inf = (float)a.inv_n;
 #pragma unroll
-            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0f(x[e], __ldg(a.gx2 + t + e * TM), gy, ef, inf));
+            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0f(x[e], __ldg(a.gx2 + a.g * (t + e * TM) + qb), gy, ef, inf));
         } else {
             const double gy = __ldg(a.gy + col);
 #pragma unroll
-            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0(x[e], __ldg(a.gx + t + e * TM) - gy, a.eps, a.inv_n));
+            for (int e = 0; e < E; ++e) x[e] = cconj(born_g0(x[e], __ldg(a.gx + a.g * (t + e * TM) + qb) - gy, a.eps, a.inv_n));
         }
     }
     C *o = const_cast<C *>(opaque(p));

@@ -10,8 +10,9 @@
 //   Perburbation.h:47-57, 80-95, 131-148), epsilon raised to GetEpsilon's
 //   minimum (Perburbation.h:326-341)
 // Compute (device), order K >= 1 (R = real-space pass, C = k-space pass):
-//   2D:   R(dpsi -> pre -> F_y) then K times C(F_x, G0/N, F_x^-1) and
-//         R(F_y^-1 -> post [-> pre -> F_y]); the last R also sums the
+//   2D:   R(dpsi -> pre -> F_y -> x split) then K times C(F_x, G0/N, F_x^-1)
+//         and R([x split^-1 ->] F_y^-1 -> post [-> pre -> F_y -> x split]);
+//         the last R also sums the
 //         delta-psi norm.  dpsi ping-pongs between two buffers so the value at
 //         the start of the compute survives until then (fLastPsiX,
 //         Perturbation2DImpl.cpp:51).
@@ -51,6 +52,7 @@ struct qsg_born {
     double *gx = nullptr, *gy = nullptr;
     float2 *gx2 = nullptr, *gy2 = nullptr;  // hi + lo float forms
     const void *tw_a = nullptr, *tw_b = nullptr, *tw_n = nullptr;
+    int g = 1;                 // 2D x split: column blocks of nx / g rows
     double *parts = nullptr;   // device partials of the last pass
     double *hparts = nullptr;  // pinned mirror
     int nparts = 0;            // doubles
@@ -304,8 +306,11 @@ int create_2d(qsg_born *b, const double *V)
     QSG_CUDA(cudaMemcpyAsync(b->gx2, gx2.data(), nx * 8, cudaMemcpyHostToDevice, b->ctx->st));
     QSG_CUDA(cudaMemcpyAsync(b->gy2, gy2.data(), ny * 8, cudaMemcpyHostToDevice, b->ctx->st));
     QSG_CUDA(cudaStreamSynchronize(b->ctx->st));
+    b->g = qsg::born_split(b->prec, nx, ny);
+    const int m = nx / b->g;
     if ((rc = get_twiddles(b->ctx, b->prec, ny, qsg::born_e(b->prec), &b->tw_a))) return rc;
-    if ((rc = get_twiddles(b->ctx, b->prec, nx, qsg::born_col_e(b->prec, nx), &b->tw_b))) return rc;
+    if ((rc = get_twiddles(b->ctx, b->prec, m, qsg::born_col_e(b->prec, m), &b->tw_b))) return rc;
+    if ((rc = get_circle(b->ctx, b->prec, nx, &b->tw_n))) return rc;
     return QSG_OK;
 }
 
@@ -319,6 +324,8 @@ template <class T> int compute_2d(qsg_born *b)
     r.ex = b->ex;
     r.ey = b->ey;
     r.tw = b->tw_a;
+    r.tw_nx = b->tw_n;
+    r.m = b->nx / b->g;
     r.ops = b->ops;
     r.in = b->dpsi[cur];
     r.tmp = b->tmp;
@@ -338,6 +345,7 @@ template <class T> int compute_2d(qsg_born *b)
     c.eps = b->eps;
     c.inv_n = 1.0 / (double)b->n;
     c.ny = b->ny;
+    c.g = b->g;
     for (int i = 1; i <= K; ++i) {
         {
             ProfScope ps(b->ctx, "born_col_pass", st);

@@ -29,7 +29,12 @@ bool born1d_supported(int prec, uint64_t n)
     return n >= 8192 && n <= (1u << 22) && (n & (n - 1)) == 0;
 }
 
-int born_row_blocks(int prec, int nx, int ny) { return nx / born_row_b(prec, ny); }
+int born_split(int prec, int nx, int ny) { return born_split_c(prec, nx, ny); }
+int born_row_blocks(int prec, int nx, int ny)
+{
+    const int g = born_split(prec, nx, ny);
+    return nx / (g * born_row_b(prec, ny, g));
+}
 int born_fs_col_blocks(int prec, int n1, int n2) { return n1 / born_fs_w(prec, n2); }
 int born_xsec_blocks(int nx) { return (nx + kXsecRows - 1) / kXsecRows; }
 

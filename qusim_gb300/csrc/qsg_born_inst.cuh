@@ -9,10 +9,23 @@ namespace qsg {
 
 template <class T> constexpr int born_prec() { return sizeof(T) == 4 ? 1 : 0; }
 
-// 2D row pass: B rows per CTA, B * NY / E = 256 threads (512 for complex128 rows of 4096)
-constexpr int born_row_b(int prec, int ny)
+// 2D row pass: B groups of G rows per CTA, B * G * NY / E >= 256 threads where
+// the rows are short (one group of G rows otherwise)
+constexpr int born_row_b(int prec, int ny, int g)
 {
-    return (prec == 1 ? 4096 : 2048) / ny > 1 ? (prec == 1 ? 4096 : 2048) / ny : 1;
+    return (prec == 1 ? 4096 : 2048) / (ny * g) > 1 ? (prec == 1 ? 4096 : 2048) / (ny * g) : 1;
+}
+// G = nx / (1024 complex64, 512 complex128 rows), at most 4, and at most
+// 512 / (ny / E) so that one group of G rows fits a CTA of 512 threads
+constexpr int born_split_g0(int prec, int nx)
+{
+    return (prec == 1 ? (nx > 1024 ? nx / 1024 : 1) : (nx > 512 ? nx / 512 : 1)) > 4
+               ? 4
+               : (prec == 1 ? (nx > 1024 ? nx / 1024 : 1) : (nx > 512 ? nx / 512 : 1));
+}
+constexpr int born_split_c(int prec, int nx, int ny)
+{
+    return born_split_g0(prec, nx) * (ny / born_e(prec)) <= 512 ? born_split_g0(prec, nx) : 512 / (ny / born_e(prec));
 }
 // 2D column pass: W adjacent columns of M rows, W * M / E <= 512 threads
 constexpr int born_col_w(int prec, int m)
@@ -28,28 +41,28 @@ constexpr int born_fs_b(int prec, int n1)
     return (prec == 1 ? 4096 : 2048) / n1 > 1 ? (prec == 1 ? 4096 : 2048) / n1 : 1;
 }
 
-template <class T, int NY>
+template <class T, int NY, int G>
 static cudaError_t run_born_row(int nx, const BornRowArgs &a, cudaStream_t st)
 {
-    constexpr int P = born_prec<T>(), E = born_e(P), B = born_row_b(P, NY);
+    constexpr int P = born_prec<T>(), E = born_e(P), B = born_row_b(P, NY, G);
     constexpr int PADS = P ? 4 : 3;
-    const size_t smem = sizeof(cplx_t<T>) * B * padded<NY, PADS>(NY);
-    auto k = k_born_row<T, NY, E, B>;
+    const size_t smem = sizeof(cplx_t<T>) * B * G * padded<NY, PADS>(NY);
+    auto k = k_born_row<T, NY, E, G, B>;
     cudaError_t e = prepare_smem(k, smem);
     if (e != cudaSuccess) return e;
-    k<<<nx / B, B * (NY / E), smem, st>>>(a);
+    k<<<nx / (G * B), B * G * (NY / E), smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <class T, int M>
-static cudaError_t run_born_col(int ny, const BornColArgs &a, cudaStream_t st)
+static cudaError_t run_born_col(int ny, int g, const BornColArgs &a, cudaStream_t st)
 {
     constexpr int P = born_prec<T>(), E = born_col_e(P, M), W = born_col_w(P, M);
     const size_t smem = sizeof(cplx_t<T>) * col_tile_elems(sizeof(cplx_t<T>), M, W, E);
     auto k = k_born_col<T, M, E, W>;
     cudaError_t e = prepare_smem(k, smem);
     if (e != cudaSuccess) return e;
-    k<<<ny / W, W * (M / E), smem, st>>>(a);
+    k<<<g * (ny / W), W * (M / E), smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -93,18 +106,33 @@ static cudaError_t run_born_fs_row(int n2, const BornFsRowArgs &a, cudaStream_t 
 
 #define QSG_BORN_2D_SIZES(X) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 
+template <class T, int NY>
+static cudaError_t run_born_row_g(int nx, const BornRowArgs &a, cudaStream_t st)
+{
+    constexpr int P = born_prec<T>(), TL = NY / born_e(P);
+    switch (born_split(P, nx, NY)) {
+    case 1: return run_born_row<T, NY, 1>(nx, a, st);
+    case 2: if constexpr (2 * TL <= 512) return run_born_row<T, NY, 2>(nx, a, st); break;
+    case 4: if constexpr (4 * TL <= 512) return run_born_row<T, NY, 4>(nx, a, st); break;
+    default: break;
+    }
+    return cudaErrorNotSupported;
+}
+
 template <class T> cudaError_t born_row(int nx, int ny, const BornRowArgs &a, cudaStream_t st)
 {
-#define X(N) case N: return run_born_row<T, N>(nx, a, st);
+#define X(N) case N: return run_born_row_g<T, N>(nx, a, st);
     switch (ny) { QSG_BORN_2D_SIZES(X) default: break; }
 #undef X
     return cudaErrorNotSupported;
 }
 
+// the column pass runs on blocks of M = nx / G rows
 template <class T> cudaError_t born_col(int nx, int ny, const BornColArgs &a, cudaStream_t st)
 {
-#define X(N) case N: return run_born_col<T, N>(ny, a, st);
-    switch (nx) { QSG_BORN_2D_SIZES(X) default: break; }
+    const int g = born_split(born_prec<T>(), nx, ny);
+#define X(N) case N: return run_born_col<T, N>(ny, g, a, st);
+    switch (nx / g) { QSG_BORN_2D_SIZES(X) default: break; }
 #undef X
     return cudaErrorNotSupported;
 }

@@ -34,9 +34,11 @@ struct BornRowArgs {
     const void *V;
     const void *ex, *ey;  // psi0 = ex[row] * ey[col]
     const void *tw;       // stage twiddles (NY, E)
+    const void *tw_nx;    // exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
     double *partials;     // 2 per CTA: sum |dnew - dstart|^2, sum |dnew|^2 (or null)
     BornOps ops;
-    int in_k, out_k;
+    int m;                // Nx / G
+    int in_k, out_k;      // input in split-k space / output to split-k space
 };
 
 // 2D k-space pass (k_born_col)
@@ -46,9 +48,9 @@ struct BornColArgs {
     const double *gy;    // fold(ky)^2 DPy^2/2m, Ny entries
     const float2 *gx2;   // the same tables as float hi + lo pairs (complex64 path)
     const float2 *gy2;
-    const void *tw;      // stage twiddles (Nx, E)
+    const void *tw;      // stage twiddles (M, E)
     double eps, inv_n;
-    int ny;
+    int ny, g;           // g: the x split (M = Nx / g)
 };
 
 // 1D, one CTA per instance (k_born1d)
@@ -109,7 +111,10 @@ bool born1d_supported(int prec, uint64_t n);
 void born_fs_split(uint64_t n, int *n1, int *n2);
 
 // column-transform radix of the 2D k-space pass
-constexpr int born_col_e(int prec, int m) { return prec == 1 ? (m >= 2048 ? 32 : 16) : (m >= 2048 ? 16 : 8); }
+constexpr int born_col_e(int prec, int m) { return prec == 1 ? (m >= 512 ? 32 : 16) : (m >= 2048 ? 16 : 8); }
+// the x split of an nx x ny grid: column blocks of <= 1024 rows (complex64) /
+// 512 (complex128), as far as a CTA of G rows of ny stays within 512 threads
+int born_split(int prec, int nx, int ny);
 
 int born_row_blocks(int prec, int nx, int ny);       // CTAs of a 2D row pass
 int born_fs_col_blocks(int prec, int n1, int n2);    // CTAs of a four-step column pass
