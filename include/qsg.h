@@ -1,5 +1,6 @@
 /*
- * qsg.h -- C ABI of the GB300 split-operator engine (libqsg.so).
+ * qsg.h -- C ABI of the GB300 split-operator engine (libqsg.so), and of its
+ * Born-series scattering solvers (qsg_born_*, at the end of this file).
  *
  * Plain C, plain pointers and sizes; no exceptions cross it.  Every call
  * returns a qsg_status (0 = ok); qsg_last_error() gives the message of the
