@@ -9,6 +9,12 @@
 //          O2: C(K1)  R(S->S, V V)            ... last step: R(S->N, V)
 //          O4: C(KD1) R(S->S, VC2) C(KD2) R(S->S, VC2) C(KD1) R(S->S, VC1 VC1)
 //                                              ... last step: R(S->N, VC1)
+//        Without renormalisation the last R(S->N) is deferred: the instance
+//        stays in split-k space, the next qsg_step opens with R(S->S, V V)
+//        (exactly the pass a longer call would have run), and any read of the
+//        state (psi, energies, reductions, a plan change) runs R(S->N) first.
+//        Norm2 of a deferred state with real dt comes from sums the last C
+//        pass took (the closing V factor has modulus 1).
 //        R = k_row_pass, C = k_col_pass, N = natural real space, S = split-k
 //        space; "V V" multiplies by the same table twice (the reference's two
 //        ExpV calls at the step boundary).
@@ -86,6 +92,11 @@ struct qsg_inst {
     double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
     double *parts = nullptr;       // four-step norm partials (col_blocks)
     uint64_t steps = 0;
+    // 2D: psi holds the split-k form of the state before the last step's closing
+    // V factor (qsg_step defers that row pass; the next step merges it with its
+    // own opening V factor, a read of the state runs it first)
+    bool pending = false;
+    double *cparts = nullptr;      // norm partials of the last column pass (one per tile)
     std::vector<void *> allocs;
     size_t bytes = 0;
 };
@@ -240,9 +251,10 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     return QSG_OK;
 }
 
-int col_pass(qsg_inst *in, int d)
+int col_pass(qsg_inst *in, int d, double *partials = nullptr)
 {
     qsg::ColPassArgs a{};
+    a.partials = partials;
     a.psi = in->psi;
     a.kx = in->kx[d];
     a.ky = in->ky[d];
@@ -271,18 +283,24 @@ int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
     const void *V0 = in->vtab[0], *V1 = in->vtab[1];
     for (uint64_t s = 0; s < nsteps; ++s) {
         const bool last = s + 1 == nsteps;
-        if (s == 0 && (rc = row_pass(in, false, true, V0, false, nullptr))) return rc;
+        // opening V factor: on natural rows, or merged with the deferred closing one
+        if (s == 0 && (rc = row_pass(in, in->pending, true, V0, in->pending, nullptr))) return rc;
+        in->pending = false;
+        // the last column pass of a deferred call also sums the norm
+        double *cp = last && !renorm ? in->cparts : nullptr;
         if (in->order == 2) {
-            if ((rc = col_pass(in, 0))) return rc;
+            if ((rc = col_pass(in, 0, cp))) return rc;
         } else {
             if ((rc = col_pass(in, 0))) return rc;
             if ((rc = row_pass(in, true, true, V1, false, nullptr))) return rc;
             if ((rc = col_pass(in, 1))) return rc;
             if ((rc = row_pass(in, true, true, V1, false, nullptr))) return rc;
-            if ((rc = col_pass(in, 0))) return rc;
+            if ((rc = col_pass(in, 0, cp))) return rc;
         }
-        if (last)
+        if (last && renorm)
             rc = row_pass(in, true, false, V0, false, parts);
+        else if (last)
+            in->pending = true;  // closing V factor deferred
         else
             rc = row_pass(in, true, true, V0, true, nullptr);
         if (rc) return rc;
@@ -295,9 +313,20 @@ int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
     return QSG_OK;
 }
 
+// run the deferred closing row pass: psi back to natural real space
+int settle(qsg_inst *in)
+{
+    if (!in->pending) return QSG_OK;
+    int rc = row_pass(in, true, false, in->vtab[0], false, nullptr);
+    if (rc) return rc;
+    in->pending = false;
+    return QSG_OK;
+}
+
 // sum over psi[lo, hi) with the given reduction mode; synchronous
 int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
 {
+    if (int rc = settle(in)) return rc;
     qsg_ctx *ctx = in->ctx;
     int np = 0;
     QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, lo, hi, mode, ctx->partials, ctx->max_partials,
@@ -430,6 +459,11 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         h.partials = in->parts;
         QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    } else {
+        // column-pass norm partials: at most G * Ny / W = 2 Ny tiles (G <= 4, W >= 2)
+        void *cp = nullptr;
+        if ((rc = inst_alloc(in, sizeof(double) * 2 * (size_t)in->ny, &cp))) return rc;
+        in->cparts = static_cast<double *>(cp);
     }
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     return QSG_OK;
@@ -867,6 +901,17 @@ int qsg_norm2(qsg_inst *in, double *out)
 {
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (in->dim == 2 && in->pending && in->dt.imag() == 0) {
+        // real dt: the deferred closing V factor has modulus 1, so the norm is
+        // the one the last column pass summed (split-k sum times G Ny)
+        qsg_ctx *ctx = in->ctx;
+        const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
+        QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, ctx->sums, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(ctx->st));
+        *out = ctx->host_sums[0] * ((double)in->geom.g * in->ny) * in->dv;
+        return QSG_OK;
+    }
     double s = 0;
     int rc = reduce(in, 0, in->n, 0, &s);
     if (rc) return rc;
@@ -880,6 +925,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
     int rc;
+    if ((rc = settle(in))) return rc;
     if (pot) {
         // Abs2Mul(psi, V) dv / Norm2 (src/EvolverImpl.cpp:45-49)
         double s1 = 0, s0 = 0;
@@ -991,6 +1037,7 @@ int qsg_get_psi(qsg_inst *in, double *out)
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_psi: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
+    if (int rc = settle(in)) return rc;
     if (in->prec == 0) {
         QSG_CUDA(cudaMemcpyAsync(out, in->psi, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
     } else {
@@ -1009,6 +1056,7 @@ int qsg_set_psi(qsg_inst *in, const double *psi)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     int rc = upload_psi(in, psi);
     if (rc) return rc;
+    in->pending = false;  // the state is replaced, with it any deferred row pass
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     return QSG_OK;
 }
@@ -1051,6 +1099,7 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
     if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_set_plan: 2D instances only");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
+    if (int rc = settle(in)) return rc;  // the split-k layout belongs to the current plan
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     return apply_plan(in, Plan2D{p->g, p->row_e, p->row_nt, p->col_e, p->col_w, p->row_kind});
 }
@@ -1069,8 +1118,9 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     cands.resize(n);
     // the trials evolve a copy; psi and the step count are restored afterwards
     const size_t bytes = in->n * csize(in->prec);
-    int rc = ensure_scratch(ctx, bytes);
+    int rc = settle(in);
     if (rc) return rc;
+    if ((rc = ensure_scratch(ctx, bytes))) return rc;
     QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     const Plan2D keep = in->plan;
     const int prof = ctx->prof;
@@ -1100,6 +1150,7 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     ctx->prof = prof;
     cudaError_t err = cudaGetLastError();
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    in->pending = false;  // the restored copy is the settled state
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     if (err != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_autotune: ") + cudaGetErrorString(err));
     if ((rc = apply_plan(in, best_p))) return rc;

@@ -361,6 +361,7 @@ struct ColPassArgs {
     int nx, ny, g;
     float inv_n;            // 1/(Nx Ny) (complex64 path)
     int tiles;              // (Ny / W) * G tiles; CTAs loop over them
+    double *partials;       // or null: per CTA, sum |psi|^2 of the output (split-k scale)
 };
 
 // A tile is block q, columns [xt*W, +W), tile index u = q * (Ny/W) + xt;
@@ -374,6 +375,7 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
     using P = Plan<M, E>;
     constexpr int TM = P::TL;
     extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[32];
     C *sm = reinterpret_cast<C *>(smraw);
     const int tid = threadIdx.x;
     const int c = tid % W, t = tid / W;
@@ -430,6 +432,16 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
         C *p = const_cast<C *>(opaque(psi)) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) st_stream(p + (size_t)e * stride, x[e]);
+    }
+    if (a.partials) {
+        // the norm of the step's state without a pass of its own: in split-k
+        // space sum |psi|^2 is 1 / (G Ny) of the real-space one (the row FFT and
+        // the radix-G stage are unnormalised, the column pass carries 1/(Nx Ny))
+        double s = 0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) s += abs2d(x[e]);
+        s = block_sum<W *(M / E)>(s, red);
+        if (tid == 0) a.partials[blockIdx.x] = s;
     }
     };
     // one tile per CTA (persistent CTAs measured slower here)
