@@ -119,7 +119,12 @@ int qsg_create_2d_spec(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double
 
 /* Advance by nsteps steps (O2: V/2 T V/2; O4: the 7-factor Forest-Ruth
  * sequence), then, if renormalize, scale psi to Norm2 == 1.  Asynchronous:
- * returns once the launches are queued.
+ * returns once the launches are queued.  2D without renormalize: the last
+ * pass of the call (closing V factor, back to natural layout) is deferred --
+ * the next qsg_step opens with it merged into its own first pass, and every
+ * call that reads the state (qsg_get_psi, qsg_norm2, qsg_energies, plan
+ * changes) runs it first -- so a caller stepping in small calls pays no pass
+ * more per step than one long call.
  * Replaces QuEvolverImpl::Step (src/EvolverImpl.cpp:56-68) with "batch" =
  * nsteps and force_normalization_each_step = renormalize, minus its device to
  * host copy of psi (qsg_get_psi does that on demand). */
@@ -130,6 +135,15 @@ int qsg_sync(qsg_inst *inst);
 
 /* Norm2 = sum |psi|^2 dv (src/EvolverImpl.cpp:51-54). */
 int qsg_norm2(qsg_inst *inst, double *out);
+
+/* Norm2 of the state the last qsg_step left, as that step summed it: for a
+ * 2D instance with real dt whose closing row pass is deferred (see qsg_step)
+ * it is read from sums the step's last column pass took in split-k space,
+ * with no pass over psi; otherwise it is qsg_norm2.  Equal to qsg_norm2 in
+ * exact arithmetic (the closing V factor has modulus 1); in complex64 the
+ * two sums differ by rounding (~1e-7 relative).  A per-step observable for
+ * monitoring; qsg_norm2 is the reference's Norm2. */
+int qsg_step_norm2(qsg_inst *inst, double *out);
 
 /* Kinetic and potential energy, as QuEvolverImpl::KinEn / PotEn
  * (src/SplittingMethod1D.cpp:91-107, src/SplittingMethod2D.cpp:123-138,

@@ -901,9 +901,20 @@ int qsg_norm2(qsg_inst *in, double *out)
 {
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    double s = 0;
+    int rc = reduce(in, 0, in->n, 0, &s);
+    if (rc) return rc;
+    *out = s * in->dv;
+    return QSG_OK;
+}
+
+int qsg_step_norm2(qsg_inst *in, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_step_norm2: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
     if (in->dim == 2 && in->pending && in->dt.imag() == 0) {
-        // real dt: the deferred closing V factor has modulus 1, so the norm is
-        // the one the last column pass summed (split-k sum times G Ny)
+        // the deferred closing V factor has modulus 1: the sums the last
+        // column pass took, times G Ny (split-k scale), are the norm
         qsg_ctx *ctx = in->ctx;
         const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
         QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, ctx->sums, ctx->st));

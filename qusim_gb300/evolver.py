@@ -234,6 +234,13 @@ class Instance:
         check(self.ctx.lib.qsg_norm2(self.h, ctypes.byref(v)))
         return v.value
 
+    def step_norm2(self) -> float:
+        """Norm2 as the last step summed it (qsg_step_norm2): no pass over psi
+        for a 2D real-time instance; equal to norm2() up to rounding."""
+        v = ctypes.c_double()
+        check(self.ctx.lib.qsg_step_norm2(self.h, ctypes.byref(v)))
+        return v.value
+
     def energies(self):
         k, p = ctypes.c_double(), ctypes.c_double()
         check(self.ctx.lib.qsg_energies(self.h, ctypes.byref(k), ctypes.byref(p)))
