@@ -124,6 +124,7 @@ class QuPerturbation1D(_ScatteringSolver):
                                           mass, hbar, ctypes.byref(o), _precision(opts), ctypes.byref(h)))
         self.h = h
         self._ctx = ctx
+        ctx._adopt(self)
         self._shape = (n,)
         self._n, self._dx, self._en, self._mass, self._hbar = n, dx, float(en), float(mass), float(hbar)
 
@@ -188,6 +189,7 @@ class QuPerturbation2D(_ScatteringSolver):
                                           ctypes.byref(h)))
         self.h = h
         self._ctx = ctx
+        ctx._adopt(self)
         self._shape = (nx, ny)
         self._en, self._mass, self._hbar = float(en), float(mass), float(hbar)
 

@@ -17,6 +17,7 @@ anything else raises, as the reference raises for unsupported solvers
 from __future__ import annotations
 
 import ctypes
+import weakref
 import enum
 
 import numpy as np
@@ -119,9 +120,16 @@ class Context:
         check(lib.qsg_init(device, hbm_budget, ctypes.byref(h)))
         self.h = h
         self.lib = lib
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, obj):
+        """obj (an instance, batch or solver of this context) is closed before the context."""
+        self._children.add(obj)
 
     def close(self):
         if self.h:
+            for c in list(self._children):
+                c.close()
             self.lib.qsg_ctx_destroy(self.h)
             self.h = None
 
@@ -173,6 +181,7 @@ class Instance:
         self.shape = shape
         self.dv = dv
         self._prec = prec
+        ctx._adopt(self)
 
     @classmethod
     def create_1d(cls, ctx, psi0, V, dx, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
@@ -332,6 +341,7 @@ class Batch:
                                       _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64, pp, vp,
                                       ctypes.byref(h)))
         self.h = h
+        ctx._adopt(self)
         self._keep = (psis, Vs)
         self.count = cnt
         self.sizes = [p.size for p in psis]
