@@ -5,10 +5,12 @@
 
 namespace qsg {
 
+// Dynamic plus static shared memory above 48 KB needs the opt-in attribute;
+// the kernels' static arrays (reduction scratch) stay below 1 KB.
 template <class K>
 static inline cudaError_t prepare_smem(K kernel, size_t smem)
 {
-    if (smem > 48 * 1024)
+    if (smem + 1024 > 48 * 1024)
         return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return cudaSuccess;
 }
