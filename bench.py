@@ -884,7 +884,7 @@ def main():
         a_p.close()
 
     # end to end through the public API: H2D of psi0 and V from pinned memory,
-    # K x (step + Norm2 read back), final psi read back
+    # K x (step + the step's Norm2 read back), final psi read back
     import torch as _t
     pin_psi = _t.from_numpy(psi0.view(np.float64).copy()).pin_memory()
     pin_V = _t.from_numpy(np.ascontiguousarray(V, dtype=np.float64)).pin_memory()
@@ -901,18 +901,22 @@ def main():
         # a new instance picks up the plan tuned above (the context remembers it)
         e2 = q.Instance.create_2d(ctx, psi_pinned, V_pinned, d[0], d[1], w["dt"], order=w["order"],
                                   precision=args.precision)
+    norms = []
     for _ in range(args.steps):
         e2.step(1)
-        e2.norm2()
+        norms.append(e2.step_norm2())
     e2.get_psi(out.numpy().view(np.complex128).reshape(psi0.shape))
+    final_norm = e2.norm2()
     e2.close()
     el = time.perf_counter() - t0
     el = world_max(el, world)
     e2e = {"value": whole_job_rate(sites * args.steps, world, el), "unit": "site-steps/s",
            "h2d_bytes_per_step": (psi0.nbytes + V.nbytes) / args.steps,
            "d2h_bytes_per_step": psi0.nbytes / args.steps + 8,
-           "includes": "instance creation (H2D psi0+V, phase tables), K x (step + Norm2 read back), "
-                       "final psi read back"}
+           "includes": "instance creation (H2D psi0+V, phase tables), K x (qsg_step(1) + the step's Norm2 "
+                       "read back: qsg_step_norm2, summed by the step itself in 2D), final psi read back",
+           "norm_first_step": norms[0] if norms else None, "norm_last_step": norms[-1] if norms else None,
+           "norm2_of_final_psi": final_norm}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
