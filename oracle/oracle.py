@@ -79,6 +79,10 @@ class Oracle:
         lib.orc_ev2d_new.restype = ctypes.c_void_p
         lib.orc_ev2d_step.argtypes = [ctypes.c_void_p, _dp, _u64]
         lib.orc_ev2d_free.argtypes = [ctypes.c_void_p]
+        lib.orc_fft3d.argtypes = [_sz, _sz, _sz, _i, _dp, _dp]
+        lib.orc_evolve3d.argtypes = [_sz, _sz, _sz, _d, _d, _d, _d, _d, _d, _d, _i, _dp, _dp, _u64]
+        lib.orc_kinen3d.argtypes = [_sz, _sz, _sz, _d, _d, _d, _d, _d, _dp]
+        lib.orc_kinen3d.restype = _d
         lib.orc_born_init1d.argtypes = [_sz, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp, _dp]
         lib.orc_born_init2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _d, _d, _d, _d, _d, _i, _i, _dp,
                                         _dp, _dp]
@@ -153,6 +157,28 @@ class Oracle:
     def norm2_range(self, psi, x0, dx, xa, xb):
         psi = _c128(psi)
         return self.lib.orc_norm2_range(psi.size, x0, dx, xa, xb, _ptr(psi))
+
+    def fft3d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        nx, ny, nz = x.shape
+        assert self.lib.orc_fft3d(nx, ny, nz, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
+
+    def evolve3d(self, psi, V, dx, dy, dz, dt, nsteps, order=2, mass=1.0, hbar=1.0):
+        """The 3D split-operator step (SplittingMethod2D's formulas with a third axis)."""
+        psi = _c128(psi).copy()
+        V = _f64(V)
+        dt = complex(dt)
+        nx, ny, nz = psi.shape
+        assert self.lib.orc_evolve3d(nx, ny, nz, dx, dy, dz, mass, hbar, dt.real, dt.imag, order, _ptr(psi),
+                                     _ptr(V), nsteps) == 0
+        return psi
+
+    def kinen3d(self, psi, dx, dy, dz, mass=1.0, hbar=1.0):
+        psi = _c128(psi)
+        nx, ny, nz = psi.shape
+        return self.lib.orc_kinen3d(nx, ny, nz, dx, dy, dz, mass, hbar, _ptr(psi))
 
     def born1d(self, V, x0, x1, en, epsilon, direction=1.0, mass=1.0, hbar=1.0, order=1,
                preconditional=False, preconditioner=1, slow=1.0, computes=1):
@@ -267,6 +293,7 @@ class Reference:
                                      _dp, _u64, _u64, _dp, _dp, _dp]
         lib.ref_fft1d.argtypes = [_sz, _i, _dp, _dp]
         lib.ref_fft2d.argtypes = [_sz, _sz, _i, _dp, _dp]
+        lib.ref_fft3d.argtypes = [_sz, _sz, _sz, _i, _dp, _dp]
         lib.ref_born1d.argtypes = [_sz, _d, _d, _dp, _d, _d, _d, _d, _d, _i, _i, ctypes.c_char_p,
                                    _d, _i, _dp, _dp, _dp, _dp]
         lib.ref_born2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _dp, _d, _d, _d, _d, _d, _d, _i, _i,
@@ -316,6 +343,13 @@ class Reference:
                                    *[ctypes.pointer(o) for o in outs])
         assert rc == 0
         return (psi,) + tuple(o.value for o in outs)
+
+    def fft3d(self, x, inverse=False):
+        x = _c128(x)
+        out = np.empty_like(x)
+        nx, ny, nz = x.shape
+        assert self.lib.ref_fft3d(nx, ny, nz, int(inverse), _ptr(x), _ptr(out)) == 0
+        return out
 
     PRECONDITIONERS = (b"BornIndentity", b"Vellekoop", b"Hao1", b"Hao2")
 

@@ -926,3 +926,176 @@ double orc_born_xsec2d(size_t nx, size_t ny, double x0, double dx, double y0, do
     const cplx s = r * (2 * mass) / (hbar * hbar) * dx * dy * (1. / 4);
     return (creal(s) * creal(s) + cimag(s) * cimag(s)) * (2 / (kPi * k0));
 }
+
+/* ------------------------------------------------------------------------ */
+/* 3D: grid index (ix*ny + iy)*nz + iz (CalGlobalIdx, include/QuSim.h:54-61) */
+/* Transform: z lines, then y lines, then x lines, as KissFourierTransform3D */
+/* (src/FourierTransform.cpp:379-440).                                      */
+/* The reference has FFT3D and a 3D kinetic multiply (MulExpK3D,            */
+/* src/DeviceTemplate.h:851-879, 1581-1589) but no 3D evolver; the 3D split-operator   */
+/* step below is SplittingMethod2D's (ExpV: psi *= exp(-i dt c V / hbar);    */
+/* ExpT: FFT, * exp(-i dt d (fold(i)^2 DTx + fold(j)^2 DTy + fold(k)^2 DTz)  */
+/* / hbar), iFFT, / N; O2 and O4 sequences, src/SplittingMethod2D.cpp:38-121) */
+/* with the third axis added.                                              */
+/* ------------------------------------------------------------------------ */
+
+static void fft3d_exec(const fft_plan *px, const fft_plan *py, const fft_plan *pz, size_t nx, size_t ny,
+                       size_t nz, const cplx *in, cplx *out, cplx *li, cplx *lo)
+{
+    for (size_t i = 0; i < nx; ++i)
+        for (size_t j = 0; j < ny; ++j) plan_exec(pz, in + (i * ny + j) * nz, out + (i * ny + j) * nz);
+    for (size_t i = 0; i < nx; ++i)
+        for (size_t k = 0; k < nz; ++k) {
+            for (size_t j = 0; j < ny; ++j) li[j] = out[(i * ny + j) * nz + k];
+            plan_exec(py, li, lo);
+            for (size_t j = 0; j < ny; ++j) out[(i * ny + j) * nz + k] = lo[j];
+        }
+    for (size_t j = 0; j < ny; ++j)
+        for (size_t k = 0; k < nz; ++k) {
+            for (size_t i = 0; i < nx; ++i) li[i] = out[(i * ny + j) * nz + k];
+            plan_exec(px, li, lo);
+            for (size_t i = 0; i < nx; ++i) out[(i * ny + j) * nz + k] = lo[i];
+        }
+}
+
+static size_t max3(size_t a, size_t b, size_t c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
+
+int orc_fft3d(size_t nx, size_t ny, size_t nz, int inverse, const double *in, double *out)
+{
+    fft_plan px, py, pz;
+    if (plan_init(&px, nx, inverse) || plan_init(&py, ny, inverse) || plan_init(&pz, nz, inverse)) return -1;
+    const size_t m = max3(nx, ny, nz);
+    cplx *li = (cplx *)malloc(sizeof(cplx) * m), *lo = (cplx *)malloc(sizeof(cplx) * m);
+    fft3d_exec(&px, &py, &pz, nx, ny, nz, (const cplx *)in, (cplx *)out, li, lo);
+    free(li); free(lo);
+    plan_free(&px); plan_free(&py); plan_free(&pz);
+    return 0;
+}
+
+typedef struct {
+    size_t nx, ny, nz, n;
+    int order;
+    fft_plan fx, fy, fz, ix, iy, iz;
+    cplx *ft, *li, *lo;
+    cplx *ev[2];
+    cplx *et[2];
+} ev3d;
+
+static void ev3d_free(ev3d *e)
+{
+    plan_free(&e->fx); plan_free(&e->fy); plan_free(&e->fz);
+    plan_free(&e->ix); plan_free(&e->iy); plan_free(&e->iz);
+    free(e->ft); free(e->li); free(e->lo);
+    for (int k = 0; k < 2; ++k) { free(e->ev[k]); free(e->et[k]); }
+}
+
+static int ev3d_init(ev3d *e, size_t nx, size_t ny, size_t nz, double dx, double dy, double dz, double mass,
+                     double hbar, double dt_re, double dt_im, int order, const double *V)
+{
+    memset(e, 0, sizeof(*e));
+    if (nx < 2 || ny < 2 || nz < 2 || (order != 2 && order != 4)) return -1;
+    e->nx = nx; e->ny = ny; e->nz = nz; e->n = nx * ny * nz; e->order = order;
+    if (plan_init(&e->fx, nx, 0) || plan_init(&e->fy, ny, 0) || plan_init(&e->fz, nz, 0) ||
+        plan_init(&e->ix, nx, 1) || plan_init(&e->iy, ny, 1) || plan_init(&e->iz, nz, 1)) return -1;
+    const size_t m = max3(nx, ny, nz);
+    e->ft = (cplx *)malloc(sizeof(cplx) * e->n);
+    e->li = (cplx *)malloc(sizeof(cplx) * m);
+    e->lo = (cplx *)malloc(sizeof(cplx) * m);
+    const cplx dt = dt_re + I * dt_im;
+    double c1, c2, d1, d2;
+    orc_splitting_constants(&c1, &c2, &d1, &d2);
+    const double vc[2] = {order == 2 ? 0.5 : c1, c2};
+    const double tc[2] = {order == 2 ? 1.0 : d1, d2};
+    const int ntab = order == 2 ? 1 : 2;
+    const double dkx = 2 * kPi / (dx * nx), dky = 2 * kPi / (dy * ny), dkz = 2 * kPi / (dz * nz);
+    const double DTx = (dkx * hbar) * (dkx * hbar) / (2 * mass);
+    const double DTy = (dky * hbar) * (dky * hbar) / (2 * mass);
+    const double DTz = (dkz * hbar) * (dkz * hbar) / (2 * mass);
+    const cplx alpha = -I * dt / hbar;
+    for (int k = 0; k < ntab; ++k) {
+        e->ev[k] = (cplx *)malloc(sizeof(cplx) * e->n);
+        e->et[k] = (cplx *)malloc(sizeof(cplx) * e->n);
+        const cplx f = expv_coef(dt, vc[k], hbar);
+        for (size_t i = 0; i < e->n; ++i) e->ev[k][i] = cexp(f * V[i]);
+        const cplx a = alpha * tc[k];
+        for (size_t i = 0; i < nx; ++i) {
+            const double fi = (double)fold_half(i, nx);
+            for (size_t j = 0; j < ny; ++j) {
+                const double fj = (double)fold_half(j, ny);
+                for (size_t l = 0; l < nz; ++l) {
+                    const double fl = (double)fold_half(l, nz);
+                    e->et[k][(i * ny + j) * nz + l] = cexp(a * ((fi * fi) * DTx + (fj * fj) * DTy + (fl * fl) * DTz));
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+static void ev3d_expt(ev3d *e, cplx *psi, const cplx *tab)
+{
+    fft3d_exec(&e->fx, &e->fy, &e->fz, e->nx, e->ny, e->nz, psi, e->ft, e->li, e->lo);
+    ev2d_mul(e->ft, tab, e->n);
+    fft3d_exec(&e->ix, &e->iy, &e->iz, e->nx, e->ny, e->nz, e->ft, psi, e->li, e->lo);
+    const double s = 1.0 / (double)e->n;
+    for (size_t i = 0; i < e->n; ++i) psi[i] = psi[i] * s;
+}
+
+static void ev3d_step(ev3d *e, cplx *psi)
+{
+    if (e->order == 2) {
+        ev2d_mul(psi, e->ev[0], e->n);
+        ev3d_expt(e, psi, e->et[0]);
+        ev2d_mul(psi, e->ev[0], e->n);
+    } else {
+        ev2d_mul(psi, e->ev[0], e->n);
+        ev3d_expt(e, psi, e->et[0]);
+        ev2d_mul(psi, e->ev[1], e->n);
+        ev3d_expt(e, psi, e->et[1]);
+        ev2d_mul(psi, e->ev[1], e->n);
+        ev3d_expt(e, psi, e->et[0]);
+        ev2d_mul(psi, e->ev[0], e->n);
+    }
+}
+
+int orc_evolve3d(size_t nx, size_t ny, size_t nz, double dx, double dy, double dz, double mass, double hbar,
+                 double dt_re, double dt_im, int order, double *psi_io, const double *V, uint64_t nsteps)
+{
+    ev3d e;
+    if (ev3d_init(&e, nx, ny, nz, dx, dy, dz, mass, hbar, dt_re, dt_im, order, V)) { ev3d_free(&e); return -1; }
+    for (uint64_t s = 0; s < nsteps; ++s) ev3d_step(&e, (cplx *)psi_io);
+    ev3d_free(&e);
+    return 0;
+}
+
+/* <T> = sum |FFT3D psi|^2 (fold(i)^2 DTx + fold(j)^2 DTy + fold(k)^2 DTz) / sum |FFT3D psi|^2 */
+double orc_kinen3d(size_t nx, size_t ny, size_t nz, double dx, double dy, double dz, double mass, double hbar,
+                   const double *psi_in)
+{
+    fft_plan px, py, pz;
+    if (plan_init(&px, nx, 0) || plan_init(&py, ny, 0) || plan_init(&pz, nz, 0)) return NAN;
+    const size_t n = nx * ny * nz, m = max3(nx, ny, nz);
+    cplx *ft = (cplx *)malloc(sizeof(cplx) * n);
+    cplx *li = (cplx *)malloc(sizeof(cplx) * m), *lo = (cplx *)malloc(sizeof(cplx) * m);
+    fft3d_exec(&px, &py, &pz, nx, ny, nz, (const cplx *)psi_in, ft, li, lo);
+    const double dkx = 2 * kPi / (dx * nx), dky = 2 * kPi / (dy * ny), dkz = 2 * kPi / (dz * nz);
+    const double DTx = (dkx * hbar) * (dkx * hbar) / (2 * mass);
+    const double DTy = (dky * hbar) * (dky * hbar) / (2 * mass);
+    const double DTz = (dkz * hbar) * (dkz * hbar) / (2 * mass);
+    double kin = 0;
+    for (size_t i = 0; i < nx; ++i) {
+        const double fi = (double)fold_half(i, nx);
+        for (size_t j = 0; j < ny; ++j) {
+            const double fj = (double)fold_half(j, ny);
+            for (size_t l = 0; l < nz; ++l) {
+                const double fl = (double)fold_half(l, nz);
+                const cplx u = ft[(i * ny + j) * nz + l];
+                kin += (creal(u) * creal(u) + cimag(u) * cimag(u)) * ((fi * fi) * DTx + (fj * fj) * DTy + (fl * fl) * DTz);
+            }
+        }
+    }
+    const double nn = norm2_raw(ft, n);
+    free(ft); free(li); free(lo);
+    plan_free(&px); plan_free(&py); plan_free(&pz);
+    return kin / nn;
+}

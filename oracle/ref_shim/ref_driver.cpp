@@ -130,6 +130,20 @@ int ref_fft2d(size_t nx, size_t ny, int inverse, const double *in, double *out)
     }
 }
 
+// KissFourierTransform3D (src/FourierTransform.cpp:379-440, created as
+// FourierTransform3D::Create(n1, n2, n3) at :521-536): n1 = nx slowest, n3 = nz
+// contiguous.
+int ref_fft3d(size_t nx, size_t ny, size_t nz, int inverse, const double *in, double *out)
+{
+    try {
+        std::unique_ptr<FourierTransform3D> f(FourierTransform3D::Create(nx, ny, nz, inverse != 0, FourierTransformLibrary::KISS));
+        f->Transform((const Complex *)in, (Complex *)out);
+        return 0;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
 // Born-series scattering solvers, driven as QuPerturbation1D/2D::init and
 // Compute() drive them (src/QuSim.cpp:499-505, 620-630): the impl's
 // InitPerturbation1D/2D (src/Perturbation1DImpl.cpp:7-42,

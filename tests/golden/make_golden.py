@@ -43,6 +43,12 @@ def main():
         x = np.arange(nx * ny, dtype=np.complex128).reshape(nx, ny)
         save(f"fft2d_ramp_{nx}x{ny}", fwd=ref.fft2d(x), inv=ref.fft2d(x, inverse=True))
 
+    # 3D FFT (KissFourierTransform3D) on ramps: the component the 3D split-operator
+    # step shares with the reference (which has no 3D evolver)
+    for shape in ((6, 10, 14), (16, 8, 32)):
+        x = np.arange(int(np.prod(shape)), dtype=np.complex128).reshape(shape) * (1 + 0.5j)
+        save("fft3d_ramp_%dx%dx%d" % shape, fwd=ref.fft3d(x), inv=ref.fft3d(x, inverse=True))
+
     # 1D evolutions.  (name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes)
     cases_1d = [
         # the 1D plain configuration: N=4096 on [-200,200), k0=1, x0=-50, s=10,
