@@ -85,6 +85,17 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
                   double hbar, double dt_re, double dt_im, int order, int precision,
                   const double *psi0, const double *V, qsg_inst **out);
 
+/* Create a 3D instance, nx*ny*nz sites, index (ix*ny + iy)*nz + iz (z
+ * contiguous, include/QuSim.h:54-61).  The reference has no 3D evolver, only
+ * the 3D transform (src/FourierTransform.cpp:379-440) and a 3D kinetic
+ * multiply; the step is SplittingMethod2D's (O2 / O4) with a third axis.
+ * Sides: powers of two, 16 .. 1024, nz >= 16 (strided-pass tile width), at
+ * most 2^30 sites.  qsg_step / qsg_norm2 / qsg_energies / qsg_get_psi /
+ * qsg_set_psi work as for 1D and 2D. */
+int qsg_create_3d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, uint64_t nz, double dx, double dy, double dz,
+                  double mass, double hbar, double dt_re, double dt_im, int order, int precision,
+                  const double *psi0, const double *V, qsg_inst **out);
+
 /* Initial state and potential given as a formula instead of arrays, sampled on
  * the device in FP64 at x_i = x0 + i*dx, y_j = y0 + j*dy (the points at which
  * the reference samples its psi / V functors, src/EvolverImpl1D.cpp:33-81,

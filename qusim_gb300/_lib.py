@@ -39,7 +39,7 @@ EXPORTS = [
     "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc", "qsg_create_1d_spec", "qsg_create_2d_spec",
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
-    "qsg_born_destroy", "qsg_step_norm2",
+    "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d",
 ]
 
 # qsg_born_preconditioner / qsg_born_field
@@ -141,6 +141,8 @@ def _declare(lib):
     lib.qsg_create_2d_spec.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _i, _i, ctypes.POINTER(Spec),
                                        ctypes.POINTER(_vp)]
     lib.qsg_create_2d.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp,
+                                  ctypes.POINTER(_vp)]
+    lib.qsg_create_3d.argtypes = [_vp, _u64, _u64, _u64, _d, _d, _d, _d, _d, _d, _d, _i, _i, _dp, _dp,
                                   ctypes.POINTER(_vp)]
     lib.qsg_step.argtypes = [_vp, _u64, _i]
     lib.qsg_sync.argtypes = [_vp]

@@ -39,6 +39,7 @@
 #include "qsg_aux.h"
 #include "qsg_host.h"
 #include "qsg_launch.h"
+#include "qsg_evolve3d.cuh"
 
 using namespace qsg_host;
 
@@ -71,8 +72,8 @@ struct qsg_inst {
     qsg_ctx *ctx = nullptr;
     int dim = 1;
     uint64_t n = 0;
-    int nx = 0, ny = 0;
-    double dx = 0, dy = 0, dv = 0, mass = 1, hbar = 1;
+    int nx = 0, ny = 0, nz = 1;
+    double dx = 0, dy = 0, dz = 0, dv = 0, mass = 1, hbar = 1;
     cd dt;
     int order = 2, prec = 0, boundary = 0;
     void *psi = nullptr;
@@ -97,6 +98,10 @@ struct qsg_inst {
     // own opening V factor, a read of the state runs it first)
     bool pending = false;
     double *cparts = nullptr;      // norm partials of the last column pass (one per tile)
+    // 3D: per-axis kinetic factors [axis x, y, z][substep table], twiddles, kinetic partials
+    void *k3[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    const void *tw3[3] = {nullptr, nullptr, nullptr};
+    double *kparts3 = nullptr;
     std::vector<void *> allocs;
     size_t bytes = 0;
 };
@@ -313,6 +318,110 @@ int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
     return QSG_OK;
 }
 
+// 3D: one pass over the lines of an axis (0 x, 1 y, 2 z): [vpre] F^-1 K F [vpost]
+template <class T>
+int pass3(qsg_inst *in, int ax, int ktab, const void *vpre, bool pre2, const void *vpost, bool post2, double *kin)
+{
+    qsg::Pass3Args a{};
+    a.psi = in->psi;
+    a.vpre = vpre;
+    a.vpre_twice = pre2 ? 1 : 0;
+    a.vpost = vpost;
+    a.vpost_twice = post2 ? 1 : 0;
+    a.k = in->k3[ax][ktab];
+    a.tw = in->tw3[ax];
+    a.partials = kin;
+    a.kinetic = kin ? 1 : 0;
+    const int nx = in->nx, ny = in->ny, nz = in->nz;
+    const int L[3] = {nx, ny, nz};
+    a.inv_l = (float)(1.0 / L[ax]);
+    if (ax == 2) {
+        ProfScope ps(in->ctx, "pass3_z", in->st);
+        QSG_CUDA(qsg::launch3_row<T>(nz, (size_t)nx * ny, a, in->st));
+    } else if (ax == 1) {
+        a.s_line = nz;
+        a.s_outer = (long long)ny * nz;
+        ProfScope ps(in->ctx, "pass3_y", in->st);
+        QSG_CUDA(qsg::launch3_col<T>(ny, nz, nx, a, in->st));
+    } else {
+        a.s_line = (long long)ny * nz;
+        a.s_outer = nz;
+        ProfScope ps(in->ctx, "pass3_x", in->st);
+        QSG_CUDA(qsg::launch3_col<T>(nx, nz, ny, a, in->st));
+    }
+    return QSG_OK;
+}
+
+// O2: z[V V', Kz] y[Ky] x[Kx, (V)];  O4: z[V1 V1', K1] y x[V2] z[K2] y x[V2] z[K1] y x[(V1)]
+template <class T> int step3d_t(qsg_inst *in, uint64_t nsteps, int renorm)
+{
+    int rc;
+    const void *V0 = in->vtab[0], *V1 = in->vtab[1];
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        const bool last = s + 1 == nsteps;
+        const void *close = last ? V0 : nullptr;
+        if (in->order == 2) {
+            if ((rc = pass3<T>(in, 2, 0, V0, s > 0, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 1, 0, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 0, 0, nullptr, false, close, false, nullptr))) return rc;
+        } else {
+            if ((rc = pass3<T>(in, 2, 0, V0, s > 0, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 1, 0, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 0, 0, nullptr, false, V1, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 2, 1, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 1, 1, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 0, 1, nullptr, false, V1, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 2, 0, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 1, 0, nullptr, false, nullptr, false, nullptr))) return rc;
+            if ((rc = pass3<T>(in, 0, 0, nullptr, false, close, false, nullptr))) return rc;
+        }
+    }
+    (void)renorm;
+    return QSG_OK;
+}
+
+int step3d(qsg_inst *in, uint64_t nsteps, int renorm)
+{
+    int rc = in->prec == 1 ? step3d_t<float>(in, nsteps, renorm) : step3d_t<double>(in, nsteps, renorm);
+    if (rc || !renorm) return rc;
+    // renormalise at the end of the call, as 2D does (QuEvolverImpl::Step, src/EvolverImpl.cpp:56-68)
+    qsg_ctx *ctx = in->ctx;
+    int np = 0;
+    QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, in->n, 0, ctx->partials, ctx->max_partials, &np, ctx->st));
+    QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
+    QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
+    return QSG_OK;
+}
+
+// <T> of a 3D state: per axis, sum |F_a psi|^2 fold^2 DT_a / sum |F_a psi|^2 (Parseval over
+// the other two axes makes these the full transform's ratios), summed over the axes
+int kinetic3d(qsg_inst *in, double *kin)
+{
+    qsg_ctx *ctx = in->ctx;
+    const int L[3] = {in->nx, in->ny, in->nz};
+    const double D[3] = {in->dx, in->dy, in->dz};
+    double total = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        const int ctas = ax == 2 ? qsg::row3_ctas(in->prec, in->nz, (size_t)in->nx * in->ny)
+                                 : qsg::col3_ctas(in->prec, L[ax], in->nz, ax == 1 ? in->nx : in->ny);
+        int rc = in->prec == 1 ? pass3<float>(in, ax, 0, nullptr, false, nullptr, false, in->kparts3)
+                               : pass3<double>(in, ax, 0, nullptr, false, nullptr, false, in->kparts3);
+        if (rc) return rc;
+        std::vector<double> h(2 * (size_t)ctas);
+        QSG_CUDA(cudaMemcpyAsync(h.data(), in->kparts3, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(ctx->st));
+        double s1 = 0, s0 = 0;
+        for (int c = 0; c < ctas; ++c) {
+            s1 += h[2 * c];
+            s0 += h[2 * c + 1];
+        }
+        const double dk = 2 * kPi / (D[ax] * L[ax]);
+        total += (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass) * (s1 / s0);
+    }
+    *kin = total;
+    return QSG_OK;
+}
+
 // run the deferred closing row pass: psi back to natural real space
 int settle(qsg_inst *in)
 {
@@ -379,6 +488,22 @@ int build_tables(qsg_inst *in)
             } else {
                 QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
                                               1.0 / (double)in->n, ctx->st));
+            }
+        }
+    } else if (in->dim == 3) {
+        // SplittingMethod2D::InitExpT with a third axis, one factor per axis:
+        // exp(a fold(i)^2 DT_axis) with 1/L folded in (complex128) or as factor - 1
+        const int L[3] = {in->nx, in->ny, in->nz};
+        const double D[3] = {in->dx, in->dy, in->dz};
+        const cd alpha = -I * in->dt / in->hbar;
+        for (int ax = 0; ax < 3; ++ax) {
+            const double dk = 2 * kPi / (D[ax] * L[ax]);
+            const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
+            for (int k = 0; k < ntab; ++k) {
+                const cd f = alpha * tc[k] * DT;
+                if ((rc = inst_alloc(in, (size_t)L[ax] * cs, &in->k3[ax][k]))) return rc;
+                QSG_CUDA(qsg::launch_ktable1d(in->prec, in->k3[ax][k], L[ax], f.real(), f.imag(),
+                                              1.0 / (double)L[ax], ctx->st));
             }
         }
     } else {
@@ -459,11 +584,22 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         h.partials = in->parts;
         QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-    } else {
+    } else if (in->dim == 2) {
         // column-pass norm partials: at most G * Ny / W = 2 Ny tiles (G <= 4, W >= 2)
         void *cp = nullptr;
         if ((rc = inst_alloc(in, sizeof(double) * 2 * (size_t)in->ny, &cp))) return rc;
         in->cparts = static_cast<double *>(cp);
+    } else {
+        // 3D: line twiddles per axis and the kinetic-energy partials (2 per CTA)
+        const int L[3] = {in->nx, in->ny, in->nz};
+        for (int ax = 0; ax < 3; ++ax)
+            if ((rc = get_twiddles(ctx, in->prec, L[ax], in->prec == 1 ? 16 : 8, &in->tw3[ax]))) return rc;
+        const size_t ctas = std::max({(size_t)qsg::row3_ctas(in->prec, in->nz, (size_t)in->nx * in->ny),
+                                      (size_t)qsg::col3_ctas(in->prec, in->ny, in->nz, in->nx),
+                                      (size_t)qsg::col3_ctas(in->prec, in->nx, in->nz, in->ny)});
+        void *kp = nullptr;
+        if ((rc = inst_alloc(in, sizeof(double) * 2 * ctas, &kp))) return rc;
+        in->kparts3 = static_cast<double *>(kp);
     }
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     return QSG_OK;
@@ -870,6 +1006,52 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     return QSG_OK;
 }
 
+int qsg_create_3d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, uint64_t nz, double dx, double dy, double dz,
+                  double mass, double hbar, double dt_re, double dt_im, int order, int precision,
+                  const double *psi0, const double *V, qsg_inst **out)
+{
+    if (!ctx || !out || !psi0 || !V) return fail(QSG_ERR_ARG, "qsg_create_3d: null argument");
+    *out = nullptr;
+    if (order != 2 && order != 4) return fail(QSG_ERR_ARG, "qsg_create_3d: order must be 2 or 4");
+    if (precision != QSG_FP64 && precision != QSG_MIXED)
+        return fail(QSG_ERR_ARG, "qsg_create_3d: precision must be QSG_FP64 or QSG_MIXED");
+    if (!finite_pos(dx) || !finite_pos(dy) || !finite_pos(dz) || !finite_pos(mass) || !finite_pos(hbar) ||
+        !std::isfinite(dt_re) || !std::isfinite(dt_im))
+        return fail(QSG_ERR_ARG, "qsg_create_3d: dx, dy, dz, mass, hbar must be finite and > 0, dt finite");
+    if (!qsg::evolve3d_supported(precision, nx, ny, nz))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_3d: grid " + std::to_string(nx) + "x" + std::to_string(ny) +
+                                             "x" + std::to_string(nz) +
+                                             " (supported: powers of two, 16 .. 1024 per side, nz a multiple of "
+                                             "the strided passes' tile width, at most 2^30 sites)");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    qsg_inst *in = new qsg_inst();
+    in->ctx = ctx;
+    in->dim = 3;
+    in->nx = (int)nx;
+    in->ny = (int)ny;
+    in->nz = (int)nz;
+    in->n = nx * ny * nz;
+    in->dx = dx;
+    in->dy = dy;
+    in->dz = dz;
+    in->dv = dx * dy * dz;
+    in->mass = mass;
+    in->hbar = hbar;
+    in->dt = cd(dt_re, dt_im);
+    in->order = order;
+    in->prec = precision;
+    in->st = ctx->st;
+    int rc = common_create(in, psi0, V);
+    if (rc) {
+        std::string msg = g_last_error;
+        free_inst(in);
+        return fail(rc, msg);
+    }
+    *out = in;
+    return QSG_OK;
+}
+
 int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
 {
     if (!in) return fail(QSG_ERR_ARG, "qsg_step: null instance");
@@ -884,7 +1066,8 @@ int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
         QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, in->ctx->sums, in->dv, in->ctx->st));
         return QSG_OK;
     }
-    rc = in->dim == 1 ? step1d(in, nsteps, renormalize) : step2d(in, nsteps, renormalize);
+    rc = in->dim == 1 ? step1d(in, nsteps, renormalize)
+         : in->dim == 2 ? step2d(in, nsteps, renormalize) : step3d(in, nsteps, renormalize);
     if (rc) return rc;
     in->steps += nsteps;
     return QSG_OK;
@@ -944,7 +1127,9 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
         if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
         *pot = (s1 * in->dv) / (s0 * in->dv);
     }
-    if (kin) {
+    if (kin && in->dim == 3) {
+        if ((rc = kinetic3d(in, kin))) return rc;
+    } else if (kin) {
         if (in->dim == 1) {
             // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102)
             const double dk = 2 * kPi / (in->dx * in->n);

@@ -77,6 +77,14 @@ cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, 
 cudaError_t launch_kinetic1d(int prec, int n, const void *psi, const void *tw, double dt_k,
                              double *sums, cudaStream_t st);
 
+// 3D split-operator passes (qsg_evolve3d.cuh)
+struct Pass3Args;
+bool evolve3d_supported(int prec, uint64_t nx, uint64_t ny, uint64_t nz);
+int row3_ctas(int prec, int l, size_t lines);
+int col3_ctas(int prec, int l, int inner, int outer);
+template <class T> cudaError_t launch3_row(int l, size_t lines, const Pass3Args &a, cudaStream_t st);
+template <class T> cudaError_t launch3_col(int l, int inner, int outer, const Pass3Args &a, cudaStream_t st);
+
 // record `msg` as the calling thread's qsg_last_error(); returns code
 int set_last_error(int code, const std::string &msg);
 

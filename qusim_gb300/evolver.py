@@ -219,6 +219,21 @@ class Instance:
         return cls(ctx, h, (nx, ny), dx * dy, 1 if precision == "mixed" else 0)
 
     @classmethod
+    def create_3d(cls, ctx, psi0, V, dx, dy, dz, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
+        """A 3D instance (index (ix*ny + iy)*nz + iz; qsg_create_3d)."""
+        psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        if psi0.ndim != 3 or V.shape != psi0.shape:
+            raise ValueError("psi0 and V must be 3D arrays of the same shape (nx, ny, nz)")
+        dt = complex(dt)
+        nx, ny, nz = psi0.shape
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_3d(ctx.h, nx, ny, nz, dx, dy, dz, mass, hbar, dt.real, dt.imag, order,
+                                    _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                    _dptr(psi0.view(np.float64)), _dptr(V), ctypes.byref(h)))
+        return cls(ctx, h, psi0.shape, dx * dy * dz, 1 if precision == "mixed" else 0)
+
+    @classmethod
     def create_2d(cls, ctx, psi0, V, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
         psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
         V = np.ascontiguousarray(V, dtype=np.float64)
