@@ -1,7 +1,7 @@
 """Benchmark of the split-operator step on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload 2d4096|2d1024|1d4096|batch1d|serving|born2d]
+                    [--workload 2d4096|2d1024|1d4096|batch1d|serving|born2d|3d256]
                     [--precision mixed|fp64]
 
 Default workload: the large 2D configuration -- 4096x4096 periodic grid on
@@ -54,6 +54,9 @@ WORKLOADS = {
                         "well 0.3 exp(-r^2/4) with a weak absorbing spot, preconditioned (Vellekoop), order 20 "
                         "updates per Compute, incident along x", dim=-2, nx=2048, ny=2048, half=150.0, en=2.0,
                    order=20, preconditioner=1),
+    "3d256": dict(desc="3D 256^3 on [-25.6,25.6)^3, Gaussian packet k=(1.5,-0.5,0.8), s=2 at the origin, "
+                       "Gaussian bump 0.8 exp(-|r-c|^2/2) (seed 0), dt=0.01, O4", dim=-3, n=256, half=25.6,
+                  dt=0.01, order=4),
     "serving": dict(desc="serving: seeded Poisson arrivals; 70% 1D N log-uniform 2^10..2^18, 30% 2D side "
                          "log-uniform 256..2048 (both rounded to powers of two); steps U{100..5000}; O2/O4 50/50; "
                          "complex64; 120 GB budget", dim=-1),
@@ -268,6 +271,10 @@ def born_cpu_sample(budget_s, order):
 def run_reference(args, w):
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if w["dim"] == -3:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no 3D evolver (only the 3D "
+                          "transform); its 2D/1D step formulas extended to three axes are the oracle's"}), flush=True)
         return
     if w["dim"] == -2:
         cpu = born_cpu_sample(120.0 / max(1, args.steps + args.warmup) * args.steps, 2)
@@ -588,6 +595,140 @@ def run_born(args, w):
         print(json.dumps(line), flush=True)
 
 
+def inputs_3d(n, half, seed=0):
+    xs = -half + 2 * half / n * np.arange(n)
+    X, Y, Z = np.meshgrid(xs, xs, xs, indexing="ij")
+    psi = np.exp(1j * (1.5 * X - 0.5 * Y + 0.8 * Z)) * np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / (4 * 2.0 ** 2))
+    c = np.random.default_rng(seed).uniform(-3, 3, size=3)
+    V = 0.8 * np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / 2.0)
+    d = 2 * half / n
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * d ** 3)
+    return psi.astype(np.complex128), V, d
+
+
+def run_3d(args, w):
+    """The 3D split-operator: a step is one O4 step of the 256^3 grid."""
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import qusim_gb300 as q
+    n, h = w["n"], w["half"]
+    psi0, V, d = inputs_3d(n, h)
+    sites = psi0.size
+    ctx = q.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    inst = q.Instance.create_3d(ctx, psi0, V, d, d, d, w["dt"], order=w["order"], precision=args.precision)
+    inst.step(args.warmup)
+    inst.sync()
+    ctx.profile(2)
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    inst.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    ms = world_max(e0.elapsed_time(e1), world)
+    counts = ctx.profile_read()
+    ctx.profile(False)
+    ctx.profile(True)
+    inst.step(args.steps)
+    inst.sync()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    value = whole_job_rate(sites * args.steps, world, ms / 1e3)
+    sc = 8 if args.precision == "mixed" else 16
+    # O4: 9 line passes of psi in and out, 3 of them also read a V table
+    step_b = (9 * 2 + 3) * sc if w["order"] == 4 else (3 * 2 + 1) * sc
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    nl, tot = dom[1]
+    # x passes: 3 per step, two of them with a V table
+    per_launch = (2 * sc + (2 * sc / 3 if dom[0] == "pass3_x" else 0)) * sites
+    ach = per_launch / (tot / nl / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom[0], "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "peak_source": peak_kind, "avg_launch_ms": tot / nl, "algorithmic_bytes_per_launch": per_launch,
+            "traffic": None, "share": tot / sum(v[1] for v in prof.values())}
+    step_roof = {"algorithmic_bytes_per_site_step": step_b, "achieved_gbs": step_b * value / world / 1e9,
+                 "frac": step_b * value / world / 1e9 / peak}
+    acc = plain = None
+    if not args.no_plain and args.precision == "mixed":
+        p64 = q.Instance.create_3d(ctx, psi0, V, d, d, d, w["dt"], order=w["order"], precision="fp64")
+        p64.step(2)
+        p64.sync()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        p64.step(10)
+        f1.record(stream)
+        f1.synchronize()
+        plain = {"value": sites * 10 / (f0.elapsed_time(f1) / 1e3), "unit": "site-steps/s", "dtype": "c128"}
+        m = q.Instance.create_3d(ctx, psi0, V, d, d, d, w["dt"], order=w["order"], precision="mixed")
+        p64.close()
+        p64 = q.Instance.create_3d(ctx, psi0, V, d, d, d, w["dt"], order=w["order"], precision="fp64")
+        nacc = args.accuracy_steps if args.accuracy_steps is not None else 500
+        m.step(nacc)
+        p64.step(nacc)
+        a, b = m.get_psi(), p64.get_psi()
+        acc = {"steps": nacc, "rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+               "norm_mixed": m.norm2(), "norm_fp64": p64.norm2()}
+        m.close()
+        p64.close()
+    # end to end: create (H2D psi0 + V from pinned memory), K x (step + Norm2 read back), psi read back
+    import torch as _t
+    pin_psi = _t.from_numpy(psi0.view(np.float64).copy()).pin_memory()
+    pin_V = _t.from_numpy(np.ascontiguousarray(V, dtype=np.float64)).pin_memory()
+    out = _t.empty(psi0.size * 2, dtype=_t.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2 = q.Instance.create_3d(ctx, pin_psi.numpy().view(np.complex128).reshape(psi0.shape),
+                              pin_V.numpy().reshape(V.shape), d, d, d, w["dt"], order=w["order"],
+                              precision=args.precision)
+    for _ in range(args.steps):
+        e2.step(1)
+        e2.step_norm2()
+    e2.get_psi(out.numpy().view(np.complex128).reshape(psi0.shape))
+    e2.close()
+    el = world_max(time.perf_counter() - t0, world)
+    e2e = {"value": whole_job_rate(sites * args.steps, world, el), "unit": "site-steps/s",
+           "h2d_bytes_per_step": (psi0.nbytes + V.nbytes) / args.steps, "d2h_bytes_per_step": psi0.nbytes / args.steps + 8,
+           "includes": "instance creation (H2D psi0+V, tables), K x (qsg_step(1) + Norm2 read back), final psi read back"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        o = orc.Oracle()
+        m_ = 64
+        ps, Vs, ds = inputs_3d(m_, h * m_ / n)
+        o.evolve3d(ps, Vs, ds, ds, ds, w["dt"], 1, order=w["order"])
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < 15.0:
+            o.evolve3d(ps, Vs, ds, ds, ds, w["dt"], 2, order=w["order"])
+            k += 2
+        cpu = {"value": ps.size * k / (time.perf_counter() - t0), "unit": "site-steps/s", "cores": 1, "kind": "port",
+               "sample": f"{k} O4 steps (in calls of 2, tables rebuilt per call) of a 64^3 grid with the workload's "
+                         "spacing, single thread"}
+    inst.close()
+    if rank == 0:
+        line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                           "parallelism": f"replicas x{world}", "l2": "psi + V tables exceed L2"},
+                "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
+                "gpu_launches": int(sum(v[0] for v in counts.values())),
+                "kernels": {k_: {"launches": v[0], "ms": v[1]} for k_, v in prof.items()},
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def serving_inputs(seed=0):
     """A pool of seeded inputs per power-of-two size (4 variants each): a packet
     and an 8-bump potential as in the batched configuration."""
@@ -744,6 +885,8 @@ def main():
         return run_serving(args, w)
     if w["dim"] == -2:
         return run_born(args, w)
+    if w["dim"] == -3:
+        return run_3d(args, w)
 
     rank, world, local = dist_env()
     import torch
