@@ -505,5 +505,11 @@ struct NamedBarrier {
         asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
     }
 };
+// a line held by the lanes of one warp (2..32 consecutive lanes): __syncwarp
+// on those lanes orders their shared-memory accesses
+struct WarpLineBarrier {
+    unsigned mask;
+    __device__ __forceinline__ void operator()() const { __syncwarp(mask); }
+};
 
 }  // namespace qsg
