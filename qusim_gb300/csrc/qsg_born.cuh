@@ -155,10 +155,7 @@ __global__ void __launch_bounds__(B *G *(NY / E), born_min_blocks(B *G *(NY / E)
     const int m = a.m;
     const int row = blockIdx.x * B + b + j * m;
     const RowLayout<PADS> lay{line * LINE};
-    constexpr bool NAMED = (TL % 32 == 0) && (NL <= 15) && (NL > 1);
-    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
-    LineBar lbar;
-    if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    const auto lbar = LineBarrierOf<TL, NL>::make(line);
     const CtaBarrier cbar{};
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
     const tw_t<C> *twx = static_cast<const tw_t<C> *>(a.tw_nx);
@@ -499,10 +496,7 @@ __global__ void __launch_bounds__(B *(N1 / E)) k_born_fs_row(BornFsRowArgs a)
     const int line = tid / TL, t = tid - line * TL;
     const int row = blockIdx.x * B + line;
     const RowLayout<PADS> lay{line * LINE};
-    constexpr bool NAMED = (TL % 32 == 0) && (B <= 15) && (B > 1);
-    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
-    LineBar lbar;
-    if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    const auto lbar = LineBarrierOf<TL, B>::make(line);
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
     C *p = static_cast<C *>(a.tmp) + (size_t)row * N1 + t;
 

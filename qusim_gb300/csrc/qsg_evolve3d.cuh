@@ -68,15 +68,7 @@ __global__ void __launch_bounds__(B *(L / E)) k3_row(Pass3Args a)
     const int line = tid / TL, t = tid - line * TL;
     const size_t base = ((size_t)blockIdx.x * B + line) * L + t;
     const RowLayout<PADS> lay{line * LINE};
-    // lines within one warp synchronise with __syncwarp; whole-warp lines with
-    // a named barrier; otherwise the CTA
-    constexpr bool WARP = TL > 1 && TL <= 32;
-    constexpr bool NAMED = !WARP && (TL % 32 == 0) && (B <= 15) && (B > 1);
-    using LineBar = typename std::conditional<WARP, WarpLineBarrier,
-                                              typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type>::type;
-    LineBar lbar;
-    if constexpr (WARP) lbar = WarpLineBarrier{(TL == 32 ? 0xffffffffu : ((1u << TL) - 1u)) << ((line * TL) & 31)};
-    if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    const auto lbar = LineBarrierOf<TL, B>::make(line);
     C *psi = static_cast<C *>(a.psi);
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
     const C *kt = static_cast<const C *>(a.k);

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace qsg {
 
 template <class T> struct CplxOf;
@@ -510,6 +512,24 @@ struct NamedBarrier {
 struct WarpLineBarrier {
     unsigned mask;
     __device__ __forceinline__ void operator()() const { __syncwarp(mask); }
+};
+
+// The barrier of one line of TL threads in a CTA of NL lines (line l holds
+// threads [l*TL, (l+1)*TL)): __syncwarp when lines are parts of one warp, a
+// named barrier per line when lines are whole warps (at most 15 of them),
+// otherwise the CTA barrier.
+template <int TL, int NL> struct LineBarrierOf {
+    static constexpr bool WARP = TL > 1 && TL <= 32 && NL > 1;
+    static constexpr bool NAMED = !WARP && (TL % 32 == 0) && NL <= 15 && NL > 1;
+    using type = typename std::conditional<
+        WARP, WarpLineBarrier, typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type>::type;
+    static __device__ __forceinline__ type make(int line)
+    {
+        type b;
+        if constexpr (WARP) b = WarpLineBarrier{(TL == 32 ? 0xffffffffu : ((1u << TL) - 1u)) << ((line * TL) & 31)};
+        if constexpr (NAMED) b = NamedBarrier{1 + line, TL};
+        return b;
+    }
 };
 
 }  // namespace qsg

@@ -172,10 +172,7 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
     const C *vt = static_cast<const C *>(a.vtab);
     const CtaBarrier cbar{};
     // lines of whole warps synchronise among themselves; otherwise CTA-wide
-    constexpr bool NAMED = (TL % 32 == 0) && (LPR <= 15) && (LPR > 1);
-    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
-    LineBar lbar;
-    if constexpr (NAMED) lbar = NamedBarrier{1 + grp, TL};
+    const auto lbar = LineBarrierOf<TL, LPR>::make(grp);
     constexpr bool via_smem_in = in_split && G > 1;
     const bool via_smem_out = out_split && G > 1;
     constexpr int XV = B * NY / NT;                       // x-split columns per thread
@@ -663,10 +660,7 @@ __global__ void __launch_bounds__(B *(N1 / E)) k_fs_row(FsRowArgs a)
     const int line = tid / TL, t = tid - line * TL;
     const int row = blockIdx.x * B + line;
     const RowLayout<PADS> lay{line * LINE};
-    constexpr bool NAMED = (TL % 32 == 0) && (B <= 15) && (B > 1);
-    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
-    LineBar lbar;
-    if constexpr (NAMED) lbar = NamedBarrier{1 + line, TL};
+    const auto lbar = LineBarrierOf<TL, B>::make(line);
     C *psi = static_cast<C *>(in.psi);
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_row);
     const size_t base = (size_t)row * N1 + t;
@@ -768,10 +762,7 @@ __global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatch
     const C *k1 = static_cast<const C *>(in.ktab[1]);
     const RowLayout<PADS> lay{line * padded<L, PADS>(L)};
     // instances are independent: lines of whole warps synchronise on their own
-    constexpr bool NAMED = (TL % 32 == 0) && NI > 1 && NI <= 15;
-    using LineBar = typename std::conditional<NAMED, NamedBarrier, CtaBarrier>::type;
-    LineBar bar;
-    if constexpr (NAMED) bar = NamedBarrier{1 + line, TL};
+    const auto bar = LineBarrierOf<TL, NI>::make(line);
     constexpr T inv_n = T(1) / T(L);
 
     C x[E];
