@@ -53,6 +53,10 @@ template <class C> __device__ __forceinline__ C k3_apply(C x, const C *kt, int k
 }
 
 // B contiguous lines (z) of L per CTA
+// strided passes: three 256-thread CTAs per SM (registers capped at 85), as
+// they are bound by the latency of their scattered loads, not by issue
+constexpr int min_blocks3(int threads) { return threads <= 256 ? 3 : 1; }
+
 template <class T, int L, int E, int B>
 __global__ void __launch_bounds__(B *(L / E)) k3_row(Pass3Args a)
 {
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(B *(L / E)) k3_row(Pass3Args a)
 // strided lines (y or x): W adjacent z positions, line element i at
 // o * s_outer + c + i * s_line (blockIdx.y = o, blockIdx.x * W + lane = c)
 template <class T, int L, int E, int W>
-__global__ void __launch_bounds__(W *(L / E)) k3_col(Pass3Args a)
+__global__ void __launch_bounds__(W *(L / E), min_blocks3(W *(L / E))) k3_col(Pass3Args a)
 {
     using C = cplx_t<T>;
     constexpr int TM = Plan<L, E>::TL;
