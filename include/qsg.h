@@ -156,6 +156,15 @@ int qsg_norm2(qsg_inst *inst, double *out);
  * monitoring; qsg_norm2 is the reference's Norm2. */
 int qsg_step_norm2(qsg_inst *inst, double *out);
 
+/* The same value, read without stalling the stream: _post queues its sum and
+ * a device-to-host copy after the work queued so far and returns a ticket;
+ * _get waits for that copy only (later steps keep running) and returns the
+ * value.  A loop can step, post, and collect the previous step's norm while
+ * the current step runs.  The instance keeps the last 64 posts; older tickets
+ * give QSG_ERR_STATE. */
+int qsg_step_norm2_post(qsg_inst *inst, uint64_t *ticket);
+int qsg_step_norm2_get(qsg_inst *inst, uint64_t ticket, double *out);
+
 /* Kinetic and potential energy, as QuEvolverImpl::KinEn / PotEn
  * (src/SplittingMethod1D.cpp:91-107, src/SplittingMethod2D.cpp:123-138,
  * src/EvolverImpl.cpp:45-49).  Either pointer may be null. */

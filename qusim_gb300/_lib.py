@@ -39,7 +39,7 @@ EXPORTS = [
     "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc", "qsg_create_1d_spec", "qsg_create_2d_spec",
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
-    "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d",
+    "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d", "qsg_step_norm2_post", "qsg_step_norm2_get",
 ]
 
 # qsg_born_preconditioner / qsg_born_field
@@ -148,6 +148,8 @@ def _declare(lib):
     lib.qsg_sync.argtypes = [_vp]
     lib.qsg_norm2.argtypes = [_vp, _dp]
     lib.qsg_step_norm2.argtypes = [_vp, _dp]
+    lib.qsg_step_norm2_post.argtypes = [_vp, ctypes.POINTER(_u64)]
+    lib.qsg_step_norm2_get.argtypes = [_vp, _u64, _dp]
     lib.qsg_energies.argtypes = [_vp, _dp, _dp]
     lib.qsg_xavg.argtypes = [_vp, _d, _dp]
     lib.qsg_norm2_range.argtypes = [_vp, _d, _d, _d, _dp]

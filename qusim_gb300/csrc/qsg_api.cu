@@ -102,6 +102,13 @@ struct qsg_inst {
     void *k3[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     const void *tw3[3] = {nullptr, nullptr, nullptr};
     double *kparts3 = nullptr;
+    // ring of posted per-step norms (qsg_step_norm2_post / _get)
+    static constexpr int kRing = 64;
+    double *ring_dev = nullptr;    // kRing device slots
+    double *ring_host = nullptr;   // pinned mirror
+    cudaEvent_t ring_ev[kRing] = {};
+    double ring_scale[kRing] = {};
+    uint64_t ring_next = 0;
     std::vector<void *> allocs;
     size_t bytes = 0;
 };
@@ -547,6 +554,9 @@ int upload_psi(qsg_inst *in, const double *psi)
 void free_inst(qsg_inst *in)
 {
     if (!in) return;
+    if (in->ring_host) cudaFreeHost(in->ring_host);
+    for (cudaEvent_t &e : in->ring_ev)
+        if (e) cudaEventDestroy(e);
     if (in->ctx) {
         // ordered after everything queued on the context stream (work on other
         // streams is joined into it before an instance is released)
@@ -1110,6 +1120,53 @@ int qsg_step_norm2(qsg_inst *in, double *out)
     int rc = reduce(in, 0, in->n, 0, &s);
     if (rc) return rc;
     *out = s * in->dv;
+    return QSG_OK;
+}
+
+int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
+{
+    if (!in || !ticket) return fail(QSG_ERR_ARG, "qsg_step_norm2_post: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    qsg_ctx *ctx = in->ctx;
+    int rc;
+    if (!in->ring_dev) {
+        void *p = nullptr;
+        if ((rc = inst_alloc(in, sizeof(double) * qsg_inst::kRing, &p))) return rc;
+        in->ring_dev = static_cast<double *>(p);
+        QSG_CUDA(cudaMallocHost(&in->ring_host, sizeof(double) * qsg_inst::kRing));
+        for (cudaEvent_t &e : in->ring_ev) QSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const int slot = (int)(in->ring_next % qsg_inst::kRing);
+    double *dst = in->ring_dev + slot;
+    if (in->dim == 2 && in->pending && in->dt.imag() == 0) {
+        // as qsg_step_norm2: the last column pass's split-k sums
+        const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
+        QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, dst, ctx->st));
+        in->ring_scale[slot] = ((double)in->geom.g * in->ny) * in->dv;
+    } else {
+        if ((rc = settle(in))) return rc;
+        int np = 0;
+        QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, in->n, 0, ctx->partials, ctx->max_partials, &np,
+                                    ctx->st));
+        QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, dst, ctx->st));
+        in->ring_scale[slot] = in->dv;
+    }
+    QSG_CUDA(cudaMemcpyAsync(in->ring_host + slot, dst, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaEventRecord(in->ring_ev[slot], ctx->st));
+    *ticket = in->ring_next++;
+    return QSG_OK;
+}
+
+int qsg_step_norm2_get(qsg_inst *in, uint64_t ticket, double *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_step_norm2_get: null argument");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (ticket >= in->ring_next) return fail(QSG_ERR_ARG, "qsg_step_norm2_get: ticket not posted");
+    if (in->ring_next - ticket > (uint64_t)qsg_inst::kRing)
+        return fail(QSG_ERR_STATE, "qsg_step_norm2_get: ticket overwritten (more than 64 posts since)");
+    const int slot = (int)(ticket % qsg_inst::kRing);
+    QSG_CUDA(cudaEventSynchronize(in->ring_ev[slot]));  // that copy only, not the work queued after it
+    *out = in->ring_host[slot] * in->ring_scale[slot];
     return QSG_OK;
 }
 

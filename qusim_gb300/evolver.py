@@ -265,6 +265,18 @@ class Instance:
         check(self.ctx.lib.qsg_step_norm2(self.h, ctypes.byref(v)))
         return v.value
 
+    def post_step_norm2(self) -> int:
+        """Queue the step's Norm2 for reading without stalling the stream; returns a ticket."""
+        t = ctypes.c_uint64()
+        check(self.ctx.lib.qsg_step_norm2_post(self.h, ctypes.byref(t)))
+        return t.value
+
+    def get_step_norm2(self, ticket: int) -> float:
+        """The Norm2 posted under `ticket` (waits for that copy only)."""
+        v = ctypes.c_double()
+        check(self.ctx.lib.qsg_step_norm2_get(self.h, ticket, ctypes.byref(v)))
+        return v.value
+
     def energies(self):
         k, p = ctypes.c_double(), ctypes.c_double()
         check(self.ctx.lib.qsg_energies(self.h, ctypes.byref(k), ctypes.byref(p)))

@@ -83,3 +83,44 @@ def test_plan_change_and_energies_settle(q):
     a.close()
     b.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_posted_step_norms(q, dim):
+    """post / get returns each step's norm while later steps run; equals step_norm2."""
+    ctx = q.Context(0)
+    if dim == 2:
+        psi0, dx, dy = gauss_packet_2d(256, 256, -30, 30, -30, 30, 1.0, 0.0, -5.0, 0.0, 3.0)
+        V = gaussian_bumps_2d(256, 256, -30, 30, -30, 30, nbumps=4, seed=7, spread=10.0)
+        a = q.Instance.create_2d(ctx, psi0 * 0.9, V, dx, dy, 0.01, order=4, precision="fp64")
+    elif dim == 1:
+        from tests.workloads import gauss_packet_1d
+        psi0, V, dx = gauss_packet_1d(4096, -200.0, 200.0, 1.0, -50.0, 10.0)
+        a = q.Instance.create_1d(ctx, psi0 * 0.9, V, dx, 0.05, order=2, precision="fp64")
+    else:
+        rng = np.random.default_rng(3)
+        psi0 = (rng.normal(size=(16, 16, 32)) + 1j * rng.normal(size=(16, 16, 32))) * 0.1
+        V = rng.uniform(0, 1, size=psi0.shape)
+        a = q.Instance.create_3d(ctx, psi0, V, 0.5, 0.5, 0.5, 0.01, order=4, precision="fp64")
+    want = a.norm2()
+    tickets, got = [], []
+    for _ in range(5):
+        a.step(1)
+        tickets.append(a.post_step_norm2())
+        if len(tickets) > 1:
+            got.append(a.get_step_norm2(tickets[-2]))
+    got.append(a.get_step_norm2(tickets[-1]))
+    assert len(got) == 5
+    for g in got:
+        assert abs(g - want) <= 1e-12 * want
+    assert abs(a.step_norm2() - got[-1]) <= 1e-13 * want
+    with pytest.raises(q.QsgError) as e:
+        a.get_step_norm2(tickets[-1] + 1)
+    assert e.value.code == 1
+    for _ in range(64):
+        a.post_step_norm2()
+    with pytest.raises(q.QsgError) as e:
+        a.get_step_norm2(tickets[0])
+    assert e.value.code == 6
+    a.close()
+    ctx.close()
