@@ -433,10 +433,20 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
     if (a.partials) {
         // the norm of the step's state without a pass of its own: in split-k
         // space sum |psi|^2 is 1 / (G Ny) of the real-space one (the row FFT and
-        // the radix-G stage are unnormalised, the column pass carries 1/(Nx Ny))
-        double s = 0;
+        // the radix-G stage are unnormalised, the column pass carries 1/(Nx Ny)).
+        // complex64 sums a thread's elements in FP32 (FP64 runs at 1/64 rate:
+        // per-element FP64 doubled this pass), the CTA sum in FP64.
+        double s;
+        if constexpr (sizeof(C) == 8) {
+            float f = 0;
 #pragma unroll
-        for (int e = 0; e < E; ++e) s += abs2d(x[e]);
+            for (int e = 0; e < E; ++e) f = fmaf(x[e].x, x[e].x, fmaf(x[e].y, x[e].y, f));
+            s = f;
+        } else {
+            s = 0;
+#pragma unroll
+            for (int e = 0; e < E; ++e) s += abs2d(x[e]);
+        }
         s = block_sum<W *(M / E)>(s, red);
         if (tid == 0) a.partials[blockIdx.x] = s;
     }

@@ -16,6 +16,7 @@ anything else raises, as the reference raises for unsupported solvers
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import weakref
 import enum
@@ -111,6 +112,20 @@ class Options:
         return self._kv.get(k, default)
 
 
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_contexts():
+    # at interpreter exit, while the CUDA runtime is still up: every context
+    # closes its instances, batches and solvers, then itself
+    for c in list(_live_contexts):
+        try:
+            c.close()
+        except Exception:
+            pass
+
+
 class Context:
     """One qsg_ctx (a device, a stream, an HBM budget)."""
 
@@ -121,6 +136,7 @@ class Context:
         self.h = h
         self.lib = lib
         self._children = weakref.WeakSet()
+        _live_contexts.add(self)
 
     def _adopt(self, obj):
         """obj (an instance, batch or solver of this context) is closed before the context."""
@@ -416,6 +432,7 @@ class Server:
         h = ctypes.c_void_p()
         check(self.lib.qsg_server_create(device, hbm_budget, max_running, ctypes.byref(h)))
         self.h = h
+        _live_contexts.add(self)  # closed at exit with the contexts
         self._shapes = {}
 
     def submit_spec(self, spec, shape, dx, dt, nsteps, order=2, precision="mixed", dy=None, mass=1.0, hbar=1.0):
