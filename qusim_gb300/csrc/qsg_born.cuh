@@ -213,13 +213,18 @@ __global__ void __launch_bounds__(B *G *(NY / E), born_min_blocks(B *G *(NY / E)
             for (int e = 0; e < E; ++e) st_stream(p + e * TL, x[e]);
         }
         if (a.partials) {
+            // complex64: a thread's sums in FP32 (FP64 per element is slow here)
             const C *p = static_cast<const C *>(a.dstart) + base;
+            using R = typename RealOf<C>::type;
+            R f0 = 0, f1 = 0;
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const C s = ld_stream(p + e * TL);
-                s0 += abs2d(csub(x[e], s));
-                s1 += abs2d(x[e]);
+                const C d = csub(x[e], ld_stream(p + e * TL));
+                f0 += d.x * d.x + d.y * d.y;
+                f1 += x[e].x * x[e].x + x[e].y * x[e].y;
             }
+            s0 = f0;
+            s1 = f1;
         }
     }
     if (a.out_k) {
