@@ -568,8 +568,10 @@ struct FsColArgs {
     int in_k, out_k;        // input in k layout / output to k layout
 };
 
+// three 256-thread CTAs per SM (registers capped at 85) for the strided
+// column pass: it waits on its scattered loads more than it issues
 template <class T, int N2, int E, int W>
-__global__ void __launch_bounds__(W *(N2 / E)) k_fs_col(FsColArgs a)
+__global__ void __launch_bounds__(W *(N2 / E), (W * (N2 / E) <= 256 && sizeof(T) == 4) ? 3 : 1) k_fs_col(FsColArgs a)
 {
     using C = cplx_t<T>;
     constexpr int TM = Plan<N2, E>::TL;
