@@ -526,12 +526,11 @@ int build_tables(qsg_inst *in)
                 QSG_CUDA(qsg::launch_ktable2d(in->ktab[k], in->nx, in->ny, a.real(), a.imag(), DTx, DTy,
                                               1.0 / ((double)in->nx * in->ny), ctx->st));
             } else {
-                // per-axis factors - 1 as float hi + lo pairs (16 B per entry)
                 const cd fx = a * DTx, fy = a * DTy;
-                if ((rc = inst_alloc(in, (size_t)in->nx * 16, &in->kx[k]))) return rc;
-                if ((rc = inst_alloc(in, (size_t)in->ny * 16, &in->ky[k]))) return rc;
-                QSG_CUDA(qsg::launch_ktable1d_hl(in->kx[k], in->nx, fx.real(), fx.imag(), ctx->st));
-                QSG_CUDA(qsg::launch_ktable1d_hl(in->ky[k], in->ny, fy.real(), fy.imag(), ctx->st));
+                if ((rc = inst_alloc(in, (size_t)in->nx * cs, &in->kx[k]))) return rc;
+                if ((rc = inst_alloc(in, (size_t)in->ny * cs, &in->ky[k]))) return rc;
+                QSG_CUDA(qsg::launch_ktable1d(1, in->kx[k], in->nx, fx.real(), fx.imag(), 1.0, ctx->st));
+                QSG_CUDA(qsg::launch_ktable1d(1, in->ky[k], in->ny, fy.real(), fy.imag(), 1.0, ctx->st));
             }
         }
     }

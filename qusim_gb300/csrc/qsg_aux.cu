@@ -38,29 +38,6 @@ __device__ __forceinline__ float2 cexpm1_f(double x, double y)
     return make_float2(float(expm1(x) - 2.0 * ex * sh * sh), float(ex * s));
 }
 
-// exp(x + iy) - 1 as float hi + lo pairs {hi.re, hi.im, lo.re, lo.im}: the
-// complex64 kinetic factors, applied every step to the same frequency, so the
-// rounding of a one-float table entry would turn into a phase drift that grows
-// linearly with the step count
-__device__ __forceinline__ float4 cexpm1_hl(double x, double y)
-{
-    double sh, ch;
-    sincos(0.5 * y, &sh, &ch);
-    double re, im;
-    if (x == 0.0) {
-        re = -2.0 * sh * sh;
-        im = 2.0 * sh * ch;
-    } else {
-        double s, c;
-        sincos(y, &s, &c);
-        const double ex = exp(x);
-        re = expm1(x) - 2.0 * ex * sh * sh;
-        im = ex * s;
-    }
-    const float hr = (float)re, hi = (float)im;
-    return make_float4(hr, hi, (float)(re - (double)hr), (float)(im - (double)hi));
-}
-
 template <class C> __device__ __forceinline__ C phase_entry(double x, double y, double scale);
 template <> __device__ __forceinline__ double2 phase_entry<double2>(double x, double y, double scale)
 {
@@ -88,15 +65,6 @@ __global__ void k_ktable1d(C *out, int n, double fre, double fim, double scale)
         const double f = double(i > n / 2 ? n - i : i);
         const double s = f * f;
         out[i] = phase_entry<C>(fre * s, fim * s, scale);
-    }
-}
-
-__global__ void k_ktable1d_hl(float4 *out, int n, double fre, double fim)
-{
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double f = double(i > n / 2 ? n - i : i);
-        const double s = f * f;
-        out[i] = cexpm1_hl(fre * s, fim * s);
     }
 }
 
@@ -244,12 +212,6 @@ cudaError_t launch_vtable(int prec, void *out, const double *V, size_t n, double
         k_vtable<float2><<<blocks_for(n), kThreads, 0, st>>>((float2 *)out, V, n, fre, fim);
     else
         k_vtable<double2><<<blocks_for(n), kThreads, 0, st>>>((double2 *)out, V, n, fre, fim);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_ktable1d_hl(void *out, int n, double fre, double fim, cudaStream_t st)
-{
-    k_ktable1d_hl<<<blocks_for(n), kThreads, 0, st>>>((float4 *)out, n, fre, fim);
     return cudaGetLastError();
 }
 

@@ -14,8 +14,6 @@ cudaError_t launch_vtable(int prec, void *out, const double *V, size_t n, double
 // i < n; fold(i) = i > n/2 ? n - i : i (src/DeviceTemplate.h:544-547, 754-769).
 cudaError_t launch_ktable1d(int prec, void *out, int n, double fre, double fim, double scale,
                             cudaStream_t st);
-// complex64 2D kinetic factors as float hi + lo pairs: exp(f fold(i)^2) - 1, i < n
-cudaError_t launch_ktable1d_hl(void *out, int n, double fre, double fim, cudaStream_t st);
 // infinite-wall kinetic table: scale * exp(f i^2) (fp64) or exp(f i^2) - 1 (complex64), i < n
 cudaError_t launch_ktable_wall(int prec, void *out, int n, double fre, double fim, double scale, cudaStream_t st);
 // four-step kinetic table in row layout: entry k2*n1 + k1 holds the factor of

@@ -71,16 +71,6 @@ template <class C> __device__ __forceinline__ C cmul1p(C a, C m)
     const auto cy = fma(a.y, m.x, a.x * m.y);
     return cmk<C>(a.x + cx, a.y + cy);
 }
-// a * (1 + mh + ml), m given as float hi + lo pairs {mh.re, mh.im, ml.re, ml.im}:
-// the full correction a*(mh + ml) is formed before it is added to a
-__device__ __forceinline__ float2 cmul1p_hl(float2 a, float4 m)
-{
-    float cx = fmaf(a.x, m.x, -(a.y * m.y));
-    float cy = fmaf(a.y, m.x, a.x * m.y);
-    cx += fmaf(a.x, m.z, -(a.y * m.w));
-    cy += fmaf(a.y, m.z, a.x * m.w);
-    return make_float2(a.x + cx, a.y + cy);
-}
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, class C> __device__ __forceinline__ C crot(C a)
 {

@@ -351,8 +351,8 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
 
 struct ColPassArgs {
     void *psi;              // in/out, Nx*Ny in split-k layout
-    const void *kx;         // complex64: x kinetic factor - 1, Nx float hi + lo pairs (float4)
-    const void *ky;         // complex64: y kinetic factor - 1, Ny float hi + lo pairs
+    const void *kx;         // complex64: x kinetic factor - 1, Nx entries
+    const void *ky;         // complex64: y kinetic factor - 1, Ny entries
     const void *k2d;        // complex128: full table Nx*Ny with 1/(Nx Ny) folded in
     const void *tw_col;     // stage-major twiddles for (M, E)
     int nx, ny, g;
@@ -403,14 +403,14 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
         line_fft<C, M, E, false>(x, sm, lay, bar, t, tw);
         if (p == 1) continue;  // (a break here makes the compiler duplicate the body)
         if constexpr (sizeof(C) == 8) {
-            const float4 *kx = opaque(static_cast<const float4 *>(a.kx));
-            const float4 ky = __ldg(static_cast<const float4 *>(a.ky) + col);
+            const C *kx = opaque(static_cast<const C *>(a.kx));
+            const C ky = ld_c(static_cast<const C *>(a.ky) + col);
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const int kxi = a.g * (t + e * TM) + q;
                 C v = cscale(x[e], a.inv_n);
-                v = cmul1p_hl(v, __ldg(kx + kxi));
-                x[e] = cconj(cmul1p_hl(v, ky));
+                v = cmul1p(v, ld_c(kx + kxi));
+                x[e] = cconj(cmul1p(v, ky));
             }
         } else {
             const C *k2 = static_cast<const C *>(a.k2d) + col;
