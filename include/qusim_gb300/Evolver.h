@@ -36,7 +36,7 @@ using Real = double;
 using Complex = std::complex<double>;
 
 enum class BoundaryCondition { Period, InfiniteWall };
-enum class SolverMethod { Unknown, SplittingMethodO2, SplittingMethodO4 };
+enum class SolverMethod { Unknown, SplittingMethodO2, SplittingMethodO4, BornSerise };
 
 template <class T> struct VectorView {
     VectorView(T const *d, size_t s) : fData(d), fSize(s) {}
@@ -71,8 +71,27 @@ template <class T> struct MatrixView {
 //   "precision"    "fp64" (default) or "mixed"
 //   "hbm_budget"   device-memory bound of the context in bytes (0 = none)
 //   "device_ordinal"
+//   Born-series solvers (QuSim.h:288-333): "order", "preconditional",
+//   "preconditioner" ("Vellekoop", "Hao1", "Hao2", "BornIndentity"), "slow"
 struct Options {
     Options &Gb300() { return SetString("device", "GPU_GB300"); }
+    Options &Order(int64_t n) { return SetInt("order", n); }
+    Options &Preconditional(bool v) { return SetInt("preconditional", v ? 1 : 0); }
+    Options &Slow(double v) { return SetReal("slow", v); }
+    Options &VellekoopPreconditioner() { return SetString("preconditioner", "Vellekoop"); }
+    Options &Hao1Preconditioner() { return SetString("preconditioner", "Hao1"); }
+    Options &Hao2Preconditioner() { return SetString("preconditioner", "Hao2"); }
+    Options &BornIdentityPreconditioner() { return SetString("preconditioner", "BornIndentity"); }
+    Options &SetReal(char const *k, double v)
+    {
+        fReals[k] = v;
+        return *this;
+    }
+    double GetReal(char const *k, double dflt) const
+    {
+        auto it = fReals.find(k);
+        return it == fReals.end() ? dflt : it->second;
+    }
     Options &Batch(int64_t n) { return SetInt("batch", n); }
     Options &PrecisionFp64() { return SetString("precision", "fp64"); }
     Options &PrecisionMixed() { return SetString("precision", "mixed"); }
@@ -102,6 +121,7 @@ struct Options {
   private:
     std::map<std::string, int64_t> fInts;
     std::map<std::string, std::string> fStrings;
+    std::map<std::string, double> fReals;
 };
 
 namespace detail {
@@ -322,6 +342,199 @@ class Evolver2D : public Evolver {
     MatrixView<Real> GetV() { return MatrixView<Real>(fVHost.data(), fNx, fNy); }
     size_t GetNx() { return fNx; }
     size_t GetNy() { return fNy; }
+
+  private:
+    size_t fNx = 0, fNy = 0;
+};
+
+// ---------------------------------------------------------------------------
+// Born-series scattering solvers: QuPerturbation1D / QuPerturbation2D
+// (QuSim.h:643-806), over qsg_born_*.  As in the reference, V is a functor
+// sampled at x_i = x0 + i*dx (complex: the absorbing layer of the
+// preconditioned series goes into its imaginary part).  One difference: the
+// reference's OptionsImpl::GetBool(key, default) returns whether the key is
+// present (src/OptionsImpl.cpp:88-91), so there Preconditional(false) selects
+// the preconditioned series; here the value is used.
+// ---------------------------------------------------------------------------
+
+namespace detail {
+inline qsg_born_opts born_opts(Options const &o)
+{
+    qsg_born_opts b;
+    qsg_born_default_opts(&b);
+    b.order = (int)o.GetInt("order", 1);
+    b.preconditional = (int)o.GetInt("preconditional", 0);
+    b.slow = o.GetReal("slow", 1.0);
+    const std::string p = o.GetString("preconditioner", "Vellekoop");
+    if (p == "Vellekoop") b.preconditioner = QSG_BORN_VELLEKOOP;
+    else if (p == "Hao1") b.preconditioner = QSG_BORN_HAO1;
+    else if (p == "Hao2") b.preconditioner = QSG_BORN_HAO2;
+    else if (p == "BornIndentity") b.preconditioner = QSG_BORN_IDENTITY;
+    else throw std::runtime_error("Unknown preconditioner");
+    return b;
+}
+}  // namespace detail
+
+class QuScatteringProblemSolver {
+  public:
+    QuScatteringProblemSolver(QuScatteringProblemSolver const &) = delete;
+    QuScatteringProblemSolver &operator=(QuScatteringProblemSolver const &) = delete;
+    virtual ~QuScatteringProblemSolver()
+    {
+        if (fBorn) qsg_born_destroy(fBorn);
+    }
+    void Compute()
+    {
+        detail::check(qsg_born_compute(fBorn));
+        fPsiValid = false;
+    }
+    Real GetEnergy() { return fE; }
+    Real GetMomentum() { return std::sqrt(2 * fMass * fE); }
+    SolverMethod GetMethod() { return SolverMethod::BornSerise; }
+    Real GetEpsilon()
+    {
+        double e;
+        detail::check(qsg_born_epsilon(fBorn, &e));
+        return e;
+    }
+
+  protected:
+    QuScatteringProblemSolver() = default;
+    int Setup(SolverMethod met, Real en, Real mass, Real hbar, Options const &opts)
+    {
+        if (met != SolverMethod::BornSerise) throw std::runtime_error("not support method!");
+        const int prec = detail::device_precision(opts);
+        fCtx = detail::context((int)opts.GetInt("device_ordinal", 0), opts.GetInt("hbm_budget", 0));
+        fE = en;
+        fMass = mass;
+        fHbar = hbar;
+        return prec;
+    }
+    void Fetch(int what, std::vector<Complex> &dst)
+    {
+        detail::check(qsg_born_get(fBorn, what, reinterpret_cast<double *>(dst.data())));
+    }
+
+    std::shared_ptr<qsg_ctx> fCtx;
+    qsg_born *fBorn = nullptr;
+    Real fE = 0, fMass = 1, fHbar = 1;
+    std::vector<Complex> fPsi, fPsi0, fV;
+    bool fPsiValid = false;
+};
+
+class QuPerturbation1D : public QuScatteringProblemSolver {
+  public:
+    QuPerturbation1D() = default;
+    void init(std::function<Complex(Real)> const &v, Real x0, Real x1, size_t n, Real en, Real epsilon,
+              Real direction, SolverMethod met, Real mass, Real hbar, Options const &opts)
+    {
+        const int prec = Setup(met, en, mass, hbar, opts);
+        fN = n;
+        fDx = (x1 - x0) / n;
+        std::vector<Complex> V(n);
+        for (size_t i = 0; i < n; ++i) V[i] = v(x0 + fDx * i);
+        const qsg_born_opts o = detail::born_opts(opts);
+        detail::check(qsg_born_create_1d(fCtx.get(), n, x0, x1, reinterpret_cast<double const *>(V.data()), en,
+                                         epsilon, direction, mass, hbar, &o, prec, &fBorn));
+        fPsi.resize(n);
+        fPsi0.resize(n);
+        fV.resize(n);
+        Fetch(QSG_BORN_PSI0, fPsi0);
+        Fetch(QSG_BORN_V, fV);
+    }
+    VectorView<Complex> GetPsi()
+    {
+        if (!fPsiValid) {
+            Fetch(QSG_BORN_PSI, fPsi);
+            fPsiValid = true;
+        }
+        return VectorView<Complex>(fPsi.data(), fN);
+    }
+    VectorView<Complex> GetPsi0() { return VectorView<Complex>(fPsi0.data(), fN); }
+    VectorView<Complex> GetV() { return VectorView<Complex>(fV.data(), fN); }
+    size_t GetNPoints() { return fN; }
+    Real GetT()
+    {
+        double r, t;
+        detail::check(qsg_born_rt(fBorn, &r, &t));
+        return t;
+    }
+    Real GetR()
+    {
+        double r, t;
+        detail::check(qsg_born_rt(fBorn, &r, &t));
+        return r;
+    }
+    // src/Perturbation1DImpl.h:22-61
+    Real GetMaxMomentum() { return 2 * M_PI / fDx * fHbar; }
+    Real GetMaxEnergy() { return 0.5 * GetMaxMomentum() * GetMaxMomentum() / fMass; }
+    Real GetMomentumGap() { return 2 * M_PI / (fDx * fN) * fHbar; }
+    Real GetEpsilonMomentumWidth() { return fMass * std::abs(GetEpsilon()) / std::sqrt(2 * fMass * fE); }
+    Real GetEnergyGap() { return std::sqrt(2 * fMass * fE) / fMass * GetMomentumGap(); }
+    Real GetEpsilonDecayLength() { return 2 * M_PI / (GetMomentum() / fHbar * GetEpsilon() / (2 * fE)); }
+    Real GetEpsilonBoundaryError()
+    {
+        return std::exp(-(fN * fDx / 2) * (GetMomentum() / fHbar) * GetEpsilon() / (2 * fE));
+    }
+
+  private:
+    size_t fN = 0;
+    Real fDx = 0;
+};
+
+class QuPerturbation2D : public QuScatteringProblemSolver {
+  public:
+    QuPerturbation2D() = default;
+    void init(std::function<Complex(Real, Real)> const &v, Real x0, Real x1, size_t nx, Real y0, Real y1, size_t ny,
+              Real en, Real epsilon, Real directionx, Real directiony, SolverMethod met, Real mass, Real hbar,
+              Options const &opts)
+    {
+        const int prec = Setup(met, en, mass, hbar, opts);
+        fNx = nx;
+        fNy = ny;
+        const Real dx = (x1 - x0) / nx, dy = (y1 - y0) / ny;
+        std::vector<Complex> V(nx * ny);
+        for (size_t i = 0; i < nx; ++i)
+            for (size_t j = 0; j < ny; ++j) V[j + i * ny] = v(x0 + dx * i, y0 + dy * j);
+        const qsg_born_opts o = detail::born_opts(opts);
+        detail::check(qsg_born_create_2d(fCtx.get(), (int)nx, (int)ny, x0, x1, y0, y1,
+                                         reinterpret_cast<double const *>(V.data()), en, epsilon, directionx,
+                                         directiony, mass, hbar, &o, prec, &fBorn));
+        fPsi.resize(nx * ny);
+        fPsi0.resize(nx * ny);
+        fV.resize(nx * ny);
+        Fetch(QSG_BORN_PSI0, fPsi0);
+        Fetch(QSG_BORN_V, fV);
+    }
+    MatrixView<Complex> GetPsi()
+    {
+        if (!fPsiValid) {
+            Fetch(QSG_BORN_PSI, fPsi);
+            fPsiValid = true;
+        }
+        return MatrixView<Complex>(fPsi.data(), fNx, fNy);
+    }
+    MatrixView<Complex> GetPsi0() { return MatrixView<Complex>(fPsi0.data(), fNx, fNy); }
+    MatrixView<Complex> GetV() { return MatrixView<Complex>(fV.data(), fNx, fNy); }
+    Real ComputeXSection(Real cosx, Real cosy)
+    {
+        const double cs[2] = {cosx, cosy};
+        double out;
+        detail::check(qsg_born_xsection(fBorn, 1, cs, &out));
+        return out;
+    }
+    Real ComputeTotalXSection(int64_t n)
+    {
+        double out;
+        detail::check(qsg_born_total_xsection(fBorn, (int)n, &out));
+        return out;
+    }
+    Real GetDeltaPsiNorm()
+    {
+        double out;
+        detail::check(qsg_born_delta_norm(fBorn, &out));
+        return out;
+    }
 
   private:
     size_t fNx = 0, fNy = 0;

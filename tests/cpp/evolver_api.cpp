@@ -62,9 +62,29 @@ int main(int argc, char **argv)
     } catch (std::invalid_argument &) {
         bad_device = true;
     }
+    // Born series through QuPerturbation1D / 2D: the preconditioned setting of
+    // applications/QuScattering1DPrecision (QuScattering1DPrecision.cpp:211-215) on a
+    // power-of-two grid, and a 2D case
+    Options bo = Options().Gb300().Order(5).Preconditional(true);
+    if (mixed) bo.PrecisionMixed();
+    QuPerturbation1D per;
+    per.init([](Real x) { return Complex(0.5 * std::exp(-x * x), 0); }, -100, 100, 2048, 0.5, 0.51, 1,
+             SolverMethod::BornSerise, 1, 1, bo);
+    per.Compute();
+    const double R = per.GetR(), T = per.GetT(), eps = per.GetEpsilon();
+    Options bo2 = Options().Gb300().Order(3).Preconditional(true).Hao2Preconditioner().Slow(0.5);
+    if (mixed) bo2.PrecisionMixed();
+    QuPerturbation2D per2;
+    per2.init([](Real x, Real y) { return Complex(0.3 * std::exp(-(x * x + y * y) / 4), 0); }, -45, 45, 128, -45, 45,
+              128, 2.0, 0.0, 1, 0, SolverMethod::BornSerise, 1, 1, bo2);
+    per2.Compute();
+    const double xs = per2.ComputeXSection(1, 0), dn = per2.GetDeltaPsiNorm();
+
     std::printf("{\"norm0\": %.17g, \"time\": %.17g, \"transmission\": %.17g, \"kin\": %.17g, \"pot\": %.17g, "
-                "\"psi0\": [%.17g, %.17g], \"norm2d\": %.17g, \"wall2d_throws\": %s, \"bad_device_throws\": %s}\n",
+                "\"psi0\": [%.17g, %.17g], \"norm2d\": %.17g, \"wall2d_throws\": %s, \"bad_device_throws\": %s, "
+                "\"born_R\": %.17g, \"born_T\": %.17g, \"born_eps\": %.17g, \"born2d_xsec0\": %.17g, "
+                "\"born2d_delta\": %.17g}\n",
                 n0, e.Time(), trans, kin, pot, psi[0].real(), psi[0].imag(), n2d, threw ? "true" : "false",
-                bad_device ? "true" : "false");
+                bad_device ? "true" : "false", R, T, eps, xs, dn);
     return 0;
 }
