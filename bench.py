@@ -77,19 +77,22 @@ def make_inputs(w):
     return psi, V, (dx, dy)
 
 
-def algorithmic_bytes(w, precision):
+def algorithmic_bytes(w, precision, form="direct"):
     """Minimal-fused-schedule HBM bytes per site-step (psi in and out per pass,
     one V table read per real-space pass): 2D O4 = 6 passes x 2 psi + 3 tables,
-    O2 = 2 passes x 2 psi + 1 table; 1D resident = one round trip per call."""
+    O2 = 2 passes x 2 psi + 1 table; 1D resident = one round trip per call.
+    The momentum form's column passes also read and write the stored state
+    (4 psi-sized transfers instead of 2)."""
     sc = 8 if precision == "mixed" else 16
+    cp = 4 if form == "momentum" else 2
     if w["dim"] == 2:
-        return (6 * 2 * sc + 3 * sc) if w["order"] == 4 else (2 * 2 * sc + sc)
+        return (3 * 2 * sc + 3 * cp * sc + 3 * sc) if w["order"] == 4 else (2 * sc + cp * sc + sc)
     return None
 
 
-def kernel_bytes_per_site(name, precision):
+def kernel_bytes_per_site(name, precision, form="direct"):
     sc = 8 if precision == "mixed" else 16
-    return {"row_pass": 3 * sc, "col_pass": 2 * sc}.get(name)
+    return {"row_pass": 3 * sc, "col_pass": (4 if form == "momentum" else 2) * sc}.get(name)
 
 
 class ClockSampler:
@@ -436,7 +439,7 @@ def run_batch(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
                            "instances": len(psis), "parallelism": f"replicas x{world}",
                            "l2": "2.2 GB of state and tables, larger than L2"},
                 "roofline": {"bound": "on-chip", "note": "resident sizes keep psi in shared memory for all "
@@ -585,7 +588,7 @@ def run_born(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
                            "updates_per_step": K, "parallelism": f"replicas x{world}",
                            "l2": "dpsi x2, V and the scratch (128 MiB in complex64) exceed L2"},
                 "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
@@ -726,7 +729,7 @@ def run_3d(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
                            "parallelism": f"replicas x{world}", "l2": "psi + V tables exceed L2"},
                 "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
                 "gpu_launches": int(sum(v[0] for v in counts.values())),
@@ -868,6 +871,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="2d4096", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--form", default="momentum", choices=["momentum", "direct"],
+                    help="2D complex64: state in momentum space with potential increments (default), or direct")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the fp64 comparison runs")
     ap.add_argument("--accuracy-steps", type=int, default=None,
@@ -907,15 +912,21 @@ def main():
     ctx = q.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
 
-    def create(precision):
+    form = args.form if (w["dim"] == 2 and args.precision == "mixed") else "direct"
+    other = {"momentum": "direct", "direct": "momentum"}[form]
+
+    def create(precision, frm=None):
         if w["dim"] == 1:
             return q.Instance.create_1d(ctx, psi0, V, d[0], w["dt"], order=w["order"], precision=precision)
-        return q.Instance.create_2d(ctx, psi0, V, d[0], d[1], w["dt"], order=w["order"], precision=precision)
+        i = q.Instance.create_2d(ctx, psi0, V, d[0], d[1], w["dt"], order=w["order"], precision=precision)
+        if precision == "mixed":
+            i.form = frm or form
+        return i
 
     tuned = {}
 
-    def tuned_instance(precision):
-        i = create(precision)
+    def tuned_instance(precision, frm=None):
+        i = create(precision, frm)
         if w["dim"] == 2 and args.plan and precision == args.precision:
             p = [int(v) for v in args.plan.split(",")]
             i.set_plan(p)
@@ -971,11 +982,11 @@ def main():
     roof = None
     if dom:
         name, (nl, tot) = dom
-        bps = kernel_bytes_per_site(name, args.precision)
+        bps = kernel_bytes_per_site(name, args.precision, form)
         avg_ms = tot / nl
         if bps:
             ach = bps * sites / (avg_ms / 1e3) / 1e9
-            tr = profile_traffic(f"{name}_{args.precision}")
+            tr = profile_traffic(f"{name}_{args.precision}" + ("_momentum" if form == "momentum" else ""))
             roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak, "peak_source": peak_kind, "avg_launch_ms": avg_ms,
                     "algorithmic_bytes_per_launch": bps * sites,
@@ -986,9 +997,9 @@ def main():
                     "avg_launch_ms": avg_ms, "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
                     "traffic": None}
     launches = int(sum(v[0] for v in counts.values()))
-    ab = algorithmic_bytes(w, args.precision)
+    ab = algorithmic_bytes(w, args.precision, form)
     step_roof = {"algorithmic_bytes_per_site_step": ab, "achieved_gbs": ab * value / world / 1e9,
-                 "frac": ab * value / world / 1e9 / peak} if ab else None
+                 "frac": ab * value / world / 1e9 / peak, "form": form} if ab else None
 
     # the fp64 path on the same workload (site-steps/s), and the accuracy of the
     # mixed form against it over the configuration's full step count
@@ -1012,6 +1023,8 @@ def main():
         ref.close()
         nacc = args.accuracy_steps if args.accuracy_steps is not None else w["full_steps"]
         a_m, a_p = tuned_instance("mixed"), tuned_instance("fp64")
+        # 2D: the other complex64 form beside it, against the same complex128 run
+        a_o = tuned_instance("mixed", other) if w["dim"] == 2 else None
         k0, p0 = a_p.energies()
         n0 = a_p.norm2()
         chunk = 250
@@ -1020,17 +1033,47 @@ def main():
             c = min(chunk, nacc - done)
             a_m.step(c)
             a_p.step(c)
+            if a_o is not None:
+                a_o.step(c)
             done += c
         a, b = a_m.get_psi(), a_p.get_psi()
         km, pm = a_m.energies()
         kr, pr = a_p.energies()
-        acc = {"steps": nacc, "rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+        acc = {"steps": nacc, "form": form, "rel_l2_vs_fp64": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
                "norm_drift_mixed": float(a_m.norm2() - n0), "norm_drift_fp64": float(a_p.norm2() - n0),
                "energy_drift_mixed": float((km + pm) - (k0 + p0)),
                "energy_drift_fp64": float((kr + pr) - (k0 + p0)),
                "energy_mixed_minus_fp64": float((km + pm) - (kr + pr)), "energy_start": float(k0 + p0)}
+        if a_o is not None:
+            o = a_o.get_psi()
+            ko, po = a_o.energies()
+            acc["other_form"] = {"form": other, "rel_l2_vs_fp64": float(np.linalg.norm(o - b) / np.linalg.norm(b)),
+                                 "norm_drift_mixed": float(a_o.norm2() - n0),
+                                 "energy_mixed_minus_fp64": float((ko + po) - (kr + pr))}
+            a_o.close()
         a_m.close()
         a_p.close()
+
+    # 2D complex64: the other form's speed on the same plan (same event timing)
+    other_speed = None
+    if w["dim"] == 2 and args.precision == "mixed" and not args.no_plain:
+        io = create("mixed", other)
+        io.set_plan(inst.plan())
+        io.step(args.warmup)
+        io.sync()
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            g0.record(stream)
+            io.step(args.steps)
+            g1.record(stream)
+        g1.synchronize()
+        oms = g0.elapsed_time(g1)
+        ov = sites * args.steps / (oms / 1e3)
+        ob = algorithmic_bytes(w, "mixed", other)
+        other_speed = {"form": other, "value": ov, "unit": "site-steps/s", "ms_per_step": oms / args.steps,
+                       "step_roofline_frac": ob * ov / 1e9 / peak, "algorithmic_bytes_per_site_step": ob}
+        io.close()
 
     # end to end through the public API: H2D of psi0 and V from pinned memory,
     # K x (step + the step's Norm2 read back), final psi read back
@@ -1050,6 +1093,8 @@ def main():
         # a new instance picks up the plan tuned above (the context remembers it)
         e2 = q.Instance.create_2d(ctx, psi_pinned, V_pinned, d[0], d[1], w["dt"], order=w["order"],
                                   precision=args.precision)
+        if args.precision == "mixed":
+            e2.form = form
     # each step's Norm2 is posted behind the step and read while the next step runs
     norms = []
     prev = None
@@ -1083,10 +1128,10 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
                            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
                 "roofline": roof, "step_roofline": step_roof, "accuracy": acc, "plain_fp64": plain,
-                "plan": tuned.get(args.precision),
+                "other_form": other_speed, "plan": tuned.get(args.precision),
                 "e2e": e2e, "gpu_launches": launches, "kernels": {k: {"launches": v[0], "ms": v[1]}
                                                                   for k, v in prof.items()},
                 "cpu_baseline": cpu, "clocks": clk}

@@ -209,6 +209,25 @@ int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out
 int qsg_get_plan(qsg_inst *inst, qsg_plan2d *out);
 int qsg_set_plan(qsg_inst *inst, const qsg_plan2d *plan);
 
+/* How a complex64 (QSG_MIXED) 2D instance holds its state between passes.
+ * Both run the same passes of the reference's step (SplittingMethod2D,
+ * src/SplittingMethod2D.cpp:81-121); they differ in rounding.
+ *  QSG_FORM_MOMENTUM (default): the state is kept in momentum space,
+ *    F psi / (nx ny), where the kinetic factor is a plain multiply; each
+ *    potential factor is added as an increment, psi += F[(V - 1) F^-1 psi],
+ *    so the FP32 rounding of its transforms scales with |V - 1| instead of
+ *    with |psi|.  A column pass reads and writes the state beside its
+ *    transform (32 instead of 16 bytes per site), and the instance holds one
+ *    more nx*ny complex64 buffer.
+ *  QSG_FORM_DIRECT: each pass transforms the state itself (16 bytes per site
+ *    per pass); faster, about 2.5x the rounding error.
+ * complex128 instances and 1D / 3D instances have one form (the direct one);
+ * setting another returns QSG_ERR_UNSUPPORTED.  Setting the form runs any
+ * deferred row pass first; the state itself is unchanged. */
+typedef enum { QSG_FORM_MOMENTUM = 0, QSG_FORM_DIRECT = 1 } qsg_form;
+int qsg_set_form(qsg_inst *inst, int form);
+int qsg_get_form(qsg_inst *inst, int *form);
+
 /* Time every candidate plan for trial_steps steps on a copy of the
  * instance's state (psi and the step count are left unchanged), switch the
  * instance to the fastest, remember it for later instances of the same grid in

@@ -40,7 +40,11 @@ EXPORTS = [
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
     "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d", "qsg_step_norm2_post", "qsg_step_norm2_get",
+    "qsg_set_form", "qsg_get_form",
 ]
+
+# qsg_form: how a complex64 2D instance holds its state between passes
+QSG_FORM_MOMENTUM, QSG_FORM_DIRECT = 0, 1
 
 # qsg_born_preconditioner / qsg_born_field
 QSG_BORN_IDENTITY, QSG_BORN_VELLEKOOP, QSG_BORN_HAO1, QSG_BORN_HAO2 = 0, 1, 2, 3
@@ -161,6 +165,8 @@ def _declare(lib):
     lib.qsg_candidate_plans.argtypes = [_i, _u64, _u64, ctypes.POINTER(Plan2D), _i]
     lib.qsg_get_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
     lib.qsg_set_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
+    lib.qsg_set_form.argtypes = [_vp, _i]
+    lib.qsg_get_form.argtypes = [_vp, ctypes.POINTER(_i)]
     lib.qsg_autotune.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan2D), _dp]
     _pp = ctypes.POINTER(_dp)
     lib.qsg_batch_create_1d.argtypes = [_vp, _i, ctypes.POINTER(_u64), _dp, _dp, _dp, _d, _d, _i, _i, _pp, _pp,

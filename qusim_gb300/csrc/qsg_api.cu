@@ -98,6 +98,11 @@ struct qsg_inst {
     // own opening V factor, a read of the state runs it first)
     bool pending = false;
     double *cparts = nullptr;      // norm partials of the last column pass (one per tile)
+    // 2D complex64 momentum form (QSG_FORM_MOMENTUM): psi holds the state
+    // F psi / (Nx Ny) between steps (split-k order), work the split-k input of
+    // the next row pass (the inverse column transform of the state)
+    int form = QSG_FORM_DIRECT;
+    void *work = nullptr;
     // 3D: per-axis kinetic factors [axis x, y, z][substep table], twiddles, kinetic partials
     void *k3[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     const void *tw3[3] = {nullptr, nullptr, nullptr};
@@ -242,14 +247,24 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
     return QSG_OK;
 }
 
+bool momentum(const qsg_inst *in) { return in->form == QSG_FORM_MOMENTUM; }
+
+// real-space sum |psi|^2 / the column pass's sums: split-k scale G Ny (direct
+// form) or Nx Ny (momentum form, Parseval)
+double cparts_scale(const qsg_inst *in)
+{
+    return momentum(in) ? (double)in->nx * in->ny : (double)in->geom.g * in->ny;
+}
+
 int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double *partials,
-             const void *src = nullptr, void *dst = nullptr)
+             const void *src = nullptr, void *dst = nullptr, bool vdiff = false)
 {
     qsg::RowPassArgs a{};
     a.in = src ? src : in->psi;
     a.out = dst ? dst : in->psi;
     a.vtab = v;
     a.vtwice = vtwice ? 1 : 0;
+    a.vdiff = vdiff ? 1 : 0;
     a.tw_row = in->tw_row;
     a.tw_nx = in->tw_nx;
     a.partials = partials;
@@ -263,11 +278,13 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     return QSG_OK;
 }
 
-int col_pass(qsg_inst *in, int d, double *partials = nullptr)
+int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false)
 {
     qsg::ColPassArgs a{};
     a.partials = partials;
     a.psi = in->psi;
+    a.work = momentum(in) ? in->work : nullptr;
+    a.first = first ? 1 : 0;
     a.kx = in->kx[d];
     a.ky = in->ky[d];
     a.k2d = in->ktab[d];
@@ -282,6 +299,53 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr)
     return QSG_OK;
 }
 
+// Momentum form of the same step.  The state P = F psi / (Nx Ny) stays in
+// psi; work carries W = (column iFFT of P), the row pass's split-k input.
+// An ExpV is P += F[(V - 1) F^-1 P]: the row pass turns W into the increment's
+// split-k form in place (row iFFT, x (V - 1), row FFT), the next column pass
+// transforms it, adds it to P, applies the kinetic factor to P, stores P and
+// writes the new W.  The closing ExpV of a call is deferred as in the direct
+// form; settling runs it on W into natural psi.
+int step2d_momentum(qsg_inst *in, uint64_t nsteps, int renorm, double *parts)
+{
+    int rc;
+    const void *V0 = in->vtab[0], *V1 = in->vtab[1];
+    void *W = in->work;
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        const bool last = s + 1 == nsteps;
+        bool first = false;
+        if (s == 0) {
+            // opening ExpV: natural psi -> the split-k form of exp(V) psi
+            // (transformed whole: P does not exist yet), or the increment of
+            // the merged closing + opening factors
+            if (in->pending)
+                rc = row_pass(in, true, true, V0, true, nullptr, W, W, true);
+            else
+                rc = row_pass(in, false, true, V0, false, nullptr, in->psi, W), first = true;
+            if (rc) return rc;
+        }
+        in->pending = false;
+        double *cp = last && !renorm ? in->cparts : nullptr;
+        if (in->order == 2) {
+            if ((rc = col_pass(in, 0, cp, first))) return rc;
+        } else {
+            if ((rc = col_pass(in, 0, nullptr, first))) return rc;
+            if ((rc = row_pass(in, true, true, V1, false, nullptr, W, W, true))) return rc;
+            if ((rc = col_pass(in, 1))) return rc;
+            if ((rc = row_pass(in, true, true, V1, false, nullptr, W, W, true))) return rc;
+            if ((rc = col_pass(in, 0, cp))) return rc;
+        }
+        if (last && renorm)
+            rc = row_pass(in, true, false, V0, false, parts, W, in->psi);
+        else if (last)
+            in->pending = true;
+        else
+            rc = row_pass(in, true, true, V0, true, nullptr, W, W, true);
+        if (rc) return rc;
+    }
+    return QSG_OK;
+}
+
 int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
     qsg_ctx *ctx = in->ctx;
@@ -293,6 +357,10 @@ int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
     }
     int rc;
     const void *V0 = in->vtab[0], *V1 = in->vtab[1];
+    if (momentum(in)) {
+        if ((rc = step2d_momentum(in, nsteps, renorm, parts))) return rc;
+        nsteps = 0;
+    }
     for (uint64_t s = 0; s < nsteps; ++s) {
         const bool last = s + 1 == nsteps;
         // opening V factor: on natural rows, or merged with the deferred closing one
@@ -433,7 +501,8 @@ int kinetic3d(qsg_inst *in, double *kin)
 int settle(qsg_inst *in)
 {
     if (!in->pending) return QSG_OK;
-    int rc = row_pass(in, true, false, in->vtab[0], false, nullptr);
+    int rc = momentum(in) ? row_pass(in, true, false, in->vtab[0], false, nullptr, in->work, in->psi)
+                          : row_pass(in, true, false, in->vtab[0], false, nullptr);
     if (rc) return rc;
     in->pending = false;
     return QSG_OK;
@@ -599,6 +668,10 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         void *cp = nullptr;
         if ((rc = inst_alloc(in, sizeof(double) * 2 * (size_t)in->ny, &cp))) return rc;
         in->cparts = static_cast<double *>(cp);
+        if (in->prec == 1) {
+            if ((rc = inst_alloc(in, in->n * csize(in->prec), &in->work))) return rc;
+            in->form = QSG_FORM_MOMENTUM;
+        }
     } else {
         // 3D: line twiddles per axis and the kinetic-energy partials (2 per CTA)
         const int L[3] = {in->nx, in->ny, in->nz};
@@ -1113,7 +1186,7 @@ int qsg_step_norm2(qsg_inst *in, double *out)
         QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, ctx->sums, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
         QSG_CUDA(cudaStreamSynchronize(ctx->st));
-        *out = ctx->host_sums[0] * ((double)in->geom.g * in->ny) * in->dv;
+        *out = ctx->host_sums[0] * cparts_scale(in) * in->dv;
         return QSG_OK;
     }
     double s = 0;
@@ -1142,7 +1215,7 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
         // as qsg_step_norm2: the last column pass's split-k sums
         const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
         QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, dst, ctx->st));
-        in->ring_scale[slot] = ((double)in->geom.g * in->ny) * in->dv;
+        in->ring_scale[slot] = cparts_scale(in) * in->dv;
     } else {
         if ((rc = settle(in))) return rc;
         int np = 0;
@@ -1355,6 +1428,26 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
     if (int rc = settle(in)) return rc;  // the split-k layout belongs to the current plan
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     return apply_plan(in, Plan2D{p->g, p->row_e, p->row_nt, p->col_e, p->col_w, p->row_kind});
+}
+
+int qsg_set_form(qsg_inst *in, int form)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_set_form: null instance");
+    if (form != QSG_FORM_MOMENTUM && form != QSG_FORM_DIRECT) return fail(QSG_ERR_ARG, "qsg_set_form: unknown form");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (form == QSG_FORM_MOMENTUM && !(in->dim == 2 && in->prec == 1 && in->work))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_set_form: the momentum form is for complex64 2D instances");
+    QSG_CUDA(cudaSetDevice(in->ctx->dev));
+    if (int rc = settle(in)) return rc;  // the deferred pass belongs to the current form
+    in->form = form;
+    return QSG_OK;
+}
+
+int qsg_get_form(qsg_inst *in, int *form)
+{
+    if (!in || !form) return fail(QSG_ERR_ARG, "qsg_get_form: null argument");
+    *form = in->form;
+    return QSG_OK;
 }
 
 int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, double *best_ms_per_step)
@@ -1675,7 +1768,8 @@ size_t request_bytes(const qsg_request &r)
     const size_t n = (size_t)r.nx * (r.dim == 2 ? r.ny : 1);
     const size_t cs = r.precision == QSG_MIXED ? 8 : 16;
     const int ntab = r.order == 2 ? 1 : 2;
-    return n * (cs + 8 + ntab * cs * 2) + n * 16 + (r.spec ? n * 24 : 0);  // psi, V, tables, staging, spec buffer
+    const size_t work = r.dim == 2 && r.precision == QSG_MIXED ? n * cs : 0;  // momentum form
+    return n * (cs + 8 + ntab * cs * 2) + n * 16 + work + (r.spec ? n * 24 : 0);  // psi, V, tables, staging, spec buffer
 }
 
 int srv_create(qsg_server *S, SrvRequest &q)

@@ -35,10 +35,18 @@ template <class C> struct PhaseOps;
 // multiplied in as a plain complex product.
 template <> struct PhaseOps<double2> {
     static __device__ __forceinline__ double2 apply(double2 a, double2 m) { return cmul(a, m); }
+    static __device__ __forceinline__ double2 increment(double2 a, double2, int) { return a; }  // unused
 };
 // complex64: tables hold factor - 1 (see cmul1p).
 template <> struct PhaseOps<float2> {
     static __device__ __forceinline__ float2 apply(float2 a, float2 m) { return cmul1p(a, m); }
+    // the increment a * (f - 1) of a factor f = 1 + m, or of f^2 (twice):
+    // (1 + m)^2 - 1 = m (2 + m)
+    static __device__ __forceinline__ float2 increment(float2 a, float2 m, int twice)
+    {
+        if (twice) m = cmul(m, cmk<float2>(m.x + 2.f, m.y));
+        return cmul(a, m);
+    }
 };
 
 template <class C> __device__ __forceinline__ C ld_c(const C *p) { return __ldg(p); }
@@ -126,6 +134,7 @@ struct RowPassArgs {
     void *out;
     const void *vtab;       // V phase table (Nx*Ny), or null (plain transform)
     int vtwice;             // apply it twice (the two ExpV calls at a step boundary)
+    int vdiff;              // complex64: multiply by factor - 1 (the increment (V - 1) psi)
     const void *tw_row;     // stage-major twiddles for (Ny, E)
     const void *tw_nx;      // full circle exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
     double *partials;       // per-unit sum |psi|^2 (natural-output passes), or null
@@ -277,7 +286,10 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
                     C mv[E];
 #pragma unroll
                     for (int e = 0; e < E; ++e) mv[e] = ld_stream(vr + e * TL);
-                    if (a.vtwice) {
+                    if (sizeof(C) == 8 && a.vdiff) {
+#pragma unroll
+                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::increment(x[e], mv[e], a.vtwice);
+                    } else if (a.vtwice) {
 #pragma unroll
                         for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(PhaseOps<C>::apply(x[e], mv[e]), mv[e]);
                     } else {
@@ -350,7 +362,10 @@ __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
 }
 
 struct ColPassArgs {
-    void *psi;              // in/out, Nx*Ny in split-k layout
+    void *psi;              // in/out, Nx*Ny in split-k layout (momentum form: the state)
+    void *work;             // momentum form (complex64): the potential increment in, the next
+                            // step's split-k input out; null in the direct form
+    int first;              // momentum form: no stored state yet (the input is the state)
     const void *kx;         // complex64: x kinetic factor - 1, Nx entries
     const void *ky;         // complex64: y kinetic factor - 1, Ny entries
     const void *k2d;        // complex128: full table Nx*Ny with 1/(Nx Ny) folded in
@@ -390,9 +405,16 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
     const int col = (u - q * ntx) * W + c;
     const size_t base = ((size_t)q * M + t) * ny + col;
 
+    // momentum form: the input is the potential increment (or, first, the
+    // state), the stored state is read, updated and written at the transform's
+    // output positions, and the output is the next step's split-k input
+    C *work = static_cast<C *>(a.work);
+    const bool mom = sizeof(C) == 8 && work != nullptr;
+    float nf = 0;  // momentum form: sum |state|^2 of this thread
+
     C x[E];
     {
-        const C *p = psi + base;
+        const C *p = (mom ? work : psi) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) x[e] = ld_stream(p + (size_t)e * stride);
     }
@@ -405,12 +427,30 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
         if constexpr (sizeof(C) == 8) {
             const C *kx = opaque(static_cast<const C *>(a.kx));
             const C ky = ld_c(static_cast<const C *>(a.ky) + col);
+            if (mom) {
+                // state += increment / (Nx Ny); state *= K; the K factor is
+                // applied to the state itself, never to a transform of it
+                C *ps = const_cast<C *>(opaque(psi)) + base;
+                const bool add = !a.first;
 #pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int kxi = a.g * (t + e * TM) + q;
-                C v = cscale(x[e], a.inv_n);
-                v = cmul1p(v, ld_c(kx + kxi));
-                x[e] = cconj(cmul1p(v, ky));
+                for (int e = 0; e < E; ++e) {
+                    const int kxi = a.g * (t + e * TM) + q;
+                    C v = cscale(x[e], a.inv_n);
+                    if (add) v = cadd(ld_stream(ps + (size_t)e * stride), v);
+                    v = cmul1p(v, ld_c(kx + kxi));
+                    v = cmul1p(v, ky);
+                    st_stream(ps + (size_t)e * stride, v);
+                    nf = fmaf(v.x, v.x, fmaf(v.y, v.y, nf));
+                    x[e] = cconj(v);
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int kxi = a.g * (t + e * TM) + q;
+                    C v = cscale(x[e], a.inv_n);
+                    v = cmul1p(v, ld_c(kx + kxi));
+                    x[e] = cconj(cmul1p(v, ky));
+                }
             }
         } else {
             const C *k2 = static_cast<const C *>(a.k2d) + col;
@@ -426,21 +466,24 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
 
     {
         // recomputed rather than kept live across both transforms
-        C *p = const_cast<C *>(opaque(psi)) + base;
+        C *p = const_cast<C *>(opaque(mom ? work : psi)) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) st_stream(p + (size_t)e * stride, x[e]);
     }
     if (a.partials) {
         // the norm of the step's state without a pass of its own: in split-k
         // space sum |psi|^2 is 1 / (G Ny) of the real-space one (the row FFT and
-        // the radix-G stage are unnormalised, the column pass carries 1/(Nx Ny)).
+        // the radix-G stage are unnormalised, the column pass carries 1/(Nx Ny));
+        // the momentum-form state holds F psi / (Nx Ny), 1 / (Nx Ny) of it.
         // complex64 sums a thread's elements in FP32 (FP64 runs at 1/64 rate:
         // per-element FP64 doubled this pass), the CTA sum in FP64.
         double s;
         if constexpr (sizeof(C) == 8) {
-            float f = 0;
+            float f = nf;
+            if (!mom) {
 #pragma unroll
-            for (int e = 0; e < E; ++e) f = fmaf(x[e].x, x[e].x, fmaf(x[e].y, x[e].y, f));
+                for (int e = 0; e < E; ++e) f = fmaf(x[e].x, x[e].x, fmaf(x[e].y, x[e].y, f));
+            }
             s = f;
         } else {
             s = 0;

@@ -194,7 +194,10 @@ __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, d
                         C mv[E];
 #pragma unroll
                         for (int e = 0; e < E; ++e) mv[e] = ld_stream(vr + e * NT);
-                        if (a.vtwice) {
+                        if (a.vdiff) {
+#pragma unroll
+                            for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::increment(x[e], mv[e], a.vtwice);
+                        } else if (a.vtwice) {
 #pragma unroll
                             for (int e = 0; e < E; ++e) x[e] = cmul1p(cmul1p(x[e], mv[e]), mv[e]);
                         } else {

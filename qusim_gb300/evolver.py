@@ -328,6 +328,19 @@ class Instance:
             plan = _lib.Plan2D(*plan)
         check(self.ctx.lib.qsg_set_plan(self.h, ctypes.byref(plan)))
 
+    @property
+    def form(self):
+        """"momentum" (complex64 2D default: state kept in momentum space,
+        potential factors added as increments) or "direct"."""
+        v = ctypes.c_int(0)
+        check(self.ctx.lib.qsg_get_form(self.h, ctypes.byref(v)))
+        return "momentum" if v.value == _lib.QSG_FORM_MOMENTUM else "direct"
+
+    @form.setter
+    def form(self, name):
+        code = {"momentum": _lib.QSG_FORM_MOMENTUM, "direct": _lib.QSG_FORM_DIRECT}[name]
+        check(self.ctx.lib.qsg_set_form(self.h, code))
+
     def candidate_plans(self, precision=None):
         lib = self.ctx.lib
         prec = self._prec if precision is None else (1 if precision == "mixed" else 0)

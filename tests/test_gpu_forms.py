@@ -1,0 +1,120 @@
+"""The two forms of a complex64 2D instance (qsg_set_form).
+
+Both run the reference's step (SplittingMethod2D, src/SplittingMethod2D.cpp:81-121)
+and agree with the complex128 path to complex64 rounding.  The momentum form
+keeps the state in momentum space and adds each potential factor as an
+increment; its rounding error against complex128 is well below the direct
+form's (the transforms' rounding scales with |V - 1|, not with |psi|).
+"""
+import numpy as np
+import pytest
+
+from tests.workloads import gauss_packet_2d, gaussian_bumps_2d
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def q():
+    import qusim_gb300 as m
+    m.load()
+    return m
+
+
+def _case(n=512, seed=3):
+    psi0, dx, dy = gauss_packet_2d(n, n, -50, 50, -50, 50, 1.5, 0.0, -20.0, 0.0, 5.0)
+    V = gaussian_bumps_2d(n, n, -50, 50, -50, 50, nbumps=16, seed=seed, spread=25.0)
+    return psi0, V, dx, dy
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_forms_against_complex128(q, order):
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case()
+    steps, dt = 200, 0.02
+    ref = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=order, precision="fp64")
+    mom = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=order, precision="mixed")
+    dirc = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=order, precision="mixed")
+    assert mom.form == "momentum" and ref.form == "direct"
+    dirc.form = "direct"
+    assert dirc.form == "direct"
+    for inst in (ref, mom, dirc):
+        inst.step(steps)
+    pr = ref.get_psi()
+    e_mom, e_dir = _rel(mom.get_psi(), pr), _rel(dirc.get_psi(), pr)
+    assert e_mom < 1e-5 and e_dir < 2e-5
+    assert e_mom < e_dir / 1.8, (e_mom, e_dir)
+    # norms and energies of the two forms agree to complex64 rounding
+    assert abs(mom.norm2() - ref.norm2()) < 1e-6
+    km, pm = mom.energies()
+    kr, pr_ = ref.energies()
+    assert abs(km - kr) < 1e-5 * abs(kr) and abs(pm - pr_) < 1e-5 * max(abs(pr_), 1e-3)
+    for inst in (ref, mom, dirc):
+        inst.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("form", ["momentum", "direct"])
+def test_small_calls_equal_one_call(q, form):
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case(256, seed=7)
+    a = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    b = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    a.form = b.form = form
+    a.step(9)
+    for _ in range(9):
+        b.step(1)
+    assert np.array_equal(a.get_psi(), b.get_psi())
+    a.close()
+    b.close()
+    ctx.close()
+
+
+def test_form_switch_mid_run(q):
+    """Switching settles the deferred pass; the state carries over."""
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case(256, seed=8)
+    ref = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="fp64")
+    a = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    ref.step(20)
+    a.step(10)
+    a.form = "direct"
+    a.step(5)
+    a.form = "momentum"
+    a.step(5)
+    assert _rel(a.get_psi(), ref.get_psi()) < 5e-6
+    a.close()
+    ref.close()
+    ctx.close()
+
+
+def test_renormalised_steps(q):
+    """renormalize = True (force normalisation each step) in the momentum form."""
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case(256, seed=9)
+    ref = q.Instance.create_2d(ctx, psi0 * 0.7, V, dx, dy, 0.01, order=4, precision="fp64")
+    a = q.Instance.create_2d(ctx, psi0 * 0.7, V, dx, dy, 0.01, order=4, precision="mixed")
+    for _ in range(3):
+        ref.step(4, renormalize=True)
+        a.step(4, renormalize=True)
+    assert abs(a.norm2() - 1.0) < 1e-6
+    assert _rel(a.get_psi(), ref.get_psi()) < 5e-6
+    a.close()
+    ref.close()
+    ctx.close()
+
+
+def test_momentum_form_only_for_complex64_2d(q):
+    from qusim_gb300 import QsgError
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case(128, seed=1)
+    a = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=2, precision="fp64")
+    with pytest.raises(QsgError):
+        a.form = "momentum"
+    a.form = "direct"
+    a.close()
+    ctx.close()
