@@ -986,7 +986,8 @@ def main():
         avg_ms = tot / nl
         if bps:
             ach = bps * sites / (avg_ms / 1e3) / 1e9
-            tr = profile_traffic(f"{name}_{args.precision}" + ("_momentum" if form == "momentum" else ""))
+            tr = profile_traffic(f"{name}_{args.precision}" + ("_momentum" if form == "momentum" and name == "col_pass"
+                                                               else ""))
             roof = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak, "peak_source": peak_kind, "avg_launch_ms": avg_ms,
                     "algorithmic_bytes_per_launch": bps * sites,

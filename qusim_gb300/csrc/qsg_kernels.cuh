@@ -66,6 +66,7 @@ __device__ __forceinline__ double2 ld_stream(const double2 *p)
     return r;
 }
 template <class C> __device__ __forceinline__ void st_stream(C *p, C v) { __stcs(p, v); }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 template <class C> __device__ __forceinline__ C cconj(C a) { return cmk<C>(a.x, -a.y); }
 
 // Every inverse transform here is computed as conj(FFT(conj(x))), which is
@@ -417,6 +418,15 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
         const C *p = (mom ? work : psi) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) x[e] = ld_stream(p + (size_t)e * stride);
+    }
+    if (mom && !a.first) {
+        // the stored state is read after the forward transform: pull it into
+        // L2 now so that those reads do not wait on HBM (no registers held).
+        // (Prefetching the tile one wave ahead as well was slower: 136 against
+        // 124 us at 4096^2.)
+        const C *p = psi + base;
+#pragma unroll
+        for (int e = 0; e < E; ++e) prefetch_l2(p + (size_t)e * stride);
     }
 
     // FFT -> K -> iFFT, the iFFT as conj(FFT(conj(x)))
