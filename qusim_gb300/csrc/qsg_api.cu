@@ -103,6 +103,8 @@ struct qsg_inst {
     // the next row pass (the inverse column transform of the state)
     int form = QSG_FORM_DIRECT;
     void *work = nullptr;
+    // complex64 plain-twiddle tables of the current plan (momentum form passes)
+    const void *tw_row_p = nullptr, *tw_col_p = nullptr, *tw_nx_p = nullptr;
     // 3D: per-axis kinetic factors [axis x, y, z][substep table], twiddles, kinetic partials
     void *k3[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     const void *tw3[3] = {nullptr, nullptr, nullptr};
@@ -256,6 +258,7 @@ double cparts_scale(const qsg_inst *in)
     return momentum(in) ? (double)in->nx * in->ny : (double)in->geom.g * in->ny;
 }
 
+// vdiff: the momentum form's increment pass, which runs with plain twiddles
 int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double *partials,
              const void *src = nullptr, void *dst = nullptr, bool vdiff = false)
 {
@@ -265,8 +268,9 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     a.vtab = v;
     a.vtwice = vtwice ? 1 : 0;
     a.vdiff = vdiff ? 1 : 0;
-    a.tw_row = in->tw_row;
-    a.tw_nx = in->tw_nx;
+    a.plain = vdiff ? 1 : 0;
+    a.tw_row = vdiff ? in->tw_row_p : in->tw_row;
+    a.tw_nx = vdiff ? in->tw_nx_p : in->tw_nx;
     a.partials = partials;
     a.nx = in->nx;
     a.m = in->geom.m;
@@ -285,10 +289,11 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false
     a.psi = in->psi;
     a.work = momentum(in) ? in->work : nullptr;
     a.first = first ? 1 : 0;
+    a.plain = momentum(in) ? 1 : 0;
     a.kx = in->kx[d];
     a.ky = in->ky[d];
     a.k2d = in->ktab[d];
-    a.tw_col = in->tw_col;
+    a.tw_col = a.plain ? in->tw_col_p : in->tw_col;
     a.nx = in->nx;
     a.ny = in->ny;
     a.g = in->geom.g;
@@ -751,6 +756,15 @@ int apply_plan(qsg_inst *in, const Plan2D &p)
     if ((rc = get_twiddles(in->ctx, in->prec, g.m, p.col_e, &tc))) return rc;
     if ((rc = get_circle(in->ctx, in->prec, in->nx, &tn))) return rc;
     if ((rc = get_twiddles(in->ctx, in->prec, g.m, g.kin_e, &tk))) return rc;
+    if (in->prec == 1) {
+        const void *pr, *pc, *pn;
+        if ((rc = get_twiddles(in->ctx, 2, in->ny, p.row_e, &pr))) return rc;
+        if ((rc = get_twiddles(in->ctx, 2, g.m, p.col_e, &pc))) return rc;
+        if ((rc = get_circle(in->ctx, 2, in->nx, &pn))) return rc;
+        in->tw_row_p = pr;
+        in->tw_col_p = pc;
+        in->tw_nx_p = pn;
+    }
     in->plan = p;
     in->geom = g;
     in->tw_row = tr;

@@ -31,12 +31,15 @@ static bool col_variant_exists(int prec, int m, int e, int w)
     return false;
 }
 
-cudaError_t launch_col_pass_f32(const Geom2D &, const ColPassArgs &, cudaStream_t);
+template <bool PL> cudaError_t launch_col_pass_f32_t(const Geom2D &, const ColPassArgs &, cudaStream_t);
+extern template cudaError_t launch_col_pass_f32_t<false>(const Geom2D &, const ColPassArgs &, cudaStream_t);
+extern template cudaError_t launch_col_pass_f32_t<true>(const Geom2D &, const ColPassArgs &, cudaStream_t);
 cudaError_t launch_col_pass_f64(const Geom2D &, const ColPassArgs &, cudaStream_t);
 
 cudaError_t launch_col_pass(int prec, const Geom2D &g, const ColPassArgs &a, cudaStream_t st)
 {
-    return prec == 1 ? launch_col_pass_f32(g, a, st) : launch_col_pass_f64(g, a, st);
+    if (prec != 1) return launch_col_pass_f64(g, a, st);
+    return a.plain ? launch_col_pass_f32_t<true>(g, a, st) : launch_col_pass_f32_t<false>(g, a, st);
 }
 
 #define QSG_M_CASES(X, T) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
@@ -54,8 +57,12 @@ cudaError_t launch_col_kinetic(int prec, const Geom2D &g, const ColPassArgs &a, 
     return cudaErrorNotSupported;
 }
 
-cudaError_t launch_row_pass_f32a(const Geom2D &, const RowPassArgs &, cudaStream_t);
-cudaError_t launch_row_pass_f32b(const Geom2D &, const RowPassArgs &, cudaStream_t);
+template <bool PL> cudaError_t launch_row_pass_f32a_t(const Geom2D &, const RowPassArgs &, cudaStream_t);
+template <bool PL> cudaError_t launch_row_pass_f32b_t(const Geom2D &, const RowPassArgs &, cudaStream_t);
+extern template cudaError_t launch_row_pass_f32a_t<false>(const Geom2D &, const RowPassArgs &, cudaStream_t);
+extern template cudaError_t launch_row_pass_f32a_t<true>(const Geom2D &, const RowPassArgs &, cudaStream_t);
+extern template cudaError_t launch_row_pass_f32b_t<false>(const Geom2D &, const RowPassArgs &, cudaStream_t);
+extern template cudaError_t launch_row_pass_f32b_t<true>(const Geom2D &, const RowPassArgs &, cudaStream_t);
 cudaError_t launch_row_pass_f64(const Geom2D &, const RowPassArgs &, cudaStream_t);
 bool row_variant_exists_f32a(int ny, int e, int g, int nt);
 bool row_variant_exists_f32b(int ny, int e, int g, int nt);
@@ -65,7 +72,8 @@ cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cud
 {
     if (g.row_kind == 1) return launch_row_pass_tm(g, a, st);
     if (prec == 0) return launch_row_pass_f64(g, a, st);
-    return g.row_e == 16 ? launch_row_pass_f32a(g, a, st) : launch_row_pass_f32b(g, a, st);
+    if (g.row_e == 16) return a.plain ? launch_row_pass_f32a_t<true>(g, a, st) : launch_row_pass_f32a_t<false>(g, a, st);
+    return a.plain ? launch_row_pass_f32b_t<true>(g, a, st) : launch_row_pass_f32b_t<false>(g, a, st);
 }
 
 bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)

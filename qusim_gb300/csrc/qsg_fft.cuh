@@ -205,11 +205,60 @@ template <> struct Roots<float2> {
     }
 };
 
+// complex64 with plain float constants (each root rounded once).  Used by
+// the transforms of the complex64 2D momentum form only: there the transforms
+// carry increments (V - 1) psi or feed only such increments, so the fixed
+// operator error of plain constants is scaled by |V - 1| as their rounding is
+// (a CPU emulation of the FP32 arithmetic: plain constants raise the direct
+// form's error 5.7x and leave the momentum form's unchanged).
+struct RootsPlain32 {
+    template <bool INV> static __device__ __forceinline__ float2 cs(float2 a, float c, float s)
+    {
+        return INV ? cmk<float2>(fmaf(a.x, c, -a.y * s), fmaf(a.y, c, a.x * s))
+                   : cmk<float2>(fmaf(a.x, c, a.y * s), fmaf(a.y, c, -a.x * s));
+    }
+    static constexpr float C1 = 0x1.d906bcp-1f, S1 = 0x1.87de2ap-2f;      // cos, sin (pi/8)
+    static constexpr float H = 0x1.6a09e6p-1f;                             // 1/sqrt(2)
+    static constexpr float C16 = 0x1.f6297cp-1f, S16 = 0x1.8f8b84p-3f;    // cos, sin (pi/16)
+    static constexpr float C316 = 0x1.a9b662p-1f, S316 = 0x1.1c73b4p-1f;  // cos, sin (3pi/16)
+    template <bool INV> static __device__ __forceinline__ float2 w16_1(float2 a) { return cs<INV>(a, C1, S1); }
+    template <bool INV> static __device__ __forceinline__ float2 w16_3(float2 a) { return cs<INV>(a, S1, C1); }
+    template <bool INV> static __device__ __forceinline__ float2 w16_9(float2 a)
+    {
+        return cs<INV>(cmk<float2>(-a.x, -a.y), C1, S1);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a)
+    {
+        const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
+        return cmk<float2>(u * H, v * H);
+    }
+    template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a) { return w8_1<INV>(crot<INV>(a)); }
+    template <bool INV> static __device__ __forceinline__ float2 w32_1(float2 a) { return cs<INV>(a, C16, S16); }
+    template <bool INV> static __device__ __forceinline__ float2 w32_3(float2 a) { return cs<INV>(a, C316, S316); }
+    template <bool INV> static __device__ __forceinline__ float2 w32_5(float2 a) { return cs<INV>(a, S316, C316); }
+    template <bool INV> static __device__ __forceinline__ float2 w32_7(float2 a) { return cs<INV>(a, S16, C16); }
+};
+
+// Table twiddles: complex128 tables hold the factor; complex64 tables hold
+// float4 {hi.x, hi.y, lo.x, lo.y}, the factor as an unevaluated sum of two
+// float pairs (lo = float(w - hi)), multiplied in by both so the product is
+// as accurate as with an exact twiddle (same coherent-modulus reason as above).
+// A complex64 transform given a float2 table (the factor rounded once) runs
+// with plain twiddles and plain constants (RootsPlain32).
+template <class C> struct TwOf;
+template <> struct TwOf<double2> { using type = double2; };
+template <> struct TwOf<float2> { using type = float4; };
+template <class C> using tw_t = typename TwOf<C>::type;
+
+// the fixed roots that go with a twiddle table type
+template <class C, class TW> struct RootsOf { using type = Roots<C>; };
+template <> struct RootsOf<float2, float2> { using type = RootsPlain32; };
+
 // a * exp(-+ 2 pi i M / 32) for a compile-time M: the r pi/16 rotation of
 // M mod 8, then (M / 8) quarter turns
-template <int M, bool INV, class C> __device__ __forceinline__ C rot32(C a)
+template <int M, bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ C rot32(C a)
 {
-    using RT = Roots<C>;
+    using RT = typename RootsOf<C, TW>::type;
     constexpr int r = M % 8, q = (M / 8) % 4;
     if constexpr (r == 1) a = RT::template w32_1<INV>(a);
     if constexpr (r == 2) a = RT::template w16_1<INV>(a);
@@ -224,16 +273,16 @@ template <int M, bool INV, class C> __device__ __forceinline__ C rot32(C a)
     return a;
 }
 
-// Table twiddles: complex128 tables hold the factor; complex64 tables hold
-// float4 {hi.x, hi.y, lo.x, lo.y}, the factor as an unevaluated sum of two
-// float pairs (lo = float(w - hi)), multiplied in by both so the product is
-// as accurate as with an exact twiddle (same coherent-modulus reason as above).
-template <class C> struct TwOf;
-template <> struct TwOf<double2> { using type = double2; };
-template <> struct TwOf<float2> { using type = float4; };
-template <class C> using tw_t = typename TwOf<C>::type;
-
 template <bool INV> __device__ __forceinline__ double2 twmul(double2 a, double2 w) { return cmulw<INV>(a, w); }
+// plain complex64 product with its FMAs spelt out, so that every kernel rounds
+// it the same way (left to contraction, the fused product can differ between
+// instantiations)
+template <bool INV> __device__ __forceinline__ float2 cmulw_f(float2 a, float2 w)
+{
+    if (INV) return cmk<float2>(fmaf(a.x, w.x, a.y * w.y), fmaf(a.y, w.x, -(a.x * w.y)));
+    return cmk<float2>(fmaf(a.x, w.x, -(a.y * w.y)), fmaf(a.x, w.y, a.y * w.x));
+}
+template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float2 w) { return cmulw_f<INV>(a, w); }
 template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float4 w)
 {
     if (INV) {  // a * conj(w)
@@ -244,12 +293,13 @@ template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float4 w)
     return cmk<float2>(fmaf(a.x, w.x, fmaf(-a.y, w.y, lx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ly)));
 }
 
-template <bool INV, class C> __device__ __forceinline__ void dft8(C (&v)[8])
+template <bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ void dft8(C (&v)[8])
 {
+    using RT = typename RootsOf<C, TW>::type;
     // even / odd halves, then combine with w8^k
     dft4<INV>(v[0], v[2], v[4], v[6]);
     dft4<INV>(v[1], v[3], v[5], v[7]);
-    C o1 = Roots<C>::template w8_1<INV>(v[3]), o2 = crot<INV>(v[5]), o3 = Roots<C>::template w8_3<INV>(v[7]);
+    C o1 = RT::template w8_1<INV>(v[3]), o2 = crot<INV>(v[5]), o3 = RT::template w8_3<INV>(v[7]);
     C e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
     v[0] = cadd(e0, v[1]);
     v[4] = csub(e0, v[1]);
@@ -261,9 +311,9 @@ template <bool INV, class C> __device__ __forceinline__ void dft8(C (&v)[8])
     v[7] = csub(e3, o3);
 }
 
-template <bool INV, class C> __device__ __forceinline__ void dft16(C (&v)[16])
+template <bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ void dft16(C (&v)[16])
 {
-    using RT = Roots<C>;
+    using RT = typename RootsOf<C, TW>::type;
     // n = 4 n1 + n2; first DFT4 over n1 for each n2
 #pragma unroll
     for (int n2 = 0; n2 < 4; ++n2) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
@@ -293,39 +343,39 @@ template <bool INV, class C> __device__ __forceinline__ void dft16(C (&v)[16])
 }
 
 // n = 8 n1 + n2: DFT4 over n1, twiddle w32^(n2 k1), DFT8 over n2; output k = k1 + 4 k2
-template <bool INV, class C> __device__ __forceinline__ void dft32(C (&v)[32])
+template <bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ void dft32(C (&v)[32])
 {
 #pragma unroll
     for (int n2 = 0; n2 < 8; ++n2) dft4<INV>(v[n2], v[8 + n2], v[16 + n2], v[24 + n2]);
     // v[8 k1 + n2] = z[n2][k1]
-    v[9] = rot32<1, INV>(v[9]);
-    v[10] = rot32<2, INV>(v[10]);
-    v[11] = rot32<3, INV>(v[11]);
-    v[12] = rot32<4, INV>(v[12]);
-    v[13] = rot32<5, INV>(v[13]);
-    v[14] = rot32<6, INV>(v[14]);
-    v[15] = rot32<7, INV>(v[15]);
-    v[17] = rot32<2, INV>(v[17]);
-    v[18] = rot32<4, INV>(v[18]);
-    v[19] = rot32<6, INV>(v[19]);
-    v[20] = rot32<8, INV>(v[20]);
-    v[21] = rot32<10, INV>(v[21]);
-    v[22] = rot32<12, INV>(v[22]);
-    v[23] = rot32<14, INV>(v[23]);
-    v[25] = rot32<3, INV>(v[25]);
-    v[26] = rot32<6, INV>(v[26]);
-    v[27] = rot32<9, INV>(v[27]);
-    v[28] = rot32<12, INV>(v[28]);
-    v[29] = rot32<15, INV>(v[29]);
-    v[30] = rot32<18, INV>(v[30]);
-    v[31] = rot32<21, INV>(v[31]);
+    v[9] = rot32<1, INV, C, TW>(v[9]);
+    v[10] = rot32<2, INV, C, TW>(v[10]);
+    v[11] = rot32<3, INV, C, TW>(v[11]);
+    v[12] = rot32<4, INV, C, TW>(v[12]);
+    v[13] = rot32<5, INV, C, TW>(v[13]);
+    v[14] = rot32<6, INV, C, TW>(v[14]);
+    v[15] = rot32<7, INV, C, TW>(v[15]);
+    v[17] = rot32<2, INV, C, TW>(v[17]);
+    v[18] = rot32<4, INV, C, TW>(v[18]);
+    v[19] = rot32<6, INV, C, TW>(v[19]);
+    v[20] = rot32<8, INV, C, TW>(v[20]);
+    v[21] = rot32<10, INV, C, TW>(v[21]);
+    v[22] = rot32<12, INV, C, TW>(v[22]);
+    v[23] = rot32<14, INV, C, TW>(v[23]);
+    v[25] = rot32<3, INV, C, TW>(v[25]);
+    v[26] = rot32<6, INV, C, TW>(v[26]);
+    v[27] = rot32<9, INV, C, TW>(v[27]);
+    v[28] = rot32<12, INV, C, TW>(v[28]);
+    v[29] = rot32<15, INV, C, TW>(v[29]);
+    v[30] = rot32<18, INV, C, TW>(v[30]);
+    v[31] = rot32<21, INV, C, TW>(v[31]);
     C r[32];
 #pragma unroll
     for (int k1 = 0; k1 < 4; ++k1) {
         C u[8];
 #pragma unroll
         for (int n2 = 0; n2 < 8; ++n2) u[n2] = v[8 * k1 + n2];
-        dft8<INV>(u);
+        dft8<INV, C, TW>(u);
 #pragma unroll
         for (int k2 = 0; k2 < 8; ++k2) r[k1 + 4 * k2] = u[k2];
     }
@@ -333,18 +383,18 @@ template <bool INV, class C> __device__ __forceinline__ void dft32(C (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = r[i];
 }
 
-template <int R, bool INV, class C> __device__ __forceinline__ void dft(C (&v)[R])
+template <int R, bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ void dft(C (&v)[R])
 {
     if constexpr (R == 2) {
         dft2<INV>(v[0], v[1]);
     } else if constexpr (R == 4) {
         dft4<INV>(v[0], v[1], v[2], v[3]);
     } else if constexpr (R == 8) {
-        dft8<INV>(v);
+        dft8<INV, C, TW>(v);
     } else if constexpr (R == 16) {
-        dft16<INV>(v);
+        dft16<INV, C, TW>(v);
     } else if constexpr (R == 32) {
-        dft32<INV>(v);
+        dft32<INV, C, TW>(v);
     } else {
         static_assert(R == 1, "radix must be 1, 2, 4, 8, 16 or 32");
     }
@@ -383,9 +433,9 @@ template <int L, int E> struct Plan {
 //
 //   lay(n)  -> shared-memory element index of line element n (this line)
 //   bar()   -> barrier over every thread that shares the buffer
-template <class C, int L, int E, bool INV, int S, class Lay, class Bar>
+template <class C, int L, int E, bool INV, int S, class Lay, class Bar, class TW>
 __device__ __forceinline__ void fft_stage(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
-                                          const tw_t<C> *__restrict__ tw)
+                                          const TW *__restrict__ tw)
 {
     using P = Plan<L, E>;
     constexpr int RL = P::radix_log(S);
@@ -405,7 +455,7 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], C *sm, const Lay &lay, cons
 #pragma unroll
             for (int q = 1; q < R; ++q) v[q] = twmul<INV>(v[q], __ldg(&tw[TWO + (q - 1) * PP + k]));
         }
-        dft<R, INV>(v);
+        dft<R, INV, C, TW>(v);
 #pragma unroll
         for (int q = 0; q < R; ++q) x[j + q * J] = v[q];
     }
@@ -425,9 +475,9 @@ __device__ __forceinline__ void fft_stage(C (&x)[E], C *sm, const Lay &lay, cons
     }
 }
 
-template <class C, int L, int E, bool INV, int S, class Lay, class Bar>
+template <class C, int L, int E, bool INV, int S, class Lay, class Bar, class TW>
 __device__ __forceinline__ void fft_stages(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
-                                           const tw_t<C> *__restrict__ tw)
+                                           const TW *__restrict__ tw)
 {
     if constexpr (S < Plan<L, E>::NST) {
         fft_stage<C, L, E, INV, S>(x, sm, lay, bar, t, tw);
@@ -447,9 +497,10 @@ template <class P> __device__ __forceinline__ const P *opaque(const P *p)
 }
 
 // Full transform of one line held in registers (natural order in and out).
-template <class C, int L, int E, bool INV, class Lay, class Bar>
+// The table's type picks the twiddle arithmetic (tw_t<C>, or float2: plain).
+template <class C, int L, int E, bool INV, class Lay, class Bar, class TW>
 __device__ __forceinline__ void line_fft(C (&x)[E], C *sm, const Lay &lay, const Bar &bar, int t,
-                                         const tw_t<C> *__restrict__ tw)
+                                         const TW *__restrict__ tw)
 {
     fft_stages<C, L, E, INV, 0>(x, sm, lay, bar, t, opaque(tw));
 }

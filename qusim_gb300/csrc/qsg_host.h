@@ -92,11 +92,16 @@ inline int dev_alloc(qsg_ctx *ctx, size_t bytes, void **p, size_t *acct, bool bu
 
 // twiddle table entry: complex128 {re, im}; complex64 {hi.re, hi.im, lo.re, lo.im}
 // with hi = float(v), lo = float(v - hi)
-inline size_t twsize(int) { return 16; }
+// table precision codes: 0 complex128, 1 complex64 hi + lo (float4),
+// 2 complex64 plain (float2, each factor rounded once)
+inline size_t twsize(int prec) { return prec == 2 ? 8 : 16; }
 
 inline void put_twiddle(int prec, unsigned char *dst, long double re, long double im)
 {
-    if (prec == 1) {
+    if (prec == 2) {
+        const float v[2] = {(float)re, (float)im};
+        std::memcpy(dst, v, 8);
+    } else if (prec == 1) {
         const float hr = (float)re, hi = (float)im;
         float v[4] = {hr, hi, (float)(re - (long double)hr), (float)(im - (long double)hi)};
         std::memcpy(dst, v, 16);

@@ -44,8 +44,8 @@ template <> struct PhaseOps<float2> {
     // (1 + m)^2 - 1 = m (2 + m)
     static __device__ __forceinline__ float2 increment(float2 a, float2 m, int twice)
     {
-        if (twice) m = cmul(m, cmk<float2>(m.x + 2.f, m.y));
-        return cmul(a, m);
+        if (twice) m = cmulw_f<false>(m, cmk<float2>(m.x + 2.f, m.y));
+        return cmulw_f<false>(a, m);
     }
 };
 
@@ -136,6 +136,7 @@ struct RowPassArgs {
     const void *vtab;       // V phase table (Nx*Ny), or null (plain transform)
     int vtwice;             // apply it twice (the two ExpV calls at a step boundary)
     int vdiff;              // complex64: multiply by factor - 1 (the increment (V - 1) psi)
+    int plain;              // complex64: tw_row / tw_nx are float2 tables (plain twiddles)
     const void *tw_row;     // stage-major twiddles for (Ny, E)
     const void *tw_nx;      // full circle exp(-2 pi i m / Nx), m < Nx (x-split twiddles)
     double *partials;       // per-unit sum |psi|^2 (natural-output passes), or null
@@ -156,10 +157,15 @@ struct RowPassArgs {
 // fits in 32 registers per thread, it is loaded while the previous unit's
 // forward x-split stage runs, so its HBM latency overlaps that stage.
 // The body, for a compile-time in_split (see k_row_pass).
-template <class T, int NY, int E, int G, int B, int RS, bool IN>
+// the twiddle table type of a pass: PL (complex64 only) selects plain float2 tables
+template <class C, bool PL> using pass_tw_t = std::conditional_t<PL, float2, tw_t<C>>;
+
+template <class T, int NY, int E, int G, int B, int RS, bool IN, bool PL>
 __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned char *smraw, double *red)
 {
     using C = cplx_t<T>;
+    using TW = pass_tw_t<C, PL>;
+    static_assert(!PL || sizeof(C) == 8, "plain twiddles are a complex64 form");
     using P = Plan<NY, E>;
     constexpr int TL = P::TL;
     constexpr int NL = B * G;
@@ -177,8 +183,8 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
     const int t = tid - grp * TL;
     const C *in = static_cast<const C *>(a.in);
     C *out = static_cast<C *>(a.out);
-    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_row);
-    const tw_t<C> *twx = static_cast<const tw_t<C> *>(a.tw_nx);
+    const TW *tw = static_cast<const TW *>(a.tw_row);
+    const TW *twx = static_cast<const TW *>(a.tw_nx);
     const C *vt = static_cast<const C *>(a.vtab);
     const CtaBarrier cbar{};
     // lines of whole warps synchronise among themselves; otherwise CTA-wide
@@ -351,15 +357,15 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
 // One kernel serves the three pass kinds of a step (runtime flags); the body
 // is specialised on in_split so that the registers holding the next unit's
 // input exist only where that input is split-k.
-template <class T, int NY, int E, int G, int B, int RS>
+template <class T, int NY, int E, int G, int B, int RS, bool PL = false>
 __global__ void __launch_bounds__(B *G *(NY / E) / RS) k_row_pass(RowPassArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[32];
     if (a.in_split)
-        row_pass_units<T, NY, E, G, B, RS, true>(a, smraw, red);
+        row_pass_units<T, NY, E, G, B, RS, true, PL>(a, smraw, red);
     else
-        row_pass_units<T, NY, E, G, B, RS, false>(a, smraw, red);
+        row_pass_units<T, NY, E, G, B, RS, false, PL>(a, smraw, red);
 }
 
 struct ColPassArgs {
@@ -367,6 +373,7 @@ struct ColPassArgs {
     void *work;             // momentum form (complex64): the potential increment in, the next
                             // step's split-k input out; null in the direct form
     int first;              // momentum form: no stored state yet (the input is the state)
+    int plain;              // complex64: tw_col is a float2 table (plain twiddles)
     const void *kx;         // complex64: x kinetic factor - 1, Nx entries
     const void *ky;         // complex64: y kinetic factor - 1, Ny entries
     const void *k2d;        // complex128: full table Nx*Ny with 1/(Nx Ny) folded in
@@ -381,10 +388,11 @@ struct ColPassArgs {
 // CTA u handles tile u.
 // Radix-32 variants (256 threads) are held to 128 registers so that two CTAs
 // share an SM.
-template <class T, int M, int E, int W>
+template <class T, int M, int E, int W, bool PL = false>
 __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPassArgs a)
 {
     using C = cplx_t<T>;
+    using TW = pass_tw_t<C, PL>;
     using P = Plan<M, E>;
     constexpr int TM = P::TL;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -395,7 +403,7 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 2 : 1) k_col_pass(ColPas
     const int ny = a.ny;
     const int ntx = ny / W;
     C *psi = static_cast<C *>(a.psi);
-    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_col);
+    const TW *tw = static_cast<const TW *>(a.tw_col);
     constexpr ColPad CP = col_pad(sizeof(C), M, W, E);
     const ColLayout<W, CP.sh, CP.p> lay{c};
     const CtaBarrier bar{};

@@ -6,11 +6,11 @@ namespace qsg {
 
 bool row_tm_supported(int ny, int g) { return g == 4 && (ny == 2048 || ny == 4096); }
 
-template <int NY>
+template <int NY, bool PL>
 static cudaError_t run_row_tm(const RowPassArgs &a, cudaStream_t st)
 {
     constexpr int NG = 512 / (NY / 16);  // independent row groups per CTA
-    auto k = k_row_pass_tm<NY>;
+    auto k = k_row_pass_tm<NY, PL>;
     const size_t smem = sizeof(float2) * NG * padded<NY, 4>(NY);  // one line buffer per group
     static bool ready = false;
     if (!ready) {
@@ -27,8 +27,8 @@ static cudaError_t run_row_tm(const RowPassArgs &a, cudaStream_t st)
 
 cudaError_t launch_row_pass_tm(const Geom2D &g, const RowPassArgs &a, cudaStream_t st)
 {
-    if (g.ny == 4096) return run_row_tm<4096>(a, st);
-    if (g.ny == 2048) return run_row_tm<2048>(a, st);
+    if (g.ny == 4096) return a.plain ? run_row_tm<4096, true>(a, st) : run_row_tm<4096, false>(a, st);
+    if (g.ny == 2048) return a.plain ? run_row_tm<2048, true>(a, st) : run_row_tm<2048, false>(a, st);
     return cudaErrorNotSupported;
 }
 

@@ -88,11 +88,12 @@ __device__ __forceinline__ double group_sum(double v, double *red, int grp, int 
 
 // One unit = the G = 4 lines n1 + j*M (j < 4) of row group n1 = u.  Group grp
 // of NG takes units grp + NG*blockIdx.x, then every NG*gridDim.x-th.
-template <int NY, bool IN>
+template <int NY, bool IN, bool PL>
 __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, double *red, uint32_t tbase,
                                              int grp, int gt)
 {
     using C = float2;
+    using TW = pass_tw_t<C, PL>;
     constexpr int E = 16, G = 4;
     constexpr int NT = NY / E;
     constexpr int NG = 512 / NT;
@@ -103,8 +104,8 @@ __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, d
     const uint32_t taddr = tbase + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)((w >> 2) * 128);
     const C *in = static_cast<const C *>(a.in);
     C *out = static_cast<C *>(a.out);
-    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw_row);
-    const tw_t<C> *twx = static_cast<const tw_t<C> *>(a.tw_nx);
+    const TW *tw = static_cast<const TW *>(a.tw_row);
+    const TW *twx = static_cast<const TW *>(a.tw_nx);
     const C *vt = static_cast<const C *>(a.vtab);
     const bool out_split = a.out_split != 0;
     const RowLayout<PADS> lay{0};
@@ -132,7 +133,7 @@ __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, d
         if constexpr (IN) {
             // inverse x-split stage, thread-local: line 0 stays in registers,
             // lines 1..3 go to TMEM slots 1..3
-            tw_t<C> tq[G];
+            TW tq[G];
 #pragma unroll
             for (int q = 1; q < G; ++q) tq[q] = __ldg(twx + u * q);
 #pragma unroll
@@ -225,7 +226,7 @@ __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, d
         if constexpr (IN) xs_load(unext < a.units ? unext : u, 0, unext < a.units);
         if (out_split) {
             // forward x-split stage, thread-local, straight to the output rows
-            tw_t<C> tq[G];
+            TW tq[G];
 #pragma unroll
             for (int q = 1; q < G; ++q) tq[q] = __ldg(twx + u * q);
             tm::wait_st();
@@ -256,7 +257,7 @@ __device__ __forceinline__ void row_tm_units(const RowPassArgs &a, float2 *sm, d
     }
 }
 
-template <int NY>
+template <int NY, bool PL = false>
 __global__ void __launch_bounds__(512, 1) k_row_pass_tm(RowPassArgs a)
 {
     constexpr int NT = NY / 16;
@@ -277,9 +278,9 @@ __global__ void __launch_bounds__(512, 1) k_row_pass_tm(RowPassArgs a)
     const int grp = threadIdx.x / NT, gt = threadIdx.x - grp * NT;
     float2 *sm = reinterpret_cast<float2 *>(smraw) + grp * LINE;
     if (a.in_split)
-        row_tm_units<NY, true>(a, sm, red, tbase, grp, gt);
+        row_tm_units<NY, true, PL>(a, sm, red, tbase, grp, gt);
     else
-        row_tm_units<NY, false>(a, sm, red, tbase, grp, gt);
+        row_tm_units<NY, false, PL>(a, sm, red, tbase, grp, gt);
     tm::wait_st();
     tm::wait_ld();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
