@@ -439,7 +439,7 @@ def run_batch(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
                            "instances": len(psis), "parallelism": f"replicas x{world}",
                            "l2": "2.2 GB of state and tables, larger than L2"},
                 "roofline": {"bound": "on-chip", "note": "resident sizes keep psi in shared memory for all "
@@ -588,7 +588,7 @@ def run_born(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
                            "updates_per_step": K, "parallelism": f"replicas x{world}",
                            "l2": "dpsi x2, V and the scratch (128 MiB in complex64) exceed L2"},
                 "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
@@ -729,7 +729,7 @@ def run_3d(args, w):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "c64" if args.precision == "mixed" else "c128", "data": "synthetic",
-                "config": {"workload": w["desc"], "precision": args.precision, "form": form, "sites": sites,
+                "config": {"workload": w["desc"], "precision": args.precision, "sites": sites,
                            "parallelism": f"replicas x{world}", "l2": "psi + V tables exceed L2"},
                 "roofline": roof, "step_roofline": step_roof, "plain_fp64": plain, "accuracy": acc, "e2e": e2e,
                 "gpu_launches": int(sum(v[0] for v in counts.values())),

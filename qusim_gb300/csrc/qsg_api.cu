@@ -806,6 +806,7 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
     qsg_ctx *ctx = new qsg_ctx();
     ctx->dev = device_ordinal;
     ctx->device_name = prop.name;
+    if (const char *g = std::getenv("QSG_BATCH_GRAPHS")) ctx->graphs = std::atoi(g) != 0;
     ctx->budget = hbm_budget_bytes;
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1542,12 +1543,23 @@ struct qsg_batch {
     };
     std::vector<Class> classes;
     uint64_t sites = 0;
+    // the launches of one qsg_batch_step(nsteps) captured as a CUDA graph
+    // (every class's launches for all nsteps, forked from and joined to the
+    // context stream); replayed while nsteps repeats
+    cudaGraphExec_t gexec = nullptr;
+    uint64_t gsteps = 0;
+    std::map<std::string, uint64_t> glaunches;  // launches per kernel name in the graph
 };
 
 static void batch_free(qsg_batch *b)
 {
     if (!b) return;
     if (b->ctx) cudaSetDevice(b->ctx->dev);
+    if (b->gexec) {
+        if (b->ctx) cudaStreamSynchronize(b->ctx->st);
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+    }
     for (auto &c : b->classes) {
         if (c.st) cudaStreamSynchronize(c.st);
         if (c.d_desc) cudaFreeAsync(c.d_desc, b->ctx->st);
@@ -1626,13 +1638,15 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
     return QSG_OK;
 }
 
-int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
+}  // extern "C"
+
+namespace {
+
+// queue every class's launches for nsteps: each class on its own stream,
+// forked from the context stream and joined back to it
+int batch_enqueue(qsg_batch *b, uint64_t nsteps)
 {
-    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_step: null batch");
-    if (nsteps == 0) return QSG_OK;
     qsg_ctx *ctx = b->ctx;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    QSG_CUDA(cudaSetDevice(ctx->dev));
     // classes start after everything already queued on the context stream
     cudaEvent_t start;
     QSG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
@@ -1669,6 +1683,66 @@ int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
         cudaStreamWaitEvent(ctx->st, c.done, 0);
     }
     cudaEventDestroy(start);
+    return rc;
+}
+
+// capture batch_enqueue(nsteps) into b->gexec
+int batch_capture(qsg_batch *b, uint64_t nsteps)
+{
+    qsg_ctx *ctx = b->ctx;
+    // count the captured launches (launch-count profiling mode during the
+    // capture, the context's own counts put back afterwards)
+    const auto saved = ctx->prof_stats;
+    const int prof = ctx->prof;
+    ctx->prof_stats.clear();
+    ctx->prof = 2;
+    cudaError_t e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal);
+    const int rc = e == cudaSuccess ? batch_enqueue(b, nsteps) : QSG_OK;
+    cudaGraph_t g = nullptr;
+    if (e == cudaSuccess) e = cudaStreamEndCapture(ctx->st, &g);
+    std::map<std::string, uint64_t> counts;
+    for (auto &kv : ctx->prof_stats) counts[kv.first] = kv.second.launches;
+    ctx->prof_stats = saved;
+    ctx->prof = prof;
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : fail(QSG_ERR_CUDA, std::string("qsg_batch_step: graph capture: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_batch_step: graph: ") + cudaGetErrorString(ei));
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = x;
+    b->gsteps = nsteps;
+    b->glaunches = counts;
+    return QSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// A step call is replayed from a captured graph (captured on the first call
+// with this nsteps); with per-launch event profiling on, the launches are
+// queued directly so that each is bracketed by its events.
+int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
+{
+    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_step: null batch");
+    if (nsteps == 0) return QSG_OK;
+    qsg_ctx *ctx = b->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    int rc;
+    if (ctx->prof == 1 || !ctx->graphs) {
+        rc = batch_enqueue(b, nsteps);
+    } else {
+        rc = b->gexec && b->gsteps == nsteps ? QSG_OK : batch_capture(b, nsteps);
+        if (!rc) QSG_CUDA(cudaGraphLaunch(b->gexec, ctx->st));
+        if (!rc && ctx->prof == 2)
+            for (auto &kv : b->glaunches) ctx->prof_stats[kv.first].launches += kv.second;
+    }
     if (rc) return rc;
     for (qsg_inst *in : b->insts) in->steps += nsteps;
     return QSG_OK;
