@@ -1724,9 +1724,9 @@ int batch_capture(qsg_batch *b, uint64_t nsteps)
 
 extern "C" {
 
-// A step call is replayed from a captured graph (captured on the first call
-// with this nsteps); with per-launch event profiling on, the launches are
-// queued directly so that each is bracketed by its events.
+// With graphs on (QSG_BATCH_GRAPHS=1), a step call is replayed from a graph
+// captured on the first call with this nsteps; with per-launch event profiling
+// on, or graphs off (the default), the launches are queued directly.
 int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
 {
     if (!b) return fail(QSG_ERR_ARG, "qsg_batch_step: null batch");

@@ -61,7 +61,10 @@ struct qsg_ctx {
     double *sums = nullptr;      // small device result buffer
     double *host_sums = nullptr; // pinned mirror
     int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
-    bool graphs = true;  // batch steps replayed from captured CUDA graphs (QSG_BATCH_GRAPHS=0: launched directly)
+    // batch steps replayed from captured CUDA graphs (QSG_BATCH_GRAPHS=1); off by default: on the
+    // 2048-instance batch the graph measured no faster than direct launches (7.34e10 against 7.41e10
+    // site-steps/s, capture included), as the size classes already overlap on their streams
+    bool graphs = false;
     std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> prof_pending;
     std::vector<cudaEvent_t> event_pool;
     std::map<std::string, qsg_host::ProfStat> prof_stats;

@@ -262,7 +262,7 @@ def test_batch_matches_solo_runs(qsg, ctx, precision):
         p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
         psis.append(p), Vs.append(v), dxs.append(dx), dts.append(0.01)
     b = qsg.Batch(ctx, psis, Vs, dxs, dts, order=2, precision=precision)
-    # a step call is captured as a CUDA graph per step count and replayed
+    # step calls of a repeated count (replayed graphs when QSG_BATCH_GRAPHS=1)
     b.step(7)
     b.step(5)
     b.step(5)
@@ -363,3 +363,28 @@ def test_tmem_row_pass_equals_shared_memory_row_pass(qsg, ctx, nx, ny):
     assert np.array_equal(out[0][0], out[1][0])
     assert out[0][1] == out[1][1]
     assert out[0][2] == out[1][2]
+
+
+def test_batch_graph_replay_equals_direct(qsg, monkeypatch):
+    """QSG_BATCH_GRAPHS=1: step calls replayed from a captured CUDA graph give the
+    same states as the same launches queued directly."""
+    rng = np.random.default_rng(11)
+    sizes = [2048, 16384, 1024, 32768]
+    psis, Vs, dxs, dts = [], [], [], []
+    for n in sizes:
+        box = 0.05 * n
+        p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
+        psis.append(p), Vs.append(v), dxs.append(dx), dts.append(0.01)
+    out = []
+    for graphs in ("0", "1"):
+        monkeypatch.setenv("QSG_BATCH_GRAPHS", graphs)
+        c = qsg.Context(0)
+        b = qsg.Batch(c, psis, Vs, dxs, dts, order=4, precision="mixed")
+        for _ in range(3):
+            b.step(4)
+        out.append([b.instance(i).get_psi() for i in range(len(sizes))])
+        assert b.instance(0).steps_taken() == 12
+        b.close()
+        c.close()
+    for a, g in zip(*out):
+        assert np.array_equal(a, g)
