@@ -95,6 +95,9 @@ struct Options {
     Options &Batch(int64_t n) { return SetInt("batch", n); }
     Options &PrecisionFp64() { return SetString("precision", "fp64"); }
     Options &PrecisionMixed() { return SetString("precision", "mixed"); }
+    // complex64 2D state form (qsg_set_form): "momentum" (default) or "direct"
+    Options &FormMomentum() { return SetString("form", "momentum"); }
+    Options &FormDirect() { return SetString("form", "direct"); }
     Options &HbmBudget(int64_t bytes) { return SetInt("hbm_budget", bytes); }
     Options &DeviceOrdinal(int64_t i) { return SetInt("device_ordinal", i); }
     Options &SetInt(char const *k, int64_t v)
@@ -331,6 +334,8 @@ class Evolver2D : public Evolver {
         }
         detail::check(qsg_create_2d(fCtx.get(), nx, ny, dx, dy, mass, hbar, dt.real(), dt.imag(), order, prec,
                                     reinterpret_cast<double const *>(fPsiHost.data()), fVHost.data(), &fInst));
+        if (prec == QSG_MIXED && opts.GetString("form", "momentum") == "direct")
+            detail::check(qsg_set_form(fInst, QSG_FORM_DIRECT));
         fPsiValid = true;
     }
 

@@ -59,6 +59,13 @@ class Options:
         self._kv["precision"] = p
         return self
 
+    def Form(self, f: str):
+        """complex64 2D state form: "momentum" (default) or "direct" (qsg_set_form)."""
+        if f not in ("momentum", "direct"):
+            raise ValueError(f"invalid form: {f}")
+        self._kv["form"] = f
+        return self
+
     def HbmBudget(self, nbytes: int):
         self._kv["hbm_budget"] = int(nbytes)
         return self
@@ -648,6 +655,8 @@ class Evolver2D(Evolver):
         self._nx, self._ny = nx, ny
         self._V = V
         self._inst = Instance.create_2d(ctx, psi0, V, dx, dy, dt, order, precision, mass, hbar)
+        if precision == "mixed":
+            self._inst.form = opts.get("form", "momentum")
 
     def GetPsi(self):
         if self._psi_cache is None:
