@@ -1121,7 +1121,7 @@ def main():
            "h2d_bytes_per_step": (psi0.nbytes + V.nbytes) / args.steps,
            "d2h_bytes_per_step": psi0.nbytes / args.steps + 8,
            "includes": "instance creation (H2D psi0+V, phase tables), K x (qsg_step(1) + the step's Norm2 "
-                       "read back: posted behind the step (qsg_step_norm2_post, summed by the step itself in 2D) "
+                       "read back: posted behind the step (qsg_step_norm2_post, summed by the step itself in 2D and in 1D one-CTA instances) "
                        "and read on the host while the next step runs), final psi read back",
            "norm_first_step": norms[0] if norms else None, "norm_last_step": norms[-1] if norms else None,
            "norm2_of_final_psi": final_norm}

@@ -91,6 +91,8 @@ struct qsg_inst {
     const void *tw_fs_col = nullptr, *tw_fs_row = nullptr, *tw_n = nullptr;
     qsg::FsInst *desc = nullptr;   // device descriptor of this instance
     double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
+    double *snorm = nullptr;       // 1D one-CTA kernels: sum |psi|^2 of the state a step call ended in
+    bool snorm_valid = false;      // ... written by the last call (no renormalisation, no state change since)
     double *parts = nullptr;       // four-step norm partials (col_blocks)
     uint64_t steps = 0;
     // 2D: psi holds the split-k form of the state before the last step's closing
@@ -224,7 +226,11 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         qsg::Evolve1DBatchArgs a{};
         a.inst = in->desc;
         a.tw = in->tw;
-        a.norm_out = nullptr;
+        // the kernel sums the final state's norm anyway when it renormalises;
+        // otherwise one block reduction at the end of the call, which serves
+        // qsg_step_norm2 / _post without a pass of their own
+        a.norm_out = renorm ? nullptr : in->snorm;
+        in->snorm_valid = !renorm;
         a.dv = in->d_dv;
         a.nsteps = nsteps;
         a.order = in->order;
@@ -239,6 +245,7 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         QSG_CUDA(qsg::launch_evolve1d(in->prec, (int)in->n, a, in->st));
         return QSG_OK;
     }
+    in->snorm_valid = false;
     int rc = step_fs(in, in->desc, 1, nsteps, in->st);
     if (rc) return rc;
     if (renorm) {
@@ -655,10 +662,11 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         // device descriptor (+ dv, + four-step norm partials) for the 1D kernels
         const int nparts = in->fourstep ? in->fsg.col_blocks : 0;
         void *blk = nullptr;
-        if ((rc = inst_alloc(in, sizeof(qsg::FsInst) + sizeof(double) * (1 + nparts), &blk))) return rc;
+        if ((rc = inst_alloc(in, sizeof(qsg::FsInst) + sizeof(double) * (2 + nparts), &blk))) return rc;
         in->desc = static_cast<qsg::FsInst *>(blk);
         in->d_dv = reinterpret_cast<double *>(in->desc + 1);
-        in->parts = nparts ? in->d_dv + 1 : nullptr;
+        in->snorm = in->d_dv + 1;
+        in->parts = nparts ? in->d_dv + 2 : nullptr;
         qsg::FsInst h{};
         h.psi = in->psi;
         h.vtab[0] = in->vtab[0];
@@ -1159,6 +1167,7 @@ int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
     int rc;
     if (nsteps == 0) {
         // renormalise only
+        in->snorm_valid = false;
         double s = 0;
         if ((rc = reduce(in, 0, in->n, 0, &s))) return rc;
         QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, in->ctx->sums, in->dv, in->ctx->st));
@@ -1204,6 +1213,13 @@ int qsg_step_norm2(qsg_inst *in, double *out)
         *out = ctx->host_sums[0] * cparts_scale(in) * in->dv;
         return QSG_OK;
     }
+    if (in->dim == 1 && in->snorm_valid) {
+        // the one-CTA 1D kernel summed the state it ended in
+        QSG_CUDA(cudaMemcpyAsync(in->ctx->host_sums, in->snorm, sizeof(double), cudaMemcpyDeviceToHost, in->st));
+        QSG_CUDA(cudaStreamSynchronize(in->st));
+        *out = in->ctx->host_sums[0] * in->dv;
+        return QSG_OK;
+    }
     double s = 0;
     int rc = reduce(in, 0, in->n, 0, &s);
     if (rc) return rc;
@@ -1226,6 +1242,14 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
     }
     const int slot = (int)(in->ring_next % qsg_inst::kRing);
     double *dst = in->ring_dev + slot;
+    if (in->dim == 1 && in->snorm_valid) {
+        // the one-CTA 1D kernel's own sum of its final state: one copy, no kernel
+        QSG_CUDA(cudaMemcpyAsync(in->ring_host + slot, in->snorm, sizeof(double), cudaMemcpyDeviceToHost, in->st));
+        QSG_CUDA(cudaEventRecord(in->ring_ev[slot], in->st));
+        in->ring_scale[slot] = in->dv;
+        *ticket = in->ring_next++;
+        return QSG_OK;
+    }
     if (in->dim == 2 && in->pending && in->dt.imag() == 0) {
         // as qsg_step_norm2: the last column pass's split-k sums
         const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
@@ -1398,6 +1422,7 @@ int qsg_set_psi(qsg_inst *in, const double *psi)
     int rc = upload_psi(in, psi);
     if (rc) return rc;
     in->pending = false;  // the state is replaced, with it any deferred row pass
+    in->snorm_valid = false;
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     return QSG_OK;
 }
@@ -1744,7 +1769,10 @@ int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
             for (auto &kv : b->glaunches) ctx->prof_stats[kv.first].launches += kv.second;
     }
     if (rc) return rc;
-    for (qsg_inst *in : b->insts) in->steps += nsteps;
+    for (qsg_inst *in : b->insts) {
+        in->steps += nsteps;
+        in->snorm_valid = false;  // batch launches do not write the per-instance sum
+    }
     return QSG_OK;
 }
 
@@ -2008,6 +2036,7 @@ void srv_loop(qsg_server *S)
             qsg::FsInst *h = S->ring_host + S->ring_pos;
             for (int k = 0; k < cnt; ++k) {
                 qsg_inst *in = g[k]->inst;
+                in->snorm_valid = false;  // grouped launches do not write the per-instance sum
                 h[k] = qsg::FsInst{};
                 h[k].psi = in->psi;
                 h[k].vtab[0] = in->vtab[0];

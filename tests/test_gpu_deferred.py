@@ -124,3 +124,25 @@ def test_posted_step_norms(q, dim):
     assert e.value.code == 6
     a.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_1d_step_norm2_from_the_step_kernel(q, precision):
+    """1D one-CTA instances: qsg_step_norm2 is the kernel's own sum of the state
+    it ended in; after renormalisation or a new state it is summed afresh."""
+    from tests.workloads import gauss_packet_1d
+    ctx = q.Context(0)
+    psi0, V, dx = gauss_packet_1d(2048, -100.0, 100.0, 1.0, -30.0, 8.0)
+    a = q.Instance.create_1d(ctx, psi0 * 1.2, V, dx, 0.02, order=4, precision=precision)
+    tol = 1e-12 if precision == "fp64" else 1e-7
+    a.step(3)
+    assert abs(a.step_norm2() - a.norm2()) <= tol * a.norm2()
+    a.step(2, renormalize=True)
+    assert abs(a.step_norm2() - 1.0) <= tol
+    a.set_psi(psi0 * 0.5)
+    assert abs(a.step_norm2() - a.norm2()) <= 1e-13 * a.norm2()
+    a.step(1)
+    t = a.post_step_norm2()
+    assert abs(a.get_step_norm2(t) - a.norm2()) <= tol * a.norm2()
+    a.close()
+    ctx.close()
