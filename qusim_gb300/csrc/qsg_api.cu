@@ -289,14 +289,22 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
     return QSG_OK;
 }
 
-int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false)
+// Momentum form: a pass whose transforms carry the whole state (the first of
+// a call from natural psi, the last before a renormalising settle, the
+// inverse-only pass of a settle) runs with hi + lo twiddles; the others with
+// plain ones.  A plain transform's fixed operator error is harmless only where
+// it is scaled by |V - 1|: on the whole state, repeated every step (a read
+// after every step), it would add up coherently.
+int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false, bool whole = false,
+             bool inv_only = false)
 {
     qsg::ColPassArgs a{};
     a.partials = partials;
     a.psi = in->psi;
     a.work = momentum(in) ? in->work : nullptr;
     a.first = first ? 1 : 0;
-    a.plain = momentum(in) ? 1 : 0;
+    a.invonly = inv_only ? 1 : 0;
+    a.plain = momentum(in) && !(first || whole || inv_only) ? 1 : 0;
     a.kx = in->kx[d];
     a.ky = in->ky[d];
     a.k2d = in->ktab[d];
@@ -338,14 +346,15 @@ int step2d_momentum(qsg_inst *in, uint64_t nsteps, int renorm, double *parts)
         }
         in->pending = false;
         double *cp = last && !renorm ? in->cparts : nullptr;
+        const bool closing = last && renorm;  // the next pass takes W to natural psi
         if (in->order == 2) {
-            if ((rc = col_pass(in, 0, cp, first))) return rc;
+            if ((rc = col_pass(in, 0, cp, first, closing))) return rc;
         } else {
             if ((rc = col_pass(in, 0, nullptr, first))) return rc;
             if ((rc = row_pass(in, true, true, V1, false, nullptr, W, W, true))) return rc;
             if ((rc = col_pass(in, 1))) return rc;
             if ((rc = row_pass(in, true, true, V1, false, nullptr, W, W, true))) return rc;
-            if ((rc = col_pass(in, 0, cp))) return rc;
+            if ((rc = col_pass(in, 0, cp, false, closing))) return rc;
         }
         if (last && renorm)
             rc = row_pass(in, true, false, V0, false, parts, W, in->psi);
@@ -513,8 +522,15 @@ int kinetic3d(qsg_inst *in, double *kin)
 int settle(qsg_inst *in)
 {
     if (!in->pending) return QSG_OK;
-    int rc = momentum(in) ? row_pass(in, true, false, in->vtab[0], false, nullptr, in->work, in->psi)
-                          : row_pass(in, true, false, in->vtab[0], false, nullptr);
+    int rc;
+    if (momentum(in)) {
+        // W again from the stored state, with hi + lo twiddles (the stepping
+        // passes made it with plain ones), then to natural psi
+        if ((rc = col_pass(in, 0, nullptr, false, false, true))) return rc;
+        rc = row_pass(in, true, false, in->vtab[0], false, nullptr, in->work, in->psi);
+    } else {
+        rc = row_pass(in, true, false, in->vtab[0], false, nullptr);
+    }
     if (rc) return rc;
     in->pending = false;
     return QSG_OK;

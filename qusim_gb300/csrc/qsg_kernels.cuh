@@ -373,6 +373,7 @@ struct ColPassArgs {
     void *work;             // momentum form (complex64): the potential increment in, the next
                             // step's split-k input out; null in the direct form
     int first;              // momentum form: no stored state yet (the input is the state)
+    int invonly;            // momentum form: only the column iFFT of the stored state, to work
     int plain;              // complex64: tw_col is a float2 table (plain twiddles)
     const void *kx;         // complex64: x kinetic factor - 1, Nx entries
     const void *ky;         // complex64: y kinetic factor - 1, Ny entries
@@ -422,13 +423,19 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 512 / (W * (M / E)) : 1)
     const bool mom = sizeof(C) == 8 && work != nullptr;
     float nf = 0;  // momentum form: sum |state|^2 of this thread
 
+    // inverse only: the stored state, conjugated for the conj(FFT(conj)) iFFT
+    const bool inv_only = mom && a.invonly;
     C x[E];
     {
-        const C *p = (mom ? work : psi) + base;
+        const C *p = (mom && !inv_only ? work : psi) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e) x[e] = ld_stream(p + (size_t)e * stride);
+        if (inv_only) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) x[e] = cconj(x[e]);
+        }
     }
-    if (mom && !a.first) {
+    if (mom && !a.first && !inv_only) {
         // the stored state is read after the forward transform: pull it into
         // L2 now so that those reads do not wait on HBM (no registers held).
         // (Prefetching the tile one wave ahead as well was slower: 136 against
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(W *(M / E), E == 32 ? 512 / (W * (M / E)) : 1)
 
     // FFT -> K -> iFFT, the iFFT as conj(FFT(conj(x)))
 #pragma unroll 1
-    for (int p = 0; p < 2; ++p) {
+    for (int p = inv_only ? 1 : 0; p < 2; ++p) {
         line_fft<C, M, E, false>(x, sm, lay, bar, t, tw);
         if (p == 1) continue;  // (a break here makes the compiler duplicate the body)
         if constexpr (sizeof(C) == 8) {

@@ -118,3 +118,28 @@ def test_momentum_form_only_for_complex64_2d(q):
     a.form = "direct"
     a.close()
     ctx.close()
+
+
+def test_read_after_every_step(q):
+    """A read after every step settles the state each time; the passes that then
+    transform the whole state keep hi + lo twiddles, so the momentum form stays
+    at least as accurate as the direct form (no coherent growth)."""
+    ctx = q.Context(0)
+    psi0, V, dx, dy = _case(512, seed=5)
+    steps, dt = 300, 0.02
+    ref = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=4, precision="fp64")
+    ref.step(steps)
+    pr = ref.get_psi()
+    errs = {}
+    for form in ("momentum", "direct"):
+        a = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=4, precision="mixed")
+        a.form = form
+        for _ in range(steps):
+            a.step(1)
+            a.norm2()
+        errs[form] = _rel(a.get_psi(), pr)
+        a.close()
+    assert errs["momentum"] < 1e-5, errs
+    assert errs["momentum"] <= 1.2 * errs["direct"], errs
+    ref.close()
+    ctx.close()
