@@ -143,3 +143,28 @@ def test_read_after_every_step(q):
     assert errs["momentum"] <= 1.2 * errs["direct"], errs
     ref.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("form", ["momentum", "direct"])
+def test_imaginary_time_non_square(q, form):
+    """Imaginary time (dt = -i tau: real decaying factors, |V - 1| up to ~tau V)
+    on a non-square grid, renormalised every call, against complex128."""
+    ctx = q.Context(0)
+    nx, ny = 512, 256
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -40, 40, -20, 20, 0.5, 0.0, -5.0, 0.0, 4.0)
+    V = gaussian_bumps_2d(nx, ny, -40, 40, -20, 20, nbumps=8, seed=12, spread=15.0, hmin=0.0, hmax=1.0)
+    dt = -0.01j
+    ref = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=4, precision="fp64")
+    a = q.Instance.create_2d(ctx, psi0, V, dx, dy, dt, order=4, precision="mixed")
+    a.form = form
+    for _ in range(10):
+        ref.step(5, renormalize=True)
+        a.step(5, renormalize=True)
+    assert _rel(a.get_psi(), ref.get_psi()) < 5e-6
+    assert abs(a.norm2() - 1.0) < 1e-6
+    ka, pa = a.energies()
+    kr, pr = ref.energies()
+    assert abs((ka + pa) - (kr + pr)) < 1e-5 * abs(kr + pr)
+    a.close()
+    ref.close()
+    ctx.close()
