@@ -107,6 +107,10 @@ struct qsg_inst {
     void *work = nullptr;
     // complex64 plain-twiddle tables of the current plan (momentum form passes)
     const void *tw_row_p = nullptr, *tw_col_p = nullptr, *tw_nx_p = nullptr;
+    // tensor maps of work and psi for the tensor-copy column pass (two CUtensorMap),
+    // built for column blocks of tma_m rows x tma_w columns; tma_w = 0: none
+    alignas(64) unsigned char tmaps[256] = {};
+    int tma_m = 0, tma_w = 0;
     // 3D: per-axis kinetic factors [axis x, y, z][substep table], twiddles, kinetic partials
     void *k3[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     const void *tw3[3] = {nullptr, nullptr, nullptr};
@@ -314,7 +318,20 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false
     a.g = in->geom.g;
     a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
     a.tiles = (in->ny / in->geom.col_w) * in->geom.g;
+    a.err = in->ctx->dev_err;
     ProfScope ps(in->ctx, "col_pass", in->st);
+    // a regular momentum-form pass: fed by tensor copies where the tile shape is compiled
+    const qsg::Geom2D &g = in->geom;
+    if (momentum(in) && !first && !inv_only && in->ctx->col_tma && qsg::col_tma_supported(g.m, g.col_e, g.col_w)) {
+        if (in->tma_m != g.m || in->tma_w != g.col_w) {
+            in->tma_m = g.m;
+            in->tma_w = qsg::encode_col_tma_maps(in->work, in->psi, in->nx, in->ny, g.col_w, in->tmaps) ? g.col_w : -1;
+        }
+        if (in->tma_w > 0) {
+            QSG_CUDA(qsg::launch_col_pass_tma(g, a, in->tmaps, in->st));
+            return QSG_OK;
+        }
+    }
     QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;
 }
@@ -537,6 +554,17 @@ int settle(qsg_inst *in)
 }
 
 // sum over psi[lo, hi) with the given reduction mode; synchronous
+// after a synchronisation that copied ctx->sums to host_sums: report (once)
+// a bounded device-side wait that ran out since the last check
+int take_dev_err(qsg_ctx *ctx)
+{
+    int flag = 0;
+    std::memcpy(&flag, ctx->host_sums + 7, sizeof(int));
+    if (!flag) return QSG_OK;
+    QSG_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->st));
+    return fail(QSG_ERR_TIMEOUT, "a column pass gave up waiting for its tensor copies (1 s)");
+}
+
 int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
 {
     if (int rc = settle(in)) return rc;
@@ -545,8 +573,9 @@ int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
     QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, lo, hi, mode, ctx->partials, ctx->max_partials,
                                 &np, ctx->st));
     QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
-    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    if (int rc = take_dev_err(ctx)) return rc;
     *out = ctx->host_sums[0];
     return QSG_OK;
 }
@@ -831,6 +860,7 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
     ctx->dev = device_ordinal;
     ctx->device_name = prop.name;
     if (const char *g = std::getenv("QSG_BATCH_GRAPHS")) ctx->graphs = std::atoi(g) != 0;
+    if (const char *g = std::getenv("QSG_COL_TMA")) ctx->col_tma = std::atoi(g) != 0;
     ctx->budget = hbm_budget_bytes;
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -858,6 +888,11 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
         return rc;
     }
     ctx->sums = (double *)p;
+    ctx->dev_err = reinterpret_cast<int *>(ctx->sums + 7);
+    if ((e = cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->st)) != cudaSuccess) {
+        qsg_ctx_destroy(ctx);
+        return fail(QSG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
+    }
     e = cudaMallocHost(&p, sizeof(double) * 8);
     if (e != cudaSuccess) {
         qsg_ctx_destroy(ctx);
@@ -1199,8 +1234,11 @@ int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
 int qsg_sync(qsg_inst *in)
 {
     if (!in) return fail(QSG_ERR_ARG, "qsg_sync: null instance");
-    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
-    return QSG_OK;
+    qsg_ctx *ctx = in->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return take_dev_err(ctx);
 }
 
 int qsg_norm2(qsg_inst *in, double *out)

@@ -58,7 +58,9 @@ struct qsg_ctx {
     size_t scratch_bytes = 0;
     double *partials = nullptr;  // reduction partials
     int max_partials = 0;
-    double *sums = nullptr;      // small device result buffer
+    double *sums = nullptr;      // small device result buffer (8 doubles; the last holds dev_err)
+    int *dev_err = nullptr;      // set by a kernel whose bounded waits ran out (tensor-copy column pass)
+    bool col_tma = true;         // momentum-form column passes fed by tensor copies (QSG_COL_TMA=0: off)
     double *host_sums = nullptr; // pinned mirror
     int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
     // batch steps replayed from captured CUDA graphs (QSG_BATCH_GRAPHS=1); off by default: on the

@@ -85,6 +85,13 @@ int col3_ctas(int prec, int l, int inner, int outer);
 template <class T> cudaError_t launch3_row(int l, size_t lines, const Pass3Args &a, cudaStream_t st);
 template <class T> cudaError_t launch3_col(int l, int inner, int outer, const Pass3Args &a, cudaStream_t st);
 
+// momentum-form column pass fed by tensor copies (qsg_col_tma.cuh): compiled
+// tile shapes, the two tensor maps (work buffer, state; 2 x 128 bytes, 64-byte
+// aligned storage at maps) and the launch
+bool col_tma_supported(int m, int e, int w);
+bool encode_col_tma_maps(void *work, void *psi, int nx, int ny, int w, void *maps);
+cudaError_t launch_col_pass_tma(const Geom2D &g, const ColPassArgs &a, const void *maps, cudaStream_t st);
+
 // record `msg` as the calling thread's qsg_last_error(); returns code
 int set_last_error(int code, const std::string &msg);
 

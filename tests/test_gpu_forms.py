@@ -168,3 +168,28 @@ def test_imaginary_time_non_square(q, form):
     a.close()
     ref.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("n", [2048, 4096])
+def test_tensor_copy_column_pass_is_bitwise_the_plain_one(q, monkeypatch, n):
+    """The momentum-form column pass fed by tensor copies (QSG_COL_TMA, on by
+    default where the tile shape is compiled) computes exactly what the
+    load-instruction pass computes: same states, same step norms."""
+    psi0, dx, dy = gauss_packet_2d(n, n, -0.05 * n, 0.05 * n, -0.05 * n, 0.05 * n, 1.5, 0.0, -0.01 * n, 0.0,
+                                   0.004 * n)
+    V = gaussian_bumps_2d(n, n, -0.05 * n, 0.05 * n, -0.05 * n, 0.05 * n, nbumps=8, seed=13, spread=0.02 * n)
+    out = []
+    for tma in ("1", "0"):
+        monkeypatch.setenv("QSG_COL_TMA", tma)
+        c = q.Context(0)
+        a = q.Instance.create_2d(c, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+        a.step(3)
+        a.step(2)
+        sn = a.step_norm2()
+        a.sync()
+        out.append((a.get_psi(), sn, a.plan().as_tuple()))
+        a.close()
+        c.close()
+    assert out[0][2] == out[1][2]
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][0], out[1][0])
