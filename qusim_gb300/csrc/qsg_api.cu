@@ -988,7 +988,7 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     } else {
         rc = get_twiddles(ctx, precision, fsg.n2, fsg.col_e, &in->tw_fs_col);
         if (!rc) rc = get_twiddles(ctx, precision, fsg.n1, fsg.row_e, &in->tw_fs_row);
-        if (!rc) rc = get_circle(ctx, precision, (int)n, &in->tw_n);
+        if (!rc) rc = get_fs_grid(ctx, precision, fsg.n1, fsg.n2, &in->tw_n);
         if (!rc) rc = get_twiddles(ctx, precision, (int)fsg.n1, qsg::elems_per_thread(precision), &in->tw);
     }
     if (!rc) rc = common_create(in, psi0, V);

@@ -178,6 +178,35 @@ inline int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
     return QSG_OK;
 }
 
+// four-step twiddles in the layout the column pass reads them: entry
+// r * n1 + c = exp(-2 pi i r c / (n1 n2)), r < n2, c < n1 (the circle's entry
+// m = r c, computed the same way, so the values are the circle's bit for bit)
+inline int get_fs_grid(qsg_ctx *ctx, int prec, int n1, int n2, const void **out)
+{
+    auto key = std::make_tuple(prec + 8, n1, n2);
+    auto it = ctx->tw_cache.find(key);
+    if (it != ctx->tw_cache.end()) {
+        *out = it->second;
+        return QSG_OK;
+    }
+    const long n = (long)n1 * n2;
+    std::vector<unsigned char> host((size_t)n * twsize(prec));
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (long r = 0; r < n2; ++r)
+        for (long c = 0; c < n1; ++c) {
+            const long double ang = two_pi * (long double)(r * c) / (long double)n;
+            put_twiddle(prec, &host[(size_t)(r * n1 + c) * twsize(prec)], cosl(ang), -sinl(ang));
+        }
+    void *d = nullptr;
+    int rc = dev_alloc(ctx, host.size(), &d, nullptr);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(d, host.data(), host.size(), cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->tw_cache[key] = d;
+    *out = d;
+    return QSG_OK;
+}
+
 // --- profiling -------------------------------------------------------------
 
 inline cudaEvent_t take_event(qsg_ctx *ctx)

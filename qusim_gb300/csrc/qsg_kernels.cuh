@@ -632,7 +632,7 @@ struct FsInst {
 struct FsColArgs {
     const FsInst *inst;
     const void *tw_col;     // stage twiddles for (N2, E)
-    const void *tw_n;       // circle exp(-2 pi i m / N), m < N
+    const void *tw_n;       // exp(-2 pi i r c / N) at r * n1 + c (row r < n2, column c < n1)
     int n1;
     int vsel, vtwice;       // V table index; apply it twice
     int in_k, out_k;        // input in k layout / output to k layout
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(W *(N2 / E), (W * (N2 / E) <= 256 && sizeof(T)
     if (in_k) {
         // iFFT(y * conj(w)) = conj(FFT(conj(y) * w))
 #pragma unroll
-        for (int e = 0; e < E; ++e) x[e] = twmul<false>(cconj(x[e]), __ldg(twn + (size_t)col * (t + e * TM)));
+        for (int e = 0; e < E; ++e) x[e] = twmul<false>(cconj(x[e]), __ldg(twn + base + e * stride));
     }
     const int npass = (in_k ? 1 : 0) + (out_k ? 1 : 0);
     const int vpos = in_k ? 1 : 0;
@@ -704,7 +704,7 @@ __global__ void __launch_bounds__(W *(N2 / E), (W * (N2 / E) <= 256 && sizeof(T)
     double nsum = 0;
     if (out_k) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) x[e] = twmul<false>(x[e], __ldg(opaque(twn) + (size_t)col * (t + e * TM)));
+        for (int e = 0; e < E; ++e) x[e] = twmul<false>(x[e], __ldg(opaque(twn) + base + e * stride));
     } else {
 #pragma unroll
         for (int e = 0; e < E; ++e) nsum += abs2d(x[e]);
