@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(W *(N2 / E)) k_born_fs_col(BornFsColArgs a)
     if (a.in_k) {
         // iFFT(y conj(w)) = conj(FFT(conj(y) w))
 #pragma unroll
-        for (int e = 0; e < E; ++e) x[e] = twmul<false>(cconj(x[e]), __ldg(twn + (size_t)col * (t + e * TM)));
+        for (int e = 0; e < E; ++e) x[e] = twmul<false>(cconj(x[e]), __ldg(twn + base + e * stride));
         line_fft<C, N2, E, false>(x, sm, lay, bar, t, tw);
         C v[E], d[E];
 #pragma unroll
@@ -469,7 +469,7 @@ __global__ void __launch_bounds__(W *(N2 / E)) k_born_fs_col(BornFsColArgs a)
         C *p = static_cast<C *>(a.tmp) + base;
 #pragma unroll
         for (int e = 0; e < E; ++e)
-            st_stream(p + e * stride, twmul<false>(x[e], __ldg(opaque(twn) + (size_t)col * (t + e * TM))));
+            st_stream(p + e * stride, twmul<false>(x[e], __ldg(opaque(twn) + base + e * stride)));
     }
     if (a.partials) {
         r0 = block_sum<NT>(r0, red);

@@ -238,7 +238,8 @@ int create_1d(qsg_born *b, const double *V, double direction)
         if ((rc = born_alloc(b, n * csize(b->prec), &b->tmp))) return rc;
         if ((rc = get_twiddles(b->ctx, b->prec, b->n2, E, &b->tw_a))) return rc;
         if ((rc = get_twiddles(b->ctx, b->prec, b->n1, E, &b->tw_b))) return rc;
-        if ((rc = get_circle(b->ctx, b->prec, (int)n, &b->tw_n))) return rc;
+        // the four-step column pass's twiddles in its own row-major layout
+        if ((rc = get_fs_grid(b->ctx, b->prec, b->n1, b->n2, &b->tw_n))) return rc;
     }
     return QSG_OK;
 }

@@ -75,7 +75,7 @@ struct BornFsColArgs {
     void *dnew;           // updated dpsi, or null
     const void *psi0, *V; // natural
     const void *tw;       // stage twiddles (N2, E)
-    const void *tw_n;     // exp(-2 pi i m / N), m < N
+    const void *tw_n;     // exp(-2 pi i r c / N) at r * n1 + c (row r < n2, column c < n1)
     double *partials;     // last pass: 4 per CTA, the ComputeRT sums (or null)
     BornOps ops;
     int n1;
