@@ -228,6 +228,16 @@ typedef enum { QSG_FORM_MOMENTUM = 0, QSG_FORM_DIRECT = 1 } qsg_form;
 int qsg_set_form(qsg_inst *inst, int form);
 int qsg_get_form(qsg_inst *inst, int *form);
 
+/* Failure-path check of the bounded device-side waits (no counterpart in the
+ * reference).  Runs one column pass of a complex64 2D momentum-form instance
+ * whose plan has the tensor-copy column pass (2048^2, 4096^2 plans) with its
+ * tensor copies withheld: every CTA's first wait runs out after 1 s, sets the
+ * context's error flag and returns before touching the state.  Returns the
+ * status the following synchronisation reports: QSG_ERR_TIMEOUT when the path
+ * works (the flag is then cleared and the context stays usable),
+ * QSG_ERR_UNSUPPORTED for an instance without that pass. */
+int qsg_check_wait_timeout(qsg_inst *inst);
+
 /* Time every candidate plan for trial_steps steps on a copy of the
  * instance's state (psi and the step count are left unchanged), switch the
  * instance to the fastest, remember it for later instances of the same grid in

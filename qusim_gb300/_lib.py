@@ -40,7 +40,7 @@ EXPORTS = [
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
     "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d", "qsg_step_norm2_post", "qsg_step_norm2_get",
-    "qsg_set_form", "qsg_get_form",
+    "qsg_set_form", "qsg_get_form", "qsg_check_wait_timeout",
 ]
 
 # qsg_form: how a complex64 2D instance holds its state between passes
@@ -167,6 +167,7 @@ def _declare(lib):
     lib.qsg_set_plan.argtypes = [_vp, ctypes.POINTER(Plan2D)]
     lib.qsg_set_form.argtypes = [_vp, _i]
     lib.qsg_get_form.argtypes = [_vp, ctypes.POINTER(_i)]
+    lib.qsg_check_wait_timeout.argtypes = [_vp]
     lib.qsg_autotune.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan2D), _dp]
     _pp = ctypes.POINTER(_dp)
     lib.qsg_batch_create_1d.argtypes = [_vp, _i, ctypes.POINTER(_u64), _dp, _dp, _dp, _d, _d, _i, _i, _pp, _pp,

@@ -300,7 +300,7 @@ int row_pass(qsg_inst *in, bool is, bool os, const void *v, bool vtwice, double 
 // it is scaled by |V - 1|: on the whole state, repeated every step (a read
 // after every step), it would add up coherently.
 int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false, bool whole = false,
-             bool inv_only = false)
+             bool inv_only = false, bool no_copies = false)
 {
     qsg::ColPassArgs a{};
     a.partials = partials;
@@ -319,6 +319,7 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false
     a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
     a.tiles = (in->ny / in->geom.col_w) * in->geom.g;
     a.err = in->ctx->dev_err;
+    a.no_copies = no_copies ? 1 : 0;
     ProfScope ps(in->ctx, "col_pass", in->st);
     // a regular momentum-form pass: fed by tensor copies where the tile shape is compiled
     const qsg::Geom2D &g = in->geom;
@@ -332,6 +333,7 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false
             return QSG_OK;
         }
     }
+    if (no_copies) return fail(QSG_ERR_UNSUPPORTED, "no tensor-copy column pass for this instance and plan");
     QSG_CUDA(qsg::launch_col_pass(in->prec, in->geom, a, in->st));
     return QSG_OK;
 }
@@ -1522,6 +1524,21 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
     if (int rc = settle(in)) return rc;  // the split-k layout belongs to the current plan
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     return apply_plan(in, Plan2D{p->g, p->row_e, p->row_nt, p->col_e, p->col_w, p->row_kind});
+}
+
+int qsg_check_wait_timeout(qsg_inst *in)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_check_wait_timeout: null instance");
+    if (!(in->dim == 2 && in->prec == 1 && momentum(in)))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_check_wait_timeout: needs a complex64 2D momentum-form instance");
+    qsg_ctx *ctx = in->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    // the withheld pass returns before any store, so a pending state stays valid
+    if (int rc = col_pass(in, 0, nullptr, false, false, false, true)) return rc;
+    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return take_dev_err(ctx);
 }
 
 int qsg_set_form(qsg_inst *in, int form)

@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(W *(M / E), 1)
     int u = blockIdx.x;
     uint32_t ph_w = 0, ph_p = 0;
     int in_flight_w = 0, in_flight_p = 0;  // (thread 0's view, for the error path)
-    if (tid == 0 && u < a.tiles) {
+    if (tid == 0 && u < a.tiles && !a.no_copies) {
         issue(mb_w, &map_w, wb, u);
         issue(mb_p, &map_p, pb, u);
         in_flight_w = in_flight_p = 1;

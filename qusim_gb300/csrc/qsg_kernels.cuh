@@ -375,6 +375,7 @@ struct ColPassArgs {
     int first;              // momentum form: no stored state yet (the input is the state)
     int invonly;            // momentum form: only the column iFFT of the stored state, to work
     int *err;               // set to 1 by a pass whose bounded waits ran out (TMA pass), or null
+    int no_copies;          // TMA pass, failure-path test only: issue no copies, so the first wait runs out
     int plain;              // complex64: tw_col is a float2 table (plain twiddles)
     const void *kx;         // complex64: x kinetic factor - 1, Nx entries
     const void *ky;         // complex64: y kinetic factor - 1, Ny entries

@@ -335,6 +335,12 @@ class Instance:
             plan = _lib.Plan2D(*plan)
         check(self.ctx.lib.qsg_set_plan(self.h, ctypes.byref(plan)))
 
+    def check_wait_timeout(self) -> int:
+        """qsg_check_wait_timeout: run one column pass with its tensor copies
+        withheld; returns the status code (4, QSG_ERR_TIMEOUT, when the bounded
+        waits work)."""
+        return int(self.ctx.lib.qsg_check_wait_timeout(self.h))
+
     @property
     def form(self):
         """"momentum" (complex64 2D default: state kept in momentum space,

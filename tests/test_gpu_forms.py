@@ -194,3 +194,27 @@ def test_tensor_copy_column_pass_is_bitwise_the_plain_one(q, monkeypatch, n):
     assert out[0][2] == out[1][2]
     assert out[0][1] == out[1][1]
     assert np.array_equal(out[0][0], out[1][0])
+
+
+def test_bounded_wait_runs_out_cleanly(q):
+    """A tensor-copy column pass whose copies are withheld: every CTA's first
+    wait runs out after 1 s, the pass returns before touching the state, the
+    next synchronisation reports QSG_ERR_TIMEOUT, and the context keeps working."""
+    n = 2048
+    psi0, dx, dy = gauss_packet_2d(n, n, -100, 100, -100, 100, 1.5, 0.0, -20.0, 0.0, 8.0)
+    V = gaussian_bumps_2d(n, n, -100, 100, -100, 100, nbumps=8, seed=14, spread=40.0)
+    ctx = q.Context(0)
+    a = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    b = q.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=4, precision="mixed")
+    a.step(2)
+    b.step(2)
+    assert a.check_wait_timeout() == 4
+    a.sync()  # the flag was cleared by the check
+    a.step(2)
+    b.step(2)
+    assert np.array_equal(a.get_psi(), b.get_psi())
+    ref = q.Instance.create_2d(ctx, psi0[:256, :256], V[:256, :256], dx, dy, 0.01, order=4, precision="fp64")
+    assert ref.check_wait_timeout() == 5  # complex128: no such pass
+    for inst in (a, b, ref):
+        inst.close()
+    ctx.close()
