@@ -2,6 +2,7 @@
 // the tensor maps of the two buffers it reads.
 #include <algorithm>
 #include "qsg_col_tma.cuh"
+#include <atomic>
 #include "qsg_dispatch.cuh"
 
 namespace qsg {
@@ -13,11 +14,15 @@ static cudaError_t run_col_tma(const ColPassArgs &a, const CUtensorMap *mw, cons
 {
     auto k = k_col_pass_tma<M, E, W, PL>;
     const size_t smem = col_tma_smem(M, W, E) + 128;
-    static bool ready = false;
-    if (!ready) {
+    // the attribute belongs to the device's context: set once per device
+    static std::atomic<uint64_t> ready{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (!bit || !(ready.load() & bit)) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        ready = true;
+        ready.fetch_or(bit);
     }
     // persistent: one CTA per SM (the staging buffers take most of its shared memory)
     const int grid = std::min(a.tiles, sm_count());

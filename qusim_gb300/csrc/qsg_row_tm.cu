@@ -1,4 +1,5 @@
 // 2D row pass with the waiting rows parked in tensor memory: instantiations + launcher.
+#include <atomic>
 #include "qsg_dispatch.cuh"
 #include "qsg_row_tm.cuh"
 
@@ -12,11 +13,15 @@ static cudaError_t run_row_tm(const RowPassArgs &a, cudaStream_t st)
     constexpr int NG = 512 / (NY / 16);  // independent row groups per CTA
     auto k = k_row_pass_tm<NY, PL>;
     const size_t smem = sizeof(float2) * NG * padded<NY, 4>(NY);  // one line buffer per group
-    static bool ready = false;
-    if (!ready) {
+    // the attribute belongs to the device's context: set once per device
+    static std::atomic<uint64_t> ready{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (!bit || !(ready.load() & bit)) {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        ready = true;
+        ready.fetch_or(bit);
     }
     // one CTA per SM: each takes all 512 TMEM columns of its SM
     const int ctas = (a.units + NG - 1) / NG;
