@@ -90,6 +90,7 @@ struct qsg_inst {
     qsg::FsGeom fsg{};
     const void *tw_fs_col = nullptr, *tw_fs_row = nullptr, *tw_n = nullptr;
     qsg::FsInst *desc = nullptr;   // device descriptor of this instance
+    void *fs_maps = nullptr;       // complex64 four-step: tensor maps of psi, V 0, V 1 (tensor-copy column pass)
     double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
     double *snorm = nullptr;       // 1D one-CTA kernels: sum |psi|^2 of the state a step call ended in
     bool snorm_valid = false;      // ... written by the last call (no renormalisation, no state change since)
@@ -169,8 +170,9 @@ void prof_drain(qsg_ctx *ctx)
 
 // --- steps -----------------------------------------------------------------
 
+// maps: the instances' tensor maps (3 each) for the tensor-copy pass, or null
 int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out_k, int vsel, bool vtwice,
-           cudaStream_t st)
+           cudaStream_t st, const void *maps = nullptr)
 {
     qsg::FsColArgs a{};
     a.inst = desc;
@@ -182,8 +184,42 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     a.in_k = in_k ? 1 : 0;
     a.out_k = out_k ? 1 : 0;
     ProfScope ps(in->ctx, "fs_col_pass", st);
+    if (maps && in->ctx->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
+        a.maps = maps;
+        a.tiles = in->fsg.col_blocks * ninst;
+        a.err = in->ctx->dev_err;
+        QSG_CUDA(qsg::launch_fs_col_tma(in->fsg, a, st));
+        return QSG_OK;
+    }
     QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, a, ninst, st));
     return QSG_OK;
+}
+
+// tensor maps (psi, V 0, V 1; V 0 stands in for an absent V 1) of
+// instances, into device memory; null when a map cannot be made
+void *fs_make_maps(qsg_ctx *ctx, qsg_inst *const *insts, size_t count, size_t *bytes)
+{
+    if (count == 0 || insts[0]->prec != 1 || !qsg::fs_tma_supported(1, insts[0]->fsg.n2)) return nullptr;
+    struct alignas(64) Map { unsigned char b[128]; };
+    std::vector<Map> h(3 * count);
+    for (size_t k = 0; k < count; ++k) {
+        qsg_inst *in = insts[k];
+        const int n1 = in->fsg.n1, n2 = in->fsg.n2;
+        const void *v1 = in->vtab[1] ? in->vtab[1] : in->vtab[0];
+        if (!qsg::encode_fs_map(in->psi, n1, n2, h[3 * k].b) ||
+            !qsg::encode_fs_map(const_cast<void *>(in->vtab[0]), n1, n2, h[3 * k + 1].b) ||
+            !qsg::encode_fs_map(const_cast<void *>(v1), n1, n2, h[3 * k + 2].b))
+            return nullptr;
+    }
+    void *d = nullptr;
+    if (cudaMallocAsync(&d, sizeof(Map) * h.size(), ctx->st) != cudaSuccess) return nullptr;
+    if (cudaMemcpyAsync(d, h.data(), sizeof(Map) * h.size(), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->st) != cudaSuccess) {
+        cudaFreeAsync(d, ctx->st);
+        return nullptr;
+    }
+    *bytes = sizeof(Map) * h.size();
+    return d;
 }
 
 int fs_row(qsg_inst *in, const qsg::FsInst *desc, int ninst, int ksel, cudaStream_t st)
@@ -201,23 +237,24 @@ int fs_row(qsg_inst *in, const qsg::FsInst *desc, int ninst, int ksel, cudaStrea
 // Four-step schedule over ninst instances sharing in's geometry and tables
 // layout (descriptors `desc`): like the 2D schedule with the roles of the
 // passes swapped -- the column pass is the real-space one.
-int step_fs(qsg_inst *in, const qsg::FsInst *desc, int ninst, uint64_t nsteps, cudaStream_t st)
+int step_fs(qsg_inst *in, const qsg::FsInst *desc, int ninst, uint64_t nsteps, cudaStream_t st,
+            const void *maps = nullptr)
 {
     int rc;
     for (uint64_t s = 0; s < nsteps; ++s) {
         const bool last = s + 1 == nsteps;
-        if (s == 0 && (rc = fs_col(in, desc, ninst, false, true, 0, false, st))) return rc;
+        if (s == 0 && (rc = fs_col(in, desc, ninst, false, true, 0, false, st, maps))) return rc;
         if (in->order == 2) {
             if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
         } else {
             if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
-            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st))) return rc;
+            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st, maps))) return rc;
             if ((rc = fs_row(in, desc, ninst, 1, st))) return rc;
-            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st))) return rc;
+            if ((rc = fs_col(in, desc, ninst, true, true, 1, false, st, maps))) return rc;
             if ((rc = fs_row(in, desc, ninst, 0, st))) return rc;
         }
-        rc = last ? fs_col(in, desc, ninst, true, false, 0, false, st)
-                  : fs_col(in, desc, ninst, true, true, 0, true, st);
+        rc = last ? fs_col(in, desc, ninst, true, false, 0, false, st, maps)
+                  : fs_col(in, desc, ninst, true, true, 0, true, st, maps);
         if (rc) return rc;
     }
     return QSG_OK;
@@ -250,7 +287,7 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         return QSG_OK;
     }
     in->snorm_valid = false;
-    int rc = step_fs(in, in->desc, 1, nsteps, in->st);
+    int rc = step_fs(in, in->desc, 1, nsteps, in->st, in->fs_maps);
     if (rc) return rc;
     if (renorm) {
         ProfScope ps(ctx, "renorm");
@@ -723,6 +760,15 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         h.partials = in->parts;
         QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+        if (in->fourstep) {
+            size_t mb = 0;
+            in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);
+            if (in->fs_maps) {
+                in->allocs.push_back(in->fs_maps);
+                in->bytes += mb;
+                ctx->in_use += mb;
+            }
+        }
     } else if (in->dim == 2) {
         // column-pass norm partials: at most G * Ny / W = 2 Ny tiles (G <= 4, W >= 2)
         void *cp = nullptr;
@@ -863,6 +909,7 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
     ctx->device_name = prop.name;
     if (const char *g = std::getenv("QSG_BATCH_GRAPHS")) ctx->graphs = std::atoi(g) != 0;
     if (const char *g = std::getenv("QSG_COL_TMA")) ctx->col_tma = std::atoi(g) != 0;
+    if (const char *g = std::getenv("QSG_FS_TMA")) ctx->fs_tma = std::atoi(g) != 0;
     ctx->budget = hbm_budget_bytes;
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1633,6 +1680,7 @@ struct qsg_batch {
         uint64_t n = 0;
         std::vector<int> members;
         qsg::FsInst *d_desc = nullptr;
+        void *d_maps = nullptr;     // complex64 four-step: the members' tensor maps (3 each)
         double *d_dv = nullptr;
         cudaStream_t st = nullptr;
         cudaEvent_t done = nullptr;
@@ -1659,6 +1707,7 @@ static void batch_free(qsg_batch *b)
     for (auto &c : b->classes) {
         if (c.st) cudaStreamSynchronize(c.st);
         if (c.d_desc) cudaFreeAsync(c.d_desc, b->ctx->st);
+        if (c.d_maps) cudaFreeAsync(c.d_maps, b->ctx->st);
         if (c.done) cudaEventDestroy(c.done);
         if (c.st) cudaStreamDestroy(c.st);
     }
@@ -1723,6 +1772,12 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
             e = cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice);
         }
         if (e == cudaSuccess) e = cudaMemcpy(c.d_dv, dv.data(), sizeof(double) * dv.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && b->insts[c.members[0]]->fourstep) {
+            std::vector<qsg_inst *> mi(c.members.size());
+            for (size_t k = 0; k < mi.size(); ++k) mi[k] = b->insts[c.members[k]];
+            size_t mb = 0;
+            c.d_maps = fs_make_maps(ctx, mi.data(), mi.size(), &mb);
+        }
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming);
         if (e != cudaSuccess) {
@@ -1772,7 +1827,7 @@ int batch_enqueue(qsg_batch *b, uint64_t nsteps)
                 rc = fail(QSG_ERR_CUDA, std::string("qsg_batch_step: ") + cudaGetErrorString(e));
                 break;
             }
-        } else if ((rc = step_fs(proto, c.d_desc, (int)c.members.size(), nsteps, c.st))) {
+        } else if ((rc = step_fs(proto, c.d_desc, (int)c.members.size(), nsteps, c.st, c.d_maps))) {
             break;
         }
         cudaEventRecord(c.done, c.st);

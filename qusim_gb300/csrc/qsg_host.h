@@ -61,6 +61,10 @@ struct qsg_ctx {
     double *sums = nullptr;      // small device result buffer (8 doubles; the last holds dev_err)
     int *dev_err = nullptr;      // set by a kernel whose bounded waits ran out (tensor-copy column pass)
     bool col_tma = true;         // momentum-form column passes fed by tensor copies (QSG_COL_TMA=0: off)
+    // four-step column passes fed by tensor copies (QSG_FS_TMA=1); off by default: on the 2048-instance
+    // batch they measured slower than the load-instruction pass (511 against 471 ms of column passes per
+    // 1000 steps: two CTAs per SM instead of three, and the twiddles still come from L2)
+    bool fs_tma = false;
     double *host_sums = nullptr; // pinned mirror
     int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
     // batch steps replayed from captured CUDA graphs (QSG_BATCH_GRAPHS=1); off by default: on the

@@ -637,6 +637,9 @@ struct FsColArgs {
     int n1;
     int vsel, vtwice;       // V table index; apply it twice
     int in_k, out_k;        // input in k layout / output to k layout
+    const void *maps;       // tensor-copy pass: 3 tensor maps per instance (state, V 0, V 1), or null
+    int tiles;              // tensor-copy pass: column blocks x instances
+    int *err;               // tensor-copy pass: set to 1 when a bounded wait ran out
 };
 
 // three 256-thread CTAs per SM (registers capped at 85) for the strided

@@ -85,6 +85,13 @@ int col3_ctas(int prec, int l, int inner, int outer);
 template <class T> cudaError_t launch3_row(int l, size_t lines, const Pass3Args &a, cudaStream_t st);
 template <class T> cudaError_t launch3_col(int l, int inner, int outer, const Pass3Args &a, cudaStream_t st);
 
+// 1D four-step column pass fed by tensor copies (qsg_fs_tma.cuh, complex64):
+// supported column lengths, one instance buffer's tensor map (128 bytes at
+// out, 64-byte aligned) and the launch (a.maps: 3 maps per instance)
+bool fs_tma_supported(int prec, int n2);
+bool encode_fs_map(void *base, int n1, int n2, void *out);
+cudaError_t launch_fs_col_tma(const FsGeom &g, const FsColArgs &a, cudaStream_t st);
+
 // momentum-form column pass fed by tensor copies (qsg_col_tma.cuh): compiled
 // tile shapes, the two tensor maps (work buffer, state; 2 x 128 bytes, 64-byte
 // aligned storage at maps) and the launch

@@ -388,3 +388,34 @@ def test_batch_graph_replay_equals_direct(qsg, monkeypatch):
         c.close()
     for a, g in zip(*out):
         assert np.array_equal(a, g)
+
+
+def test_fourstep_tensor_copy_pass_is_bitwise_the_plain_one(qsg, monkeypatch):
+    """The complex64 four-step column pass fed by tensor copies (QSG_FS_TMA=1;
+    off by default, measured slower) computes exactly what the load-instruction
+    pass computes: a mixed-size batch and a single large instance."""
+    rng = np.random.default_rng(21)
+    sizes = [16384, 32768, 65536, 131072, 262144, 8192, 1024]
+    psis, Vs, dxs, dts = [], [], [], []
+    for n in sizes:
+        box = 0.05 * n
+        p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
+        psis.append(p), Vs.append(v), dxs.append(dx), dts.append(0.01)
+    out = []
+    for tma in ("1", "0"):
+        monkeypatch.setenv("QSG_FS_TMA", tma)
+        c = qsg.Context(0)
+        b = qsg.Batch(c, psis, Vs, dxs, dts, order=4, precision="mixed")
+        b.step(3)
+        b.step(2)
+        got = [b.instance(i).get_psi() for i in range(len(sizes))]
+        b.close()
+        solo = qsg.Instance.create_1d(c, psis[3], Vs[3], dxs[3], 0.01, order=2, precision="mixed")
+        solo.step(4)
+        got.append(solo.get_psi())
+        got.append(solo.step_norm2())
+        solo.close()
+        c.close()
+        out.append(got)
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)
