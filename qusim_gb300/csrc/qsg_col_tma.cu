@@ -47,9 +47,8 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
 EncodeTiled encode_fn()
 {
     static EncodeTiled fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static std::atomic<bool> tried{false};
+    if (!tried.load()) {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
@@ -57,30 +56,33 @@ EncodeTiled encode_fn()
             q == cudaDriverEntryPointSuccess)
             fn = reinterpret_cast<EncodeTiled>(p);
         cudaGetLastError();
+        tried.store(true);
     }
     return fn;
 }
-// an nx x ny complex64 buffer (y contiguous) as a 2D tensor of 8-byte elements,
-// boxes of w columns x 256 rows
-bool encode_one(CUtensorMap *map, void *base, int nx, int ny, int w)
+}  // namespace
+
+bool encode_2d_map(void *base, uint64_t inner, uint64_t outer, uint32_t box_inner, uint32_t box_outer, void *out)
 {
     EncodeTiled fn = encode_fn();
-    if (!fn) return false;
-    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((size_t)ny * 8) % 16 || (w * 8) % 16 || nx < 256) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)ny, (cuuint64_t)nx};
-    const cuuint64_t strides[1] = {(cuuint64_t)ny * 8};
-    const cuuint32_t box[2] = {(cuuint32_t)w, 256};
+    if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15) || (inner * 8) % 16 || (box_inner * 8) % 16 ||
+        box_inner == 0 || box_inner > 256 || box_outer == 0 || box_outer > 256 || outer < box_outer ||
+        inner % box_inner || outer % box_outer)
+        return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+    const cuuint64_t strides[1] = {(cuuint64_t)inner * 8};
+    const cuuint32_t box[2] = {box_inner, box_outer};
     const cuuint32_t estr[2] = {1, 1};
-    return fn(map, CU_TENSOR_MAP_DATA_TYPE_INT64, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
-           CUDA_SUCCESS;
+    return fn(static_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_INT64, 2, base, dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
-}  // namespace
 
 bool encode_col_tma_maps(void *work, void *psi, int nx, int ny, int w, void *out)
 {
     CUtensorMap *m = static_cast<CUtensorMap *>(out);
-    return encode_one(m, work, nx, ny, w) && encode_one(m + 1, psi, nx, ny, w);
+    return encode_2d_map(work, (uint64_t)ny, (uint64_t)nx, (uint32_t)w, 256, m) &&
+           encode_2d_map(psi, (uint64_t)ny, (uint64_t)nx, (uint32_t)w, 256, m + 1);
 }
 
 }  // namespace qsg

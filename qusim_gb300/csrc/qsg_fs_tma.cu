@@ -38,43 +38,11 @@ cudaError_t launch_fs_col_tma(const FsGeom &g, const FsColArgs &a, cudaStream_t 
     return cudaErrorNotSupported;
 }
 
-namespace {
-using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiled encode_fn()
-{
-    static EncodeTiled fn = nullptr;
-    static std::atomic<bool> tried{false};
-    if (!tried.load()) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(p);
-        cudaGetLastError();
-        tried.store(true);
-    }
-    return fn;
-}
-}  // namespace
-
 // one instance's n2 x n1 complex64 buffer (row-major) as a 2D tensor of
 // 8-byte elements, boxes of W = 4096 / n2 columns x min(n2, 256) rows
 bool encode_fs_map(void *base, int n1, int n2, void *out)
 {
-    EncodeTiled fn = encode_fn();
-    if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15) || ((size_t)n1 * 8) % 16) return false;
-    const int w = 4096 / n2;
-    if (n1 % w) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)n1, (cuuint64_t)n2};
-    const cuuint64_t strides[1] = {(cuuint64_t)n1 * 8};
-    const cuuint32_t box[2] = {(cuuint32_t)w, (cuuint32_t)(n2 < 256 ? n2 : 256)};
-    const cuuint32_t estr[2] = {1, 1};
-    return fn(static_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_INT64, 2, base, dims, strides, box, estr,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return encode_2d_map(base, (uint64_t)n1, (uint64_t)n2, (uint32_t)(4096 / n2), (uint32_t)(n2 < 256 ? n2 : 256), out);
 }
 
 }  // namespace qsg

@@ -85,6 +85,12 @@ int col3_ctas(int prec, int l, int inner, int outer);
 template <class T> cudaError_t launch3_row(int l, size_t lines, const Pass3Args &a, cudaStream_t st);
 template <class T> cudaError_t launch3_col(int l, int inner, int outer, const Pass3Args &a, cudaStream_t st);
 
+// a row-major buffer of outer x inner 8-byte elements as a 2D tensor map
+// (CUtensorMap, 128 bytes at out) with boxes of box_inner x box_outer; false
+// when the driver entry point is missing or a TMA rule (16-byte base, strides
+// and box rows; boxes of at most 256) would be broken
+bool encode_2d_map(void *base, uint64_t inner, uint64_t outer, uint32_t box_inner, uint32_t box_outer, void *out);
+
 // 1D four-step column pass fed by tensor copies (qsg_fs_tma.cuh, complex64):
 // supported column lengths, one instance buffer's tensor map (128 bytes at
 // out, 64-byte aligned) and the launch (a.maps: 3 maps per instance)
