@@ -92,6 +92,7 @@ struct qsg_inst {
     qsg::FsInst *desc = nullptr;   // device descriptor of this instance
     void *fs_maps = nullptr;       // complex64 four-step: tensor maps of psi, V 0, V 1 (tensor-copy column pass)
     double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
+    std::vector<std::tuple<int, int, int, double, double>> shared_k;  // four-step kinetic tables in use (ctx->fs_ktabs)
     double *snorm = nullptr;       // 1D one-CTA kernels: sum |psi|^2 of the state a step call ended in
     bool snorm_valid = false;      // ... written by the last call (no renormalisation, no state change since)
     double *parts = nullptr;       // four-step norm partials (col_blocks)
@@ -653,11 +654,25 @@ int build_tables(qsg_inst *in)
         const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
         for (int k = 0; k < ntab; ++k) {
             const cd f = -I * DT * in->dt * tc[k] / in->hbar;
-            if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
             if (in->fourstep) {
-                QSG_CUDA(qsg::launch_ktable_fs(in->prec, in->ktab[k], in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
-                                               1.0 / (double)in->n, ctx->st));
-            } else {
+                // shared by every instance of the context with the same size and coefficient (a batch
+                // of equal-dx, equal-dt instances reads one table per size from L2 instead of one each)
+                const auto key = std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag());
+                auto it = ctx->fs_ktabs.find(key);
+                if (it == ctx->fs_ktabs.end()) {
+                    void *p = nullptr;
+                    if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
+                    QSG_CUDA(qsg::launch_ktable_fs(in->prec, p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
+                                                   1.0 / (double)in->n, ctx->st));
+                    it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
+                }
+                it->second.users += 1;
+                in->shared_k.push_back(key);
+                in->ktab[k] = it->second.p;
+                continue;
+            }
+            if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
+            {
                 QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
                                               1.0 / (double)in->n, ctx->st));
             }
@@ -727,6 +742,13 @@ void free_inst(qsg_inst *in)
         // streams is joined into it before an instance is released)
         for (void *p : in->allocs) cudaFreeAsync(p, in->ctx->st);
         in->ctx->in_use -= in->bytes;
+        for (const auto &key : in->shared_k) {
+            auto it = in->ctx->fs_ktabs.find(key);
+            if (it == in->ctx->fs_ktabs.end() || --it->second.users > 0) continue;
+            cudaFreeAsync(it->second.p, in->ctx->st);
+            in->ctx->in_use -= it->second.bytes;
+            in->ctx->fs_ktabs.erase(it);
+        }
     }
     delete in;
 }

@@ -66,6 +66,14 @@ struct qsg_ctx {
     // 1000 steps: two CTAs per SM instead of three, and the twiddles still come from L2)
     bool fs_tma = false;
     double *host_sums = nullptr; // pinned mirror
+    // complex64 / complex128 four-step kinetic tables shared by the instances with the same
+    // (precision, n1, n2, coefficient): table pointer, bytes, instances using it
+    struct SharedTable {
+        void *p;
+        size_t bytes;
+        int users;
+    };
+    std::map<std::tuple<int, int, int, double, double>, SharedTable> fs_ktabs;
     int prof = 0;  // 0 off, 1 CUDA-event timing of every launch, 2 launch counts only
     // batch steps replayed from captured CUDA graphs (QSG_BATCH_GRAPHS=1); off by default: on the
     // 2048-instance batch the graph measured no faster than direct launches (7.34e10 against 7.41e10
