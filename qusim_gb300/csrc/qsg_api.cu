@@ -654,28 +654,27 @@ int build_tables(qsg_inst *in)
         const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
         for (int k = 0; k < ntab; ++k) {
             const cd f = -I * DT * in->dt * tc[k] / in->hbar;
-            if (in->fourstep) {
-                // shared by every instance of the context with the same size and coefficient (a batch
-                // of equal-dx, equal-dt instances reads one table per size from L2 instead of one each)
-                const auto key = std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag());
-                auto it = ctx->fs_ktabs.find(key);
-                if (it == ctx->fs_ktabs.end()) {
-                    void *p = nullptr;
-                    if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
+            // shared by every instance of the context with the same size and coefficient (a batch of
+            // equal-dx, equal-dt instances reads one table per size from L2 instead of one each);
+            // key (precision, n1, n2) for the four-step layout, (precision, n, 0) for the natural one
+            const auto key = in->fourstep ? std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag())
+                                          : std::make_tuple(in->prec, (int)in->n, 0, f.real(), f.imag());
+            auto it = ctx->fs_ktabs.find(key);
+            if (it == ctx->fs_ktabs.end()) {
+                void *p = nullptr;
+                if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
+                if (in->fourstep) {
                     QSG_CUDA(qsg::launch_ktable_fs(in->prec, p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
                                                    1.0 / (double)in->n, ctx->st));
-                    it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
+                } else {
+                    QSG_CUDA(qsg::launch_ktable1d(in->prec, p, (int)in->n, f.real(), f.imag(), 1.0 / (double)in->n,
+                                                  ctx->st));
                 }
-                it->second.users += 1;
-                in->shared_k.push_back(key);
-                in->ktab[k] = it->second.p;
-                continue;
+                it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
             }
-            if ((rc = inst_alloc(in, in->n * cs, &in->ktab[k]))) return rc;
-            {
-                QSG_CUDA(qsg::launch_ktable1d(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
-                                              1.0 / (double)in->n, ctx->st));
-            }
+            it->second.users += 1;
+            in->shared_k.push_back(key);
+            in->ktab[k] = it->second.p;
         }
     } else if (in->dim == 3) {
         // SplittingMethod2D::InitExpT with a third axis, one factor per axis:

@@ -66,8 +66,9 @@ struct qsg_ctx {
     // 1000 steps: two CTAs per SM instead of three, and the twiddles still come from L2)
     bool fs_tma = false;
     double *host_sums = nullptr; // pinned mirror
-    // complex64 / complex128 four-step kinetic tables shared by the instances with the same
-    // (precision, n1, n2, coefficient): table pointer, bytes, instances using it
+    // 1D periodic kinetic tables shared by the instances with the same (precision, size,
+    // coefficient); key (precision, n1, n2, f) in the four-step layout, (precision, n, 0, f) in
+    // the natural one: table pointer, bytes, instances using it
     struct SharedTable {
         void *p;
         size_t bytes;
