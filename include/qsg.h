@@ -19,6 +19,16 @@
  * (re, im) doubles (std::complex<double>), a 2D grid is stored with index
  * iy + ix*ny (y contiguous; include/QuSim.h:47-52), and grid point i sits at
  * x0 + i*dx with dx = (x1 - x0)/n (src/EvolverImpl1D.cpp:11).
+ *
+ * Environment, read when a context is created (qsg_init):
+ *   QSG_PLAN_CACHE      2D plan cache file (default ~/.cache/qusim_gb300/plans.tsv)
+ *   QSG_COL_TMA=0       complex64 2D momentum-form column passes load their
+ *                       tiles with load instructions instead of tensor copies
+ *   QSG_FS_TMA=1        1D four-step column passes staged by tensor copies
+ *                       (off by default: measured slower)
+ *   QSG_BATCH_GRAPHS=1  batch steps replayed from captured CUDA graphs (off by
+ *                       default: measured no faster)
+ * Every setting computes the same result bit for bit.
  */
 #ifndef QSG_H
 #define QSG_H
