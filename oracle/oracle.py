@@ -64,6 +64,7 @@ class Oracle:
         lib.orc_kinen2d.restype = _d
         lib.orc_norm2.argtypes = [_sz, _d, _dp]
         lib.orc_norm2.restype = _d
+        lib.orc_renormalize.argtypes = [_sz, _d, _dp]
         lib.orc_poten.argtypes = [_sz, _d, _dp, _dp]
         lib.orc_poten.restype = _d
         lib.orc_xavg.argtypes = [_sz, _d, _d, _dp]
@@ -117,7 +118,7 @@ class Oracle:
                                    int(wall), 0, _ptr(psi), _ptr(V), nsteps)
         assert rc == 0
         if renormalize:
-            psi /= np.sqrt(self.norm2(psi, dx))
+            self.lib.orc_renormalize(psi.size, dx, _ptr(psi))
         return psi
 
     def evolve2d(self, psi, V, dx, dy, dt, nsteps, order=2, mass=1.0, hbar=1.0,
@@ -130,7 +131,7 @@ class Oracle:
                                    _ptr(psi), _ptr(V), nsteps)
         assert rc == 0
         if renormalize:
-            psi /= np.sqrt(self.norm2(psi, dx * dy))
+            self.lib.orc_renormalize(psi.size, dx * dy, _ptr(psi))
         return psi
 
     def norm2(self, psi, dv):

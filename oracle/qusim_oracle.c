@@ -269,12 +269,46 @@ void orc_splitting_constants(double *c1, double *c2, double *d1, double *d2)
 
 static size_t fold_half(size_t i, size_t n) { return i > n / 2 ? n - i : i; }
 
-static double norm2_raw(const cplx *p, size_t n)
-{
-    double s = 0;
-    for (size_t i = 0; i < n; ++i) s += creal(p[i]) * creal(p[i]) + cimag(p[i]) * cimag(p[i]);
-    return s;
-}
+/* The reference's CPU reductions are std::transform_reduce with the sequential
+ * policy (src/DeviceTemplate.h:404-407), which libstdc++ evaluates four
+ * elements at a time: init + ((f0 + f1) + (f2 + f3)), then the tail one by
+ * one.  Restated with that pairing so the sums agree to the last bit. */
+#define TR_SUM(n, F)                                                           \
+    ({                                                                         \
+        double acc_ = 0;                                                       \
+        size_t i_ = 0;                                                         \
+        for (; (n) - i_ >= 4; i_ += 4) {                                       \
+            size_t i = i_;                                                     \
+            const double f0_ = (F);                                            \
+            i = i_ + 1;                                                        \
+            const double f1_ = (F);                                            \
+            i = i_ + 2;                                                        \
+            const double f2_ = (F);                                            \
+            i = i_ + 3;                                                        \
+            const double f3_ = (F);                                            \
+            acc_ = acc_ + ((f0_ + f1_) + (f2_ + f3_));                         \
+        }                                                                      \
+        for (; i_ < (n); ++i_) {                                               \
+            size_t i = i_;                                                     \
+            acc_ = acc_ + (F);                                                 \
+        }                                                                      \
+        acc_;                                                                  \
+    })
+
+/* The two-range reductions (Abs2Mul, Abs2K1D/2D, Abs2Idx: a data range zipped
+ * with V or an index range) go through the sequential policy's inner_product
+ * brick instead: init = init + f(i), one element at a time. */
+#define SEQ_SUM(n, F)                                                          \
+    ({                                                                         \
+        double acc_ = 0;                                                       \
+        for (size_t i = 0; i < (n); ++i) acc_ = acc_ + (F);                    \
+        acc_;                                                                  \
+    })
+
+static double abs2c(cplx z) { return cimag(z) * cimag(z) + creal(z) * creal(z); }  /* op_Abs2 */
+
+/* Device::Norm2 without dv (DeviceTemplate.h:1222-1229) */
+static double norm2_raw(const cplx *p, size_t n) { return TR_SUM(n, abs2c(p[i])); }
 
 /* the complex coefficient -i * dt * t / hbar of ExpV, SplittingMethod1D.cpp:87 */
 static cplx expv_coef(cplx dt, double t, double hbar) { return (-I / hbar) * dt * t; }
@@ -409,10 +443,8 @@ double orc_kinen1d(size_t n, double dx, double mass, double hbar, int wall, cons
         plan_exec(&p, psi, ft);
         const double dk = 2 * kPi / (dx * n);
         const double DT = dk * dk / (2 * mass);
-        for (size_t i = 0; i < n; ++i) {
-            const double fi = (double)fold_half(i, n);
-            kin += (creal(ft[i]) * creal(ft[i]) + cimag(ft[i]) * cimag(ft[i])) * (fi * fi) * DT;
-        }
+        /* Abs2K1D (DeviceTemplate.h:1527-1536, op :738-752) */
+        kin = SEQ_SUM(n, abs2c(ft[i]) * ((double)fold_half(i, n) * (double)fold_half(i, n)) * DT);
         nn = norm2_raw(ft, n);
         free(ft);
         plan_free(&p);
@@ -426,10 +458,8 @@ double orc_kinen1d(size_t n, double dx, double mass, double hbar, int wall, cons
         plan_exec(&p, iw, iwk);
         const double dk = kPi / (dx * n);
         const double DT = (dk * hbar) * (dk * hbar) / (2 * mass);
-        double s = 0;
-        for (size_t i = 0; i < n; ++i)
-            s += (creal(iwk[i]) * creal(iwk[i]) + cimag(iwk[i]) * cimag(iwk[i])) * ((double)i * (double)i);
-        kin = s * DT;
+        /* Abs2Idx2 (op_Abs2MulSquare) */
+        kin = SEQ_SUM(n, abs2c(iwk[i]) * ((double)i * (double)i)) * DT;
         nn = norm2_raw(iwk, n);
         free(iw); free(iwk);
         plan_free(&p);
@@ -557,15 +587,12 @@ double orc_kinen2d(size_t nx, size_t ny, double dx, double dy, double mass, doub
     const double dkx = 2 * kPi / (dx * nx), dky = 2 * kPi / (dy * ny);
     const double DTx = (dkx * hbar) * (dkx * hbar) / (2 * mass);
     const double DTy = (dky * hbar) * (dky * hbar) / (2 * mass);
-    double kin = 0;
-    for (size_t i = 0; i < nx; ++i) {
-        const double fi = (double)fold_half(i, nx);
-        for (size_t j = 0; j < ny; ++j) {
-            const double fj = (double)fold_half(j, ny);
-            const cplx u = ft[i * ny + j];
-            kin += (creal(u) * creal(u) + cimag(u) * cimag(u)) * ((fi * fi) * DTx + (fj * fj) * DTy);
-        }
-    }
+    /* Abs2K2D (DeviceTemplate.h:1539-1548, op :772-792), element index i*ny + j */
+#define KIN2D_TERM(k)                                                                   \
+    (abs2c(ft[k]) * (((double)fold_half((k) / ny, nx) * (double)fold_half((k) / ny, nx)) * DTx + \
+                     ((double)fold_half((k) % ny, ny) * (double)fold_half((k) % ny, ny)) * DTy))
+    const double kin = SEQ_SUM(n, KIN2D_TERM(i));
+#undef KIN2D_TERM
     const double nn = norm2_raw(ft, n);
     free(ft); free(ci); free(co);
     plan_free(&px); plan_free(&py);
@@ -581,20 +608,28 @@ double orc_norm2(size_t n, double dv, const double *psi)
     return norm2_raw((const cplx *)psi, n) * dv;
 }
 
+/* The renormalisation that ends QuEvolverImpl::Step when
+ * force_normalization_each_step is set (EvolverImpl.cpp:60-63):
+ * scale = 1 / sqrt(Norm2()), psi_i = scale * psi_i (Device::Scale). */
+void orc_renormalize(size_t n, double dv, double *psi_io)
+{
+    cplx *psi = (cplx *)psi_io;
+    const double sc = 1.0 / sqrt(norm2_raw(psi, n) * dv);
+    for (size_t i = 0; i < n; ++i) psi[i] = sc * psi[i];
+}
+
 /* Sum |psi|^2 V dv / Norm2 */
 double orc_poten(size_t n, double dv, const double *psi_in, const double *V)
 {
     const cplx *psi = (const cplx *)psi_in;
-    double s = 0;
-    for (size_t i = 0; i < n; ++i) s += (creal(psi[i]) * creal(psi[i]) + cimag(psi[i]) * cimag(psi[i])) * V[i];
+    const double s = SEQ_SUM(n, abs2c(psi[i]) * V[i]);  /* Abs2Mul (DeviceTemplate.h:1601-1609) */
     return (s * dv) / orc_norm2(n, dv, psi_in);
 }
 
 double orc_xavg(size_t n, double x0, double dx, const double *psi_in)
 {
     const cplx *psi = (const cplx *)psi_in;
-    double s = 0;
-    for (size_t i = 0; i < n; ++i) s += (creal(psi[i]) * creal(psi[i]) + cimag(psi[i]) * cimag(psi[i])) * (double)i;
+    const double s = SEQ_SUM(n, abs2c(psi[i]) * (double)i);  /* Abs2Idx (DeviceTemplate.h:1200-1209) */
     return x0 + dx * (s / norm2_raw(psi, n));
 }
 
@@ -691,33 +726,6 @@ static double cal_v15(double x, double k0, double e0)  /* Perburbation.h:47-57 *
     return (-0.8 * e0) * (u > 0 ? exp(-0.015 * x * x * 1. / sqrt(1 - x * x / (15. * 15))) : 0);
 }
 
-/* The reference's CPU reductions are std::transform_reduce with the sequential
- * policy (src/DeviceTemplate.h:404-407), which libstdc++ evaluates four
- * elements at a time: init + ((f0 + f1) + (f2 + f3)), then the tail one by
- * one.  Restated with that pairing so the sums agree to the last bit. */
-#define TR_SUM(n, F)                                                           \
-    ({                                                                         \
-        double acc_ = 0;                                                       \
-        size_t i_ = 0;                                                         \
-        for (; (n) - i_ >= 4; i_ += 4) {                                       \
-            size_t i = i_;                                                     \
-            const double f0_ = (F);                                            \
-            i = i_ + 1;                                                        \
-            const double f1_ = (F);                                            \
-            i = i_ + 2;                                                        \
-            const double f2_ = (F);                                            \
-            i = i_ + 3;                                                        \
-            const double f3_ = (F);                                            \
-            acc_ = acc_ + ((f0_ + f1_) + (f2_ + f3_));                         \
-        }                                                                      \
-        for (; i_ < (n); ++i_) {                                               \
-            size_t i = i_;                                                     \
-            acc_ = acc_ + (F);                                                 \
-        }                                                                      \
-        acc_;                                                                  \
-    })
-
-static double abs2c(cplx z) { return cimag(z) * cimag(z) + creal(z) * creal(z); }  /* op_Abs2 */
 
 /* epsilon actually used by the preconditioned series (GetEpsilon) */
 static double born_min_epsilon(const cplx *v, size_t n, int precer)

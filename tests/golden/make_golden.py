@@ -6,7 +6,10 @@ compiled from its sources by ``make -C oracle ref`` (oracle/_ref), on seeded
 inputs and stores inputs + outputs as .npz.  The reference tree is needed
 only here; the committed fixtures travel without it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name-prefix ...]
+
+With name prefixes, only the fixtures whose names start with one of them are
+written (the others are left as they are).
 """
 from __future__ import annotations
 
@@ -25,7 +28,16 @@ from tests.workloads import (BORN_1D_CASES, BORN_2D_CASES, BORN_XSEC_TOTAL,  # n
                              gauss_packet_2d, gaussian_bumps_2d, xsec_cosines)
 
 
+ONLY = tuple(sys.argv[1:])
+
+
+def wanted(name):
+    return not ONLY or name.startswith(ONLY)
+
+
 def save(name, **arrays):
+    if not wanted(name):
+        return
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **arrays)
     print("wrote", os.path.relpath(path, ROOT), os.path.getsize(path), "bytes")
@@ -49,7 +61,7 @@ def main():
         x = np.arange(int(np.prod(shape)), dtype=np.complex128).reshape(shape) * (1 + 0.5j)
         save("fft3d_ramp_%dx%dx%d" % shape, fwd=ref.fft3d(x), inv=ref.fft3d(x, inverse=True))
 
-    # 1D evolutions.  (name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes)
+    # 1D evolutions.  (name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes[, mass, hbar])
     cases_1d = [
         # the 1D plain configuration: N=4096 on [-200,200), k0=1, x0=-50, s=10,
         # V=0.5 exp(-x^2/2), dt=0.05, 2000 O2 steps
@@ -59,34 +71,53 @@ def main():
         ("evolve1d_n1024_o4_imag", 1024, -50.0, 50.0, 1.5, -10.0, 3.0, 4, False, 0.02 - 0.005j, 40, 1, False),
         ("evolve1d_n512_o2_wall", 512, -40.0, 40.0, 1.0, -10.0, 3.0, 2, True, 0.02, 100, 1, False),
         ("evolve1d_n1000_o2", 1000, -50.0, 50.0, 1.0, -10.0, 3.0, 2, False, 0.02, 100, 1, False),
+        # hbar and mass away from 1: the periodic KinEn omits hbar^2
+        # (src/SplittingMethod1D.cpp:101-102), the wall KinEn keeps it (:118)
+        ("evolve1d_n1024_o2_hbar07_m2", 1024, -50.0, 50.0, 1.5, -10.0, 3.0, 2, False, 0.02, 150, 1, False,
+         2.0, 0.7),
+        ("evolve1d_n512_o4_wall_hbar07_m2", 512, -40.0, 40.0, 1.0, -10.0, 3.0, 4, True, 0.02, 60, 1, False,
+         2.0, 0.7),
     ]
-    for name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes in cases_1d:
+    for case in cases_1d:
+        name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes = case[:13]
+        mass, hbar = case[13:] if len(case) > 13 else (1.0, 1.0)
+        if not wanted(name):
+            continue
         psi0, V, dx = gauss_packet_1d(n, x0, x1, k0, xc, s, barrier=0.5)
         psi, nrm, kin, pot = ref.evolve1d(psi0, V, x0, x1, dt, batch, calls=calls, order=order,
-                                          wall=wall, fnes=fnes)
+                                          mass=mass, hbar=hbar, wall=wall, fnes=fnes)
+        extra = {} if (mass, hbar) == (1.0, 1.0) else dict(mass=np.float64(mass), hbar=np.float64(hbar))
         save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
              params=np.array([n, x0, x1, order, int(wall), batch, calls, int(fnes)], dtype=np.float64),
-             dt=np.complex128(dt))
+             dt=np.complex128(dt), **extra)
 
-    # 2D evolutions.  (name, nx, ny, half_x, half_y, order, dt, batch, calls, fnes)
+    # 2D evolutions.  (name, nx, ny, half_x, half_y, order, dt, batch, calls, fnes[, mass, hbar])
     cases_2d = [
         ("evolve2d_128x256_o2_50", 128, 256, 20.0, 40.0, 2, 0.02, 50, 1, False),
         ("evolve2d_256x128_o4_20", 256, 128, 30.0, 30.0, 4, 0.02, 20, 1, False),
         ("evolve2d_128x128_o4_b5x2_fnes", 128, 128, 10.0, 20.0, 4, 0.01 - 0.002j, 5, 2, True),
+        ("evolve2d_128x256_o4_hbar07_m2", 128, 256, 20.0, 40.0, 4, 0.02, 20, 1, False, 2.0, 0.7),
     ]
-    for name, nx, ny, hx, hy, order, dt, batch, calls, fnes in cases_2d:
+    for case in cases_2d:
+        name, nx, ny, hx, hy, order, dt, batch, calls, fnes = case[:10]
+        mass, hbar = case[10:] if len(case) > 10 else (1.0, 1.0)
+        if not wanted(name):
+            continue
         x0, x1, y0, y1 = -hx, hx, -hy, hy
         psi0, dx, dy = gauss_packet_2d(nx, ny, x0, x1, y0, y1, kx=1.5, ky=0.0, xc=-0.3 * hx, yc=0.0, s=0.1 * hx)
         V = gaussian_bumps_2d(nx, ny, x0, x1, y0, y1, nbumps=16, seed=0, spread=0.5 * hx)
         psi, nrm, kin, pot = ref.evolve2d(psi0, V, x0, x1, y0, y1, dt, batch, calls=calls,
-                                          order=order, fnes=fnes)
+                                          order=order, mass=mass, hbar=hbar, fnes=fnes)
+        extra = {} if (mass, hbar) == (1.0, 1.0) else dict(mass=np.float64(mass), hbar=np.float64(hbar))
         save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
              params=np.array([nx, ny, x0, x1, y0, y1, order, batch, calls, int(fnes)], dtype=np.float64),
-             dt=np.complex128(dt))
+             dt=np.complex128(dt), **extra)
 
     # Born-series scattering, 1D and 2D (tests/workloads.py BORN_*_CASES)
     for (name, n, x0, x1, v0, en, eps, direction, order, pre, precer, slow,
          computes) in BORN_1D_CASES:
+        if not wanted(name):
+            continue
         V, _ = born_potential_1d(n, x0, x1, v0)
         r = ref.born1d(V, x0, x1, en, eps, direction=direction, order=order, preconditional=pre,
                        preconditioner=precer, slow=slow, computes=computes)
@@ -96,6 +127,8 @@ def main():
     cs = xsec_cosines()
     for (name, nx, ny, hx, hy, en, eps, dirx, diry, order, pre, precer, slow,
          computes) in BORN_2D_CASES:
+        if not wanted(name):
+            continue
         V, _, _ = born_potential_2d(nx, ny, -hx, hx, -hy, hy)
         r = ref.born2d(V, -hx, hx, -hy, hy, en, eps, dirx=dirx, diry=diry, order=order,
                        preconditional=pre, preconditioner=precer, slow=slow, computes=computes,

@@ -34,21 +34,32 @@ def ctx(qsg):
     return qsg.Context(0)
 
 
+def mass_hbar(g):
+    """(mass, hbar) of a fixture; 1, 1 where it stores none."""
+    return float(g.get("mass", 1.0)), float(g.get("hbar", 1.0))
+
+
 def run_1d(qsg, ctx, g, precision):
     n, x0, x1, order, wall, batch, calls, fnes = g["params"]
     n, order, batch, calls = int(n), int(order), int(batch), int(calls)
     dx = (x1 - x0) / n
+    mass, hbar = mass_hbar(g)
     bc = qsg.BoundaryCondition.InfiniteWall if int(wall) else qsg.BoundaryCondition.Period
     inst = qsg.Instance.create_1d(ctx, g["psi0"], g["V"], dx, complex(g["dt"]), order=order,
-                                  precision=precision, boundary=bc)
+                                  precision=precision, mass=mass, hbar=hbar, boundary=bc)
     for _ in range(calls):
         inst.step(batch, renormalize=bool(fnes))
     return inst, dx
 
 
+# hbar07_m2: hbar = 0.7, mass = 2; their kinetic energies pin the reference's
+# two KinEn formulas (the periodic 1D one omits hbar^2,
+# src/SplittingMethod1D.cpp:101-102; the wall and 2D ones use (Dk hbar)^2 / 2m)
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
-             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall"]
-GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes"]
+             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1024_o2_hbar07_m2",
+             "evolve1d_n512_o4_wall_hbar07_m2"]
+GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
+             "evolve2d_128x256_o4_hbar07_m2"]
 
 
 @pytest.mark.parametrize("name", GOLDEN_1D)
@@ -78,8 +89,9 @@ def test_evolve2d_matches_reference(qsg, ctx, name, precision):
     nx, ny, x0, x1, y0, y1, order, batch, calls, fnes = g["params"]
     nx, ny, order, batch, calls = int(nx), int(ny), int(order), int(batch), int(calls)
     dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+    mass, hbar = mass_hbar(g)
     inst = qsg.Instance.create_2d(ctx, g["psi0"], g["V"], dx, dy, complex(g["dt"]), order=order,
-                                  precision=precision)
+                                  precision=precision, mass=mass, hbar=hbar)
     for _ in range(calls):
         inst.step(batch, renormalize=bool(fnes))
     tol = PLAIN_TOL if precision == "fp64" else MIXED_TOL

@@ -2,7 +2,8 @@
 
 CPU only.  The fixtures in tests/golden/ were produced by the reference's own
 sources compiled as they lie (tests/golden/make_golden.py); the oracle must
-reproduce them to the last bit (same algorithm, same operation order).
+reproduce them to the last bit (same algorithm, same operation order): psi is
+compared with np.array_equal and Norm2, KinEn and PotEn with ==.
 """
 import numpy as np
 import pytest
@@ -10,8 +11,15 @@ import pytest
 from tests.conftest import load_golden
 
 EVOLVE_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
-             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1000_o2"]
-EVOLVE_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes"]
+             "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1000_o2",
+             "evolve1d_n1024_o2_hbar07_m2", "evolve1d_n512_o4_wall_hbar07_m2"]
+EVOLVE_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
+             "evolve2d_128x256_o4_hbar07_m2"]
+
+
+def mass_hbar(g):
+    """(mass, hbar) of a fixture; 1, 1 where it stores none."""
+    return float(g.get("mass", 1.0)), float(g.get("hbar", 1.0))
 
 
 def rel_l2(a, b):
@@ -45,14 +53,15 @@ def test_evolve1d_matches_reference(oracle, name):
     n, x0, x1, order, wall, batch, calls, fnes = g["params"]
     n, order, batch, calls = int(n), int(order), int(batch), int(calls)
     dx = (x1 - x0) / n
+    mass, hbar = mass_hbar(g)
     psi = g["psi0"]
     for _ in range(calls):
-        psi = oracle.evolve1d(psi, g["V"], dx, complex(g["dt"]), batch, order=order,
-                              wall=bool(wall), renormalize=bool(fnes))
-    assert rel_l2(psi, g["psi"]) < 1e-14
-    assert abs(oracle.norm2(psi, dx) - g["norm2"]) < 1e-13
-    assert abs(oracle.kinen1d(psi, dx, wall=bool(wall)) - g["kin"]) < 1e-12 * max(1, abs(g["kin"]))
-    assert abs(oracle.poten(psi, g["V"], dx) - g["pot"]) < 1e-13
+        psi = oracle.evolve1d(psi, g["V"], dx, complex(g["dt"]), batch, order=order, mass=mass,
+                              hbar=hbar, wall=bool(wall), renormalize=bool(fnes))
+    assert np.array_equal(psi, g["psi"])
+    assert oracle.norm2(psi, dx) == g["norm2"]
+    assert oracle.kinen1d(psi, dx, mass=mass, hbar=hbar, wall=bool(wall)) == g["kin"]
+    assert oracle.poten(psi, g["V"], dx) == g["pot"]
 
 
 @pytest.mark.parametrize("name", EVOLVE_2D)
@@ -61,14 +70,15 @@ def test_evolve2d_matches_reference(oracle, name):
     nx, ny, x0, x1, y0, y1, order, batch, calls, fnes = g["params"]
     nx, ny, order, batch, calls = int(nx), int(ny), int(order), int(batch), int(calls)
     dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+    mass, hbar = mass_hbar(g)
     psi = g["psi0"]
     for _ in range(calls):
-        psi = oracle.evolve2d(psi, g["V"], dx, dy, complex(g["dt"]), batch, order=order,
-                              renormalize=bool(fnes))
-    assert rel_l2(psi, g["psi"]) < 1e-14
-    assert abs(oracle.norm2(psi, dx * dy) - g["norm2"]) < 1e-13
-    assert abs(oracle.kinen2d(psi, dx, dy) - g["kin"]) < 1e-12 * max(1, abs(g["kin"]))
-    assert abs(oracle.poten(psi, g["V"], dx * dy) - g["pot"]) < 1e-13
+        psi = oracle.evolve2d(psi, g["V"], dx, dy, complex(g["dt"]), batch, order=order, mass=mass,
+                              hbar=hbar, renormalize=bool(fnes))
+    assert np.array_equal(psi, g["psi"])
+    assert oracle.norm2(psi, dx * dy) == g["norm2"]
+    assert oracle.kinen2d(psi, dx, dy, mass=mass, hbar=hbar) == g["kin"]
+    assert oracle.poten(psi, g["V"], dx * dy) == g["pot"]
 
 
 def test_splitting_constants(oracle):
