@@ -155,6 +155,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def clocks_over(run_once, device, timed_ms, clk, min_s=1.5):
+    """The timed region's clock record, or, when it was too short for the
+    sampler (fewer than 3 samples at 200 ms), a record taken over untimed
+    repeats of the same work lasting min_s, marked as such."""
+    if clk.get("samples", 0) >= 3 or "nvidia-smi unavailable" in clk.get("reasons", []):
+        clk["window"] = "the timed region"
+        return clk
+    cs = ClockSampler(device)
+    cs.start()
+    t0, reps = time.perf_counter(), 0
+    while time.perf_counter() - t0 < min_s:
+        run_once()
+        reps += 1
+    el = time.perf_counter() - t0
+    c2 = cs.stop()
+    c2["window"] = (f"{reps} untimed repeats of the timed work ({el:.2f} s) right after it: the timed region "
+                    f"itself ({timed_ms:.1f} ms) is shorter than the sampler's 200 ms period")
+    c2["timed_region_samples"] = clk.get("samples", 0)
+    return c2
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -171,6 +192,40 @@ def profile_traffic(kernel):
             return json.load(f).get(kernel)
     except (OSError, ValueError):
         return None
+
+
+SERIAL_NOTE = ("one core: the reference's CPU path for one grid is serial (its CPU_PAR device falls back to "
+               "libstdc++'s serial parallel-STL backend without TBB, and its FFT plans are single-threaded)")
+
+
+def oracle_2d_rows(w, per_step_s, calib_rows=256):
+    """Rows of the workload's own grid (its own psi0 and V, full-length rows)
+    whose O4 step the oracle finishes in about per_step_s on this host: the full
+    grid when it fits, else the largest power-of-two slab around the centre.
+    Returns (rows, seconds per full-grid step, measured)."""
+    from oracle import oracle as orc
+    o = orc.Oracle()
+    psi, V, (dx, dy) = make_inputs(w)
+    nx = w["nx"]
+    r0 = (nx - calib_rows) // 2
+    st = orc.Stepper2D(o, psi[r0:r0 + calib_rows], V[r0:r0 + calib_rows], dx, dy, w["dt"], order=w["order"])
+    st.step(1)
+    t0 = time.perf_counter()
+    st.step(1)
+    per_row = (time.perf_counter() - t0) / calib_rows
+    st.close()
+    rows = nx
+    while rows > 32 and per_row * rows > per_step_s:
+        rows //= 2
+    return rows, per_row * nx
+
+
+def oracle_2d_slab(w, rows):
+    """The oracle stepper on `rows` full-length rows of the workload's own inputs."""
+    from oracle import oracle as orc
+    psi, V, (dx, dy) = make_inputs(w)
+    r0 = (w["nx"] - rows) // 2
+    return orc.Stepper2D(orc.Oracle(), psi[r0:r0 + rows], V[r0:r0 + rows], dx, dy, w["dt"], order=w["order"])
 
 
 def cpu_sample(w, budget_s=15.0):
@@ -192,21 +247,11 @@ def cpu_sample(w, budget_s=15.0):
         st.close()
         return dict(value=w["n"] * n / el, unit="site-steps/s", cores=1, kind=kind,
                     sample=f"{n} steps of the N={w['n']} workload, single thread")
-    # 2D: a slab of R full-length rows (row FFT length unchanged) stepped once
-    h = w["half"]
-    nx_full, ny = w["nx"], w["ny"]
-    rows = nx_full
-    est = 9.0 * (nx_full * ny) / (4096 * 4096)  # seconds per O4 step, measured scale
-    while rows > 256 and est * rows / nx_full > budget_s:
-        rows //= 2
-    dy = 2 * h / ny
-    dx = 2 * h / nx_full
-    ys = -h + dy * np.arange(ny)
-    xs = -h + dx * np.arange(rows) + (nx_full - rows) // 2 * dx
-    X, Y = np.meshgrid(xs, ys, indexing="ij")
-    psi = np.exp(1j * (w["k"][0] * X)) * np.exp(-((X - w["c"][0]) ** 2 + Y ** 2) / (4 * w["s"] ** 2)) + 1e-3
-    V = np.where(np.abs(X) < 1, 10.0, 0.0)
-    st = orc.Stepper2D(o, psi, V, dx, dy, w["dt"], order=w["order"])
+    # 2D: O4 steps of the workload's own grid (a slab of full-length rows of its
+    # own inputs only when one full step would not fit the budget)
+    ny = w["ny"]
+    rows, _ = oracle_2d_rows(w, budget_s * 0.5)
+    st = oracle_2d_slab(w, rows)
     n, t0 = 0, time.perf_counter()
     while True:
         st.step(1)
@@ -215,8 +260,10 @@ def cpu_sample(w, budget_s=15.0):
             break
     el = time.perf_counter() - t0
     st.close()
+    what = f"the full {w['nx']}x{ny} grid" if rows == w["nx"] else f"a {rows}x{ny} slab (full-length rows)"
     return dict(value=rows * ny * n / el, unit="site-steps/s", cores=1, kind=kind,
-                sample=f"{n} O4 step(s) of a {rows}x{ny} slab of the workload (full-length rows), single thread")
+                sample=f"{n} O4 step(s) of {what} of the workload's own inputs; " + SERIAL_NOTE,
+                host_cores=os.cpu_count())
 
 
 def world_max(x: float, world: int, device: str = "cuda") -> float:
@@ -303,26 +350,20 @@ def run_reference(args, w):
         el = time.perf_counter() - t0
         sites, sample = w["n"], f"full N={w['n']} grid, K={args.steps} steps"
     else:
-        # each step: one O4 step of a slab of full-length rows, sized so the run stays within minutes
-        h = w["half"]
+        # each step: one O4 step of the workload's own grid and inputs; a slab of
+        # full-length rows of them only when the whole run would not end within
+        # a few minutes
         ny = w["ny"]
-        per_step_budget = 150.0 / max(1, args.steps + args.warmup)
-        rows = w["nx"]
-        while rows > 32 and 9.0 * rows * ny / (4096 * 4096) > per_step_budget:
-            rows //= 2
-        dx, dy = 2 * h / w["nx"], 2 * h / ny
-        xs = -h + dx * np.arange(rows) + (w["nx"] - rows) // 2 * dx
-        ys = -h + dy * np.arange(ny)
-        X, Y = np.meshgrid(xs, ys, indexing="ij")
-        psi = np.exp(1j * (w["k"][0] * X)) * np.exp(-((X - w["c"][0]) ** 2 + Y ** 2) / (4 * w["s"] ** 2)) + 1e-3
-        V = np.where(np.abs(X) < 1, 10.0, 0.0)
-        st = orc.Stepper2D(o, psi, V, dx, dy, w["dt"], order=w["order"])
+        per_step_budget = 240.0 / max(1, args.steps + args.warmup)
+        rows, full_s = oracle_2d_rows(w, per_step_budget)
+        st = oracle_2d_slab(w, rows)
         st.step(args.warmup)
         t0 = time.perf_counter()
         st.step(args.steps)
         el = time.perf_counter() - t0
         sites = rows * ny
-        sample = f"each step: one O4 step of a {rows}x{ny} slab (full-length rows) of the workload"
+        what = f"the full {w['nx']}x{ny} grid" if rows == w["nx"] else f"a {rows}x{ny} slab (full-length rows)"
+        sample = f"each step: one O4 step of {what} of the workload's own inputs"
     st.close()
     v = sites * args.steps / el
     line = {"metric": "site-steps/s", "value": v, "unit": "site-steps/s", "n_gpus": world,
@@ -330,9 +371,45 @@ def run_reference(args, w):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": w["desc"], "precision": "fp64", "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": v, "unit": "site-steps/s", "cores": 1, "kind": kind, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": "site-steps/s", "cores": 1, "kind": kind,
+                             "sample": sample + "; " + SERIAL_NOTE, "host_cores": os.cpu_count()},
             "e2e": {"value": v, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def batch_cpu_sample(psis, Vs, dxs, w, threads, budget_s=12.0, steps=20):
+    """The oracle on the batch's instances, one instance per host thread at a
+    time (instances are independent; the oracle's C calls release the GIL):
+    `steps` O2 steps of each instance taken from a shared queue in batch order
+    until budget_s has passed."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as orc
+    o = orc.Oracle()
+    lock = threading.Lock()
+    state = {"next": 0, "sites": 0, "instances": 0}
+    t0 = time.perf_counter()
+
+    def worker():
+        while time.perf_counter() - t0 < budget_s:
+            with lock:
+                i = state["next"]
+                state["next"] += 1
+            if i >= len(psis):
+                return
+            st = orc.Stepper1D(o, psis[i], Vs[i], dxs[i], w["dt"], order=w["order"])
+            st.step(steps)
+            st.close()
+            with lock:
+                state["sites"] += psis[i].size * steps
+                state["instances"] += 1
+
+    with ThreadPoolExecutor(threads) as ex:
+        for f in [ex.submit(worker) for _ in range(threads)]:
+            f.result()
+    el = time.perf_counter() - t0
+    return {"value": state["sites"] / el, "unit": "site-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} O2 steps of each of {state['instances']} instances of the batch (in batch order), "
+                      f"one instance per thread at a time, {threads} thread(s)", "host_cores": os.cpu_count()}
 
 
 def run_batch(args, w):
@@ -363,12 +440,43 @@ def run_batch(args, w):
     ms = e0.elapsed_time(e1)
     counts = ctx.profile_read()
     ctx.profile(False)
+
+    def repeat_timed_work():
+        b.step(args.steps)
+        b.sync()
+
+    clk = clocks_over(repeat_timed_work, local, ms, clk)
     ctx.profile(True)  # per-kernel event times: the same K steps again
     b.step(args.steps)
     b.sync()
     prof = ctx.profile_read()
     ctx.profile(False)
     value = sites * args.steps * world / (ms / 1e3)
+    # the same batch with one launch per resident size class instead of the
+    # tile-queue launch (QSG_BATCH_QUEUE=0, read when a context is created)
+    per_class = None
+    if args.precision == "mixed" and not args.no_plain:
+        os.environ["QSG_BATCH_QUEUE"] = "0"
+        try:
+            ctx2 = q.Context(local)
+        finally:
+            del os.environ["QSG_BATCH_QUEUE"]
+        s2 = torch.cuda.ExternalStream(ctx2.stream, device=torch.device("cuda", local))
+        b2 = q.Batch(ctx2, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision=args.precision)
+        b2.step(args.warmup)
+        b2.sync()
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h0.record(s2)
+        b2.step(args.steps)
+        h1.record(s2)
+        h1.synchronize()
+        ms2 = h0.elapsed_time(h1)
+        per_class = {"value": sites * args.steps * world / (ms2 / 1e3), "unit": "site-steps/s",
+                     "ms_per_step": ms2 / args.steps,
+                     "launch": "one launch per resident size class (QSG_BATCH_QUEUE=0); the states are bitwise "
+                               "those of the tile-queue launch (tests/test_gpu_parity.py)"}
+        b2.close()
+        ctx2.close()
     # four-step instances (N > one CTA) move 2 HBM round trips of psi plus one
     # V table and one K table entry per site-step (O2): 6 complex elements
     peak, peak_kind = measured_peaks()
@@ -380,20 +488,23 @@ def run_batch(args, w):
                "note": "four-step bytes over the whole batch time (resident classes run beside them)"}
     acc = None
     if not args.no_plain and args.precision == "mixed":
-        nacc = args.accuracy_steps if args.accuracy_steps is not None else 50
-        sub = list(range(0, len(psis), max(1, len(psis) // 64)))
-        bm = q.Batch(ctx, [psis[i] for i in sub], [Vs[i] for i in sub], [dxs[i] for i in sub],
-                     [w["dt"]] * len(sub), order=w["order"], precision="mixed")
-        bp = q.Batch(ctx, [psis[i] for i in sub], [Vs[i] for i in sub], [dxs[i] for i in sub],
-                     [w["dt"]] * len(sub), order=w["order"], precision="fp64")
+        # every instance of the batch over the configuration's full step count,
+        # complex64 against complex128 (each batched the same way)
+        nacc = args.accuracy_steps if args.accuracy_steps is not None else w["full_steps"]
+        bm = q.Batch(ctx, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision="mixed")
+        bp = q.Batch(ctx, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision="fp64")
+        n0 = [bp.instance(k).norm2() for k in range(len(psis))]
         bm.step(nacc)
         bp.step(nacc)
-        errs = []
-        for k in range(len(sub)):
+        errs, drifts = [], []
+        for k in range(len(psis)):
             a, r = bm.instance(k).get_psi(), bp.instance(k).get_psi()
             errs.append(float(np.linalg.norm(a - r) / np.linalg.norm(r)))
-        acc = {"steps": nacc, "instances": len(sub), "rel_l2_vs_fp64_max": max(errs),
-               "rel_l2_vs_fp64_median": float(np.median(errs))}
+            drifts.append(abs(bm.instance(k).norm2() - n0[k]))
+        bm.close()
+        bp.close()
+        acc = {"steps": nacc, "instances": len(psis), "rel_l2_vs_fp64_max": max(errs),
+               "rel_l2_vs_fp64_median": float(np.median(errs)), "norm_drift_mixed_max": float(max(drifts))}
     # the complex128 path instance by instance (one qsg_step per instance), on
     # the first 256 instances of the batch
     plain = None
@@ -420,20 +531,8 @@ def run_batch(args, w):
             s_.close()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import oracle as orc
-        o = orc.Oracle()
-        t0 = time.perf_counter()
-        done = 0
-        i = 0
-        while time.perf_counter() - t0 < 15.0 and i < len(psis):
-            st = orc.Stepper1D(o, psis[i], Vs[i], dxs[i], w["dt"], order=w["order"])
-            st.step(20)
-            st.close()
-            done += psis[i].size * 20
-            i += 1
-        el = time.perf_counter() - t0
-        cpu = {"value": done / el, "unit": "site-steps/s", "cores": 1, "kind": "port",
-               "sample": f"20 O2 steps of each of the first {i} instances, single thread"}
+        cpu = batch_cpu_sample(psis, Vs, dxs, w, os.cpu_count() or 1)
+        cpu["one_core"] = batch_cpu_sample(psis, Vs, dxs, w, 1)
     if rank == 0:
         line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -444,7 +543,7 @@ def run_batch(args, w):
                            "l2": "2.2 GB of state and tables, larger than L2"},
                 "roofline": {"bound": "on-chip", "note": "resident sizes keep psi in shared memory for all "
                              "K steps; four-step sizes make 2 HBM passes per step"},
-                "step_roofline": fs_roof, "plain_fp64": plain,
+                "step_roofline": fs_roof, "plain_fp64": plain, "resident_per_class_launches": per_class,
                 "accuracy": acc, "gpu_launches": int(sum(v[0] for v in counts.values())),
                 "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
                 "cpu_baseline": cpu, "clocks": clk}
@@ -769,6 +868,66 @@ def serving_inputs(seed=0):
     return pool
 
 
+def serving_fp64_one_at_a_time(q, device, reqs, arrivals):
+    """The same request stream run one request at a time in complex128.
+
+    Every request kind (dimension, size, order) is measured once alone in
+    complex128 on this GPU: instance creation from a device-sampled spec, a few
+    steps (site-steps/s of the kind), the result read back.  Each request's
+    service time is then creation + read + its steps at its kind's rate, and
+    the stream's arrival times are replayed through a first-in first-out
+    single server (one request on the GPU at a time).  Returns the throughput
+    and the latency percentiles of that replay."""
+    from tests.workloads import grid
+    ctx = q.Context(device)
+    kinds = sorted({(key, order) for key, _, _, order in reqs})
+    rate, fixed = {}, {}
+    for (dim, n), order in kinds:
+        half = 0.05 * n
+        _, dx = grid(n, -half, half)
+        sp = q.Spec.make(x0=-half, y0=-half, s=5.0, kx=1.0, cx=-0.25 * half,
+                         bumps=[(0.5, 0.0, 0.0, 2.0)])
+        sites = n if dim == 1 else n * n
+        steps = int(max(4, min(200, 3e8 / sites)))
+        t0 = time.perf_counter()
+        if dim == 1:
+            inst = q.Instance.create_1d_spec(ctx, sp, n, dx, 0.01, order=order, precision="fp64")
+        else:
+            inst = q.Instance.create_2d_spec(ctx, sp, n, n, dx, dx, 0.01, order=order, precision="fp64")
+        inst.sync()
+        t1 = time.perf_counter()
+        inst.step(2)
+        inst.sync()
+        t2 = time.perf_counter()
+        inst.step(steps)
+        inst.sync()
+        t3 = time.perf_counter()
+        inst.get_psi()
+        t4 = time.perf_counter()
+        inst.close()
+        rate[((dim, n), order)] = sites * steps / (t3 - t2)
+        fixed[((dim, n), order)] = (t1 - t0) + (t4 - t3)
+    ctx.close()
+    free_at, lat, work, busy = 0.0, [], 0.0, 0.0
+    for i, (key, _, steps, order) in enumerate(reqs):
+        sites = key[1] if key[0] == 1 else key[1] * key[1]
+        service = fixed[(key, order)] + sites * steps / rate[(key, order)]
+        start = max(arrivals[i], free_at)
+        free_at = start + service
+        lat.append(free_at - arrivals[i])
+        work += sites * steps
+        busy += service
+    lat = np.array(lat)
+    return {"value": work / free_at, "unit": "site-steps/s", "dtype": "c128",
+            "busy_value": work / busy, "makespan_s": free_at,
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+            "kinds_measured": len(kinds),
+            "method": "each request kind measured alone in complex128 on this GPU (creation + read back + steps at "
+                      "the kind's site-steps/s); the stream's arrivals replayed through a FIFO single server with "
+                      "those service times"}
+
+
 def run_serving(args, w):
     """Requests arrive at Poisson times; the server admits them against its HBM
     budget and batches them continuously.  Reports latency percentiles and the
@@ -843,6 +1002,9 @@ def run_serving(args, w):
     st = srv.stats()
     srv.close()
     lats = np.array(lats)
+    solo = None
+    if rank == 0 and not args.no_plain:
+        solo = serving_fp64_one_at_a_time(q, local, reqs, arrivals)
     if rank == 0:
         value = site_steps * world / t_end
         line = {"metric": "site-steps/s", "value": value, "unit": "site-steps/s", "n_gpus": world,
@@ -859,6 +1021,8 @@ def run_serving(args, w):
                 "offered_site_steps_per_s": site_steps / max(arrivals[-1], 1e-9),
                 "makespan_s": t_end, "peak_device_bytes": st["peak_device_bytes"],
                 "completed": st["completed"], "failed": st["failed"], "clocks": clk,
+                "admitted_mid_flight": st["admitted_mid_flight"], "max_in_flight": st["max_in_flight"],
+                "fp64_one_at_a_time": solo,
                 "note": "a 'step' here is one request; ms_per_step = makespan / requests"}
         print(json.dumps(line), flush=True)
 
@@ -966,6 +1130,12 @@ def main():
     ms = e0.elapsed_time(e1)
     counts = ctx.profile_read()
     ctx.profile(False)
+
+    def repeat_timed_work():
+        inst.step(args.steps)
+        inst.sync()
+
+    clk = clocks_over(repeat_timed_work, local, ms, clk)
     # per-kernel CUDA-event times for the roofline: the same K steps again,
     # every launch bracketed by events on the context stream
     ctx.profile(True)

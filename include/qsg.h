@@ -12,8 +12,8 @@
  *     (src/EvolverImpl.h:54-57, src/SplittingMethod1D.h, src/SplittingMethod2D.h)
  *   - its Device ops and FFT wrappers on the GPU_CUDA device
  *     (src/CudaDevice.cu:98-302, src/FourierTransform.cpp:84-127, 336-360)
- * A host evolver (include/qusim_gb300/Evolver.h, or the reference's own
- * QuEvolverImpl subclass shown in INTEGRATION.md) drives it.
+ * A host evolver (include/qusim_gb300/Evolver.h, or a QuEvolverImpl subclass
+ * inside the reference such as tests/cpp/ref_binding.cpp) drives it.
  *
  * Layout conventions are the reference's: complex values are interleaved
  * (re, im) doubles (std::complex<double>), a 2D grid is stored with index
@@ -29,6 +29,12 @@
  *   QSG_BATCH_GRAPHS=1  batch steps replayed from captured CUDA graphs (off by
  *                       default: measured no faster)
  * Every setting computes the same result bit for bit.
+ * Read when a server is created (qsg_server_create):
+ *   QSG_SERVER_FAIL_REQUEST=<id>  fault injection for tests of the failure
+ *                       paths: every dispatch of request <id> fails on the host
+ *                       with QSG_ERR_CUDA instead of launching (no device work
+ *                       is faulted); the request ends failed and the other
+ *                       requests run on unaffected
  */
 #ifndef QSG_H
 #define QSG_H
@@ -299,7 +305,19 @@ typedef struct {
 typedef struct {
     uint64_t completed, failed, site_steps;
     size_t peak_device_bytes, budget_bytes;
+    uint64_t admitted_mid_flight; /* admissions made while other requests had work on the device */
+    uint32_t max_in_flight;       /* most requests with device work queued (not yet finished) at once */
+    uint32_t reserved;
 } qsg_server_info;
+/* One request's progress, times in seconds since the server was created
+ * (-1: not reached yet).  Valid until qsg_server_take releases the request. */
+typedef struct {
+    int32_t state;               /* 0 queued, 1 running, 2 done, 3 failed */
+    int32_t admitted_mid_flight; /* 1: admitted while other requests had work on the device */
+    uint64_t chunks;             /* launches (or batched launches) made for it */
+    uint64_t steps_dispatched;
+    double t_submit, t_admit, t_first_dispatch, t_finish;
+} qsg_request_info;
 int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_running, qsg_server **out);
 int qsg_server_submit(qsg_server *server, const qsg_request *req, uint64_t *id);
 int qsg_server_poll(qsg_server *server, uint64_t id, int *state);
@@ -308,6 +326,7 @@ int qsg_server_wait(qsg_server *server, uint64_t id, double timeout_s, int *stat
  * the request.  A failed request returns its error here. */
 int qsg_server_take(qsg_server *server, uint64_t id, double *psi_out, double *latency_s);
 int qsg_server_stats(qsg_server *server, qsg_server_info *out);
+int qsg_server_request_info(qsg_server *server, uint64_t id, qsg_request_info *out);
 void qsg_server_destroy(qsg_server *server);
 
 /* Per-kernel timing of this context's launches, for roofline reporting.
@@ -332,15 +351,17 @@ int qsg_profile_read(qsg_ctx *ctx, int cap, const char **names, uint64_t *launch
  *
  * psi: n complex values on a CUDA device (complex128 for QSG_FP64, complex64
  * for QSG_MIXED), aligned to the element size.  *out = dv * sum |psi_i|^2,
- * written after the work queued on `stream` (a cudaStream_t; NULL = the
- * default stream) has finished.
+ * written after the work queued on `stream` (a cudaStream_t on psi's device;
+ * NULL = the default stream) has finished.  The call is synchronous: it waits
+ * for that stream, so it cannot be made while the stream is being captured
+ * into a graph (it returns QSG_ERR_STATE then); a stream of another device is
+ * refused with QSG_ERR_ARG.
  *
  * Its scratch is one fixed 33,024-byte device array inside libqsg.so, which
  * every GPU that loads the library keeps until the process exits; n above
  * QSG_NORM2_NOALLOC_MAX_SITES (2^26) is rejected with QSG_ERR_ARG.  It calls
  * no cudaMalloc, cudaFree or other allocating routine.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture begins.  All calls on a device share
+ * device looks up the array's device address (cudaGetSymbolAddress).  All calls on a device share
  * the one array: calls that overlap on the GPU (different streams, or host
  * threads not ordered with each other) race and can return wrong sums. */
 #define QSG_NORM2_NOALLOC_MAX_SITES 67108864ull

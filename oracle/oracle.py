@@ -29,10 +29,12 @@ _i = ctypes.c_int
 _u64 = ctypes.c_uint64
 
 
-def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and the reference build when ``ref``)."""
+def build(ref: bool = False, ref_path: str | None = None) -> None:
+    """Compile liboracle.so (and the reference build when ``ref``, from the
+    QuSim source tree at ``ref_path``, the Makefile's default if None)."""
     targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True)
+    extra = [f"REF={ref_path}"] if ref and ref_path else []
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets + extra, check=True)
 
 
 def _ptr(a: np.ndarray):

@@ -35,7 +35,8 @@ EXPORTS = [
     "qsg_steps_taken", "qsg_destroy", "qsg_candidate_plans", "qsg_get_plan", "qsg_set_plan",
     "qsg_autotune", "qsg_batch_create_1d", "qsg_batch_step", "qsg_batch_sync", "qsg_batch_size",
     "qsg_batch_instance", "qsg_batch_destroy", "qsg_server_create", "qsg_server_submit",
-    "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_destroy",
+    "qsg_server_poll", "qsg_server_wait", "qsg_server_take", "qsg_server_stats", "qsg_server_request_info",
+    "qsg_server_destroy",
     "qsg_profile_enable", "qsg_profile_read", "qsg_norm2_noalloc", "qsg_create_1d_spec", "qsg_create_2d_spec",
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
@@ -90,7 +91,16 @@ class Request(ctypes.Structure):
 
 class ServerInfo(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("site_steps", ctypes.c_uint64),
-                ("peak_device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t)]
+                ("peak_device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t),
+                ("admitted_mid_flight", ctypes.c_uint64), ("max_in_flight", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class RequestInfo(ctypes.Structure):
+    """qsg_request_info: one served request's progress (times in s since the server started; -1 = not yet)."""
+    _fields_ = [("state", ctypes.c_int32), ("admitted_mid_flight", ctypes.c_int32), ("chunks", ctypes.c_uint64),
+                ("steps_dispatched", ctypes.c_uint64), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_first_dispatch", ctypes.c_double), ("t_finish", ctypes.c_double)]
 
 
 class Plan2D(ctypes.Structure):
@@ -184,6 +194,7 @@ def _declare(lib):
     lib.qsg_server_wait.argtypes = [_vp, _u64, _d, ctypes.POINTER(_i)]
     lib.qsg_server_take.argtypes = [_vp, _u64, _dp, _dp]
     lib.qsg_server_stats.argtypes = [_vp, ctypes.POINTER(ServerInfo)]
+    lib.qsg_server_request_info.argtypes = [_vp, _u64, ctypes.POINTER(RequestInfo)]
     lib.qsg_server_destroy.argtypes = [_vp]
     lib.qsg_server_destroy.restype = None
     lib.qsg_profile_enable.argtypes = [_vp, _i]

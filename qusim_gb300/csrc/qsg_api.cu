@@ -124,6 +124,14 @@ struct qsg_inst {
     cudaEvent_t ring_ev[kRing] = {};
     double ring_scale[kRing] = {};
     uint64_t ring_next = 0;
+    // Bounded device-side waits that ran out: a pass whose waits give up adds
+    // 1 to the counter `err` (in device memory; the members of a batched
+    // four-step class share their first member's) and returns with some tiles
+    // of the state updated and some not.  err_seen is the count this instance
+    // has acknowledged; lost marks its state as unusable until qsg_set_psi.
+    unsigned *err = nullptr;
+    unsigned err_seen = 0;
+    bool lost = false;
     std::vector<void *> allocs;
     size_t bytes = 0;
 };
@@ -188,7 +196,7 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     if (maps && in->ctx->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
         a.maps = maps;
         a.tiles = in->fsg.col_blocks * ninst;
-        a.err = in->ctx->dev_err;
+        a.err = reinterpret_cast<int *>(in->err);
         QSG_CUDA(qsg::launch_fs_col_tma(in->fsg, a, st));
         return QSG_OK;
     }
@@ -356,7 +364,7 @@ int col_pass(qsg_inst *in, int d, double *partials = nullptr, bool first = false
     a.g = in->geom.g;
     a.inv_n = (float)(1.0 / ((double)in->nx * in->ny));
     a.tiles = (in->ny / in->geom.col_w) * in->geom.g;
-    a.err = in->ctx->dev_err;
+    a.err = reinterpret_cast<int *>(in->err);
     a.no_copies = no_copies ? 1 : 0;
     ProfScope ps(in->ctx, "col_pass", in->st);
     // a regular momentum-form pass: fed by tensor copies where the tile shape is compiled
@@ -593,17 +601,54 @@ int settle(qsg_inst *in)
     return QSG_OK;
 }
 
-// sum over psi[lo, hi) with the given reduction mode; synchronous
-// after a synchronisation that copied ctx->sums to host_sums: report (once)
-// a bounded device-side wait that ran out since the last check
-int take_dev_err(qsg_ctx *ctx)
+// An instance whose state a timed-out pass left half-updated refuses every
+// call but qsg_set_psi (and destruction).
+int lost_state(const qsg_inst *in, const char *who)
 {
-    int flag = 0;
-    std::memcpy(&flag, ctx->host_sums + 7, sizeof(int));
-    if (!flag) return QSG_OK;
-    QSG_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->st));
-    return fail(QSG_ERR_TIMEOUT, "a column pass gave up waiting for its tensor copies (1 s)");
+    if (!in->lost) return QSG_OK;
+    return fail(QSG_ERR_TIMEOUT, std::string(who) +
+                                     ": the instance's state was lost when a pass gave up waiting for its tensor "
+                                     "copies (bounded wait); set a new state with qsg_set_psi");
 }
+
+// Queue a copy of the instance's failure counter into the pinned slot
+// host_sums[7], on the stream whose synchronisation the caller waits for next.
+int queue_err_copy(qsg_inst *in, cudaStream_t st)
+{
+    QSG_CUDA(cudaMemcpyAsync(in->ctx->host_sums + 7, in->err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    return QSG_OK;
+}
+
+// After that synchronisation: a count above the acknowledged one means a pass
+// of this instance (or of its batched launch) ran out of time since the last
+// check, so its state is lost; report that (QSG_ERR_TIMEOUT) now and on every
+// later call until qsg_set_psi.
+int err_after_sync(qsg_inst *in, const char *who)
+{
+    unsigned count = 0;
+    std::memcpy(&count, in->ctx->host_sums + 7, sizeof(unsigned));
+    if (count != in->err_seen) {
+        in->err_seen = count;
+        in->lost = true;
+    }
+    return lost_state(in, who);
+}
+
+// pinned slot of the failure counter copied with posted norm `slot`
+unsigned *ring_err(qsg_inst *in, int slot)
+{
+    return reinterpret_cast<unsigned *>(in->ring_host + qsg_inst::kRing) + slot;
+}
+
+// synchronise `st` and check the instance's failure counter
+int sync_checked(qsg_inst *in, cudaStream_t st, const char *who)
+{
+    if (int rc = queue_err_copy(in, st)) return rc;
+    QSG_CUDA(cudaStreamSynchronize(st));
+    return err_after_sync(in, who);
+}
+
+// sum over psi[lo, hi) with the given reduction mode; synchronous
 
 int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
 {
@@ -613,9 +658,8 @@ int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
     QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, lo, hi, mode, ctx->partials, ctx->max_partials,
                                 &np, ctx->st));
     QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
-    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
-    QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    if (int rc = take_dev_err(ctx)) return rc;
+    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    if (int rc = sync_checked(in, ctx->st, "reduction")) return rc;
     *out = ctx->host_sums[0];
     return QSG_OK;
 }
@@ -758,6 +802,9 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     int rc;
     if ((rc = inst_alloc(in, in->n * csize(in->prec), &in->psi))) return rc;
     void *v = nullptr;
+    if ((rc = inst_alloc(in, 256, &v))) return rc;
+    in->err = static_cast<unsigned *>(v);
+    QSG_CUDA(cudaMemsetAsync(in->err, 0, sizeof(unsigned), ctx->st));
     if ((rc = inst_alloc(in, in->n * 8, &v))) return rc;
     in->V = (double *)v;
     QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyDefault, ctx->st));  // host or device source
@@ -931,6 +978,7 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
     if (const char *g = std::getenv("QSG_BATCH_GRAPHS")) ctx->graphs = std::atoi(g) != 0;
     if (const char *g = std::getenv("QSG_COL_TMA")) ctx->col_tma = std::atoi(g) != 0;
     if (const char *g = std::getenv("QSG_FS_TMA")) ctx->fs_tma = std::atoi(g) != 0;
+    if (const char *g = std::getenv("QSG_BATCH_QUEUE")) ctx->batch_queue = std::atoi(g) != 0;
     ctx->budget = hbm_budget_bytes;
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -958,11 +1006,6 @@ int qsg_init(int device_ordinal, size_t hbm_budget_bytes, qsg_ctx **out)
         return rc;
     }
     ctx->sums = (double *)p;
-    ctx->dev_err = reinterpret_cast<int *>(ctx->sums + 7);
-    if ((e = cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->st)) != cudaSuccess) {
-        qsg_ctx_destroy(ctx);
-        return fail(QSG_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
-    }
     e = cudaMallocHost(&p, sizeof(double) * 8);
     if (e != cudaSuccess) {
         qsg_ctx_destroy(ctx);
@@ -1284,6 +1327,7 @@ int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
     if (!in) return fail(QSG_ERR_ARG, "qsg_step: null instance");
     if (nsteps == 0 && !renormalize) return QSG_OK;
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_step")) return rc;
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
     int rc;
     if (nsteps == 0) {
@@ -1306,15 +1350,15 @@ int qsg_sync(qsg_inst *in)
     if (!in) return fail(QSG_ERR_ARG, "qsg_sync: null instance");
     qsg_ctx *ctx = in->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);
-    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
-    QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    return take_dev_err(ctx);
+    if (int rc = lost_state(in, "qsg_sync")) return rc;
+    return sync_checked(in, in->st, "qsg_sync");
 }
 
 int qsg_norm2(qsg_inst *in, double *out)
 {
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_norm2")) return rc;
     double s = 0;
     int rc = reduce(in, 0, in->n, 0, &s);
     if (rc) return rc;
@@ -1326,6 +1370,7 @@ int qsg_step_norm2(qsg_inst *in, double *out)
 {
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_step_norm2: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_step_norm2")) return rc;
     if (in->dim == 2 && in->pending && in->dt.imag() == 0) {
         // the deferred closing V factor has modulus 1: the sums the last
         // column pass took, times G Ny (split-k scale), are the norm
@@ -1333,14 +1378,14 @@ int qsg_step_norm2(qsg_inst *in, double *out)
         const int tiles = (in->ny / in->geom.col_w) * in->geom.g;
         QSG_CUDA(qsg::launch_finalize(in->cparts, tiles, 1, ctx->sums, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-        QSG_CUDA(cudaStreamSynchronize(ctx->st));
+        if (int rc = sync_checked(in, ctx->st, "qsg_step_norm2")) return rc;
         *out = ctx->host_sums[0] * cparts_scale(in) * in->dv;
         return QSG_OK;
     }
     if (in->dim == 1 && in->snorm_valid) {
         // the one-CTA 1D kernel summed the state it ended in
         QSG_CUDA(cudaMemcpyAsync(in->ctx->host_sums, in->snorm, sizeof(double), cudaMemcpyDeviceToHost, in->st));
-        QSG_CUDA(cudaStreamSynchronize(in->st));
+        if (int rc = sync_checked(in, in->st, "qsg_step_norm2")) return rc;
         *out = in->ctx->host_sums[0] * in->dv;
         return QSG_OK;
     }
@@ -1355,13 +1400,15 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
 {
     if (!in || !ticket) return fail(QSG_ERR_ARG, "qsg_step_norm2_post: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_step_norm2_post")) return rc;
     qsg_ctx *ctx = in->ctx;
     int rc;
     if (!in->ring_dev) {
         void *p = nullptr;
         if ((rc = inst_alloc(in, sizeof(double) * qsg_inst::kRing, &p))) return rc;
         in->ring_dev = static_cast<double *>(p);
-        QSG_CUDA(cudaMallocHost(&in->ring_host, sizeof(double) * qsg_inst::kRing));
+        // kRing values, then kRing copies of the failure counter (one per post)
+        QSG_CUDA(cudaMallocHost(&in->ring_host, (sizeof(double) + sizeof(unsigned)) * qsg_inst::kRing));
         for (cudaEvent_t &e : in->ring_ev) QSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     const int slot = (int)(in->ring_next % qsg_inst::kRing);
@@ -1369,6 +1416,7 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
     if (in->dim == 1 && in->snorm_valid) {
         // the one-CTA 1D kernel's own sum of its final state: one copy, no kernel
         QSG_CUDA(cudaMemcpyAsync(in->ring_host + slot, in->snorm, sizeof(double), cudaMemcpyDeviceToHost, in->st));
+        QSG_CUDA(cudaMemcpyAsync(ring_err(in, slot), in->err, sizeof(unsigned), cudaMemcpyDeviceToHost, in->st));
         QSG_CUDA(cudaEventRecord(in->ring_ev[slot], in->st));
         in->ring_scale[slot] = in->dv;
         *ticket = in->ring_next++;
@@ -1388,6 +1436,7 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
         in->ring_scale[slot] = in->dv;
     }
     QSG_CUDA(cudaMemcpyAsync(in->ring_host + slot, dst, sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(ring_err(in, slot), in->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
     QSG_CUDA(cudaEventRecord(in->ring_ev[slot], ctx->st));
     *ticket = in->ring_next++;
     return QSG_OK;
@@ -1400,8 +1449,11 @@ int qsg_step_norm2_get(qsg_inst *in, uint64_t ticket, double *out)
     if (ticket >= in->ring_next) return fail(QSG_ERR_ARG, "qsg_step_norm2_get: ticket not posted");
     if (in->ring_next - ticket > (uint64_t)qsg_inst::kRing)
         return fail(QSG_ERR_STATE, "qsg_step_norm2_get: ticket overwritten (more than 64 posts since)");
+    if (int rc = lost_state(in, "qsg_step_norm2_get")) return rc;
     const int slot = (int)(ticket % qsg_inst::kRing);
     QSG_CUDA(cudaEventSynchronize(in->ring_ev[slot]));  // that copy only, not the work queued after it
+    std::memcpy(in->ctx->host_sums + 7, ring_err(in, slot), sizeof(unsigned));
+    if (int rc = err_after_sync(in, "qsg_step_norm2_get")) return rc;
     *out = in->ring_host[slot] * in->ring_scale[slot];
     return QSG_OK;
 }
@@ -1412,6 +1464,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
     int rc;
+    if ((rc = lost_state(in, "qsg_energies"))) return rc;
     if ((rc = settle(in))) return rc;
     if (pot) {
         // Abs2Mul(psi, V) dv / Norm2 (src/EvolverImpl.cpp:45-49)
@@ -1462,7 +1515,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             }
             QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                                      ctx->st));
-            QSG_CUDA(cudaStreamSynchronize(ctx->st));
+            if ((rc = sync_checked(in, ctx->st, "qsg_energies"))) return rc;
             *kin = ctx->host_sums[0] / ctx->host_sums[1];
         } else {
             const double dkx = 2 * kPi / (in->dx * in->nx), dky = 2 * kPi / (in->dy * in->ny);
@@ -1482,7 +1535,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             QSG_CUDA(qsg::launch_finalize(ctx->partials, nblk, 2, ctx->sums, ctx->st));
             QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                                      ctx->st));
-            QSG_CUDA(cudaStreamSynchronize(ctx->st));
+            if ((rc = sync_checked(in, ctx->st, "qsg_energies"))) return rc;
             *kin = ctx->host_sums[0] / ctx->host_sums[1];
         }
     }
@@ -1496,6 +1549,7 @@ int qsg_xavg(qsg_inst *in, double x0, double *out)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     double s2 = 0, s0 = 0;
     int rc;
+    if ((rc = lost_state(in, "qsg_xavg"))) return rc;
     if ((rc = reduce(in, 0, in->n, 2, &s2))) return rc;
     if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
     *out = x0 + in->dx * (s2 / s0);
@@ -1507,6 +1561,7 @@ int qsg_norm2_range(qsg_inst *in, double x0, double xa, double xb, double *out)
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_norm2_range: null argument");
     if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_norm2_range: 1D instances only");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_norm2_range")) return rc;
     int64_t i1 = (int64_t)((xa - x0) / in->dx), i2 = (int64_t)((xb - x0) / in->dx);
     if (i1 <= 0) i1 = 0;
     if (i2 >= (int64_t)in->n) i2 = (int64_t)in->n;
@@ -1526,6 +1581,7 @@ int qsg_get_psi(qsg_inst *in, double *out)
     if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_psi: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
+    if (int rc = lost_state(in, "qsg_get_psi")) return rc;
     if (int rc = settle(in)) return rc;
     if (in->prec == 0) {
         QSG_CUDA(cudaMemcpyAsync(out, in->psi, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
@@ -1535,8 +1591,8 @@ int qsg_get_psi(qsg_inst *in, double *out)
         QSG_CUDA(qsg::launch_c64_to_c128(ctx->scratch, in->psi, in->n, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(out, ctx->scratch, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
     }
-    QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    return QSG_OK;
+    // a pass that timed out before this read leaves out holding a half-updated state: reported here
+    return sync_checked(in, ctx->st, "qsg_get_psi");
 }
 
 int qsg_set_psi(qsg_inst *in, const double *psi)
@@ -1547,7 +1603,11 @@ int qsg_set_psi(qsg_inst *in, const double *psi)
     if (rc) return rc;
     in->pending = false;  // the state is replaced, with it any deferred row pass
     in->snorm_valid = false;
+    // the new state makes an earlier timed-out pass irrelevant: acknowledge its count
+    if ((rc = queue_err_copy(in, in->ctx->st))) return rc;
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    std::memcpy(&in->err_seen, in->ctx->host_sums + 7, sizeof(unsigned));
+    in->lost = false;
     return QSG_OK;
 }
 
@@ -1588,6 +1648,7 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
     if (!in || !p) return fail(QSG_ERR_ARG, "qsg_set_plan: null argument");
     if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_set_plan: 2D instances only");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_set_plan")) return rc;
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
     if (int rc = settle(in)) return rc;  // the split-k layout belongs to the current plan
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
@@ -1602,11 +1663,11 @@ int qsg_check_wait_timeout(qsg_inst *in)
     qsg_ctx *ctx = in->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);
     QSG_CUDA(cudaSetDevice(ctx->dev));
-    // the withheld pass returns before any store, so a pending state stays valid
+    if (int rc = lost_state(in, "qsg_check_wait_timeout")) return rc;
+    // The withheld pass returns before any store, but it is reported as any
+    // pass that ran out of time is: the instance's state counts as lost.
     if (int rc = col_pass(in, 0, nullptr, false, false, false, true)) return rc;
-    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double) * 8, cudaMemcpyDeviceToHost, ctx->st));
-    QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    return take_dev_err(ctx);
+    return sync_checked(in, in->st, "qsg_check_wait_timeout");
 }
 
 int qsg_set_form(qsg_inst *in, int form)
@@ -1616,6 +1677,7 @@ int qsg_set_form(qsg_inst *in, int form)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     if (form == QSG_FORM_MOMENTUM && !(in->dim == 2 && in->prec == 1 && in->work))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_set_form: the momentum form is for complex64 2D instances");
+    if (int rc = lost_state(in, "qsg_set_form")) return rc;
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
     if (int rc = settle(in)) return rc;  // the deferred pass belongs to the current form
     in->form = form;
@@ -1636,6 +1698,7 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     if (trial_steps < 1) trial_steps = 4;
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
+    if (int rc = lost_state(in, "qsg_autotune")) return rc;
     QSG_CUDA(cudaSetDevice(ctx->dev));
     std::vector<Plan2D> cands(256);
     const int n = qsg::candidate_plans(in->prec, in->nx, in->ny, cands.data(), (int)cands.size());
@@ -1676,7 +1739,10 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     cudaError_t err = cudaGetLastError();
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     in->pending = false;  // the restored copy is the settled state
+    // a trial pass that ran out of time worked on the copy: acknowledge its count
+    if ((rc = queue_err_copy(in, ctx->st))) return rc;
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    std::memcpy(&in->err_seen, ctx->host_sums + 7, sizeof(unsigned));
     if (err != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_autotune: ") + cudaGetErrorString(err));
     if ((rc = apply_plan(in, best_p))) return rc;
     ctx->plans[std::make_tuple(in->prec, in->nx, in->ny)] = best_p;
@@ -1705,8 +1771,19 @@ struct qsg_batch {
         double *d_dv = nullptr;
         cudaStream_t st = nullptr;
         cudaEvent_t done = nullptr;
+        bool queued = false;        // stepped by the tile-queue launch, not a launch of its own
     };
     std::vector<Class> classes;
+    // the tile queue over the queued classes (complex64 resident lengths 1024 .. 8192):
+    // descriptors and dv of their members in class order, the tiles, the queue counter
+    qsg::FsInst *q_desc = nullptr;
+    double *q_dv = nullptr;
+    qsg::QueueTile *q_tiles = nullptr;
+    unsigned *q_counter = nullptr;
+    int q_ntiles = 0;
+    const void *q_tw = nullptr;     // any queued class's twiddles (the tiles carry their own)
+    cudaStream_t q_st = nullptr;
+    cudaEvent_t q_done = nullptr;
     uint64_t sites = 0;
     // the launches of one qsg_batch_step(nsteps) captured as a CUDA graph
     // (every class's launches for all nsteps, forked from and joined to the
@@ -1725,6 +1802,10 @@ static void batch_free(qsg_batch *b)
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
+    if (b->q_st) cudaStreamSynchronize(b->q_st);
+    if (b->q_desc) cudaFreeAsync(b->q_desc, b->ctx->st);
+    if (b->q_done) cudaEventDestroy(b->q_done);
+    if (b->q_st) cudaStreamDestroy(b->q_st);
     for (auto &c : b->classes) {
         if (c.st) cudaStreamSynchronize(c.st);
         if (c.d_desc) cudaFreeAsync(c.d_desc, b->ctx->st);
@@ -1734,6 +1815,61 @@ static void batch_free(qsg_batch *b)
     }
     for (qsg_inst *in : b->insts) free_inst(in);
     delete b;
+}
+
+// Gather the complex64 resident classes of length 1024 .. 8192 into one tile
+// queue: tiles of 8192 sites (8192 / n instances of one class each), the
+// members' descriptors and dv in class order, a zeroed queue counter.
+static int batch_make_queue(qsg_batch *b)
+{
+    qsg_ctx *ctx = b->ctx;
+    const int qt = qsg::queue_tile_sites(b->insts.empty() ? 0 : b->insts[0]->prec);
+    if (!ctx->batch_queue || qt == 0) return QSG_OK;
+    std::vector<qsg::FsInst> desc;
+    std::vector<double> dv;
+    std::vector<qsg::QueueTile> tiles;
+    for (auto &c : b->classes) {
+        qsg_inst *proto = b->insts[c.members[0]];
+        if (proto->fourstep || c.n < 1024 || c.n > (uint64_t)qt) continue;
+        c.queued = true;
+        const int per = qt / (int)c.n;
+        const int first = (int)desc.size();
+        for (size_t k = 0; k < c.members.size(); ++k) {
+            qsg_inst *in = b->insts[c.members[k]];
+            qsg::FsInst h{};
+            h.psi = in->psi;
+            h.vtab[0] = in->vtab[0];
+            h.vtab[1] = in->vtab[1];
+            h.ktab[0] = in->ktab[0];
+            h.ktab[1] = in->ktab[1];
+            desc.push_back(h);
+            dv.push_back(in->dv);
+        }
+        for (int k = 0; k < (int)c.members.size(); k += per)
+            tiles.push_back(qsg::QueueTile{proto->tw, (int)c.n, first + k, std::min(per, (int)c.members.size() - k), 0});
+        b->q_tw = proto->tw;
+    }
+    if (tiles.empty()) return QSG_OK;
+    // biggest lengths first: their tiles are the longest
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const qsg::QueueTile &x, const qsg::QueueTile &y) { return x.L > y.L; });
+    const size_t bd = sizeof(qsg::FsInst) * desc.size(), bv = sizeof(double) * dv.size();
+    const size_t bt = sizeof(qsg::QueueTile) * tiles.size();
+    void *p = nullptr;
+    QSG_CUDA(cudaMallocAsync(&p, bd + bv + bt + 256, ctx->st));
+    b->q_desc = static_cast<qsg::FsInst *>(p);
+    b->q_dv = reinterpret_cast<double *>(static_cast<char *>(p) + bd);
+    b->q_tiles = reinterpret_cast<qsg::QueueTile *>(static_cast<char *>(p) + bd + bv);
+    b->q_counter = reinterpret_cast<unsigned *>(static_cast<char *>(p) + bd + bv + bt);
+    b->q_ntiles = (int)tiles.size();
+    QSG_CUDA(cudaMemcpyAsync(b->q_desc, desc.data(), bd, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(b->q_dv, dv.data(), bv, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(b->q_tiles, tiles.data(), bt, cudaMemcpyHostToDevice, ctx->st));
+    QSG_CUDA(cudaMemsetAsync(b->q_counter, 0, 2 * sizeof(unsigned), ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    QSG_CUDA(cudaStreamCreateWithFlags(&b->q_st, cudaStreamNonBlocking));
+    QSG_CUDA(cudaEventCreateWithFlags(&b->q_done, cudaEventDisableTiming));
+    return QSG_OK;
 }
 
 extern "C" {
@@ -1793,6 +1929,8 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
             e = cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice);
         }
         if (e == cudaSuccess) e = cudaMemcpy(c.d_dv, dv.data(), sizeof(double) * dv.size(), cudaMemcpyHostToDevice);
+        // a four-step class's launches report bounded-wait failures in its first member's counter
+        for (size_t k = 1; k < c.members.size(); ++k) b->insts[c.members[k]]->err = b->insts[c.members[0]]->err;
         if (e == cudaSuccess && b->insts[c.members[0]]->fourstep) {
             std::vector<qsg_inst *> mi(c.members.size());
             for (size_t k = 0; k < mi.size(); ++k) mi[k] = b->insts[c.members[k]];
@@ -1805,6 +1943,11 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
             batch_free(b);
             return fail(QSG_ERR_CUDA, std::string("qsg_batch_create_1d: ") + cudaGetErrorString(e));
         }
+    }
+    if (int rc = batch_make_queue(b)) {
+        const std::string msg = g_last_error;
+        batch_free(b);
+        return fail(rc, "qsg_batch_create_1d: " + msg);
     }
     *out = b;
     return QSG_OK;
@@ -1830,8 +1973,30 @@ int batch_enqueue(qsg_batch *b, uint64_t nsteps)
         return b->classes[x].n * b->classes[x].members.size() > b->classes[y].n * b->classes[y].members.size();
     });
     int rc = QSG_OK;
+    if (b->q_ntiles > 0) {
+        // every queued class in one persistent launch
+        qsg::Evolve1DQueueArgs qa{};
+        qa.b.inst = b->q_desc;
+        qa.b.tw = b->q_tw;
+        qa.b.dv = b->q_dv;
+        qa.b.nsteps = nsteps;
+        qa.b.order = b->insts[0]->order;
+        qa.tiles = b->q_tiles;
+        qa.ntiles = b->q_ntiles;
+        qa.counter = b->q_counter;
+        cudaError_t e = cudaStreamWaitEvent(b->q_st, start, 0);
+        if (e == cudaSuccess) {
+            ProfScope ps(ctx, "evolve1d_queue", b->q_st);
+            e = qsg::launch_evolve1d_queue(b->insts[0]->prec, qa, b->q_st);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(b->q_done, b->q_st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->st, b->q_done, 0);
+        if (e != cudaSuccess) rc = fail(QSG_ERR_CUDA, std::string("qsg_batch_step: tile queue: ") + cudaGetErrorString(e));
+    }
     for (int ci : order) {
+        if (rc) break;
         auto &c = b->classes[ci];
+        if (c.queued) continue;
         qsg_inst *proto = b->insts[c.members[0]];
         cudaStreamWaitEvent(c.st, start, 0);
         if (!proto->fourstep) {
@@ -1995,12 +2160,15 @@ struct SrvRequest {
     int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
     int error = 0;
     std::string message;
-    clk::time_point submit, finish;
+    clk::time_point submit, admit, first_dispatch, finish;
     qsg_inst *inst = nullptr;
-    uint64_t dispatched = 0;
+    uint64_t dispatched = 0, chunks = 0;
     cudaStream_t st = nullptr;
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t ev = nullptr;  // recorded after this request's latest queued work (whichever stream ran it)
     bool in_flight = false;
+    bool admitted_mid_flight = false;  // admitted while another request had work on the device
+    int fail_rc = 0;                   // a dispatch failed: finish with this status once nothing is in flight
+    std::string fail_msg;
 };
 
 }  // namespace
@@ -2021,7 +2189,13 @@ struct qsg_server {
     int ring_size = 4096, ring_pos = 0;
     // statistics
     uint64_t done_site_steps = 0, completed = 0, failed = 0;
+    uint64_t admitted_mid_flight = 0;  // admissions while other requests had work on the device
+    uint32_t max_in_flight = 0;        // most requests with device work queued at one time
     size_t peak_bytes = 0;
+    clk::time_point t0 = clk::now();
+    // host-side fault injection for tests (QSG_SERVER_FAIL_REQUEST=<id>): the
+    // dispatches of that request fail with QSG_ERR_CUDA instead of launching
+    uint64_t inject_fail_id = 0;
 };
 
 namespace {
@@ -2062,10 +2236,22 @@ int srv_create(qsg_server *S, SrvRequest &q)
 void srv_finish(qsg_server *S, SrvRequest &q, int err, const std::string &msg)
 {
     if (q.inst) {
+        // the read back and the release run on the context stream, after the
+        // request's last queued work (also on the failure paths: a dispatch
+        // that failed part-way may have queued launches)
+        if (q.ev) {
+            const cudaError_t e = cudaStreamWaitEvent(S->ctx->st, q.ev, 0);
+            if (e != cudaSuccess) {
+                cudaStreamSynchronize(q.st);  // fall back to waiting on the host
+                if (!err) {
+                    err = QSG_ERR_CUDA;
+                    q.message = std::string("cudaStreamWaitEvent: ") + cudaGetErrorString(e);
+                }
+            }
+        }
         if (!err) {
             q.result.resize(2 * (size_t)q.inst->n);
             q.inst->st = S->ctx->st;
-            cudaStreamWaitEvent(S->ctx->st, q.ev, 0);
             S->ctx->mu.unlock();
             int rc = qsg_get_psi(q.inst, q.result.data());
             S->ctx->mu.lock();
@@ -2097,6 +2283,17 @@ void srv_finish(qsg_server *S, SrvRequest &q, int err, const std::string &msg)
         S->done_site_steps += q.req.nx * (q.req.dim == 2 ? q.req.ny : 1) * q.req.nsteps;
     }
     S->cv.notify_all();
+}
+
+// A dispatch of q failed: its work so far is marked by q.ev (recorded on st
+// where possible) and the request finishes with rc once nothing is in flight.
+void srv_mark_failed(SrvRequest &q, cudaStream_t st, int rc, const std::string &msg)
+{
+    if (q.fail_rc) return;
+    q.fail_rc = rc;
+    q.fail_msg = msg;
+    if (q.ev && st && cudaEventRecord(q.ev, st) != cudaSuccess) cudaStreamSynchronize(st);
+    q.in_flight = false;
 }
 
 void srv_loop(qsg_server *S)
@@ -2141,30 +2338,51 @@ void srv_loop(qsg_server *S)
             }
             q->st = S->streams[rr++ % S->streams.size()];
             q->inst->st = q->st;
-            cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming);
+            const cudaError_t ee = cudaEventCreateWithFlags(&q->ev, cudaEventDisableTiming);
+            if (ee != cudaSuccess) {
+                q->ev = nullptr;
+                srv_finish(S, *q, QSG_ERR_CUDA, std::string("cudaEventCreateWithFlags: ") + cudaGetErrorString(ee));
+                continue;
+            }
+            bool busy = false;
+            for (auto &r : running) busy = busy || r->in_flight;
             {
                 std::lock_guard<std::mutex> lk(S->mu);
                 q->state = 1;
+                q->admit = clk::now();
+                q->admitted_mid_flight = busy;
+                if (busy) ++S->admitted_mid_flight;
             }
             running.push_back(q);
         }
         S->peak_bytes = std::max(S->peak_bytes, ctx->in_use);
         // completions
+        uint32_t in_flight_now = 0;
         for (size_t i = 0; i < running.size();) {
             auto &q = running[i];
-            if (q->in_flight && cudaEventQuery(q->ev) == cudaSuccess) q->in_flight = false;
-            if (!q->in_flight && q->dispatched >= q->req.nsteps) {
-                srv_finish(S, *q, 0, "");
+            if (q->in_flight) {
+                const cudaError_t eq = cudaEventQuery(q->ev);
+                if (eq == cudaSuccess) {
+                    q->in_flight = false;
+                } else if (eq != cudaErrorNotReady) {
+                    cudaGetLastError();
+                    srv_mark_failed(*q, nullptr, QSG_ERR_CUDA, std::string("cudaEventQuery: ") + cudaGetErrorString(eq));
+                }
+            }
+            if (!q->in_flight && (q->fail_rc || q->dispatched >= q->req.nsteps)) {
+                srv_finish(S, *q, q->fail_rc, q->fail_msg);
                 running.erase(running.begin() + i);
                 progress = true;
                 continue;
             }
+            in_flight_now += q->in_flight ? 1 : 0;
             ++i;
         }
         // dispatch: batched resident groups
         std::map<std::tuple<uint64_t, int, int>, std::vector<SrvRequest *>> groups;
         for (auto &q : running)
-            if (!q->in_flight && q->dispatched < q->req.nsteps && q->req.dim == 1 && !q->inst->fourstep)
+            if (!q->in_flight && !q->fail_rc && q->dispatched < q->req.nsteps && q->req.dim == 1 &&
+                !q->inst->fourstep)
                 groups[std::make_tuple(q->req.nx, q->req.order, q->req.precision)].push_back(q.get());
         for (auto &kv : groups) {
             auto &g = kv.second;
@@ -2193,46 +2411,83 @@ void srv_loop(qsg_server *S)
             }
             qsg::FsInst *d = S->ring + S->ring_pos;
             cudaStream_t st = g[0]->st;
-            for (int k = 1; k < cnt; ++k) cudaStreamWaitEvent(st, g[k]->ev, 0);
-            cudaMemcpyAsync(d, h, sizeof(qsg::FsInst) * cnt, cudaMemcpyHostToDevice, st);
-            qsg::Evolve1DBatchArgs a{};
-            a.inst = d;
-            a.tw = g[0]->inst->tw;
-            a.nsteps = chunk;
-            a.order = g[0]->req.order;
-            a.count = cnt;
-            cudaError_t e = qsg::launch_evolve1d(g[0]->req.precision, (int)g[0]->req.nx, a, st);
+            cudaError_t e = cudaSuccess;
+            const char *what = "";
+            for (int k = 1; k < cnt && e == cudaSuccess; ++k) {
+                e = cudaStreamWaitEvent(st, g[k]->ev, 0);
+                what = "cudaStreamWaitEvent";
+            }
+            if (e == cudaSuccess) {
+                e = cudaMemcpyAsync(d, h, sizeof(qsg::FsInst) * cnt, cudaMemcpyHostToDevice, st);
+                what = "cudaMemcpyAsync";
+            }
+            bool injected = false;
+            for (int k = 0; k < cnt; ++k) injected = injected || g[k]->id == S->inject_fail_id;
+            if (e == cudaSuccess && !injected) {
+                qsg::Evolve1DBatchArgs a{};
+                a.inst = d;
+                a.tw = g[0]->inst->tw;
+                a.nsteps = chunk;
+                a.order = g[0]->req.order;
+                a.count = cnt;
+                e = qsg::launch_evolve1d(g[0]->req.precision, (int)g[0]->req.nx, a, st);
+                what = "resident 1D launch";
+            }
             // ring slots (device and pinned staging) stay busy until this event
             cudaEvent_t done = g[0]->ev;
-            cudaEventRecord(done, st);
-            for (int k = 0; k < cnt; ++k) {
-                ring_events[S->ring_pos + k] = done;
-                if (e != cudaSuccess) continue;
-                g[k]->dispatched += chunk;
-                g[k]->in_flight = true;
-                if (k) cudaEventRecord(g[k]->ev, st);
-            }
+            const cudaError_t er = cudaEventRecord(done, st);
+            if (er != cudaSuccess) cudaStreamSynchronize(st);  // no event to wait on: the slots are free after this
+            for (int k = 0; k < cnt; ++k) ring_events[S->ring_pos + k] = er == cudaSuccess ? done : nullptr;
             S->ring_pos += cnt;
             progress = true;
+            if (e != cudaSuccess || injected) {
+                // the group's launch failed: every member fails with it
+                cudaGetLastError();
+                const std::string msg = injected ? std::string("injected dispatch failure (QSG_SERVER_FAIL_REQUEST)")
+                                                 : std::string(what) + ": " + cudaGetErrorString(e);
+                for (int k = 0; k < cnt; ++k) srv_mark_failed(*g[k], st, QSG_ERR_CUDA, msg);
+                continue;
+            }
+            for (int k = 0; k < cnt; ++k) {
+                if (k && cudaEventRecord(g[k]->ev, st) != cudaSuccess) {
+                    srv_mark_failed(*g[k], st, QSG_ERR_CUDA, "cudaEventRecord failed after a resident 1D launch");
+                    continue;
+                }
+                if (!g[k]->chunks++) g[k]->first_dispatch = clk::now();
+                g[k]->dispatched += chunk;
+                g[k]->in_flight = true;
+                ++in_flight_now;
+            }
         }
         // dispatch: stepped requests (four-step 1D, 2D), one chunk each
         for (auto &q : running) {
-            if (q->in_flight || q->dispatched >= q->req.nsteps) continue;
+            if (q->in_flight || q->fail_rc || q->dispatched >= q->req.nsteps) continue;
             if (q->req.dim == 1 && !q->inst->fourstep) continue;
             const double sites = (double)q->inst->n;
             uint64_t chunk = (uint64_t)std::max(1.0, 1e8 / (sites * (q->req.order == 4 ? 3 : 1)));
             chunk = std::min(chunk, q->req.nsteps - q->dispatched);
-            int rc = q->req.dim == 1 ? step1d(q->inst, chunk, 0) : step2d(q->inst, chunk, 0);
+            progress = true;
+            int rc = q->id == S->inject_fail_id
+                         ? fail(QSG_ERR_CUDA, "injected dispatch failure (QSG_SERVER_FAIL_REQUEST)")
+                         : q->req.dim == 1 ? step1d(q->inst, chunk, 0) : step2d(q->inst, chunk, 0);
             if (rc) {
-                q->dispatched = q->req.nsteps;
-                q->in_flight = false;
+                srv_mark_failed(*q, q->st, rc, g_last_error);
                 continue;
             }
+            const cudaError_t er = cudaEventRecord(q->ev, q->st);
+            if (er != cudaSuccess) {
+                srv_mark_failed(*q, q->st, QSG_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(er));
+                continue;
+            }
+            if (!q->chunks++) q->first_dispatch = clk::now();
             q->dispatched += chunk;
             q->inst->steps += chunk;
-            cudaEventRecord(q->ev, q->st);
             q->in_flight = true;
-            progress = true;
+            ++in_flight_now;
+        }
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->max_in_flight = std::max(S->max_in_flight, in_flight_now);
         }
         clk_ctx.unlock();
         if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(200));
@@ -2273,6 +2528,7 @@ int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_runni
     }
     S->ring = static_cast<qsg::FsInst *>(p);
     S->ring_host = static_cast<qsg::FsInst *>(ph);
+    if (const char *inj = std::getenv("QSG_SERVER_FAIL_REQUEST")) S->inject_fail_id = std::strtoull(inj, nullptr, 10);
     S->th = std::thread(srv_loop, S);
     *out = S;
     return QSG_OK;
@@ -2367,6 +2623,28 @@ int qsg_server_stats(qsg_server *S, qsg_server_info *out)
     out->site_steps = S->done_site_steps;
     out->peak_device_bytes = S->peak_bytes;
     out->budget_bytes = S->ctx->budget;
+    out->admitted_mid_flight = S->admitted_mid_flight;
+    out->max_in_flight = S->max_in_flight;
+    return QSG_OK;
+}
+
+int qsg_server_request_info(qsg_server *S, uint64_t id, qsg_request_info *out)
+{
+    if (!S || !out) return fail(QSG_ERR_ARG, "qsg_server_request_info: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->all.find(id);
+    if (it == S->all.end()) return fail(QSG_ERR_ARG, "qsg_server_request_info: unknown request id");
+    const SrvRequest &q = *it->second;
+    auto since = [&](clk::time_point t) { return std::chrono::duration<double>(t - S->t0).count(); };
+    *out = qsg_request_info{};
+    out->state = q.state;
+    out->admitted_mid_flight = q.admitted_mid_flight ? 1 : 0;
+    out->chunks = q.chunks;
+    out->steps_dispatched = q.dispatched;
+    out->t_submit = since(q.submit);
+    out->t_admit = q.state >= 1 && q.admit != clk::time_point{} ? since(q.admit) : -1;
+    out->t_first_dispatch = q.chunks ? since(q.first_dispatch) : -1;
+    out->t_finish = q.state >= 2 ? since(q.finish) : -1;
     return QSG_OK;
 }
 

@@ -80,6 +80,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity, uint64_t
 }  // namespace tma
 
 constexpr uint64_t kTmaWaitNs = 1000000000ull;  // 1 s
+// After a wait ran out, the issuing thread gives the copies it still has in
+// flight this much longer to land before the CTA exits; a copy that lands
+// later would write into shared memory the CTA no longer owns, so this limit is
+// the longer one (the first wait can also run out on a time-sliced GPU).
+constexpr uint64_t kTmaDrainNs = 4 * kTmaWaitNs;
 
 // shared-memory bytes of the exchange buffer, rounded up so that the staging
 // buffers after it start on a 1024-byte boundary
@@ -216,9 +221,9 @@ __global__ void __launch_bounds__(W *(M / E), 1)
     if (!ok && tid == 0) {
         // record the timeout, then give the copies still in flight a bounded
         // chance to land before the CTA (and its shared memory) goes away
-        if (a.err) atomicExch(a.err, 1);
-        if (in_flight_w) tma::mbar_wait(mb_w, ph_w, kTmaWaitNs);
-        if (in_flight_p) tma::mbar_wait(mb_p, ph_p, kTmaWaitNs);
+        if (a.err) atomicAdd(a.err, 1);  // a count: each failure is seen by every instance it touched
+        if (in_flight_w) tma::mbar_wait(mb_w, ph_w, kTmaDrainNs);
+        if (in_flight_p) tma::mbar_wait(mb_p, ph_p, kTmaDrainNs);
     }
 }
 

@@ -39,6 +39,32 @@ static cudaError_t run_kinetic1d(const void *psi, const void *tw, double dtk, do
     return cudaGetLastError();
 }
 
+// The queue kernel (complex64): tiles of QT = 8192 sites, the largest
+// resident length, QT / E = 512 threads per CTA.  complex128 batches keep one
+// launch per size class (its instantiation over lengths 1024 .. 4096 spilled).
+int queue_tile_sites(int prec) { return prec == 1 ? 8192 : 0; }
+
+template <class T, int QT>
+static cudaError_t run_queue(const Evolve1DQueueArgs &a, cudaStream_t st)
+{
+    constexpr int E = sizeof(T) == 4 ? 16 : 8;
+    constexpr int PADS = sizeof(T) == 4 ? 4 : 3;
+    const size_t smem = sizeof(cplx_t<T>) * padded<QT, PADS>(QT);
+    auto k = k_evolve1d_queue<T, QT, E>;
+    cudaError_t e = prepare_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    static int occ = 0;
+    k<<<persistent_grid(k, QT / E, smem, a.ntiles, occ), QT / E, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evolve1d_queue(int prec, const Evolve1DQueueArgs &a, cudaStream_t st)
+{
+    if (a.ntiles <= 0) return cudaSuccess;
+    if (prec != 1) return cudaErrorNotSupported;
+    return run_queue<float, 8192>(a, st);
+}
+
 #define QSG_1D_CASES(X, T) \
     X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048) X(T, 4096)
 

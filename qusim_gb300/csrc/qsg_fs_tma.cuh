@@ -159,9 +159,9 @@ __global__ void __launch_bounds__(W *(N2 / 16), 2) k_fs_col_tma(FsColArgs a)
         }
     }
     if (!ok && tid == 0) {
-        if (a.err) atomicExch(a.err, 1);
-        if (in_flight_x) tma::mbar_wait(mb_x, ph_x, kTmaWaitNs);
-        if (in_flight_v) tma::mbar_wait(mb_v, ph_v, kTmaWaitNs);
+        if (a.err) atomicAdd(a.err, 1);  // a count: each failure is seen by every instance it touched
+        if (in_flight_x) tma::mbar_wait(mb_x, ph_x, kTmaDrainNs);
+        if (in_flight_v) tma::mbar_wait(mb_v, ph_v, kTmaDrainNs);
     }
 }
 

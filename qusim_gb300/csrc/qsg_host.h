@@ -58,14 +58,13 @@ struct qsg_ctx {
     size_t scratch_bytes = 0;
     double *partials = nullptr;  // reduction partials
     int max_partials = 0;
-    double *sums = nullptr;      // small device result buffer (8 doubles; the last holds dev_err)
-    int *dev_err = nullptr;      // set by a kernel whose bounded waits ran out (tensor-copy column pass)
+    double *sums = nullptr;      // small device result buffer (8 doubles)
     bool col_tma = true;         // momentum-form column passes fed by tensor copies (QSG_COL_TMA=0: off)
     // four-step column passes fed by tensor copies (QSG_FS_TMA=1); off by default: on the 2048-instance
     // batch they measured slower than the load-instruction pass (511 against 471 ms of column passes per
     // 1000 steps: two CTAs per SM instead of three, and the twiddles still come from L2)
     bool fs_tma = false;
-    double *host_sums = nullptr; // pinned mirror
+    double *host_sums = nullptr; // pinned mirror (slot 7: an instance's failure counter, copied for a check)
     // 1D periodic kinetic tables shared by the instances with the same (precision, size,
     // coefficient); key (precision, n1, n2, f) in the four-step layout, (precision, n, 0, f) in
     // the natural one: table pointer, bytes, instances using it
@@ -80,6 +79,9 @@ struct qsg_ctx {
     // 2048-instance batch the graph measured no faster than direct launches (7.34e10 against 7.41e10
     // site-steps/s, capture included), as the size classes already overlap on their streams
     bool graphs = false;
+    // complex64 batches: the resident classes of length 1024 .. 8192 share one persistent
+    // launch fed by a tile queue (QSG_BATCH_QUEUE=0: one launch per class instead)
+    bool batch_queue = true;
     std::vector<std::tuple<std::string, cudaEvent_t, cudaEvent_t>> prof_pending;
     std::vector<cudaEvent_t> event_pool;
     std::map<std::string, qsg_host::ProfStat> prof_stats;

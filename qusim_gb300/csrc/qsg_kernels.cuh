@@ -374,7 +374,7 @@ struct ColPassArgs {
                             // step's split-k input out; null in the direct form
     int first;              // momentum form: no stored state yet (the input is the state)
     int invonly;            // momentum form: only the column iFFT of the stored state, to work
-    int *err;               // set to 1 by a pass whose bounded waits ran out (TMA pass), or null
+    int *err;               // counter a pass whose bounded waits ran out adds 1 to (TMA pass), or null
     int no_copies;          // TMA pass, failure-path test only: issue no copies, so the first wait runs out
     int plain;              // complex64: tw_col is a float2 table (plain twiddles)
     const void *kx;         // complex64: x kinetic factor - 1, Nx entries
@@ -639,7 +639,7 @@ struct FsColArgs {
     int in_k, out_k;        // input in k layout / output to k layout
     const void *maps;       // tensor-copy pass: 3 tensor maps per instance (state, V 0, V 1), or null
     int tiles;              // tensor-copy pass: column blocks x instances
-    int *err;               // tensor-copy pass: set to 1 when a bounded wait ran out
+    int *err;               // tensor-copy pass: counter it adds 1 to when a bounded wait ran out
 };
 
 // three 256-thread CTAs per SM (registers capped at 85) for the strided
@@ -826,22 +826,25 @@ struct Evolve1DBatchArgs {
     int count;              // instances in the launch
 };
 
+// The lines of NI instances of length L, held by the NI * (L / E) threads of
+// the CTA: instance `first + line` for line < count (the other lines run on
+// instance `first` without storing), for all a.nsteps steps.
 template <class T, int L, int E, int NI>
-__global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatchArgs a)
+__device__ __forceinline__ void evolve1d_lines(const Evolve1DBatchArgs &a, int first, int count, const void *twp,
+                                               unsigned char *smraw)
 {
     using C = cplx_t<T>;
     using P = Plan<L, E>;
     constexpr int TL = P::TL;
     constexpr int PADS = sizeof(C) == 8 ? 4 : 3;
-    extern __shared__ __align__(16) unsigned char smraw[];
     C *sm = reinterpret_cast<C *>(smraw);
     const int line = threadIdx.x / TL;
     const int t = threadIdx.x - line * TL;
-    const int idx = blockIdx.x * NI + line;
-    const bool active = idx < a.count;
-    const FsInst in = a.inst[active ? idx : 0];
+    const int idx = first + line;
+    const bool active = line < count;
+    const FsInst in = a.inst[active ? idx : first];
     C *psi = static_cast<C *>(in.psi);
-    const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);
+    const tw_t<C> *tw = static_cast<const tw_t<C> *>(twp);
     const C *v0 = static_cast<const C *>(in.vtab[0]);
     const C *v1 = static_cast<const C *>(in.vtab[1]);
     const C *k0 = static_cast<const C *>(in.ktab[0]);
@@ -924,6 +927,71 @@ __global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatch
     if (active) {
 #pragma unroll
         for (int e = 0; e < E; ++e) psi[t + e * TL] = x[e];
+    }
+}
+
+template <class T, int L, int E, int NI>
+__global__ void __launch_bounds__(NI *(L / E)) k_evolve1d_resident(Evolve1DBatchArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int first = blockIdx.x * NI;
+    evolve1d_lines<T, L, E, NI>(a, first, a.count - first, a.tw, smraw);
+}
+
+// One persistent launch over the resident-size classes of a batch with
+// lengths 1024 .. QT (smaller lengths, whose bodies would push the shared
+// register allocation into spills, keep their own launches): a work queue of
+// tiles of QT sites (QT / L instances of one length L, every tile filling the
+// CTA's QT / E threads); each CTA takes the next tile from a
+// device counter until the queue is empty.  Tiles are independent (a tile
+// holds its instances for all the steps of the call), so no CTA ever waits on
+// another.  The last CTA to finish resets the counter for the next launch.
+struct QueueTile {
+    const void *tw;  // stage-major twiddles of the tile's length
+    int L;           // line length
+    int first;       // first instance (index into the launch's descriptors)
+    int count;       // instances in the tile (<= QT / L)
+    int pad;
+};
+struct Evolve1DQueueArgs {
+    Evolve1DBatchArgs b;    // descriptors, dv, norm_out, nsteps, order, renormalize
+    const QueueTile *tiles;
+    int ntiles;
+    unsigned *counter;      // [0]: next tile, [1]: CTAs finished
+};
+
+template <class T, int QT, int E>
+__global__ void __launch_bounds__(QT / E) k_evolve1d_queue(Evolve1DQueueArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ int tile_s;
+#pragma unroll 1
+    for (;;) {
+        __syncthreads();  // every thread is done with the previous tile (and tile_s)
+        if (threadIdx.x == 0) tile_s = (int)atomicAdd(a.counter, 1u);
+        __syncthreads();
+        const int k = tile_s;
+        if (k >= a.ntiles) break;
+        const QueueTile tl = a.tiles[k];
+        switch (tl.L) {
+#define QSG_QUEUE_CASE(LL) \
+    case LL: \
+        if constexpr (LL <= QT) evolve1d_lines<T, LL, E, QT / LL>(a.b, tl.first, tl.count, tl.tw, smraw); \
+        break;
+            QSG_QUEUE_CASE(1024) QSG_QUEUE_CASE(2048) QSG_QUEUE_CASE(4096) QSG_QUEUE_CASE(8192)
+#undef QSG_QUEUE_CASE
+        default:
+            break;
+        }
+    }
+    if (threadIdx.x == 0) {
+        // the last CTA out resets the queue (every CTA has taken its final,
+        // out-of-range ticket by now)
+        __threadfence();
+        if (atomicAdd(a.counter + 1, 1u) == gridDim.x - 1) {
+            a.counter[0] = 0u;
+            a.counter[1] = 0u;
+        }
     }
 }
 

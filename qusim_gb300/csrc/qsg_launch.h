@@ -17,6 +17,11 @@ inline int elems_per_thread(int prec) { return prec == 1 ? 16 : 8; }
 bool evolve1d_supported(int prec, uint64_t n);
 cudaError_t launch_evolve1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);
 
+// 1D resident evolver, every resident size in one persistent launch fed by a
+// tile queue (k_evolve1d_queue): sites per tile, and the launch
+int queue_tile_sites(int prec);
+cudaError_t launch_evolve1d_queue(int prec, const Evolve1DQueueArgs &a, cudaStream_t st);
+
 // 1D infinite wall (2n line per CTA)
 bool wall1d_supported(int prec, uint64_t n);
 cudaError_t launch_wall1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);

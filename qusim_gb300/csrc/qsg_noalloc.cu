@@ -147,6 +147,18 @@ extern "C" int qsg_norm2_noalloc(const void *psi, uint64_t n, int precision, dou
     const size_t esize = precision == QSG_MIXED ? 8 : 16;
     if (reinterpret_cast<uintptr_t>(psi) % esize)
         return qsg::set_last_error(QSG_ERR_ARG, "qsg_norm2_noalloc: psi is not aligned to its element size");
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    {
+        // The call waits for its result on the host, which a stream being
+        // captured cannot do.  Checked first: any other query of a capturing
+        // stream would end the caller's capture with an error.
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            return qsg::set_last_error(QSG_ERR_STATE, "qsg_norm2_noalloc: the stream is being captured; this call "
+                                                      "is synchronous and cannot be part of a graph");
+        }
+    }
     cudaPointerAttributes attr{};
     if (cudaPointerGetAttributes(&attr, psi) != cudaSuccess || attr.device < 0 || attr.device >= kMaxDevices ||
         (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)) {
@@ -154,9 +166,21 @@ extern "C" int qsg_norm2_noalloc(const void *psi, uint64_t n, int precision, dou
         return qsg::set_last_error(QSG_ERR_ARG, "qsg_norm2_noalloc: psi is not device memory");
     }
 
+    if (st) {
+        // the launch goes to the caller's stream: it must belong to psi's device
+        int sdev = -1;
+        if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            return qsg::set_last_error(QSG_ERR_ARG, "qsg_norm2_noalloc: stream is not a valid CUDA stream");
+        }
+        if (sdev != attr.device)
+            return qsg::set_last_error(QSG_ERR_ARG, "qsg_norm2_noalloc: stream belongs to device " +
+                                                        std::to_string(sdev) + ", psi to device " +
+                                                        std::to_string(attr.device));
+    }
+
     int prev = -1, rc = QSG_OK;
     double *scratch = nullptr, sum = 0;
-    const cudaStream_t st = static_cast<cudaStream_t>(stream);
     const unsigned blocks = (unsigned)((n + kSitesPerBlock - 1) / kSitesPerBlock);
     NA_CUDA(cudaGetDevice(&prev));
     if (prev != attr.device) NA_CUDA(cudaSetDevice(attr.device));

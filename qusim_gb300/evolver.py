@@ -528,6 +528,14 @@ class Server:
     def stats(self):
         s = _lib.ServerInfo()
         check(self.lib.qsg_server_stats(self.h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_ if f != "reserved"}
+
+    def request_info(self, rid):
+        """Progress of a request not yet taken: state, admitted_mid_flight, chunks,
+        steps_dispatched and the t_submit / t_admit / t_first_dispatch / t_finish
+        times (seconds since the server started, -1 where not reached)."""
+        s = _lib.RequestInfo()
+        check(self.lib.qsg_server_request_info(self.h, rid, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in s._fields_}
 
     def close(self):

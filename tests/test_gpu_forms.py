@@ -198,8 +198,11 @@ def test_tensor_copy_column_pass_is_bitwise_the_plain_one(q, monkeypatch, n):
 
 def test_bounded_wait_runs_out_cleanly(q):
     """A tensor-copy column pass whose copies are withheld: every CTA's first
-    wait runs out after 1 s, the pass returns before touching the state, the
-    next synchronisation reports QSG_ERR_TIMEOUT, and the context keeps working."""
+    wait runs out after 1 s and the pass returns.  A pass that ran out of time
+    may leave some tiles of the state updated and others not, so the instance's
+    state counts as lost: the check reports QSG_ERR_TIMEOUT, and every later
+    call on that instance (sync, reads, steps) does too until qsg_set_psi gives
+    it a new state.  The context and its other instances keep working."""
     n = 2048
     psi0, dx, dy = gauss_packet_2d(n, n, -100, 100, -100, 100, 1.5, 0.0, -20.0, 0.0, 8.0)
     V = gaussian_bumps_2d(n, n, -100, 100, -100, 100, nbumps=8, seed=14, spread=40.0)
@@ -209,7 +212,13 @@ def test_bounded_wait_runs_out_cleanly(q):
     a.step(2)
     b.step(2)
     assert a.check_wait_timeout() == 4
-    a.sync()  # the flag was cleared by the check
+    for call in (a.sync, a.get_psi, a.norm2, a.energies, lambda: a.step(1)):
+        with pytest.raises(q.QsgError) as e:
+            call()
+        assert e.value.code == 4 and "qsg_set_psi" in str(e.value)
+    b.step(1)  # the other instance is unaffected
+    b_state = b.get_psi()
+    a.set_psi(b_state)  # a new state makes the instance usable again
     a.step(2)
     b.step(2)
     assert np.array_equal(a.get_psi(), b.get_psi())

@@ -431,3 +431,47 @@ def test_fourstep_tensor_copy_pass_is_bitwise_the_plain_one(qsg, monkeypatch):
         out.append(got)
     for x, y in zip(*out):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_batch_tile_queue_is_bitwise_the_per_class_launches(qsg, monkeypatch, order):
+    """complex64 batches step their resident classes of length 1024 .. 8192 in
+    one persistent launch fed by a tile queue (8192-site tiles).  Members get
+    exactly the states the per-class launches (QSG_BATCH_QUEUE=0) give.  The
+    batch has more tiles than the launch has CTAs (so CTAs take several tiles
+    and the queue counter is reused by the next call), classes whose last tile
+    is partial, sizes below 1024 and four-step sizes beside the queue."""
+    rng = np.random.default_rng(33)
+    sizes = [1024] * 700 + [2048] * 301 + [4096] * 75 + [8192] * 40 + [512] * 5 + [16384] * 3
+    rng.shuffle(sizes)
+    psis, Vs, dxs, dts = [], [], [], []
+    for n in sizes:
+        box = 0.05 * n
+        p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
+        psis.append(p), Vs.append(v), dxs.append(dx), dts.append(0.01)
+    out = []
+    for queue in ("1", "0"):
+        monkeypatch.setenv("QSG_BATCH_QUEUE", queue)
+        c = qsg.Context(0)
+        c.profile(2)
+        b = qsg.Batch(c, psis, Vs, dxs, dts, order=order, precision="mixed")
+        b.step(3)
+        b.step(2)
+        out.append([b.instance(i).get_psi() for i in range(len(sizes))])
+        kernels = {name: v[0] for name, v in c.profile_read().items()}
+        if queue == "1":
+            assert kernels.get("evolve1d_queue") == 2
+            assert kernels.get("evolve1d_resident") == 2  # the 512-site class
+        else:
+            assert "evolve1d_queue" not in kernels
+        b.close()
+        c.close()
+    for i, (a, g) in enumerate(zip(*out)):
+        assert np.array_equal(a, g), (i, sizes[i])
+    c = qsg.Context(0)
+    for i in (0, 1, sizes.index(8192), sizes.index(4096)):
+        solo = qsg.Instance.create_1d(c, psis[i], Vs[i], dxs[i], 0.01, order=order, precision="mixed")
+        solo.step(5)
+        assert np.array_equal(solo.get_psi(), out[0][i]), i
+        solo.close()
+    c.close()

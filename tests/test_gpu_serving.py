@@ -90,3 +90,85 @@ def test_bad_requests_are_refused():
     rid = srv.submit(ok, ok.real, 0.1, 0.01, 10)
     assert srv.wait(rid, 60) == q.Server.DONE
     srv.close()
+
+
+@pytest.mark.parametrize("bad", [8, 4])
+def test_failed_dispatch_fails_only_its_request(monkeypatch, bad):
+    """A dispatch that fails ends its request FAILED with the failure's status
+    and message; the other requests finish DONE, bitwise equal to solo runs.
+    The failure is injected on the host (QSG_SERVER_FAIL_REQUEST): request 8
+    is the first 2D request (a chunked, stepped dispatch), request 4 the only
+    2048-site 1D request (a batched resident launch with one member).  No device
+    work faults."""
+    import qusim_gb300 as q
+    monkeypatch.setenv("QSG_SERVER_FAIL_REQUEST", str(bad))
+    reqs = make_requests()
+    srv = q.Server(0, max_running=64)
+    ids = [srv.submit(r["psi0"], r["V"], r["dx"], r["dt"], r["nsteps"], order=r["order"], precision="mixed",
+                      dy=r.get("dy")) for r in reqs]
+    assert ids == list(range(1, len(reqs) + 1))
+    results = {}
+    for i in ids:
+        state = srv.wait(i, 300)
+        if i == bad:
+            assert state == q.Server.FAILED
+            with pytest.raises(q.QsgError) as e:
+                srv.take(i)
+            assert e.value.code == 3 and "injected" in str(e.value)
+        else:
+            assert state == q.Server.DONE
+            results[i] = srv.take(i)[0]
+    st = srv.stats()
+    srv.close()
+    assert st["failed"] == 1 and st["completed"] == len(reqs) - 1
+    ctx = q.Context(0)
+    for i, r in zip(ids, reqs):
+        if i != bad:
+            assert np.array_equal(results[i], solo(q, ctx, r, "mixed")), i
+    ctx.close()
+
+
+def test_requests_admitted_while_others_run():
+    """Continuous batching: a long complex128 2D request is submitted first;
+    once it is RUNNING with a chunk on the device, more requests arrive.  They
+    are admitted while the first one's work is in flight, their work is queued
+    beside it (server statistics), they finish before it, and every result is
+    bitwise the one a solo run gives."""
+    import time
+
+    import qusim_gb300 as q
+    h = 51.2
+    p, dx, dy = gauss_packet_2d(1024, 1024, -h, h, -h, h, 1.0, 0.3, -10.0, 0.0, 4.0)
+    v = gaussian_bumps_2d(1024, 1024, -h, h, -h, h, nbumps=8, seed=7, spread=20.0)
+    first = dict(psi0=p, V=v, dx=dx, dy=dy, dt=0.01, nsteps=400, order=4)
+    later = make_requests(seed=11)
+    srv = q.Server(0, max_running=64)
+    fid = srv.submit(first["psi0"], first["V"], dx, 0.01, 400, order=4, precision="fp64", dy=dy)
+    t_end = time.time() + 60
+    while time.time() < t_end:
+        info = srv.request_info(fid)
+        if info["state"] == q.Server.RUNNING and info["chunks"] >= 1:
+            break
+        time.sleep(0.001)
+    assert info["state"] == q.Server.RUNNING and info["chunks"] >= 1, info
+    ids = [srv.submit(r["psi0"], r["V"], r["dx"], r["dt"], r["nsteps"], order=r["order"], precision="mixed",
+                      dy=r.get("dy")) for r in later]
+    infos = {}
+    for i in ids + [fid]:
+        assert srv.wait(i, 300) == q.Server.DONE
+        infos[i] = srv.request_info(i)
+    results = {i: srv.take(i)[0] for i in ids + [fid]}
+    st = srv.stats()
+    srv.close()
+    f = infos[fid]
+    assert f["chunks"] >= 2  # the long request advanced in several chunks
+    for i in ids:
+        assert f["t_first_dispatch"] < infos[i]["t_admit"] < f["t_finish"], (f, infos[i])
+    assert sum(infos[i]["admitted_mid_flight"] for i in ids) >= 1
+    assert st["admitted_mid_flight"] >= 1 and st["max_in_flight"] >= 2, st
+    assert any(infos[i]["t_finish"] < f["t_finish"] for i in ids)
+    ctx = q.Context(0)
+    assert np.array_equal(results[fid], solo(q, ctx, first, "fp64"))
+    for i, r in zip(ids, later):
+        assert np.array_equal(results[i], solo(q, ctx, r, "mixed")), i
+    ctx.close()

@@ -90,3 +90,48 @@ def test_noalloc_rejects_bad_arguments(lib):
     assert rc == 1 and b"not device memory" in lib.qsg_last_error()
     rc = lib.qsg_norm2_noalloc(ctypes.c_void_p(t.data_ptr()), 16, 7, 1.0, None, ctypes.byref(out))
     assert rc == 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_noalloc_at_the_limit_then_a_ragged_length(lib, precision):
+    """A call at the maximum size (2^26 sites: every block of the fixed array in
+    use), then one whose length is not a multiple of a block's 16,384 sites, so
+    the last block is partial and fewer partial sums are read than the first
+    call wrote.  Each is compared with a float64 sum of the same buffer."""
+    torch = pytest.importorskip("torch")
+    dt = torch.float32 if precision == "mixed" else torch.float64
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    n_max = 1 << 26
+    big = torch.rand(2 * n_max, dtype=dt, device="cuda", generator=gen) - 0.5
+    want = float((big.double() ** 2).sum())
+    got = norm2_noalloc(lib, torch, big, n_max, precision, 0.25)
+    assert abs(got - 0.25 * want) <= 1e-12 * 0.25 * want, (got, want)
+    n_rag = 16384 * 5 + 37
+    rag = big[: 2 * n_rag] * 3.0
+    torch.cuda.synchronize()
+    want = float((rag.double() ** 2).sum())
+    got = norm2_noalloc(lib, torch, rag, n_rag, precision, 1.0)
+    assert abs(got - want) <= 1e-12 * want, (got, want)
+    del big, rag
+
+
+def test_noalloc_refuses_a_stream_being_captured(lib):
+    """The call waits for its result on the host, so a stream under graph
+    capture is refused (QSG_ERR_STATE) before anything is queued on it."""
+    from qusim_gb300 import _lib
+    torch = pytest.importorskip("torch")
+    t = torch.ones(2 * 4096, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    out = ctypes.c_double(-1.0)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+            rc = lib.qsg_norm2_noalloc(ctypes.c_void_p(t.data_ptr()), 4096, _lib.QSG_FP64, 1.0,
+                                       ctypes.c_void_p(s.cuda_stream), ctypes.byref(out))
+            t.mul_(1.0)  # something for the graph to hold
+    assert rc == _lib.QSG_ERR_STATE and b"captured" in lib.qsg_last_error()
+    assert out.value == -1.0
+    # outside the capture the same call works: 4096 sites of 1 + 1i, dv = 2
+    rc = lib.qsg_norm2_noalloc(ctypes.c_void_p(t.data_ptr()), 4096, _lib.QSG_FP64, 2.0, None, ctypes.byref(out))
+    assert rc == 0 and out.value == 2.0 * 4096 * 2.0
