@@ -40,6 +40,7 @@
 #include "qsg_host.h"
 #include "qsg_launch.h"
 #include "qsg_evolve3d.cuh"
+#include "qsg_blue.cuh"
 
 using namespace qsg_host;
 
@@ -87,6 +88,26 @@ struct qsg_inst {
     cudaStream_t st = nullptr;     // launch stream of the stepping kernels (the context's unless set)
     // 1D: resident (one CTA holds the instance) or four-step (two passes per substep)
     bool fourstep = false;
+    // 1D InfiniteWall above the one-CTA sizes: the state is the odd extension
+    // of psi to 2 n_out sites (psi_j, 0 at j = n_out, -psi_{2 n_out - j}
+    // above), stepped as a periodic four-step instance of n = 2 n_out sites;
+    // reads, reductions and writes of the state cover its first n_out sites
+    bool wall_ext = false;
+    uint64_t n_out = 0;
+    // 1D periodic n that is not a power of two: Bluestein transforms of length
+    // blue_m (qsg_blue.cuh); chirp and FFT_M(conj chirp) / M tables, K / n in ktab
+    bool blue = false;
+    int blue_m = 0;
+    void *bw = nullptr, *bhs = nullptr;
+    // 2D grids with a side that is not a power of two: natural-layout Bluestein row
+    // and column passes (qsg_blue.cuh); per side the transform length, chirp,
+    // FFT_M(conj chirp) / M and twiddles, and per kinetic coefficient the factors
+    // along x (with 1 / (nx ny)) and along y
+    bool blue2 = false;
+    int bmx = 0, bmy = 0;
+    void *bwx = nullptr, *bhsx = nullptr, *bwy = nullptr, *bhsy = nullptr;
+    const void *btwx = nullptr, *btwy = nullptr;
+    void *bkx[2] = {nullptr, nullptr}, *bky[2] = {nullptr, nullptr};
     qsg::FsGeom fsg{};
     const void *tw_fs_col = nullptr, *tw_fs_row = nullptr, *tw_n = nullptr;
     qsg::FsInst *desc = nullptr;   // device descriptor of this instance
@@ -177,6 +198,9 @@ void prof_drain(qsg_ctx *ctx)
     ctx->prof_pending.clear();
 }
 
+// sites of the state a caller sees (the first n_out of a wall extension)
+uint64_t user_n(const qsg_inst *in) { return in->wall_ext ? in->n_out : in->n; }
+
 // --- steps -----------------------------------------------------------------
 
 // maps: the instances' tensor maps (3 each) for the tensor-copy pass, or null
@@ -192,8 +216,9 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     a.vtwice = vtwice ? 1 : 0;
     a.in_k = in_k ? 1 : 0;
     a.out_k = out_k ? 1 : 0;
+    a.wall = in->wall_ext ? 1 : 0;
     ProfScope ps(in->ctx, "fs_col_pass", st);
-    if (maps && in->ctx->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
+    if (maps && !in->wall_ext && in->ctx->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
         a.maps = maps;
         a.tiles = in->fsg.col_blocks * ninst;
         a.err = reinterpret_cast<int *>(in->err);
@@ -272,6 +297,27 @@ int step_fs(qsg_inst *in, const qsg::FsInst *desc, int ninst, uint64_t nsteps, c
 int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
     qsg_ctx *ctx = in->ctx;
+    if (in->blue) {
+        qsg::BlueArgs a{};
+        a.psi = in->psi;
+        a.tw = in->tw;
+        a.w = in->bw;
+        a.hs = in->bhs;
+        a.vtab[0] = in->vtab[0];
+        a.vtab[1] = in->vtab[1];
+        a.ktab[0] = in->ktab[0];
+        a.ktab[1] = in->ktab[1];
+        a.norm_out = renorm ? nullptr : in->snorm;
+        in->snorm_valid = !renorm;
+        a.dv = in->dv;
+        a.nsteps = nsteps;
+        a.n = (int)in->n;
+        a.order = in->order;
+        a.renormalize = renorm;
+        ProfScope ps(ctx, "evolve1d_blue", in->st);
+        QSG_CUDA(qsg::launch_evolve1d_blue(in->prec, in->blue_m, a, in->st));
+        return QSG_OK;
+    }
     if (!in->fourstep) {
         qsg::Evolve1DBatchArgs a{};
         a.inst = in->desc;
@@ -298,7 +344,15 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
     in->snorm_valid = false;
     int rc = step_fs(in, in->desc, 1, nsteps, in->st, in->fs_maps);
     if (rc) return rc;
-    if (renorm) {
+    if (renorm && in->wall_ext) {
+        // Norm2 over the first n_out sites, then the whole extension scaled
+        ProfScope ps(ctx, "renorm");
+        int np = 0;
+        QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, in->n_out, 0, ctx->partials, ctx->max_partials,
+                                    &np, ctx->st));
+        QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
+        QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
+    } else if (renorm) {
         ProfScope ps(ctx, "renorm");
         QSG_CUDA(qsg::launch_finalize(in->parts, in->fsg.col_blocks, 1, ctx->sums, ctx->st));
         QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
@@ -432,9 +486,72 @@ int step2d_momentum(qsg_inst *in, uint64_t nsteps, int renorm, double *parts)
     return QSG_OK;
 }
 
+// 2D step on a grid without a power-of-two plan (qsg_blue.cuh): natural layout,
+// R(V, row DFT) then per substep C(column DFT, K, inverse) R(inverse row DFT, V,
+// row DFT), the last row pass of the call ending in natural rows (no deferral)
+int step2d_blue(qsg_inst *in, uint64_t nsteps, int renorm)
+{
+    qsg_ctx *ctx = in->ctx;
+    auto row = [&](bool in_k, const void *v, bool twice, bool out_k) -> int {
+        qsg::Blue2DArgs a{};
+        a.psi = in->psi;
+        a.vtab = v;
+        a.vtwice = twice ? 1 : 0;
+        a.in_k = in_k ? 1 : 0;
+        a.out_k = out_k ? 1 : 0;
+        a.tw = in->btwy;
+        a.w = in->bwy;
+        a.hs = in->bhsy;
+        a.nx = in->nx;
+        a.ny = in->ny;
+        ProfScope ps(ctx, "row_pass_blue", in->st);
+        QSG_CUDA(qsg::launch_row_blue(in->prec, in->bmy, a, in->st));
+        return QSG_OK;
+    };
+    auto col = [&](int d) -> int {
+        qsg::Blue2DArgs a{};
+        a.psi = in->psi;
+        a.tw = in->btwx;
+        a.w = in->bwx;
+        a.hs = in->bhsx;
+        a.kx = in->bkx[d];
+        a.ky = in->bky[d];
+        a.nx = in->nx;
+        a.ny = in->ny;
+        ProfScope ps(ctx, "col_pass_blue", in->st);
+        QSG_CUDA(qsg::launch_col_blue(in->prec, in->bmx, a, false, 0, 0, nullptr, in->st));
+        return QSG_OK;
+    };
+    const int nsub = in->order == 2 ? 1 : 3;
+    int rc;
+    if ((rc = row(false, in->vtab[0], false, true))) return rc;
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        for (int u = 0; u < nsub; ++u) {
+            // O2: V1/2 T V1/2;  O4: VC1 TD1 VC2 TD2 VC2 TD1 VC1 (tables 0: C1 / D1, 1: C2 / D2)
+            if ((rc = col(in->order == 4 && u == 1 ? 1 : 0))) return rc;
+            const bool last = u == nsub - 1;
+            if (last && s + 1 == nsteps)
+                rc = row(true, in->vtab[0], false, false);
+            else
+                rc = row(true, (in->order == 4 && !last) ? in->vtab[1] : in->vtab[0], last, true);
+            if (rc) return rc;
+        }
+    }
+    if (renorm) {
+        ProfScope ps(ctx, "renorm");
+        int np = 0;
+        QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, in->n, 0, ctx->partials, ctx->max_partials, &np,
+                                    ctx->st));
+        QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
+        QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, ctx->sums, in->dv, ctx->st));
+    }
+    return QSG_OK;
+}
+
 int step2d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
     qsg_ctx *ctx = in->ctx;
+    if (in->blue2) return step2d_blue(in, nsteps, renorm);
     double *parts = nullptr;
     if (renorm) {
         if (in->geom.row_blocks > ctx->max_partials)
@@ -664,6 +781,27 @@ int reduce(qsg_inst *in, size_t lo, size_t hi, int mode, double *out)
     return QSG_OK;
 }
 
+// complex factors computed on the host (long double) into a new device array of
+// the instance's precision
+int upload_factors(qsg_inst *in, const std::vector<std::complex<long double>> &src, void **dst)
+{
+    const size_t cs = csize(in->prec);
+    if (int r = inst_alloc(in, src.size() * cs, dst)) return r;
+    std::vector<unsigned char> h(src.size() * cs);
+    for (size_t i = 0; i < src.size(); ++i) {
+        if (in->prec == 0) {
+            const double v[2] = {(double)src[i].real(), (double)src[i].imag()};
+            std::memcpy(&h[i * cs], v, cs);
+        } else {
+            const float v[2] = {(float)src[i].real(), (float)src[i].imag()};
+            std::memcpy(&h[i * cs], v, cs);
+        }
+    }
+    // pageable source: the call returns once the bytes are staged
+    QSG_CUDA(cudaMemcpyAsync(*dst, h.data(), h.size(), cudaMemcpyHostToDevice, in->ctx->st));
+    return QSG_OK;
+}
+
 int build_tables(qsg_inst *in)
 {
     qsg_ctx *ctx = in->ctx;
@@ -680,7 +818,7 @@ int build_tables(qsg_inst *in)
         if ((rc = inst_alloc(in, in->n * cs, &in->vtab[k]))) return rc;
         QSG_CUDA(qsg::launch_vtable(in->prec, in->vtab[k], in->V, in->n, f.real(), f.imag(), ctx->st));
     }
-    if (in->dim == 1 && in->boundary == QSG_INFINITE_WALL) {
+    if (in->dim == 1 && in->boundary == QSG_INFINITE_WALL && !in->wall_ext) {
         // ExpT wall: K_i = exp(f i^2), f = -i DT dt t / hbar, DT = Dp^2/(2m), Dp = hbar pi/(dx N),
         // with the final -1/(2N) folded into the complex128 table (SplittingMethod1D.cpp:72-80)
         const double dp = in->hbar * kPi / (in->dx * in->n);
@@ -691,9 +829,65 @@ int build_tables(qsg_inst *in)
             QSG_CUDA(qsg::launch_ktable_wall(in->prec, in->ktab[k], (int)in->n, f.real(), f.imag(),
                                              -1.0 / (2.0 * (double)in->n), ctx->st));
         }
+    } else if (in->dim == 1 && in->blue) {
+        // Bluestein: chirp, FFT_M(conj chirp) / M and K_k / n (k < n, 0 above) as plain
+        // complex factors, computed in long double (K as in the periodic branch below)
+        const int m = in->blue_m;
+        const uint64_t n = in->n;
+        std::vector<std::complex<long double>> w, hs;
+        qsg::blue_tables(n, m, w, hs);
+        const long double dk = 2 * (long double)kPi / ((long double)in->dx * n);
+        const long double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * (long double)in->mass);
+        std::vector<std::vector<std::complex<long double>>> kt(ntab, std::vector<std::complex<long double>>(m, 0.0L));
+        for (int k = 0; k < ntab; ++k) {
+            // exp(f q), f = -i DT dt t / hbar: real part DT q t Im(dt) / hbar, imaginary -DT q t Re(dt) / hbar
+            for (uint64_t i = 0; i < n; ++i) {
+                const long double fo = (long double)(i > n / 2 ? n - i : i), q = fo * fo;
+                const long double re = DT * q * tc[k] * (long double)in->dt.imag() / in->hbar;
+                const long double im = -DT * q * tc[k] * (long double)in->dt.real() / in->hbar;
+                kt[k][i] = std::exp(re) * std::complex<long double>(cosl(im), sinl(im)) / (long double)n;
+            }
+        }
+        if ((rc = upload_factors(in, w, &in->bw))) return rc;
+        if ((rc = upload_factors(in, hs, &in->bhs))) return rc;
+        for (int k = 0; k < ntab; ++k)
+            if ((rc = upload_factors(in, kt[k], &in->ktab[k]))) return rc;
+    } else if (in->dim == 2 && in->blue2) {
+        // per side: Bluestein tables; per kinetic coefficient d: exp(a d DTx fold(i)^2) / (nx ny)
+        // and exp(a d DTy fold(j)^2), a = -i dt / hbar (SplittingMethod2D::InitExpT,
+        // src/SplittingMethod2D.cpp:56-79, as a product of the two axes' factors)
+        std::vector<std::complex<long double>> w, hs;
+        qsg::blue_tables(in->nx, in->bmx, w, hs);
+        if ((rc = upload_factors(in, w, &in->bwx))) return rc;
+        if ((rc = upload_factors(in, hs, &in->bhsx))) return rc;
+        qsg::blue_tables(in->ny, in->bmy, w, hs);
+        if ((rc = upload_factors(in, w, &in->bwy))) return rc;
+        if ((rc = upload_factors(in, hs, &in->bhsy))) return rc;
+        const long double nn = (long double)in->nx * in->ny;
+        for (int k = 0; k < ntab; ++k) {
+            const long double d = in->order == 2 ? 1.0L : (long double)tc[k];
+            for (int ax = 0; ax < 2; ++ax) {
+                const int L = ax == 0 ? in->nx : in->ny;
+                const long double D = ax == 0 ? in->dx : in->dy;
+                const long double dk = 2 * (long double)kPi / (D * L);
+                const long double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * (long double)in->mass);
+                std::vector<std::complex<long double>> f(L);
+                for (int i = 0; i < L; ++i) {
+                    const long double fo = (long double)(i > L / 2 ? L - i : i), q = fo * fo * DT * d;
+                    const long double re = q * (long double)in->dt.imag() / in->hbar;
+                    const long double im = -q * (long double)in->dt.real() / in->hbar;
+                    f[i] = std::exp(re) * std::complex<long double>(cosl(im), sinl(im)) / (ax == 0 ? nn : 1.0L);
+                }
+                if ((rc = upload_factors(in, f, ax == 0 ? &in->bkx[k] : &in->bky[k]))) return rc;
+            }
+        }
     } else if (in->dim == 1) {
         // ExpT periodic: f = -i DT dt t / hbar, DT = (Dk hbar)^2/(2m), Dk = 2 pi/(dx N)
-        // (SplittingMethod1D.cpp:51-53)
+        // (SplittingMethod1D.cpp:51-53).  A wall extension of N = 2 n sites gets the
+        // same table: Dk = 2 pi/(dx 2n) is the wall's Dp/hbar = pi/(dx n)
+        // (SplittingMethod1D.cpp:72-74), and two inverse 2n-transforms with the
+        // final -1/(2n) equal a forward and an inverse one with 1/(2n) on an odd
+        // sequence, whose transform is odd as well
         const double dk = 2 * kPi / (in->dx * in->n);
         const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
         for (int k = 0; k < ntab; ++k) {
@@ -704,21 +898,24 @@ int build_tables(qsg_inst *in)
             const auto key = in->fourstep ? std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag())
                                           : std::make_tuple(in->prec, (int)in->n, 0, f.real(), f.imag());
             auto it = ctx->fs_ktabs.find(key);
-            if (it == ctx->fs_ktabs.end()) {
+            const bool fresh = it == ctx->fs_ktabs.end();
+            if (fresh) {
                 void *p = nullptr;
                 if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
-                if (in->fourstep) {
-                    QSG_CUDA(qsg::launch_ktable_fs(in->prec, p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
-                                                   1.0 / (double)in->n, ctx->st));
-                } else {
-                    QSG_CUDA(qsg::launch_ktable1d(in->prec, p, (int)in->n, f.real(), f.imag(), 1.0 / (double)in->n,
-                                                  ctx->st));
-                }
                 it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
             }
+            // registered before the table is filled, so that releasing the instance
+            // after a failed launch below also releases the table
             it->second.users += 1;
             in->shared_k.push_back(key);
             in->ktab[k] = it->second.p;
+            if (fresh && in->fourstep) {
+                QSG_CUDA(qsg::launch_ktable_fs(in->prec, it->second.p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
+                                               1.0 / (double)in->n, ctx->st));
+            } else if (fresh) {
+                QSG_CUDA(qsg::launch_ktable1d(in->prec, it->second.p, (int)in->n, f.real(), f.imag(),
+                                              1.0 / (double)in->n, ctx->st));
+            }
         }
     } else if (in->dim == 3) {
         // SplittingMethod2D::InitExpT with a third axis, one factor per axis:
@@ -736,7 +933,7 @@ int build_tables(qsg_inst *in)
                                               1.0 / (double)L[ax], ctx->st));
             }
         }
-    } else {
+    } else if (!in->blue2) {
         // SplittingMethod2D::InitExpT (src/SplittingMethod2D.cpp:56-79)
         const double dkx = 2 * kPi / (in->dx * in->nx), dky = 2 * kPi / (in->dy * in->ny);
         const double DTx = (dkx * in->hbar) * (dkx * in->hbar) / (2 * in->mass);
@@ -842,7 +1039,7 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         void *cp = nullptr;
         if ((rc = inst_alloc(in, sizeof(double) * 2 * (size_t)in->ny, &cp))) return rc;
         in->cparts = static_cast<double *>(cp);
-        if (in->prec == 1) {
+        if (in->prec == 1 && !in->blue2) {
             if ((rc = inst_alloc(in, in->n * csize(in->prec), &in->work))) return rc;
             in->form = QSG_FORM_MOMENTUM;
         }
@@ -1045,6 +1242,38 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
                             double dt_im, int order, int precision, int boundary, const double *psi0,
                             const double *V, qsg_inst **out);
 
+namespace {
+
+// The 2n-site odd extension of a wall state (host or device source, n
+// complex): ext_j = psi_j (j < n), 0 at j = n, ext_{2n-j} = -psi_j (0 < j < n).
+// Site 0 keeps psi_0 as given: the reference discards it (and site n) only when
+// a kinetic factor is applied, which the four-step column pass mirrors.
+int wall_odd_extension(const double *psi, uint64_t n, std::vector<double> &ext)
+{
+    std::vector<double> h(2 * n);
+    QSG_CUDA(cudaMemcpy(h.data(), psi, sizeof(double) * 2 * n, cudaMemcpyDefault));
+    ext.assign(4 * n, 0.0);
+    std::memcpy(ext.data(), h.data(), sizeof(double) * 2 * n);
+    for (uint64_t j = 1; j < n; ++j) {
+        ext[2 * (2 * n - j)] = -h[2 * j];
+        ext[2 * (2 * n - j) + 1] = -h[2 * j + 1];
+    }
+    return QSG_OK;
+}
+
+// V on the extension: even (V_{2n-j} = V_j), 0 at j = n (where the state is 0)
+int wall_even_extension(const double *V, uint64_t n, std::vector<double> &ext)
+{
+    std::vector<double> h(n);
+    QSG_CUDA(cudaMemcpy(h.data(), V, sizeof(double) * n, cudaMemcpyDefault));
+    ext.assign(2 * n, 0.0);
+    std::memcpy(ext.data(), h.data(), sizeof(double) * n);
+    for (uint64_t j = 1; j < n; ++j) ext[2 * n - j] = h[j];
+    return QSG_OK;
+}
+
+}  // namespace
+
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
                   double dt_im, int order, int precision, int boundary, const double *psi0,
                   const double *V, qsg_inst **out)
@@ -1069,19 +1298,32 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     if (boundary != QSG_PERIOD && boundary != QSG_INFINITE_WALL)
         return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
     const bool wall = boundary == QSG_INFINITE_WALL;
-    if (wall && !qsg::wall1d_supported(precision, n))
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + " (supported: powers of two, 64 .. " +
-                                             (precision == QSG_MIXED ? "4096" : "2048") + ")");
+    const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
+    if (wall && !pow2)
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) +
+                                             " (supported: powers of two, 64 .. 131072)");
+    // walls above one CTA: a four-step periodic instance of the 2n odd extension
+    const bool wall_ext = wall && !qsg::wall1d_supported(precision, n);
+    // periodic lengths that are not powers of two: Bluestein transforms of length blue_m
+    const int blue_m = !wall && !pow2 ? qsg::blue_m_for(precision, n) : 0;
     qsg::FsGeom fsg{};
-    const bool resident = wall || qsg::evolve1d_supported(precision, n);
-    if (!resident && !qsg::fs_geom(precision, n, &fsg))
+    const bool resident = wall ? !wall_ext : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
+    if (wall_ext && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) +
+                                             " (supported: powers of two, 64 .. 131072)");
+    if (!wall && !pow2 && !blue_m)
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) + " (lengths that are not powers of "
+                                             "two: 2 .. " + (precision == QSG_MIXED ? "4096" : "2048") + ")");
+    if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (supported: powers of two, 64 .. 262144)");
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();
     in->ctx = ctx;
     in->dim = 1;
-    in->n = n;
+    in->n = wall_ext ? 2 * n : n;
+    in->n_out = n;
+    in->wall_ext = wall_ext;
     in->nx = (int)n;
     in->dx = dx;
     in->dv = dx;
@@ -1094,8 +1336,12 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     in->st = ctx->st;
     in->fourstep = !resident;
     in->fsg = fsg;
+    in->blue = blue_m > 0;
+    in->blue_m = blue_m;
     int rc = QSG_OK;
-    if (resident) {
+    if (in->blue) {
+        rc = get_twiddles(ctx, precision, blue_m, qsg::blue_elems(precision), &in->tw);
+    } else if (resident) {
         // the wall transforms run on the 2n odd extension
         rc = get_twiddles(ctx, precision, (int)(wall ? 2 * n : n), qsg::elems_per_thread(precision), &in->tw);
     } else {
@@ -1104,7 +1350,14 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
         if (!rc) rc = get_fs_grid(ctx, precision, fsg.n1, fsg.n2, &in->tw_n);
         if (!rc) rc = get_twiddles(ctx, precision, (int)fsg.n1, qsg::elems_per_thread(precision), &in->tw);
     }
-    if (!rc) rc = common_create(in, psi0, V);
+    if (!rc && wall_ext) {
+        std::vector<double> pe, ve;
+        rc = wall_odd_extension(psi0, n, pe);
+        if (!rc) rc = wall_even_extension(V, n, ve);
+        if (!rc) rc = common_create(in, pe.data(), ve.data());
+    } else if (!rc) {
+        rc = common_create(in, psi0, V);
+    }
     if (rc) {
         std::string msg = g_last_error;
         free_inst(in);
@@ -1241,10 +1494,13 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
         !std::isfinite(dt_re) || !std::isfinite(dt_im))
         return fail(QSG_ERR_ARG, "qsg_create_2d: dx, dy, mass, hbar must be finite and > 0, dt finite");
     Plan2D plan{};
-    if (nx > 8192 || ny > 8192 || !qsg::default_plan(precision, (int)nx, (int)ny, &plan))
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" +
-                                             std::to_string(ny) +
-                                             " (supported: powers of two, 128 .. 4096 per side)");
+    // grids without a power-of-two plan: Bluestein passes on sides up to 4096 (complex64) / 2048 (complex128)
+    const bool pow2_plan = nx <= 8192 && ny <= 8192 && qsg::default_plan(precision, (int)nx, (int)ny, &plan);
+    const int bmx = pow2_plan ? 0 : qsg::blue_m_for(precision, nx), bmy = pow2_plan ? 0 : qsg::blue_m_for(precision, ny);
+    if (!pow2_plan && (!bmx || !bmy))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" + std::to_string(ny) +
+                                             " (supported: sides 2 .. " + (precision == QSG_MIXED ? "4096" : "2048") +
+                                             ", and powers of two 128 .. 4096)");
     std::lock_guard<std::mutex> lk(ctx->mu);
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();
@@ -1262,10 +1518,19 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     in->order = order;
     in->prec = precision;
     in->st = ctx->st;
-    load_plans(ctx);
-    auto it = ctx->plans.find(std::make_tuple(precision, (int)nx, (int)ny));
-    if (it != ctx->plans.end()) plan = it->second;
-    int rc = apply_plan(in, plan);
+    int rc = QSG_OK;
+    if (pow2_plan) {
+        load_plans(ctx);
+        auto it = ctx->plans.find(std::make_tuple(precision, (int)nx, (int)ny));
+        if (it != ctx->plans.end()) plan = it->second;
+        rc = apply_plan(in, plan);
+    } else {
+        in->blue2 = true;
+        in->bmx = bmx;
+        in->bmy = bmy;
+        rc = get_twiddles(ctx, precision, bmx, qsg::blue_elems(precision), &in->btwx);
+        if (!rc) rc = get_twiddles(ctx, precision, bmy, qsg::blue_elems(precision), &in->btwy);
+    }
     if (!rc) rc = common_create(in, psi0, V);
     if (rc) {
         std::string msg = g_last_error;
@@ -1334,7 +1599,7 @@ int qsg_step(qsg_inst *in, uint64_t nsteps, int renormalize)
         // renormalise only
         in->snorm_valid = false;
         double s = 0;
-        if ((rc = reduce(in, 0, in->n, 0, &s))) return rc;
+        if ((rc = reduce(in, 0, user_n(in), 0, &s))) return rc;
         QSG_CUDA(qsg::launch_renorm(in->prec, in->psi, in->n, in->ctx->sums, in->dv, in->ctx->st));
         return QSG_OK;
     }
@@ -1360,7 +1625,7 @@ int qsg_norm2(qsg_inst *in, double *out)
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     if (int rc = lost_state(in, "qsg_norm2")) return rc;
     double s = 0;
-    int rc = reduce(in, 0, in->n, 0, &s);
+    int rc = reduce(in, 0, user_n(in), 0, &s);
     if (rc) return rc;
     *out = s * in->dv;
     return QSG_OK;
@@ -1390,7 +1655,7 @@ int qsg_step_norm2(qsg_inst *in, double *out)
         return QSG_OK;
     }
     double s = 0;
-    int rc = reduce(in, 0, in->n, 0, &s);
+    int rc = reduce(in, 0, user_n(in), 0, &s);
     if (rc) return rc;
     *out = s * in->dv;
     return QSG_OK;
@@ -1430,8 +1695,8 @@ int qsg_step_norm2_post(qsg_inst *in, uint64_t *ticket)
     } else {
         if ((rc = settle(in))) return rc;
         int np = 0;
-        QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, in->n, 0, ctx->partials, ctx->max_partials, &np,
-                                    ctx->st));
+        QSG_CUDA(qsg::launch_reduce(in->prec, in->psi, in->V, 0, user_n(in), 0, ctx->partials, ctx->max_partials,
+                                    &np, ctx->st));
         QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, dst, ctx->st));
         in->ring_scale[slot] = in->dv;
     }
@@ -1469,18 +1734,30 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
     if (pot) {
         // Abs2Mul(psi, V) dv / Norm2 (src/EvolverImpl.cpp:45-49)
         double s1 = 0, s0 = 0;
-        if ((rc = reduce(in, 0, in->n, 1, &s1))) return rc;
-        if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
+        if ((rc = reduce(in, 0, user_n(in), 1, &s1))) return rc;
+        if ((rc = reduce(in, 0, user_n(in), 0, &s0))) return rc;
         *pot = (s1 * in->dv) / (s0 * in->dv);
     }
     if (kin && in->dim == 3) {
         if ((rc = kinetic3d(in, kin))) return rc;
     } else if (kin) {
         if (in->dim == 1) {
-            // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102)
+            // periodic branch omits hbar^2 (src/SplittingMethod1D.cpp:101-102); a wall
+            // extension of 2n sites keeps it, with Dk = 2 pi/(dx 2n) = pi/(dx n) the wall's
+            // Dk (:117-119): |F|^2 of the odd extension is even, so the 2n-periodic ratio
+            // sum |F_k|^2 fold(k)^2 / sum |F_k|^2 is the wall's ratio over k < n
             const double dk = 2 * kPi / (in->dx * in->n);
-            const double DT = dk * dk / (2 * in->mass);
-            if (in->boundary == QSG_INFINITE_WALL) {
+            const double DT = in->wall_ext ? (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass)
+                                           : dk * dk / (2 * in->mass);
+            if (in->blue) {
+                qsg::BlueArgs ba{};
+                ba.psi = in->psi;
+                ba.tw = in->tw;
+                ba.w = in->bw;
+                ba.hs = in->bhs;
+                ba.n = (int)in->n;
+                QSG_CUDA(qsg::launch_kinetic1d_blue(in->prec, in->blue_m, ba, DT, ctx->sums, ctx->st));
+            } else if (in->boundary == QSG_INFINITE_WALL && !in->wall_ext) {
                 // wall branch: Dk = pi/(dx N), DT = (Dk hbar)^2/(2m) (src/SplittingMethod1D.cpp:117-119)
                 const double dkw = kPi / (in->dx * in->n);
                 const double DTw = (dkw * in->hbar) * (dkw * in->hbar) / (2 * in->mass);
@@ -1505,6 +1782,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
                 ca.vsel = 0;
                 ca.in_k = 0;
                 ca.out_k = 1;
+                ca.wall = in->wall_ext ? 1 : 0;  // the wall KinEn transforms psi with sites 0 and n zeroed
                 QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, ca, 1, ctx->st));
                 qsg::FsRowArgs ra{};
                 ra.inst = dd;
@@ -1522,6 +1800,34 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
             const double DTx = (dkx * in->hbar) * (dkx * in->hbar) / (2 * in->mass);
             const double DTy = (dky * in->hbar) * (dky * in->hbar) / (2 * in->mass);
             if ((rc = ensure_scratch(ctx, in->n * csize(in->prec)))) return rc;
+            if (in->blue2) {
+                // SplittingMethod2D::CalKinEn on a copy: row DFTs, then the column DFTs with the sums
+                QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, in->n * csize(in->prec), cudaMemcpyDeviceToDevice,
+                                         ctx->st));
+                qsg::Blue2DArgs a{};
+                a.psi = ctx->scratch;
+                a.out_k = 1;
+                a.tw = in->btwy;
+                a.w = in->bwy;
+                a.hs = in->bhsy;
+                a.nx = in->nx;
+                a.ny = in->ny;
+                QSG_CUDA(qsg::launch_row_blue(in->prec, in->bmy, a, ctx->st));
+                a.out_k = 0;
+                a.tw = in->btwx;
+                a.w = in->bwx;
+                a.hs = in->bhsx;
+                const int w = qsg::blue_cols_per_cta(in->prec, in->bmx);
+                const int nblk = (in->ny + w - 1) / w;
+                if (nblk > ctx->max_partials) return fail(QSG_ERR_STATE, "partials buffer too small");
+                QSG_CUDA(qsg::launch_col_blue(in->prec, in->bmx, a, true, DTx, DTy, ctx->partials, ctx->st));
+                QSG_CUDA(qsg::launch_finalize(ctx->partials, nblk, 2, ctx->sums, ctx->st));
+                QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                         ctx->st));
+                if ((rc = sync_checked(in, ctx->st, "qsg_energies"))) return rc;
+                *kin = ctx->host_sums[0] / ctx->host_sums[1];
+                return QSG_OK;
+            }
             if ((rc = row_pass(in, false, true, nullptr, false, nullptr, in->psi, ctx->scratch))) return rc;
             qsg::ColPassArgs a{};
             a.psi = ctx->scratch;
@@ -1550,8 +1856,8 @@ int qsg_xavg(qsg_inst *in, double x0, double *out)
     double s2 = 0, s0 = 0;
     int rc;
     if ((rc = lost_state(in, "qsg_xavg"))) return rc;
-    if ((rc = reduce(in, 0, in->n, 2, &s2))) return rc;
-    if ((rc = reduce(in, 0, in->n, 0, &s0))) return rc;
+    if ((rc = reduce(in, 0, user_n(in), 2, &s2))) return rc;
+    if ((rc = reduce(in, 0, user_n(in), 0, &s0))) return rc;
     *out = x0 + in->dx * (s2 / s0);
     return QSG_OK;
 }
@@ -1564,7 +1870,7 @@ int qsg_norm2_range(qsg_inst *in, double x0, double xa, double xb, double *out)
     if (int rc = lost_state(in, "qsg_norm2_range")) return rc;
     int64_t i1 = (int64_t)((xa - x0) / in->dx), i2 = (int64_t)((xb - x0) / in->dx);
     if (i1 <= 0) i1 = 0;
-    if (i2 >= (int64_t)in->n) i2 = (int64_t)in->n;
+    if (i2 >= (int64_t)user_n(in)) i2 = (int64_t)user_n(in);
     if (i1 >= i2) {
         *out = 0;
         return QSG_OK;
@@ -1583,13 +1889,14 @@ int qsg_get_psi(qsg_inst *in, double *out)
     qsg_ctx *ctx = in->ctx;
     if (int rc = lost_state(in, "qsg_get_psi")) return rc;
     if (int rc = settle(in)) return rc;
+    const uint64_t n = user_n(in);
     if (in->prec == 0) {
-        QSG_CUDA(cudaMemcpyAsync(out, in->psi, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(out, in->psi, n * 16, cudaMemcpyDeviceToHost, ctx->st));
     } else {
-        int rc = ensure_scratch(ctx, in->n * 16);
+        int rc = ensure_scratch(ctx, n * 16);
         if (rc) return rc;
-        QSG_CUDA(qsg::launch_c64_to_c128(ctx->scratch, in->psi, in->n, ctx->st));
-        QSG_CUDA(cudaMemcpyAsync(out, ctx->scratch, in->n * 16, cudaMemcpyDeviceToHost, ctx->st));
+        QSG_CUDA(qsg::launch_c64_to_c128(ctx->scratch, in->psi, n, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(out, ctx->scratch, n * 16, cudaMemcpyDeviceToHost, ctx->st));
     }
     // a pass that timed out before this read leaves out holding a half-updated state: reported here
     return sync_checked(in, ctx->st, "qsg_get_psi");
@@ -1599,7 +1906,15 @@ int qsg_set_psi(qsg_inst *in, const double *psi)
 {
     if (!in || !psi) return fail(QSG_ERR_ARG, "qsg_set_psi: null argument");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
-    int rc = upload_psi(in, psi);
+    int rc;
+    if (in->wall_ext) {
+        std::vector<double> pe;
+        if ((rc = wall_odd_extension(psi, in->n_out, pe))) return rc;
+        rc = upload_psi(in, pe.data());
+        if (!rc) QSG_CUDA(cudaStreamSynchronize(in->ctx->st));  // pe is pageable and goes out of scope
+    } else {
+        rc = upload_psi(in, psi);
+    }
     if (rc) return rc;
     in->pending = false;  // the state is replaced, with it any deferred row pass
     in->snorm_valid = false;
@@ -1647,6 +1962,7 @@ int qsg_set_plan(qsg_inst *in, const qsg_plan2d *p)
 {
     if (!in || !p) return fail(QSG_ERR_ARG, "qsg_set_plan: null argument");
     if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_set_plan: 2D instances only");
+    if (in->blue2) return fail(QSG_ERR_UNSUPPORTED, "qsg_set_plan: no plans for a grid with a side that is not a power of two");
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     if (int rc = lost_state(in, "qsg_set_plan")) return rc;
     QSG_CUDA(cudaSetDevice(in->ctx->dev));
@@ -1695,6 +2011,7 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
 {
     if (!in) return fail(QSG_ERR_ARG, "qsg_autotune: null instance");
     if (in->dim != 2) return fail(QSG_ERR_ARG, "qsg_autotune: 2D instances only");
+    if (in->blue2) return fail(QSG_ERR_UNSUPPORTED, "qsg_autotune: no plans for a grid with a side that is not a power of two");
     if (trial_steps < 1) trial_steps = 4;
     std::lock_guard<std::mutex> lk(in->ctx->mu);
     qsg_ctx *ctx = in->ctx;
@@ -1890,6 +2207,10 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
         qsg_inst *in = nullptr;
         int rc = create_1d_locked(ctx, n[i], dx[i], mass, hbar, dt_re[i], dt_im ? dt_im[i] : 0.0, order, precision,
                                   QSG_PERIOD, psi0[i], V[i], &in);
+        if (!rc && in->blue) {
+            free_inst(in);
+            rc = fail(QSG_ERR_UNSUPPORTED, "n=" + std::to_string(n[i]) + ": batches take powers of two");
+        }
         if (rc) {
             std::string msg = g_last_error;
             batch_free(b);
@@ -2382,7 +2703,7 @@ void srv_loop(qsg_server *S)
         std::map<std::tuple<uint64_t, int, int>, std::vector<SrvRequest *>> groups;
         for (auto &q : running)
             if (!q->in_flight && !q->fail_rc && q->dispatched < q->req.nsteps && q->req.dim == 1 &&
-                !q->inst->fourstep)
+                !q->inst->fourstep && !q->inst->blue)
                 groups[std::make_tuple(q->req.nx, q->req.order, q->req.precision)].push_back(q.get());
         for (auto &kv : groups) {
             auto &g = kv.second;
@@ -2462,7 +2783,7 @@ void srv_loop(qsg_server *S)
         // dispatch: stepped requests (four-step 1D, 2D), one chunk each
         for (auto &q : running) {
             if (q->in_flight || q->fail_rc || q->dispatched >= q->req.nsteps) continue;
-            if (q->req.dim == 1 && !q->inst->fourstep) continue;
+            if (q->req.dim == 1 && !q->inst->fourstep && !q->inst->blue) continue;
             const double sites = (double)q->inst->n;
             uint64_t chunk = (uint64_t)std::max(1.0, 1e8 / (sites * (q->req.order == 4 ? 3 : 1)));
             chunk = std::min(chunk, q->req.nsteps - q->dispatched);

@@ -36,8 +36,74 @@ __device__ __forceinline__ C cmk(typename RealOf<C>::type x, typename RealOf<C>:
     r.y = y;
     return r;
 }
+
+// Packed FP32 pairs (the f32x2 arithmetic of sm_100 and later): one
+// instruction computes both lanes, each lane rounded exactly as the scalar
+// operation, so a complex64 add or a pair of FMAs issues once instead of twice.
+// Every packed helper below rounds exactly as the scalar code it replaces (same
+// products rounded, same FMAs), so results do not depend on the choice.  The
+// pairs must sit in aligned register pairs, which raises register demand: a
+// translation unit opts in with QSG_PACKED_F32 (defined before this header)
+// where its kernels have the registers to spare (measured per kernel).
+#ifdef QSG_PACKED_F32
+inline constexpr bool kPackedF32 = true;
+#else
+inline constexpr bool kPackedF32 = false;
+#endif
+namespace pk {
+__device__ __forceinline__ unsigned long long b64(float2 a)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 f2(unsigned long long v)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ float2 add(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(b64(a)), "l"(b64(b)));
+    return f2(r);
+}
+__device__ __forceinline__ float2 sub(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(b64(a)), "l"(b64(b)));
+    return f2(r);
+}
+__device__ __forceinline__ float2 mul(float2 a, float2 b)
+{
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(b64(a)), "l"(b64(b)));
+    return f2(r);
+}
+// a * b + c, one rounding per lane
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c)
+{
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(b64(a)), "l"(b64(b)), "l"(b64(c)));
+    return f2(r);
+}
+__device__ __forceinline__ float2 swap(float2 a) { return float2{a.y, a.x}; }
+__device__ __forceinline__ float2 bc(float v) { return float2{v, v}; }
+}  // namespace pk
+
 template <class C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
 template <class C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b)
+{
+    if constexpr (kPackedF32) return pk::add(a, b);
+    return float2{a.x + b.x, a.y + b.y};
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+    if constexpr (kPackedF32) return pk::sub(a, b);
+    return float2{a.x - b.x, a.y - b.y};
+}
 template <class C> __device__ __forceinline__ C cmul(C a, C b)
 {
     return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -71,6 +137,16 @@ template <class C> __device__ __forceinline__ C cmul1p(C a, C m)
     const auto cy = fma(a.y, m.x, a.x * m.y);
     return cmk<C>(a.x + cx, a.y + cy);
 }
+// packed: (-(a.y m.y), a.x m.y), then the FMAs with m.x, then a + c
+__device__ __forceinline__ float2 cmul1p(float2 a, float2 m)
+{
+    if constexpr (!kPackedF32) {
+        const float cx = fmaf(a.x, m.x, -(a.y * m.y)), cy = fmaf(a.y, m.x, a.x * m.y);
+        return float2{a.x + cx, a.y + cy};
+    }
+    const float2 t = pk::mul(pk::swap(a), float2{-m.y, m.y});
+    return pk::add(a, pk::fma(a, pk::bc(m.x), t));
+}
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, class C> __device__ __forceinline__ C crot(C a)
 {
@@ -91,11 +167,23 @@ template <bool INV, class C> __device__ __forceinline__ void dft2(C &a0, C &a1)
 template <bool INV, class C> __device__ __forceinline__ void dft4(C &a0, C &a1, C &a2, C &a3)
 {
     C s02 = cadd(a0, a2), d02 = csub(a0, a2);
-    C s13 = cadd(a1, a3), d13 = crot<INV>(csub(a1, a3));
-    a0 = cadd(s02, s13);
-    a2 = csub(s02, s13);
-    a1 = cadd(d02, d13);
-    a3 = csub(d02, d13);
+    C s13 = cadd(a1, a3);
+    if constexpr (std::is_same<C, float2>::value && kPackedF32) {
+        // d02 -+ i (a1 - a3): the difference's lanes swapped, its signs applied by
+        // FMAs with +-1 (exact, so the sums round as the scalar adds do)
+        const float2 d13s = pk::swap(csub(a1, a3));
+        const float2 k = INV ? float2{-1.f, 1.f} : float2{1.f, -1.f};
+        a0 = cadd(s02, s13);
+        a2 = csub(s02, s13);
+        a1 = pk::fma(d13s, k, d02);
+        a3 = pk::fma(d13s, float2{-k.x, -k.y}, d02);
+    } else {
+        C d13 = crot<INV>(csub(a1, a3));
+        a0 = cadd(s02, s13);
+        a2 = csub(s02, s13);
+        a1 = cadd(d02, d13);
+        a3 = csub(d02, d13);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -152,6 +240,8 @@ template <> struct Roots<float2> {
     static constexpr float S1H = 0x1.87de2ap-2f, S1L = 0x1.abaa58p-28f;  // sin(pi/8)
     static constexpr float HH = 0x1.6a09e6p-1f, HL = 0x1.9fcef4p-27f;    // 1/sqrt(2)
     // a * exp(-+ i th), th given by (cos th, sin th) = (ch + cl, sh + sl)
+    // (scalar: the constants are instruction immediates; packed pairs of them
+    // would each take a register pair, and the radix-32 passes then spill)
     template <bool INV>
     static __device__ __forceinline__ float2 cs(float2 a, float ch, float cl, float sh, float sl)
     {
@@ -177,8 +267,13 @@ template <> struct Roots<float2> {
     // exp(-+ i pi/4) = (1 -+ i) / sqrt(2)
     template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a)
     {
-        const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
-        return cmk<float2>(fmaf(u, HH, u * HL), fmaf(v, HH, v * HL));
+        if constexpr (!kPackedF32) {
+            const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
+            return cmk<float2>(fmaf(u, HH, u * HL), fmaf(v, HH, v * HL));
+        }
+        // (u, v) = forward (a.x + a.y, a.y - a.x), inverse (a.x - a.y, a.x + a.y)
+        const float2 uv = pk::fma(pk::swap(a), INV ? float2{-1.f, 1.f} : float2{1.f, -1.f}, a);
+        return pk::fma(uv, pk::bc(HH), pk::mul(uv, pk::bc(HL)));
     }
     // exp(-+ 3 i pi/4) = exp(-+ i pi/4) * (-+ i)
     template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a) { return w8_1<INV>(crot<INV>(a)); }
@@ -212,6 +307,7 @@ template <> struct Roots<float2> {
 // (a CPU emulation of the FP32 arithmetic: plain constants raise the direct
 // form's error 5.7x and leave the momentum form's unchanged).
 struct RootsPlain32 {
+    // scalar, as Roots<float2>::cs: its constants stay instruction immediates
     template <bool INV> static __device__ __forceinline__ float2 cs(float2 a, float c, float s)
     {
         return INV ? cmk<float2>(fmaf(a.x, c, -a.y * s), fmaf(a.y, c, a.x * s))
@@ -229,8 +325,12 @@ struct RootsPlain32 {
     }
     template <bool INV> static __device__ __forceinline__ float2 w8_1(float2 a)
     {
-        const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
-        return cmk<float2>(u * H, v * H);
+        if constexpr (!kPackedF32) {
+            const float u = INV ? a.x - a.y : a.x + a.y, v = INV ? a.x + a.y : a.y - a.x;
+            return cmk<float2>(u * H, v * H);
+        }
+        const float2 uv = pk::fma(pk::swap(a), INV ? float2{-1.f, 1.f} : float2{1.f, -1.f}, a);
+        return pk::mul(uv, pk::bc(H));
     }
     template <bool INV> static __device__ __forceinline__ float2 w8_3(float2 a) { return w8_1<INV>(crot<INV>(a)); }
     template <bool INV> static __device__ __forceinline__ float2 w32_1(float2 a) { return cs<INV>(a, C16, S16); }
@@ -279,18 +379,35 @@ template <bool INV> __device__ __forceinline__ double2 twmul(double2 a, double2 
 // instantiations)
 template <bool INV> __device__ __forceinline__ float2 cmulw_f(float2 a, float2 w)
 {
-    if (INV) return cmk<float2>(fmaf(a.x, w.x, a.y * w.y), fmaf(a.y, w.x, -(a.x * w.y)));
-    return cmk<float2>(fmaf(a.x, w.x, -(a.y * w.y)), fmaf(a.x, w.y, a.y * w.x));
+    if constexpr (!kPackedF32) {
+        if (INV) return cmk<float2>(fmaf(a.x, w.x, a.y * w.y), fmaf(a.y, w.x, -(a.x * w.y)));
+        return cmk<float2>(fmaf(a.x, w.x, -(a.y * w.y)), fmaf(a.x, w.y, a.y * w.x));
+    }
+    // forward (fma(a.x, w.x, -(a.y w.y)), fma(a.x, w.y, a.y w.x)),
+    // inverse (fma(a.x, w.x, a.y w.y), fma(a.y, w.x, -(a.x w.y)))
+    if (INV) return pk::fma(a, pk::bc(w.x), pk::mul(pk::swap(a), float2{w.y, -w.y}));
+    return pk::fma(pk::bc(a.x), w, pk::mul(pk::bc(a.y), float2{-w.y, w.x}));
 }
 template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float2 w) { return cmulw_f<INV>(a, w); }
 template <bool INV> __device__ __forceinline__ float2 twmul(float2 a, float4 w)
 {
-    if (INV) {  // a * conj(w)
-        const float lx = fmaf(a.x, w.z, a.y * w.w), ly = fmaf(a.y, w.z, -a.x * w.w);
-        return cmk<float2>(fmaf(a.x, w.x, fmaf(a.y, w.y, lx)), fmaf(a.y, w.x, fmaf(-a.x, w.y, ly)));
+    if constexpr (!kPackedF32) {
+        if (INV) {  // a * conj(w)
+            const float lx = fmaf(a.x, w.z, a.y * w.w), ly = fmaf(a.y, w.z, -a.x * w.w);
+            return cmk<float2>(fmaf(a.x, w.x, fmaf(a.y, w.y, lx)), fmaf(a.y, w.x, fmaf(-a.x, w.y, ly)));
+        }
+        const float lx = fmaf(a.x, w.z, -a.y * w.w), ly = fmaf(a.x, w.w, a.y * w.z);
+        return cmk<float2>(fmaf(a.x, w.x, fmaf(-a.y, w.y, lx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ly)));
     }
-    const float lx = fmaf(a.x, w.z, -a.y * w.w), ly = fmaf(a.x, w.w, a.y * w.z);
-    return cmk<float2>(fmaf(a.x, w.x, fmaf(-a.y, w.y, lx)), fmaf(a.x, w.y, fmaf(a.y, w.x, ly)));
+    if (INV) {  // a * conj(w): lanes (a.x wx + a.y wy, a.y wx - a.x wy), lo parts (z, w) first
+        const float2 sa = pk::swap(a);
+        const float2 l = pk::fma(a, pk::bc(w.z), pk::mul(sa, float2{w.w, -w.w}));
+        return pk::fma(a, pk::bc(w.x), pk::fma(sa, float2{w.y, -w.y}, l));
+    }
+    // lanes (a.x wx - a.y wy, a.x wy + a.y wx)
+    const float2 ax = pk::bc(a.x), ay = pk::bc(a.y);
+    const float2 l = pk::fma(ax, float2{w.z, w.w}, pk::mul(ay, float2{-w.w, w.z}));
+    return pk::fma(ax, float2{w.x, w.y}, pk::fma(ay, float2{-w.y, w.x}, l));
 }
 
 template <bool INV, class C, class TW = tw_t<C>> __device__ __forceinline__ void dft8(C (&v)[8])

@@ -640,6 +640,9 @@ struct FsColArgs {
     const void *maps;       // tensor-copy pass: 3 tensor maps per instance (state, V 0, V 1), or null
     int tiles;              // tensor-copy pass: column blocks x instances
     int *err;               // tensor-copy pass: counter it adds 1 to when a bounded wait ran out
+    int wall;               // the state is a wall's 2n odd extension: sites 0 and n (rows 0 and
+                            // n2 / 2 of column 0) are zeroed before each forward transform, as the
+                            // reference's wall ExpT discards them (src/SplittingMethod1D.cpp:63-65)
 };
 
 // three 256-thread CTAs per SM (registers capped at 85) for the strided
@@ -701,6 +704,11 @@ __global__ void __launch_bounds__(W *(N2 / E), (W * (N2 / E) <= 256 && sizeof(T)
 #pragma unroll
                     for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], mv[e]);
                 }
+            }
+            // row t + e * TM of column col: site 0 is (t, e) = (0, 0), site n (row n2 / 2) is (0, E / 2)
+            if (a.wall && out_k && col == 0 && t == 0) {
+                x[0] = cmk<C>(0, 0);
+                x[E / 2] = cmk<C>(0, 0);
             }
         }
         if (p < npass) line_fft<C, N2, E, false>(x, sm, lay, bar, t, tw);

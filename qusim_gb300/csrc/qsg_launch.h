@@ -2,7 +2,9 @@
 // the compiled instantiation for the runtime sizes; sizes with no
 // instantiation return cudaErrorNotSupported (surfaced as QSG_ERR_UNSUPPORTED).
 #pragma once
+#include <complex>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "qsg_kernels.cuh"
@@ -21,6 +23,25 @@ cudaError_t launch_evolve1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStr
 // tile queue (k_evolve1d_queue): sites per tile, and the launch
 int queue_tile_sites(int prec);
 cudaError_t launch_evolve1d_queue(int prec, const Evolve1DQueueArgs &a, cudaStream_t st);
+
+// 1D periodic evolution of a length that is not a power of two (Bluestein,
+// qsg_blue.cuh): the transform length M for n (0: unsupported), the chirp w
+// and FFT_M(conj chirp) / M in long double, the launches
+struct BlueArgs;
+int blue_m_for(int prec, uint64_t n);
+int blue_elems(int prec);
+void blue_tables(uint64_t n, int m, std::vector<std::complex<long double>> &w,
+                 std::vector<std::complex<long double>> &hs);
+cudaError_t launch_evolve1d_blue(int prec, int m, const BlueArgs &a, cudaStream_t st);
+cudaError_t launch_kinetic1d_blue(int prec, int m, const BlueArgs &a, double dtk, double *sums, cudaStream_t st);
+// 2D grids with a side that is not a power of two: row pass (rows of ny), column pass
+// (columns of nx; with kinetic, the forward transform and the kinetic-energy partials)
+struct Blue2DArgs;
+int blue_rows_per_cta(int prec, int m);
+int blue_cols_per_cta(int prec, int m);
+cudaError_t launch_row_blue(int prec, int m, const Blue2DArgs &a, cudaStream_t st);
+cudaError_t launch_col_blue(int prec, int m, const Blue2DArgs &a, bool kinetic, double dtx, double dty,
+                            double *partials, cudaStream_t st);
 
 // 1D infinite wall (2n line per CTA)
 bool wall1d_supported(int prec, uint64_t n);

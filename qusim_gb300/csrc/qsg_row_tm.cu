@@ -1,4 +1,7 @@
 // 2D row pass with the waiting rows parked in tensor memory: instantiations + launcher.
+// Packed f32x2 arithmetic (qsg_fft.cuh), as the shared-memory row pass: with every
+// complex add an explicit packed instruction the two row passes round alike.
+#define QSG_PACKED_F32 1
 #include <atomic>
 #include "qsg_dispatch.cuh"
 #include "qsg_row_tm.cuh"

@@ -57,7 +57,7 @@ def run_1d(qsg, ctx, g, precision):
 # src/SplittingMethod1D.cpp:101-102; the wall and 2D ones use (Dk hbar)^2 / 2m)
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1024_o2_hbar07_m2",
-             "evolve1d_n512_o4_wall_hbar07_m2"]
+             "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2"]
 GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
              "evolve2d_128x256_o4_hbar07_m2"]
 
@@ -159,16 +159,25 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    psi0, V, dx = gauss_packet_1d(1000, -50, 50, 1.0, -10, 3.0)
+    # lengths that are not powers of two: up to 4096 (complex64) / 2048 (complex128)
+    psi0, V, dx = gauss_packet_1d(5000, -50, 50, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02)
+        qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision="mixed")
+    assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, precision="fp64")
+    assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:1000], V[:1000], dx, 0.02,
+                               boundary=qsg.BoundaryCondition.InfiniteWall)
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:512], V[:512], dx, 0.02, order=3)
     assert e.value.code == 1
-    z = np.zeros((100, 128), np.complex128)
+    # 2D sides that are not powers of two: up to 4096 (complex64) / 2048 (complex128)
+    z = np.zeros((5000, 128), np.complex128)
     with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_2d(ctx, z, z.real, 0.1, 0.1, 0.02)
+        qsg.Instance.create_2d(ctx, z, z.real, 0.1, 0.1, 0.02, precision="mixed")
     assert e.value.code == 5
 
 
@@ -340,8 +349,10 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 
 def test_wall_limits_are_reported(qsg, ctx):
+    """InfiniteWall: powers of two 64 .. 131072 (the 2n extension of the largest
+    fits the four-step passes' 262144 sites)."""
     wall = qsg.BoundaryCondition.InfiniteWall
-    psi0, V, dx = gauss_packet_1d(4096, -50, 50, 1.0, -10, 3.0)
+    psi0, V, dx = gauss_packet_1d(262144, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
@@ -475,3 +486,157 @@ def test_batch_tile_queue_is_bitwise_the_per_class_launches(qsg, monkeypatch, or
         assert np.array_equal(solo.get_psi(), out[0][i]), i
         solo.close()
     c.close()
+
+
+def wall_packet(n):
+    """A packet 30 sites from the left wall moving into it (k0 = -2) plus the
+    barrier 0.7 exp(-x^2/2), on [-0.05 n, 0.05 n) (dx = 0.1)."""
+    x0, x1 = -0.05 * n, 0.05 * n
+    xs = x0 + 0.1 * np.arange(n)
+    psi = np.exp(-2j * xs) * np.exp(-((xs - (x0 + 3.0)) ** 2) / 4.0)
+    psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * 0.1)
+    return psi.astype(np.complex128), 0.7 * np.exp(-xs * xs / 2), 0.1
+
+
+@pytest.mark.parametrize("n", [4096, 8192, 32768, 131072])
+@pytest.mark.parametrize("order", [2, 4])
+def test_wall_beyond_one_cta_vs_oracle(qsg, ctx, oracle, n, order):
+    """InfiniteWall above the one-CTA sizes (n > 4096 complex64, > 2048
+    complex128) runs as a four-step periodic instance of the 2n odd extension
+    (src/SplittingMethod1D.cpp:61-81).  The packet reflects off the wall within
+    the run; hbar = 0.7 and m = 2 pin the wall KinEn, which keeps hbar^2
+    (:117-119).  complex128 <= 1e-12, complex64 <= 1e-5, with Norm2, KinEn,
+    PotEn, <x> and a renormalising call."""
+    psi0, V, dx = wall_packet(n)
+    mass, hbar, dt, steps = 2.0, 0.7, 0.2, 30
+    ref = oracle.evolve1d(psi0, V, dx, dt, steps, order=order, mass=mass, hbar=hbar, wall=True)
+    ref2 = oracle.evolve1d(ref, V, dx, dt, 3, order=order, mass=mass, hbar=hbar, wall=True, renormalize=True)
+    kin_ref = oracle.kinen1d(ref, dx, mass=mass, hbar=hbar, wall=True)
+    for precision, tol, otol in (("fp64", PLAIN_TOL, 1e-11), ("mixed", MIXED_TOL, 1e-5)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, dt, order=order, precision=precision, mass=mass,
+                                      hbar=hbar, boundary=qsg.BoundaryCondition.InfiniteWall)
+        inst.step(steps)
+        got = inst.get_psi()
+        assert got.shape == (n,)
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        kin, pot = inst.energies()
+        assert abs(kin - kin_ref) <= otol * abs(kin_ref), (precision, kin, kin_ref)
+        assert abs(pot - oracle.poten(ref, V, dx)) <= otol, precision
+        assert abs(inst.norm2() - oracle.norm2(ref, dx)) <= otol, precision
+        assert abs(inst.xavg(-0.05 * n) - oracle.xavg(ref, -0.05 * n, dx)) <= otol * 0.05 * n, precision
+        inst.step(3, renormalize=True)
+        assert rel_l2(inst.get_psi(), ref2) <= tol, precision
+        assert abs(inst.norm2() - 1.0) <= (1e-12 if precision == "fp64" else 1e-6)
+        inst.close()
+
+
+def test_wall_extension_set_psi_round_trip(qsg, ctx, oracle):
+    """qsg_set_psi on a wall extension takes n sites and rebuilds the odd
+    extension: stepping from it equals stepping a fresh instance."""
+    n = 16384
+    psi0, V, dx = wall_packet(n)
+    a = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.2, order=4, precision="fp64",
+                               boundary=qsg.BoundaryCondition.InfiniteWall)
+    a.step(5)
+    mid = a.get_psi()
+    b = qsg.Instance.create_1d(ctx, mid, V, dx, 0.2, order=4, precision="fp64",
+                               boundary=qsg.BoundaryCondition.InfiniteWall)
+    a.set_psi(mid)
+    a.step(4)
+    b.step(4)
+    assert np.array_equal(a.get_psi(), b.get_psi())
+    ref = oracle.evolve1d(oracle.evolve1d(psi0, V, dx, 0.2, 5, order=4, wall=True), V, dx, 0.2, 4, order=4, wall=True)
+    assert rel_l2(b.get_psi(), ref) <= PLAIN_TOL
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("n", [3, 5, 100, 1000, 1234, 2047, 4095])
+@pytest.mark.parametrize("order", [2, 4])
+def test_lengths_not_powers_of_two_vs_oracle(qsg, ctx, oracle, n, order):
+    """Periodic 1D grids of any length (the reference transforms them with KISS's
+    mixed radix, src/kissfft.hh:26-45; 1234 is its FFT test's length,
+    applications/QuSimTest/TestFFT.cpp:89-99): Bluestein transforms of a
+    power-of-two length.  Against the oracle (bit-exact with the reference's
+    KISS evolution): complex128 <= 1e-12 with Norm2, KinEn and PotEn to 1e-11,
+    complex64 <= 1e-5 (complex128 is built up to n = 2048)."""
+    L = max(10.0, 0.1 * n)
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.5, -0.2 * L, max(0.08 * L, 2 * 2 * L / n), barrier=0.7)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02, 25, order=order)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        if precision == "fp64" and n > 2048:
+            continue
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision)
+        inst.step(20)
+        inst.step(5)
+        got = inst.get_psi()
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        if precision == "fp64":
+            kin, pot = inst.energies()
+            kr = oracle.kinen1d(ref, dx)
+            assert abs(kin - kr) <= 1e-11 * max(1.0, abs(kr))
+            assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-11
+            assert abs(inst.norm2() - oracle.norm2(ref, dx)) <= 1e-12
+            assert abs(inst.step_norm2() - oracle.norm2(ref, dx)) <= 1e-12
+        inst.close()
+
+
+def test_length_not_power_of_two_renormalising_and_batches(qsg, ctx, oracle):
+    """Renormalising calls on a Bluestein instance; a batch refuses such lengths."""
+    n = 1234
+    psi0, V, dx = gauss_packet_1d(n, -60, 60, 1.0, -10, 3.0)
+    inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02 - 0.004j, order=4, precision="fp64")
+    inst.step(7, renormalize=True)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02 - 0.004j, 7, order=4, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1.0) <= 1e-13
+    inst.close()
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Batch(ctx, [psi0, psi0[:1024]], [V, V[:1024]], [dx, dx], [0.02, 0.02])
+    assert e.value.code == 5
+
+
+@pytest.mark.parametrize("nx,ny", [(123, 234), (100, 128), (64, 96), (5, 3), (2048, 100), (96, 4095)])
+@pytest.mark.parametrize("order", [2, 4])
+def test_2d_grids_not_powers_of_two_vs_oracle(qsg, ctx, oracle, nx, ny, order):
+    """SplittingMethod2D on grids with a side that is not a power of two (the
+    reference's own FFT test uses 123 x 234, applications/QuSimTest/TestFFT.cpp:
+    89-99) and on power-of-two sides without a compiled plan (64): Bluestein
+    row and column passes in natural layout.  Against the oracle: complex128
+    <= 1e-12 with Norm2, KinEn and PotEn to 1e-11; complex64 <= 1e-5 (sides up
+    to 2048 in complex128, 4096 in complex64)."""
+    hx, hy = 0.1 * max(nx, 20), 0.1 * max(ny, 20)
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=max(0.1 * min(hx, hy), 2 * max(2 * hx / nx, 2 * hy / ny)))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=6, seed=4, spread=0.5 * min(hx, hy))
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.02, 6, order=order)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        if precision == "fp64" and max(nx, ny) > 2048:
+            continue
+        inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.02, order=order, precision=precision)
+        inst.step(4)
+        inst.step(2)
+        got = inst.get_psi()
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        if precision == "fp64":
+            kin, pot = inst.energies()
+            kr = oracle.kinen2d(ref, dx, dy)
+            assert abs(kin - kr) <= 1e-11 * max(1.0, abs(kr))
+            assert abs(pot - oracle.poten(ref, V, dx * dy)) <= 1e-11
+            assert abs(inst.norm2() - oracle.norm2(ref, dx * dy)) <= 1e-12
+        inst.close()
+
+
+def test_2d_grid_not_power_of_two_renormalising(qsg, ctx, oracle):
+    nx, ny = 123, 234
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -12, 12, -20, 20, 1.0, 0.0, -3.0, 0.0, 2.0)
+    V = gaussian_bumps_2d(nx, ny, -12, 12, -20, 20, nbumps=6, seed=2, spread=6.0)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01 - 0.003j, order=4, precision="fp64")
+    inst.step(5, renormalize=True)
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.01 - 0.003j, 5, order=4, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1.0) <= 1e-13
+    with pytest.raises(qsg.QsgError) as e:
+        inst.set_plan((2, 8, 256, 8, 4, 0))
+    assert e.value.code == 5
+    inst.close()

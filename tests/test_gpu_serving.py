@@ -80,7 +80,7 @@ def test_bad_requests_are_refused():
     with pytest.raises(q.QsgError) as e:
         srv.submit(big, big.real, 0.1, 0.01, 10, dy=0.1)
     assert e.value.code == 2
-    odd = np.ones(1000, np.complex128)
+    odd = np.ones(5000, np.complex128)  # not a power of two and above 4096: no transform for it
     rid = srv.submit(odd, odd.real, 0.1, 0.01, 10)
     assert srv.wait(rid, 60) == q.Server.FAILED
     with pytest.raises(q.QsgError) as e:
@@ -171,4 +171,24 @@ def test_requests_admitted_while_others_run():
     assert np.array_equal(results[fid], solo(q, ctx, first, "fp64"))
     for i, r in zip(ids, later):
         assert np.array_equal(results[i], solo(q, ctx, r, "mixed")), i
+    ctx.close()
+
+
+def test_served_length_not_power_of_two_equals_solo():
+    """A request on a 1000-site grid (Bluestein transforms) beside power-of-two
+    ones: served in chunks, bitwise its solo run."""
+    import qusim_gb300 as q
+    p, v, dx = gauss_packet_1d(1000, -50, 50, 1.0, -10, 3.0, barrier=0.8)
+    reqs = make_requests()[:3] + [dict(psi0=p, V=v, dx=dx, dt=0.01, nsteps=333, order=4)]
+    srv = q.Server(0)
+    ids = [srv.submit(r["psi0"], r["V"], r["dx"], r["dt"], r["nsteps"], order=r["order"], precision="mixed",
+                      dy=r.get("dy")) for r in reqs]
+    out = []
+    for i in ids:
+        assert srv.wait(i, 300) == q.Server.DONE
+        out.append(srv.take(i)[0])
+    srv.close()
+    ctx = q.Context(0)
+    for r, psi in zip(reqs, out):
+        assert np.array_equal(psi, solo(q, ctx, r, "mixed"))
     ctx.close()
