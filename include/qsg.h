@@ -147,6 +147,32 @@ int qsg_create_2d_spec(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double
                        double hbar, double dt_re, double dt_im, int order, int precision,
                        const qsg_spec *spec, qsg_inst **out);
 
+/* Initial state and potential as expressions in the language of the
+ * reference's calculator (src/Cal.cpp: the strings FunctorWrapper /
+ * Functor2DWrapper take, include/QuSim.h:502-538), sampled on the device in
+ * complex128 at x_i = x0 + i dx (and y_j = y0 + j dy): numbers, x, y, Pi, I,
+ * + - * / ^, comparisons < <= > >= == (real parts), && ||, c ? a : b, and sin
+ * cos tan asin acos atan sinh tanh atanh exp log sqrt abs sign gauss(x, mu,
+ * sigma).  V keeps the real part, as the reference does; psi0 is scaled to
+ * sum |psi0|^2 dv = 1 when normalize (force_normalization).  A parse error
+ * returns QSG_ERR_ARG with the message.  The samples pass through a temporary
+ * device buffer of 24 bytes per site, counted against the HBM budget while it
+ * lives.  Example (the double slit of the large 2D benchmark, without its
+ * noise): "abs(x) < 1 ? (abs(y - 6) < 1 || abs(y + 6) < 1 ? 0 : 10) : 0". */
+int qsg_create_1d_expr(qsg_ctx *ctx, uint64_t n, double x0, double dx, double mass, double hbar,
+                       double dt_re, double dt_im, int order, int precision, int boundary,
+                       const char *psi_expr, const char *v_expr, int normalize, qsg_inst **out);
+int qsg_create_2d_expr(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double x0, double y0, double dx,
+                       double dy, double mass, double hbar, double dt_re, double dt_im, int order,
+                       int precision, const char *psi_expr, const char *v_expr, int normalize,
+                       qsg_inst **out);
+
+/* Evaluate an expression of that language on the host (the reference's
+ * Calculator::Evaluate, include/QuSim.h:527-538): nvars variables names[i]
+ * with complex values values[2i], values[2i + 1]; *out = (re, im). */
+int qsg_expr_eval(const char *expr, int nvars, const char *const *names, const double *values,
+                  double *out);
+
 /* Advance by nsteps steps (O2: V/2 T V/2; O4: the 7-factor Forest-Ruth
  * sequence), then, if renormalize, scale psi to Norm2 == 1.  Asynchronous:
  * returns once the launches are queued.  2D without renormalize: the last

@@ -167,6 +167,73 @@ inline int order_of(SolverMethod s)
 
 }  // namespace detail
 
+// The reference's expression calculator API (include/QuSim.h:502-538) over
+// qsg_expr_eval: the same language (src/Cal.cpp), evaluated by libqsg.so on
+// the host.  A FunctorWrapper / Functor2DWrapper can be passed to
+// Evolver1D / Evolver2D::init wherever a functor is taken.
+class Calculator {
+public:
+    explicit Calculator(char const *expr) : fExpr(expr)
+    {
+        // syntax errors throw here, as the reference's constructor does; an
+        // undefined variable waits until Evaluate
+        double out[2];
+        const int rc = qsg_expr_eval(fExpr.c_str(), 0, nullptr, nullptr, out);
+        if (rc != QSG_OK && std::string(qsg_last_error()).find("var not defined") == std::string::npos)
+            detail::check(rc);
+    }
+    Calculator(Calculator const &) = delete;
+    Calculator &operator=(Calculator const &) = delete;
+    Complex &SetVaraible(char const *name, Complex v)
+    {
+        fVars[name] = v;
+        return fVars[name];
+    }
+    Complex &GetVaraible(char const *name) { return fVars.at(name); }
+    Complex Evaluate()
+    {
+        std::vector<char const *> names;
+        std::vector<double> vals;
+        for (auto const &kv : fVars) {
+            names.push_back(kv.first.c_str());
+            vals.push_back(kv.second.real());
+            vals.push_back(kv.second.imag());
+        }
+        double out[2];
+        detail::check(qsg_expr_eval(fExpr.c_str(), (int)names.size(), names.data(), vals.data(), out));
+        return Complex(out[0], out[1]);
+    }
+
+private:
+    std::string fExpr;
+    std::map<std::string, Complex> fVars;
+};
+
+struct FunctorWrapper {
+    explicit FunctorWrapper(char const *expr) : fCal(std::make_shared<Calculator>(expr)) {}
+    Complex operator()(Real x) const
+    {
+        fCal->SetVaraible("x", x);
+        return fCal->Evaluate();
+    }
+
+private:
+    std::shared_ptr<Calculator> fCal;
+};
+
+struct Functor2DWrapper {
+    explicit Functor2DWrapper(char const *expr) : fCal(std::make_shared<Calculator>(expr)) {}
+    Complex operator()(Real x, Real y) const
+    {
+        fCal->SetVaraible("x", x);
+        fCal->SetVaraible("y", y);
+        return fCal->Evaluate();
+    }
+
+private:
+    std::shared_ptr<Calculator> fCal;
+};
+
 class Evolver {
   public:
     Evolver(Evolver const &) = delete;

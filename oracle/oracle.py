@@ -299,6 +299,7 @@ class Reference:
         lib.ref_fft3d.argtypes = [_sz, _sz, _sz, _i, _dp, _dp]
         lib.ref_born1d.argtypes = [_sz, _d, _d, _dp, _d, _d, _d, _d, _d, _i, _i, ctypes.c_char_p,
                                    _d, _i, _dp, _dp, _dp, _dp]
+        lib.ref_cal_eval.argtypes = [ctypes.c_char_p, _i, ctypes.POINTER(ctypes.c_char_p), _dp, _dp]
         lib.ref_born2d.argtypes = [_sz, _sz, _d, _d, _d, _d, _dp, _d, _d, _d, _d, _d, _d, _i, _i,
                                    ctypes.c_char_p, _d, _i, _dp, _dp, _dp, _dp, _dp, _i, _dp, _i,
                                    _dp]
@@ -353,6 +354,14 @@ class Reference:
         nx, ny, nz = x.shape
         assert self.lib.ref_fft3d(nx, ny, nz, int(inverse), _ptr(x), _ptr(out)) == 0
         return out
+
+    def cal_eval(self, expr, variables):
+        """The reference's Cal(expr) with the variables set, then Val(); None if it does not parse."""
+        names = (ctypes.c_char_p * max(1, len(variables)))(*[k.encode() for k in variables])
+        vals = np.array([[complex(v).real, complex(v).imag] for v in variables.values()] or [[0.0, 0.0]])
+        out = np.zeros(2)
+        rc = self.lib.ref_cal_eval(expr.encode(), len(variables), names, _ptr(vals), _ptr(out))
+        return None if rc != 0 else complex(out[0], out[1])
 
     PRECONDITIONERS = (b"BornIndentity", b"Vellekoop", b"Hao1", b"Hao2")
 

@@ -13,6 +13,7 @@
 #include "Perturbation1DImpl.h"
 #include "Perturbation2DImpl.h"
 #include "OptionsImpl.h"
+#include "Cal.h"
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -218,6 +219,23 @@ int ref_born2d(size_t nx, size_t ny, double x0, double x1, double y0, double y1,
         }
         for (int i = 0; i < ncos; ++i) xsec[i] = impl.ComputeXSection(cosxy[2 * i], cosxy[2 * i + 1]);
         if (ntot > 0 && tot) *tot = impl.ComputeTotalXSection(ntot);
+        return 0;
+    } catch (std::exception &) {
+        return -1;
+    }
+}
+
+// The reference's expression calculator (src/Cal.cpp): nvars variables
+// names[i] = values[2i] + i values[2i + 1], then Val(); out = (re, im).
+// Returns -1 (and leaves out) when the expression does not parse.
+int ref_cal_eval(const char *expr, int nvars, const char *const *names, const double *values, double *out)
+{
+    try {
+        Cal cal(expr);
+        for (int i = 0; i < nvars; ++i) cal.SetVarVal(names[i], CCom(values[2 * i], values[2 * i + 1]));
+        const CCom r = cal.Val();
+        out[0] = r.real();
+        out[1] = r.imag();
         return 0;
     } catch (std::exception &) {
         return -1;

@@ -7,6 +7,6 @@ Evolver/Options API (evolver.py) and of its Born-series scattering solvers
 QuPerturbation1D/2D (born.py).
 """
 from ._lib import QsgError, Spec, load  # noqa: F401
-from .evolver import (Batch, BoundaryCondition, Context, Evolver1D, Evolver2D, Instance,  # noqa: F401
-                      Options, Server, SolverMethod, default_context)
+from .evolver import (Batch, BoundaryCondition, Calculator, Context, Evolver1D, Evolver2D,  # noqa: F401
+                      Functor2DWrapper, FunctorWrapper, Instance, Options, Server, SolverMethod, default_context)
 from .born import QuPerturbation1D, QuPerturbation2D  # noqa: F401

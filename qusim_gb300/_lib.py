@@ -41,7 +41,8 @@ EXPORTS = [
     "qsg_born_default_opts", "qsg_born_create_1d", "qsg_born_create_2d", "qsg_born_compute", "qsg_born_get",
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
     "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d", "qsg_step_norm2_post", "qsg_step_norm2_get",
-    "qsg_set_form", "qsg_get_form", "qsg_check_wait_timeout",
+    "qsg_set_form", "qsg_get_form", "qsg_check_wait_timeout", "qsg_create_1d_expr", "qsg_create_2d_expr",
+    "qsg_expr_eval",
 ]
 
 # qsg_form: how a complex64 2D instance holds its state between passes
@@ -195,6 +196,12 @@ def _declare(lib):
     lib.qsg_server_take.argtypes = [_vp, _u64, _dp, _dp]
     lib.qsg_server_stats.argtypes = [_vp, ctypes.POINTER(ServerInfo)]
     lib.qsg_server_request_info.argtypes = [_vp, _u64, ctypes.POINTER(RequestInfo)]
+    _cp = ctypes.c_char_p
+    lib.qsg_create_1d_expr.argtypes = [_vp, _u64, _d, _d, _d, _d, _d, _d, _i, _i, _i, _cp, _cp, _i,
+                                       ctypes.POINTER(_vp)]
+    lib.qsg_create_2d_expr.argtypes = [_vp, _u64, _u64, _d, _d, _d, _d, _d, _d, _d, _d, _i, _i, _cp, _cp, _i,
+                                       ctypes.POINTER(_vp)]
+    lib.qsg_expr_eval.argtypes = [_cp, _i, ctypes.POINTER(_cp), _dp, _dp]
     lib.qsg_server_destroy.argtypes = [_vp]
     lib.qsg_server_destroy.restype = None
     lib.qsg_profile_enable.argtypes = [_vp, _i]

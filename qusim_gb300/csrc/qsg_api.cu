@@ -1439,6 +1439,80 @@ void release_spec(qsg_ctx *ctx, void *buf, size_t n)
 
 extern "C" {
 
+// psi0 and V sampled from expressions into a temporary device buffer of 24
+// bytes per site (counted against the budget while it lives), psi0 normalised
+// if asked; the buffer then feeds the array creation path
+static int sample_expr_buf(qsg_ctx *ctx, int dim, uint64_t nx, uint64_t ny, double x0, double y0, double dx, double dy,
+                           const char *psi_expr, const char *v_expr, int normalize, void **buf)
+{
+    const size_t n = (size_t)nx * ny;
+    const size_t bytes = n * 24;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->budget && ctx->in_use + bytes > ctx->budget)
+        return fail(QSG_ERR_BUDGET, "expression sampling needs " + std::to_string(bytes) + " bytes of the HBM budget");
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    QSG_CUDA(cudaMallocAsync(buf, bytes, ctx->st));
+    ctx->in_use += bytes;
+    double *psi = static_cast<double *>(*buf);
+    std::string err;
+    int rc = qsg::sample_expr(dim, psi_expr, v_expr, (int)nx, (int)ny, x0, y0, dx, dy, psi, psi + 2 * n, ctx->st, err);
+    cudaError_t e = cudaSuccess;
+    if (!rc && normalize) {
+        // psi *= 1 / sqrt(sum |psi|^2 dv), the reference's force_normalization (src/EvolverImpl1D.cpp:64-69)
+        int np = 0;
+        e = qsg::launch_reduce(0, psi, nullptr, 0, n, 0, ctx->partials, ctx->max_partials, &np, ctx->st);
+        if (e == cudaSuccess) e = qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st);
+        if (e == cudaSuccess) e = qsg::launch_renorm(0, psi, n, ctx->sums, dim == 2 ? dx * dy : dx, ctx->st);
+        if (e != cudaSuccess) {
+            rc = QSG_ERR_CUDA;
+            err = std::string("expression sampling: ") + cudaGetErrorString(e);
+        }
+    }
+    if (rc) {
+        cudaFreeAsync(*buf, ctx->st);
+        ctx->in_use -= bytes;
+        *buf = nullptr;
+        return fail(rc, err);
+    }
+    return QSG_OK;
+}
+
+int qsg_create_1d_expr(qsg_ctx *ctx, uint64_t n, double x0, double dx, double mass, double hbar, double dt_re,
+                       double dt_im, int order, int precision, int boundary, const char *psi_expr, const char *v_expr,
+                       int normalize, qsg_inst **out)
+{
+    if (!ctx || !out || !psi_expr || !v_expr) return fail(QSG_ERR_ARG, "qsg_create_1d_expr: null argument");
+    if (n == 0 || n > 262144 || !(dx > 0) || !std::isfinite(x0))
+        return fail(QSG_ERR_ARG, "qsg_create_1d_expr: bad n, x0 or dx");
+    void *buf = nullptr;
+    int rc = sample_expr_buf(ctx, 1, n, 1, x0, 0.0, dx, 0.0, psi_expr, v_expr, normalize, &buf);
+    if (rc) return rc;
+    const double *psi = static_cast<const double *>(buf);
+    rc = qsg_create_1d(ctx, n, dx, mass, hbar, dt_re, dt_im, order, precision, boundary, psi, psi + 2 * n, out);
+    const std::string msg = rc ? std::string(g_last_error) : std::string();
+    release_spec(ctx, buf, n);
+    return rc ? fail(rc, msg) : QSG_OK;
+}
+
+int qsg_create_2d_expr(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double x0, double y0, double dx, double dy,
+                       double mass, double hbar, double dt_re, double dt_im, int order, int precision,
+                       const char *psi_expr, const char *v_expr, int normalize, qsg_inst **out)
+{
+    if (!ctx || !out || !psi_expr || !v_expr) return fail(QSG_ERR_ARG, "qsg_create_2d_expr: null argument");
+    if (nx == 0 || ny == 0 || nx * ny > ((uint64_t)1 << 26) || !(dx > 0) || !(dy > 0) || !std::isfinite(x0) ||
+        !std::isfinite(y0))
+        return fail(QSG_ERR_ARG, "qsg_create_2d_expr: bad sizes, origin or spacing");
+    void *buf = nullptr;
+    int rc = sample_expr_buf(ctx, 2, nx, ny, x0, y0, dx, dy, psi_expr, v_expr, normalize, &buf);
+    if (rc) return rc;
+    const double *psi = static_cast<const double *>(buf);
+    const size_t n = (size_t)nx * ny;
+    rc = qsg_create_2d(ctx, nx, ny, dx, dy, mass, hbar, dt_re, dt_im, order, precision, psi, psi + 2 * n, out);
+    const std::string msg = rc ? std::string(g_last_error) : std::string();
+    release_spec(ctx, buf, n);
+    return rc ? fail(rc, msg) : QSG_OK;
+}
+
 int qsg_create_1d_spec(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar, double dt_re,
                        double dt_im, int order, int precision, int boundary, const qsg_spec *spec,
                        qsg_inst **out)

@@ -43,6 +43,11 @@ cudaError_t launch_row_blue(int prec, int m, const Blue2DArgs &a, cudaStream_t s
 cudaError_t launch_col_blue(int prec, int m, const Blue2DArgs &a, bool kinetic, double dtx, double dty,
                             double *partials, cudaStream_t st);
 
+// psi0 / V from expressions in the reference calculator's language (qsg_expr.cu):
+// compile both and sample them into psi (nx ny complex128) and V (real) on st
+int sample_expr(int dim, const char *psi_expr, const char *v_expr, int nx, int ny, double x0, double y0, double dx,
+                double dy, void *psi, double *V, cudaStream_t st, std::string &err);
+
 // 1D infinite wall (2n line per CTA)
 bool wall1d_supported(int prec, uint64_t n);
 cudaError_t launch_wall1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStream_t st);

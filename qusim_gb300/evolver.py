@@ -242,6 +242,31 @@ class Instance:
         return cls(ctx, h, (nx, ny), dx * dy, 1 if precision == "mixed" else 0)
 
     @classmethod
+    def create_1d_expr(cls, ctx, psi_expr, v_expr, n, x0, x1, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
+                       boundary=BoundaryCondition.Period, normalize=True):
+        """psi0 and V from expressions of the reference's calculator language
+        (FunctorWrapper strings), sampled on the device at x_i = x0 + i dx."""
+        dt = complex(dt)
+        dx = (x1 - x0) / n
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_1d_expr(ctx.h, n, x0, dx, mass, hbar, dt.real, dt.imag, order,
+                                         _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64, boundary.value,
+                                         psi_expr.encode(), v_expr.encode(), int(normalize), ctypes.byref(h)))
+        return cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+
+    @classmethod
+    def create_2d_expr(cls, ctx, psi_expr, v_expr, nx, ny, x0, x1, y0, y1, dt, order=2, precision="fp64", mass=1.0,
+                       hbar=1.0, normalize=True):
+        """2D: Functor2DWrapper strings in x and y, sampled at (x0 + i dx, y0 + j dy)."""
+        dt = complex(dt)
+        dx, dy = (x1 - x0) / nx, (y1 - y0) / ny
+        h = ctypes.c_void_p()
+        check(ctx.lib.qsg_create_2d_expr(ctx.h, nx, ny, x0, y0, dx, dy, mass, hbar, dt.real, dt.imag, order,
+                                         _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
+                                         psi_expr.encode(), v_expr.encode(), int(normalize), ctypes.byref(h)))
+        return cls(ctx, h, (nx, ny), dx * dy, 1 if precision == "mixed" else 0)
+
+    @classmethod
     def create_3d(cls, ctx, psi0, V, dx, dy, dz, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
         """A 3D instance (index (ix*ny + iy)*nz + iz; qsg_create_3d)."""
         psi0 = np.ascontiguousarray(psi0, dtype=np.complex128)
@@ -689,3 +714,62 @@ class Evolver2D(Evolver):
 
 __all__ = ["BoundaryCondition", "SolverMethod", "Options", "Context", "Instance", "Batch", "Server", "Evolver1D",
            "Evolver2D", "QsgError", "default_context"]
+
+
+class Calculator:
+    """The reference's Calculator (include/QuSim.h:527-538): an expression of
+    the calculator language with variables set by SetVaraible (the reference's
+    spelling) and evaluated on the host by libqsg.so (qsg_expr_eval)."""
+
+    def __init__(self, expr: str):
+        self.expr = expr
+        self.vars = {}
+        self.lib = _lib.load()
+        # syntax errors surface here, as the reference's constructor throws;
+        # variables are set after construction, so an undefined one waits for Evaluate
+        self._eval(allow_undefined=True)
+
+    def SetVaraible(self, name, value):
+        self.vars[name] = complex(value)
+        return self.vars[name]
+
+    def GetVaraible(self, name):
+        return self.vars[name]
+
+    def _eval(self, allow_undefined=False):
+        names = (ctypes.c_char_p * max(1, len(self.vars)))(*[k.encode() for k in self.vars])
+        vals = np.array([[v.real, v.imag] for v in self.vars.values()] or [[0.0, 0.0]], dtype=np.float64)
+        out = np.zeros(2)
+        rc = self.lib.qsg_expr_eval(self.expr.encode(), len(self.vars), names, _dptr(vals), _dptr(out))
+        if allow_undefined and rc == _lib.QSG_ERR_ARG and b"var not defined" in self.lib.qsg_last_error():
+            return None
+        check(rc)
+        return complex(out[0], out[1])
+
+    def Evaluate(self):
+        return self._eval()
+
+
+class FunctorWrapper:
+    """psi(x) / V(x) from an expression string (include/QuSim.h:506-516)."""
+
+    def __init__(self, expr: str):
+        self.expr = expr
+        self._c = Calculator(expr)
+
+    def __call__(self, x):
+        self._c.SetVaraible("x", x)
+        return self._c.Evaluate()
+
+
+class Functor2DWrapper:
+    """psi(x, y) / V(x, y) from an expression string (include/QuSim.h:518-525)."""
+
+    def __init__(self, expr: str):
+        self.expr = expr
+        self._c = Calculator(expr)
+
+    def __call__(self, x, y):
+        self._c.SetVaraible("x", x)
+        self._c.SetVaraible("y", y)
+        return self._c.Evaluate()

@@ -80,11 +80,22 @@ int main(int argc, char **argv)
     per2.Compute();
     const double xs = per2.ComputeXSection(1, 0), dn = per2.GetDeltaPsiNorm();
 
+    // the same tunnelling run with the reference's expression strings (FunctorWrapper)
+    Evolver1D ex;
+    ex.init(FunctorWrapper("gauss(x,-20,5)*exp(I*x)"), true, 0.02, false, FunctorWrapper("exp(-x*x)"), -100, 100,
+            2048, BoundaryCondition::Period, SolverMethod::SplittingMethodO4, 1, 1, o);
+    while (ex.Time() < 64 - 1e-9) ex.step();
+    const double trans_expr = ex.Norm2(0.0, 100.0);
+    Calculator cal("a*x^2 + I");
+    cal.SetVaraible("a", 2.0);
+    cal.SetVaraible("x", 3.0);
+    const Complex calv = cal.Evaluate();
+
     std::printf("{\"norm0\": %.17g, \"time\": %.17g, \"transmission\": %.17g, \"kin\": %.17g, \"pot\": %.17g, "
                 "\"psi0\": [%.17g, %.17g], \"norm2d\": %.17g, \"wall2d_throws\": %s, \"bad_device_throws\": %s, "
                 "\"born_R\": %.17g, \"born_T\": %.17g, \"born_eps\": %.17g, \"born2d_xsec0\": %.17g, "
-                "\"born2d_delta\": %.17g}\n",
+                "\"born2d_delta\": %.17g, \"transmission_expr\": %.17g, \"calculator\": [%.17g, %.17g]}\n",
                 n0, e.Time(), trans, kin, pot, psi[0].real(), psi[0].imag(), n2d, threw ? "true" : "false",
-                bad_device ? "true" : "false", R, T, eps, xs, dn);
+                bad_device ? "true" : "false", R, T, eps, xs, dn, trans_expr, calv.real(), calv.imag());
     return 0;
 }

@@ -23,8 +23,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as orc  # noqa: E402
-from tests.workloads import (BORN_1D_CASES, BORN_2D_CASES, BORN_XSEC_TOTAL,  # noqa: E402
-                             born_potential_1d, born_potential_2d, gauss_packet_1d,
+from tests.workloads import (BORN_1D_CASES, BORN_2D_CASES, BORN_XSEC_TOTAL, CAL_BAD,  # noqa: E402
+                             CAL_EXPRESSIONS, CAL_POINTS, born_potential_1d, born_potential_2d, gauss_packet_1d,
                              gauss_packet_2d, gaussian_bumps_2d, xsec_cosines)
 
 
@@ -112,6 +112,18 @@ def main():
         save(name, psi0=psi0, V=V, psi=psi, norm2=nrm, kin=kin, pot=pot,
              params=np.array([nx, ny, x0, x1, y0, y1, order, batch, calls, int(fnes)], dtype=np.float64),
              dt=np.complex128(dt), **extra)
+
+    # expressions of the reference's calculator (src/Cal.cpp) at a few points
+    # (tests/workloads.py CAL_EXPRESSIONS / CAL_POINTS)
+    if wanted("cal_exprs"):
+        vals = np.zeros((len(CAL_EXPRESSIONS), len(CAL_POINTS)), np.complex128)
+        for i, e in enumerate(CAL_EXPRESSIONS):
+            for j, (x, y) in enumerate(CAL_POINTS):
+                v = ref.cal_eval(e, {"x": x, "y": y})
+                assert v is not None, e
+                vals[i, j] = v
+        bad = np.array([ref.cal_eval(e, {"x": 1.0, "y": 2.0}) is None for e in CAL_BAD])
+        save("cal_exprs", values=vals, bad_fail=bad)
 
     # Born-series scattering, 1D and 2D (tests/workloads.py BORN_*_CASES)
     for (name, n, x0, x1, v0, en, eps, direction, order, pre, precer, slow,

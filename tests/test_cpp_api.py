@@ -41,6 +41,9 @@ def test_cpp_api_tunnelling_known_answer(exe, precision, tol):
     assert abs(r["transmission"] - ref) < tol
     assert abs(r["norm2d"] - 1) < 1e-5
     assert r["wall2d_throws"] and r["bad_device_throws"]
+    # the same run from the reference's expression strings (FunctorWrapper), and a Calculator
+    assert abs(r["transmission_expr"] - r["transmission"]) < 1e-12
+    assert r["calculator"] == [18.0, 1.0]
 
 
 @pytest.mark.gpu

@@ -163,3 +163,32 @@ def born_potential_2d(nx, ny, x0, x1, y0, y1, v0=0.3, seed=0):
 def xsec_cosines(count=BORN_XSEC_ANGLES):
     th = 2 * np.pi * np.arange(count) / count
     return np.stack([np.cos(th), np.sin(th)], axis=1)
+
+
+# --- expressions of the reference's calculator (src/Cal.cpp) -------------------
+
+# every operator and function of the language, at the points CAL_POINTS (x, y)
+CAL_EXPRESSIONS = [
+    "gauss(x,-20,5)*exp(I*x)",
+    "exp(-x*x)",
+    "0.5*exp(-x^2/2)",
+    "exp(I*1.5*x)*exp(-((x+40)^2+y^2)/256)",
+    "abs(x) < 1 ? (abs(y - 6) < 1 || abs(y + 6) < 1 ? 0 : 10) : 0",
+    "2^-x^2 + 3*x - y/2",
+    "sin(x)*cos(y) + tan(x/3) - asin(x/10) + acos(y/10) + atan(x*y)",
+    "sinh(x/5) + tanh(y) + atanh(x/20) + log(1 + x*x) + sqrt(2 + y)",
+    "abs(x + I*y) * (x - 0.5)",
+    "x > 0 && y < 1 ? exp(I*(x+y)) : -1",
+    "x >= 1 || y <= -1",
+    "(x + I*y)^2.5",
+    "-x^2",
+    "+x*2 - -y",
+    "1.5e-1*x + 2E2",
+    "gauss(x, 0, 1 + I)",
+    "Pi*x/ (1 + y*y)",
+    "x < 0 ? x < -5 ? 1 : 2 : 3",
+    "sqrt(-1 - x*x) + log(-2 + I*y)",
+]
+CAL_POINTS = [(-18.0, -6.5), (-0.3, 0.0), (0.5, 6.4), (1.7, 0.25), (6.2, -1.0)]
+# expressions both calculators refuse
+CAL_BAD = ["sin(x", "foo(x)", "x +", "unknownvar + 1", "(x", "x ? 1"]
