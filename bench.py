@@ -412,17 +412,43 @@ def batch_cpu_sample(psis, Vs, dxs, w, threads, budget_s=12.0, steps=20):
                       f"one instance per thread at a time, {threads} thread(s)", "host_cores": os.cpu_count()}
 
 
+def time_batch(q, ctx, psis, Vs, dxs, w, args, local, plans=None):
+    """K steps of a freshly built batch in ctx (on `plans` {n: Plan1D} where
+    given), timed with events on its stream."""
+    import torch
+    s = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    b = q.Batch(ctx, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision=args.precision)
+    for n, p in (plans or {}).items():
+        if p.kind == 1:
+            b.set_plan(n, p)
+    b.step(args.warmup)
+    b.sync()
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(s)
+    b.step(args.steps)
+    h1.record(s)
+    h1.synchronize()
+    ms = h0.elapsed_time(h1)
+    sites = b.sites()
+    b.close()
+    return {"value": sites * args.steps / (ms / 1e3), "unit": "site-steps/s", "ms_per_step": ms / args.steps}
+
+
 def run_batch(args, w):
     """The batched 1D configuration: every instance advances K steps per timed call."""
     from tests.workloads import batch_1d
+    import tempfile
     rank, world, local = dist_env()
     import torch
     torch.cuda.set_device(local)
     import qusim_gb300 as q
     psis, Vs, dxs = batch_1d(w["count"], seed=rank)
+    # no plan cache entries from elsewhere: the batch starts on the default plans
+    os.environ["QSG_PLAN_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="qsg_plans_"), "plans.tsv")
     ctx = q.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     b = q.Batch(ctx, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision=args.precision)
+    tuned, tune_ms = (None, None) if args.no_tune else b.autotune(trial_steps=8)
     sites = b.sites()
     b.step(args.warmup)
     b.sync()
@@ -461,22 +487,18 @@ def run_batch(args, w):
             ctx2 = q.Context(local)
         finally:
             del os.environ["QSG_BATCH_QUEUE"]
-        s2 = torch.cuda.ExternalStream(ctx2.stream, device=torch.device("cuda", local))
-        b2 = q.Batch(ctx2, psis, Vs, dxs, [w["dt"]] * len(psis), order=w["order"], precision=args.precision)
-        b2.step(args.warmup)
-        b2.sync()
-        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        h0.record(s2)
-        b2.step(args.steps)
-        h1.record(s2)
-        h1.synchronize()
-        ms2 = h0.elapsed_time(h1)
-        per_class = {"value": sites * args.steps * world / (ms2 / 1e3), "unit": "site-steps/s",
-                     "ms_per_step": ms2 / args.steps,
-                     "launch": "one launch per resident size class (QSG_BATCH_QUEUE=0); the states are bitwise "
-                               "those of the tile-queue launch (tests/test_gpu_parity.py)"}
-        b2.close()
+        per_class = time_batch(q, ctx2, psis, Vs, dxs, w, args, local, plans=tuned)
+        per_class["value"] *= world
+        per_class["launch"] = ("one launch per resident size class (QSG_BATCH_QUEUE=0), the same plans; the states "
+                               "are bitwise those of the tile-queue launch (tests/test_gpu_parity.py)")
         ctx2.close()
+    # the same batch on the default plans
+    default_plans = None
+    if tuned:
+        ctx3 = q.Context(local)
+        default_plans = time_batch(q, ctx3, psis, Vs, dxs, w, args, local)
+        default_plans["value"] *= world
+        ctx3.close()
     # four-step instances (N > one CTA) move 2 HBM round trips of psi plus one
     # V table and one K table entry per site-step (O2): 6 complex elements
     peak, peak_kind = measured_peaks()
@@ -544,6 +566,13 @@ def run_batch(args, w):
                 "roofline": {"bound": "on-chip", "note": "resident sizes keep psi in shared memory for all "
                              "K steps; four-step sizes make 2 HBM passes per step"},
                 "step_roofline": fs_roof, "plain_fp64": plain, "resident_per_class_launches": per_class,
+                "plans_1d": {"tuned": {str(k): list(v.as_tuple()) for k, v in (tuned or {}).items()},
+                             "tuned_classes_ms_per_step": tune_ms, "default_plans": default_plans,
+                             "default": {str(n): list(q.candidate_plans_1d(args.precision, n)[0].as_tuple())
+                                         for n in sorted({p.size for p in psis})},
+                             "note": "qsg_batch_autotune: each four-step size class timed alone in the batch on "
+                                     "every four-step plan of its length (kind, n1, tma), keeping its fastest; "
+                                     "default_plans = the same batch on the default plans"},
                 "accuracy": acc, "gpu_launches": int(sum(v[0] for v in counts.values())),
                 "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()},
                 "cpu_baseline": cpu, "clocks": clk}

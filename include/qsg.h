@@ -21,11 +21,13 @@
  * x0 + i*dx with dx = (x1 - x0)/n (src/EvolverImpl1D.cpp:11).
  *
  * Environment, read when a context is created (qsg_init):
- *   QSG_PLAN_CACHE      2D plan cache file (default ~/.cache/qusim_gb300/plans.tsv)
+ *   QSG_PLAN_CACHE      plan cache file of qsg_autotune / qsg_autotune_1d
+ *                       (default ~/.cache/qusim_gb300/plans.tsv)
  *   QSG_COL_TMA=0       complex64 2D momentum-form column passes load their
  *                       tiles with load instructions instead of tensor copies
- *   QSG_FS_TMA=1        1D four-step column passes staged by tensor copies
- *                       (off by default: measured slower)
+ *   QSG_FS_TMA=1        1D four-step column passes staged by tensor copies in
+ *                       the default plans (off by default: measured slower on the
+ *                       2048-instance batch; qsg_autotune_1d picks per size)
  *   QSG_BATCH_GRAPHS=1  batch steps replayed from captured CUDA graphs (off by
  *                       default: measured no faster)
  * Every setting computes the same result bit for bit.
@@ -35,6 +37,9 @@
  *                       with QSG_ERR_CUDA instead of launching (no device work
  *                       is faulted); the request ends failed and the other
  *                       requests run on unaffected
+ *   QSG_SERVER_RING=<k> descriptor slots of the batched resident launches
+ *                       (default 4096, at least max_running); tests set a small
+ *                       ring so that its slots are reused many times over
  */
 #ifndef QSG_H
 #define QSG_H
@@ -53,7 +58,8 @@ typedef enum {
     QSG_ERR_CUDA = 3,         /* a CUDA runtime error (message in qsg_last_error)   */
     QSG_ERR_TIMEOUT = 4,      /* a bounded device-side wait ran out                 */
     QSG_ERR_UNSUPPORTED = 5,  /* valid for the reference, not built here (e.g. a
-                                 non-power-of-two grid, InfiniteWall in 2D)         */
+                                 side above the supported lengths, InfiniteWall
+                                 in 2D)                                             */
     QSG_ERR_STATE = 6         /* call not valid in the object's current state       */
 } qsg_status;
 
@@ -81,7 +87,9 @@ void *qsg_ctx_stream(qsg_ctx *ctx);
 /* Device bytes currently held by the context's instances and scratch. */
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
 
-/* Create a 1D instance (n a power of two, 64 .. 262144).  psi0: n complex (re,im); V: n real (the reference keeps
+/* Create a 1D instance: n a power of two, 64 .. 262144, or any other length
+ * from 2 to 4096 (QSG_MIXED) / 2048 (QSG_FP64), stepped through Bluestein
+ * transforms (as are the powers of two below 64).  psi0: n complex (re,im); V: n real (the reference keeps
  * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
@@ -98,7 +106,10 @@ int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
                   const double *psi0, const double *V, qsg_inst **out);
 
 /* Create a 2D instance, nx*ny sites, index iy + ix*ny.  Periodic only, as in
- * the reference (src/SplittingMethod2D.cpp:21-29).
+ * the reference (src/SplittingMethod2D.cpp:21-29).  Sides that are powers of
+ * two (128 .. 4096) run the split-k passes with plans; a grid with a
+ * side that is not a power of two (each side 2 .. 4096 for QSG_MIXED, 2 ..
+ * 2048 for QSG_FP64) runs row and column passes of Bluestein transforms.
  * Replaces SplittingMethod2D::InitSystem2D (src/SplittingMethod2D.cpp:5-31). */
 int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
                   double hbar, double dt_re, double dt_im, int order, int precision,
@@ -124,8 +135,9 @@ int qsg_create_3d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, uint64_t nz, double dx
  *             force_normalization);
  *   V(r)    = v0 + sum_b h_b exp(-|r - b_b|^2 / (2 w_b^2)), bumps[b] = {h, bx, by, w}.
  * In 1D the y terms (ky, cy, by) are unused.  This is the packet-plus-bumps
- * family of the benchmark and serving inputs; a general expression (the
- * reference's Cal.cpp calculator) is not parsed. */
+ * family of the benchmark and serving inputs; general expressions of the
+ * reference's calculator language go through qsg_create_1d_expr /
+ * qsg_create_2d_expr. */
 #define QSG_SPEC_MAX_BUMPS 32
 typedef struct {
     double x0, y0;
@@ -292,6 +304,46 @@ int qsg_check_wait_timeout(qsg_inst *inst);
 int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
                  double *best_ms_per_step);
 
+/* 1D execution plan (no counterpart in the reference, whose periodic ExpT is
+ * one FFT call each way per substep, src/SplittingMethod1D.cpp:40-60):
+ *   kind 0: resident -- one CTA holds the whole line for the whole call
+ *           (periodic n <= 8192 complex64 / 4096 complex128, one-CTA walls);
+ *   kind 1: four-step -- two passes per substep over the n2 x n1 view of the
+ *           line (n = n1 * n2, n from 8192 to 262144, n1 and n2 powers of two
+ *           from 64 to 1024): column transforms of length n2, row transforms
+ *           of length n1;
+ *   tma:    four-step complex64 with n2 = 128 .. 512: the column pass stages
+ *           its tiles with tensor copies instead of load instructions.
+ * A wall above one CTA is stepped as its periodic 2n odd extension, so its
+ * plans are the four-step plans of 2n (without tma).  Lengths that are not
+ * powers of two (Bluestein) have one plan, kind 0.  Every plan computes the
+ * same result to rounding; they differ in speed.  New instances of a size
+ * take the plan qsg_autotune_1d last chose for that size and precision in
+ * this context or in the plan cache file, else the default (resident where
+ * it fits, else four-step with n1 = n2 or 2 n2, load-instruction columns). */
+typedef struct {
+    int32_t kind;
+    int32_t n1;
+    int32_t tma;
+    int32_t reserved;
+} qsg_plan1d;
+
+/* Plans for a 1D instance of n sites, `boundary` and `precision`; fills up to
+ * cap (out may be null), returns the count (0: no instance of that shape). */
+int qsg_candidate_plans_1d(int precision, uint64_t n, int boundary, qsg_plan1d *out, int cap);
+int qsg_get_plan_1d(qsg_inst *inst, qsg_plan1d *out);
+/* Switch an instance to another plan between steps (its state is kept).
+ * QSG_ERR_UNSUPPORTED for a plan that is not a candidate, QSG_ERR_STATE for a
+ * member of a batch (the batch's launches are built on its members' plans). */
+int qsg_set_plan_1d(qsg_inst *inst, const qsg_plan1d *plan);
+/* qsg_autotune for a 1D instance: every candidate plan timed for trial_steps
+ * steps on a copy of the state (psi and the step count are left unchanged);
+ * the instance switches to the fastest, which is remembered for new instances
+ * of its size in this context and, if persist, appended to the plan cache file
+ * ($QSG_PLAN_CACHE). */
+int qsg_autotune_1d(qsg_inst *inst, int trial_steps, int persist, qsg_plan1d *best,
+                    double *best_ms_per_step);
+
 /* A batch of independent 1D instances of (possibly) different sizes, shared
  * order / precision / mass / hbar, per-instance dx, dt, psi0, V -- advanced
  * together.  Instances of one size are evolved by launches over all of them
@@ -308,6 +360,21 @@ int qsg_batch_sync(qsg_batch *batch);
 int qsg_batch_size(qsg_batch *batch, int *count, uint64_t *sites);
 int qsg_batch_instance(qsg_batch *batch, int i, qsg_inst **out);
 void qsg_batch_destroy(qsg_batch *batch);
+
+/* Plans of a batch's size classes (no counterpart in the reference).  A batch
+ * is built on each size's cached plan (see qsg_plan1d); qsg_batch_autotune
+ * tunes the four-step classes in the batch itself, because a launch over many
+ * instances loads the GPU differently from one instance alone: each such class
+ * is timed alone (all its members, at least trial_steps steps and 2^22
+ * site-steps, on copies of their states, which are put back) on every
+ * four-step plan of its length and keeps its fastest.  The choice stays with
+ * the batch.  ms_per_step (may be null): the sum of the tuned classes' best
+ * times per step.  qsg_batch_get_plan_1d / qsg_batch_set_plan_1d read and set
+ * the plan of the members of length n (four-step plans only for four-step
+ * classes; QSG_ERR_ARG for a length the batch does not hold). */
+int qsg_batch_autotune(qsg_batch *batch, int trial_steps, double *ms_per_step);
+int qsg_batch_get_plan_1d(qsg_batch *batch, uint64_t n, qsg_plan1d *out);
+int qsg_batch_set_plan_1d(qsg_batch *batch, uint64_t n, const qsg_plan1d *plan);
 
 /* Serving: evolution requests submitted as they arrive, run by a scheduler
  * thread with continuous batching under an HBM budget (new to this engine).

@@ -42,7 +42,8 @@ EXPORTS = [
     "qsg_born_rt", "qsg_born_delta_norm", "qsg_born_epsilon", "qsg_born_xsection", "qsg_born_total_xsection",
     "qsg_born_destroy", "qsg_step_norm2", "qsg_create_3d", "qsg_step_norm2_post", "qsg_step_norm2_get",
     "qsg_set_form", "qsg_get_form", "qsg_check_wait_timeout", "qsg_create_1d_expr", "qsg_create_2d_expr",
-    "qsg_expr_eval",
+    "qsg_expr_eval", "qsg_candidate_plans_1d", "qsg_get_plan_1d", "qsg_set_plan_1d", "qsg_autotune_1d",
+    "qsg_batch_autotune", "qsg_batch_get_plan_1d", "qsg_batch_set_plan_1d",
 ]
 
 # qsg_form: how a complex64 2D instance holds its state between passes
@@ -117,6 +118,18 @@ class Plan2D(ctypes.Structure):
                 f"col_w={self.col_w}, row_kind={self.row_kind})")
 
 
+class Plan1D(ctypes.Structure):
+    """qsg_plan1d: kind 0 resident (one CTA) / 1 four-step (n = n1 * n2), row length n1, tensor-copy columns."""
+    _fields_ = [("kind", ctypes.c_int32), ("n1", ctypes.c_int32), ("tma", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+    def as_tuple(self):
+        return (self.kind, self.n1, self.tma)
+
+    def __repr__(self):
+        return f"Plan1D(kind={self.kind}, n1={self.n1}, tma={self.tma})"
+
+
 class BornOpts(ctypes.Structure):
     """qsg_born_opts: the order / preconditional / preconditioner / slow options."""
     _fields_ = [("order", ctypes.c_int), ("preconditional", ctypes.c_int), ("preconditioner", ctypes.c_int),
@@ -180,6 +193,13 @@ def _declare(lib):
     lib.qsg_get_form.argtypes = [_vp, ctypes.POINTER(_i)]
     lib.qsg_check_wait_timeout.argtypes = [_vp]
     lib.qsg_autotune.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan2D), _dp]
+    lib.qsg_candidate_plans_1d.argtypes = [_i, _u64, _i, ctypes.POINTER(Plan1D), _i]
+    lib.qsg_get_plan_1d.argtypes = [_vp, ctypes.POINTER(Plan1D)]
+    lib.qsg_set_plan_1d.argtypes = [_vp, ctypes.POINTER(Plan1D)]
+    lib.qsg_autotune_1d.argtypes = [_vp, _i, _i, ctypes.POINTER(Plan1D), _dp]
+    lib.qsg_batch_autotune.argtypes = [_vp, _i, _dp]
+    lib.qsg_batch_get_plan_1d.argtypes = [_vp, _u64, ctypes.POINTER(Plan1D)]
+    lib.qsg_batch_set_plan_1d.argtypes = [_vp, _u64, ctypes.POINTER(Plan1D)]
     _pp = ctypes.POINTER(_dp)
     lib.qsg_batch_create_1d.argtypes = [_vp, _i, ctypes.POINTER(_u64), _dp, _dp, _dp, _d, _d, _i, _i, _pp, _pp,
                                         ctypes.POINTER(_vp)]

@@ -88,6 +88,10 @@ struct qsg_inst {
     cudaStream_t st = nullptr;     // launch stream of the stepping kernels (the context's unless set)
     // 1D: resident (one CTA holds the instance) or four-step (two passes per substep)
     bool fourstep = false;
+    qsg_plan1d plan1d{};           // 1D: the plan in use (kind 1 = fourstep, split n1, tma)
+    bool fs_tma = false;           // four-step column passes staged by tensor copies
+    bool batch_member = false;     // owned by a batch, whose launches are built on its plan
+    double *parts_buf = nullptr;   // four-step norm partials (allocated for every n >= 8192)
     // 1D InfiniteWall above the one-CTA sizes: the state is the odd extension
     // of psi to 2 n_out sites (psi_j, 0 at j = n_out, -psi_{2 n_out - j}
     // above), stepped as a periodic four-step instance of n = 2 n_out sites;
@@ -112,6 +116,7 @@ struct qsg_inst {
     const void *tw_fs_col = nullptr, *tw_fs_row = nullptr, *tw_n = nullptr;
     qsg::FsInst *desc = nullptr;   // device descriptor of this instance
     void *fs_maps = nullptr;       // complex64 four-step: tensor maps of psi, V 0, V 1 (tensor-copy column pass)
+    size_t fs_maps_bytes = 0;
     double *d_dv = nullptr;        // device copy of dv (resident renormalisation)
     std::vector<std::tuple<int, int, int, double, double>> shared_k;  // four-step kinetic tables in use (ctx->fs_ktabs)
     double *snorm = nullptr;       // 1D one-CTA kernels: sum |psi|^2 of the state a step call ended in
@@ -218,7 +223,7 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     a.out_k = out_k ? 1 : 0;
     a.wall = in->wall_ext ? 1 : 0;
     ProfScope ps(in->ctx, "fs_col_pass", st);
-    if (maps && !in->wall_ext && in->ctx->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
+    if (maps && !in->wall_ext && in->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
         a.maps = maps;
         a.tiles = in->fsg.col_blocks * ninst;
         a.err = reinterpret_cast<int *>(in->err);
@@ -802,6 +807,119 @@ int upload_factors(qsg_inst *in, const std::vector<std::complex<long double>> &s
     return QSG_OK;
 }
 
+// --- 1D plans ----------------------------------------------------------------
+
+// four-step plans of a stepped length n: the default split first, then the
+// others from the longest rows down, each with and without tensor-copy columns
+void add_fs_plans(int prec, uint64_t n, bool tma_ok, std::vector<qsg_plan1d> &out)
+{
+    const int d = qsg::fs_default_n1(n);
+    std::vector<int> n1s{d};
+    for (int n1 = 1024; n1 >= 64; n1 >>= 1)
+        if (n1 != d) n1s.push_back(n1);
+    for (int n1 : n1s) {
+        qsg::FsGeom g;
+        if (!qsg::fs_geom(prec, n, &g, n1)) continue;
+        out.push_back(qsg_plan1d{1, n1, 0, 0});
+        if (tma_ok && qsg::fs_tma_supported(prec, g.n2)) out.push_back(qsg_plan1d{1, n1, 1, 0});
+    }
+}
+
+// every plan of a 1D instance of n sites (the default first)
+void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
+{
+    out.clear();
+    if (prec != QSG_FP64 && prec != QSG_MIXED) return;
+    const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
+    if (boundary == QSG_INFINITE_WALL) {
+        if (!pow2 || n < 64 || n > 131072) return;
+        if (qsg::wall1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+        else add_fs_plans(prec, 2 * n, false, out);  // the periodic 2n odd extension
+        return;
+    }
+    if (boundary != QSG_PERIOD) return;
+    if (!pow2 || n < 64) {
+        if (qsg::blue_m_for(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+        return;
+    }
+    if (qsg::evolve1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+    add_fs_plans(prec, n, true, out);
+}
+
+bool same_plan1d(const qsg_plan1d &a, const qsg_plan1d &b)
+{
+    return a.kind == b.kind && (a.kind == 0 || (a.n1 == b.n1 && a.tma == b.tma));
+}
+
+bool plan1d_valid(int prec, uint64_t n, int boundary, const qsg_plan1d &p)
+{
+    std::vector<qsg_plan1d> c;
+    plans_1d(prec, n, boundary, c);
+    for (const auto &q : c)
+        if (same_plan1d(q, p)) return true;
+    return false;
+}
+
+// norm partials of the four-step passes: one per column-pass CTA, n / 4096
+// (complex64) or n / 2048 (complex128) whatever the split; 0 where no
+// four-step plan exists
+int fs_parts_for(const qsg_inst *in)
+{
+    if (in->dim != 1 || in->blue) return 0;
+    qsg::FsGeom g;
+    if (!qsg::fs_geom(in->prec, in->n, &g)) return 0;
+    return g.col_blocks;
+}
+
+// 1D periodic kinetic tables of the instance's current layout (natural for
+// one-CTA kernels, row layout for four-step passes), shared across instances
+int build_ktab_1d(qsg_inst *in)
+{
+    qsg_ctx *ctx = in->ctx;
+    const SplitConsts sc;
+    const int ntab = in->order == 2 ? 1 : 2;
+    const double tc[2] = {in->order == 2 ? 1.0 : sc.d1, sc.d2};
+    const size_t cs = csize(in->prec);
+    const cd I(0, 1);
+    int rc;
+    // ExpT periodic: f = -i DT dt t / hbar, DT = (Dk hbar)^2/(2m), Dk = 2 pi/(dx N)
+    // (SplittingMethod1D.cpp:51-53).  A wall extension of N = 2 n sites gets the
+    // same table: Dk = 2 pi/(dx 2n) is the wall's Dp/hbar = pi/(dx n)
+    // (SplittingMethod1D.cpp:72-74), and two inverse 2n-transforms with the
+    // final -1/(2n) equal a forward and an inverse one with 1/(2n) on an odd
+    // sequence, whose transform is odd as well
+    const double dk = 2 * kPi / (in->dx * in->n);
+    const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
+    for (int k = 0; k < ntab; ++k) {
+        const cd f = -I * DT * in->dt * tc[k] / in->hbar;
+        // shared by every instance of the context with the same size and coefficient (a batch of
+        // equal-dx, equal-dt instances reads one table per size from L2 instead of one each);
+        // key (precision, n1, n2) for the four-step layout, (precision, n, 0) for the natural one
+        const auto key = in->fourstep ? std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag())
+                                      : std::make_tuple(in->prec, (int)in->n, 0, f.real(), f.imag());
+        auto it = ctx->fs_ktabs.find(key);
+        const bool fresh = it == ctx->fs_ktabs.end();
+        if (fresh) {
+            void *p = nullptr;
+            if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
+            it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
+        }
+        // registered before the table is filled, so that releasing the instance
+        // after a failed launch below also releases the table
+        it->second.users += 1;
+        in->shared_k.push_back(key);
+        in->ktab[k] = it->second.p;
+        if (fresh && in->fourstep) {
+            QSG_CUDA(qsg::launch_ktable_fs(in->prec, it->second.p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
+                                           1.0 / (double)in->n, ctx->st));
+        } else if (fresh) {
+            QSG_CUDA(qsg::launch_ktable1d(in->prec, it->second.p, (int)in->n, f.real(), f.imag(),
+                                          1.0 / (double)in->n, ctx->st));
+        }
+    }
+    return QSG_OK;
+}
+
 int build_tables(qsg_inst *in)
 {
     qsg_ctx *ctx = in->ctx;
@@ -882,41 +1000,7 @@ int build_tables(qsg_inst *in)
             }
         }
     } else if (in->dim == 1) {
-        // ExpT periodic: f = -i DT dt t / hbar, DT = (Dk hbar)^2/(2m), Dk = 2 pi/(dx N)
-        // (SplittingMethod1D.cpp:51-53).  A wall extension of N = 2 n sites gets the
-        // same table: Dk = 2 pi/(dx 2n) is the wall's Dp/hbar = pi/(dx n)
-        // (SplittingMethod1D.cpp:72-74), and two inverse 2n-transforms with the
-        // final -1/(2n) equal a forward and an inverse one with 1/(2n) on an odd
-        // sequence, whose transform is odd as well
-        const double dk = 2 * kPi / (in->dx * in->n);
-        const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
-        for (int k = 0; k < ntab; ++k) {
-            const cd f = -I * DT * in->dt * tc[k] / in->hbar;
-            // shared by every instance of the context with the same size and coefficient (a batch of
-            // equal-dx, equal-dt instances reads one table per size from L2 instead of one each);
-            // key (precision, n1, n2) for the four-step layout, (precision, n, 0) for the natural one
-            const auto key = in->fourstep ? std::make_tuple(in->prec, in->fsg.n1, in->fsg.n2, f.real(), f.imag())
-                                          : std::make_tuple(in->prec, (int)in->n, 0, f.real(), f.imag());
-            auto it = ctx->fs_ktabs.find(key);
-            const bool fresh = it == ctx->fs_ktabs.end();
-            if (fresh) {
-                void *p = nullptr;
-                if ((rc = dev_alloc(ctx, in->n * cs, &p, nullptr))) return rc;
-                it = ctx->fs_ktabs.emplace(key, qsg_ctx::SharedTable{p, in->n * cs, 0}).first;
-            }
-            // registered before the table is filled, so that releasing the instance
-            // after a failed launch below also releases the table
-            it->second.users += 1;
-            in->shared_k.push_back(key);
-            in->ktab[k] = it->second.p;
-            if (fresh && in->fourstep) {
-                QSG_CUDA(qsg::launch_ktable_fs(in->prec, it->second.p, in->fsg.n1, in->fsg.n2, f.real(), f.imag(),
-                                               1.0 / (double)in->n, ctx->st));
-            } else if (fresh) {
-                QSG_CUDA(qsg::launch_ktable1d(in->prec, it->second.p, (int)in->n, f.real(), f.imag(),
-                                              1.0 / (double)in->n, ctx->st));
-            }
-        }
+        if ((rc = build_ktab_1d(in))) return rc;
     } else if (in->dim == 3) {
         // SplittingMethod2D::InitExpT with a third axis, one factor per axis:
         // exp(a fold(i)^2 DT_axis) with 1/L folded in (complex128) or as factor - 1
@@ -971,6 +1055,20 @@ int upload_psi(qsg_inst *in, const double *psi)
     return QSG_OK;
 }
 
+// drop the instance's uses of shared kinetic tables (a table is freed, in
+// stream order, when its last user lets go)
+void release_shared_k(qsg_inst *in)
+{
+    for (const auto &key : in->shared_k) {
+        auto it = in->ctx->fs_ktabs.find(key);
+        if (it == in->ctx->fs_ktabs.end() || --it->second.users > 0) continue;
+        cudaFreeAsync(it->second.p, in->ctx->st);
+        in->ctx->in_use -= it->second.bytes;
+        in->ctx->fs_ktabs.erase(it);
+    }
+    in->shared_k.clear();
+}
+
 void free_inst(qsg_inst *in)
 {
     if (!in) return;
@@ -982,13 +1080,7 @@ void free_inst(qsg_inst *in)
         // streams is joined into it before an instance is released)
         for (void *p : in->allocs) cudaFreeAsync(p, in->ctx->st);
         in->ctx->in_use -= in->bytes;
-        for (const auto &key : in->shared_k) {
-            auto it = in->ctx->fs_ktabs.find(key);
-            if (it == in->ctx->fs_ktabs.end() || --it->second.users > 0) continue;
-            cudaFreeAsync(it->second.p, in->ctx->st);
-            in->ctx->in_use -= it->second.bytes;
-            in->ctx->fs_ktabs.erase(it);
-        }
+        release_shared_k(in);
     }
     delete in;
 }
@@ -1009,13 +1101,15 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     if ((rc = build_tables(in))) return rc;
     if (in->dim == 1) {
         // device descriptor (+ dv, + four-step norm partials) for the 1D kernels
-        const int nparts = in->fourstep ? in->fsg.col_blocks : 0;
+        // (partials for every length that has four-step plans, so that a plan switch needs none)
+        const int nparts = fs_parts_for(in);
         void *blk = nullptr;
         if ((rc = inst_alloc(in, sizeof(qsg::FsInst) + sizeof(double) * (2 + nparts), &blk))) return rc;
         in->desc = static_cast<qsg::FsInst *>(blk);
         in->d_dv = reinterpret_cast<double *>(in->desc + 1);
         in->snorm = in->d_dv + 1;
-        in->parts = nparts ? in->d_dv + 2 : nullptr;
+        in->parts_buf = nparts ? in->d_dv + 2 : nullptr;
+        in->parts = in->fourstep ? in->parts_buf : nullptr;
         qsg::FsInst h{};
         h.psi = in->psi;
         h.vtab[0] = in->vtab[0];
@@ -1025,11 +1119,12 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         h.partials = in->parts;
         QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-        if (in->fourstep) {
+        if (in->fourstep && in->fs_tma) {
             size_t mb = 0;
             in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);
             if (in->fs_maps) {
                 in->allocs.push_back(in->fs_maps);
+                in->fs_maps_bytes = mb;
                 in->bytes += mb;
                 ctx->in_use += mb;
             }
@@ -1069,7 +1164,9 @@ std::string plan_cache_path()
     return std::string(home ? home : ".") + "/.cache/qusim_gb300/plans.tsv";
 }
 
-// lines: device \t prec \t nx \t ny \t g \t row_e \t row_nt \t col_e \t col_w \t ms_per_step [\t row_kind]
+// 2D lines: device \t prec \t nx \t ny \t g \t row_e \t row_nt \t col_e \t col_w \t ms_per_step [\t row_kind]
+// 1D lines: device \t 1d \t prec \t n \t boundary \t kind \t n1 \t tma \t ms_per_step
+// (later lines win)
 void load_plans(qsg_ctx *ctx)
 {
     if (ctx->plans_loaded) return;
@@ -1083,6 +1180,18 @@ void load_plans(qsg_ctx *ctx)
         Plan2D p;
         double ms;
         if (!std::getline(is, dev, '\t')) continue;
+        if (is.peek() == '1' && line.find("\t1d\t") != std::string::npos) {
+            std::string tag;
+            uint64_t n = 0;
+            int boundary = 0;
+            qsg_plan1d q{};
+            if (!(is >> tag >> prec >> n >> boundary >> q.kind >> q.n1 >> q.tma >> ms) || tag != "1d") continue;
+            if (dev == ctx->device_name && plan1d_valid(prec, n, boundary, q)) {
+                const bool ext = boundary == QSG_INFINITE_WALL && !qsg::wall1d_supported(prec, n);
+                ctx->plans1d[std::make_tuple(prec, ext ? 2 * n : n, ext ? 1 : 0)] = q;
+            }
+            continue;
+        }
         if (!(is >> prec >> nx >> ny >> p.g >> p.row_e >> p.row_nt >> p.col_e >> p.col_w >> ms)) continue;
         int kind = 0;
         if (is >> kind) p.row_kind = kind;
@@ -1108,6 +1217,101 @@ void save_plan(qsg_ctx *ctx, int prec, int nx, int ny, const Plan2D &p, double m
     if (!f) return;
     f << ctx->device_name << '\t' << prec << '\t' << nx << '\t' << ny << '\t' << p.g << '\t' << p.row_e << '\t'
       << p.row_nt << '\t' << p.col_e << '\t' << p.col_w << '\t' << ms << '\t' << p.row_kind << '\n';
+}
+
+void save_plan_1d(qsg_ctx *ctx, int prec, uint64_t n, int boundary, const qsg_plan1d &p, double ms)
+{
+    const std::string path = plan_cache_path();
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {
+        std::string dir = path.substr(0, slash);
+        for (size_t i = 1; i <= dir.size(); ++i)
+            if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
+    }
+    std::ofstream f(path, std::ios::app);
+    if (!f) return;
+    f << ctx->device_name << "\t1d\t" << prec << '\t' << n << '\t' << boundary << '\t' << p.kind << '\t' << p.n1
+      << '\t' << p.tma << '\t' << ms << '\n';
+}
+
+// give back one of the instance's own allocations (stream-ordered)
+void inst_release(qsg_inst *in, void *p, size_t bytes)
+{
+    auto it = std::find(in->allocs.begin(), in->allocs.end(), p);
+    if (it == in->allocs.end()) return;
+    in->allocs.erase(it);
+    cudaFreeAsync(p, in->ctx->st);
+    in->bytes -= bytes;
+    in->ctx->in_use -= bytes;
+}
+
+// Switch a 1D instance to plan p between steps: geometry, twiddles, kinetic
+// tables in the plan's layout, descriptor and tensor maps.  The state is in
+// natural order between steps in every plan, so it is kept as it is.
+int apply_plan_1d(qsg_inst *in, const qsg_plan1d &p)
+{
+    qsg_ctx *ctx = in->ctx;
+    if (!plan1d_valid(in->prec, user_n(in), in->boundary, p))
+        return fail(QSG_ERR_UNSUPPORTED, "1D plan (kind " + std::to_string(p.kind) + ", n1 " + std::to_string(p.n1) +
+                                             ", tma " + std::to_string(p.tma) + ") not available for this instance");
+    if (same_plan1d(p, in->plan1d)) return QSG_OK;
+    const bool fs = p.kind == 1;
+    qsg::FsGeom g{};
+    if (fs && !qsg::fs_geom(in->prec, in->n, &g, p.n1)) return fail(QSG_ERR_UNSUPPORTED, "four-step split not built");
+    int rc;
+    const void *tfc = nullptr, *tfr = nullptr, *tn = nullptr, *tw = nullptr;
+    if (fs) {
+        if ((rc = get_twiddles(ctx, in->prec, g.n2, g.col_e, &tfc))) return rc;
+        if ((rc = get_twiddles(ctx, in->prec, g.n1, g.row_e, &tfr))) return rc;
+        if ((rc = get_fs_grid(ctx, in->prec, g.n1, g.n2, &tn))) return rc;
+        if ((rc = get_twiddles(ctx, in->prec, g.n1, qsg::elems_per_thread(in->prec), &tw))) return rc;
+    } else {
+        if ((rc = get_twiddles(ctx, in->prec, (int)in->n, qsg::elems_per_thread(in->prec), &tw))) return rc;
+    }
+    // launches already queued read the old tables
+    QSG_CUDA(cudaStreamSynchronize(in->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    release_shared_k(in);
+    in->ktab[0] = in->ktab[1] = nullptr;
+    in->fourstep = fs;
+    in->fsg = g;
+    in->tw_fs_col = tfc;
+    in->tw_fs_row = tfr;
+    in->tw_n = tn;
+    in->tw = tw;
+    in->fs_tma = p.tma != 0;
+    in->plan1d = p;
+    in->parts = fs ? in->parts_buf : nullptr;
+    in->snorm_valid = false;
+    if (in->fs_maps) {
+        inst_release(in, in->fs_maps, in->fs_maps_bytes);
+        in->fs_maps = nullptr;
+        in->fs_maps_bytes = 0;
+    }
+    if ((rc = build_ktab_1d(in))) {
+        in->lost = true;  // no kinetic tables for the plan: the instance cannot step
+        return rc;
+    }
+    qsg::FsInst h{};
+    h.psi = in->psi;
+    h.vtab[0] = in->vtab[0];
+    h.vtab[1] = in->vtab[1];
+    h.ktab[0] = in->ktab[0];
+    h.ktab[1] = in->ktab[1];
+    h.partials = in->parts;
+    QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
+    if (fs && in->fs_tma) {
+        size_t mb = 0;
+        in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);
+        if (in->fs_maps) {
+            in->allocs.push_back(in->fs_maps);
+            in->fs_maps_bytes = mb;
+            in->bytes += mb;
+            ctx->in_use += mb;
+        }
+    }
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return QSG_OK;
 }
 
 // point the instance at a plan: geometry + the twiddle tables it needs
@@ -1304,8 +1508,9 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
                                              " (supported: powers of two, 64 .. 131072)");
     // walls above one CTA: a four-step periodic instance of the 2n odd extension
     const bool wall_ext = wall && !qsg::wall1d_supported(precision, n);
-    // periodic lengths that are not powers of two: Bluestein transforms of length blue_m
-    const int blue_m = !wall && !pow2 ? qsg::blue_m_for(precision, n) : 0;
+    // periodic lengths that are not powers of two (and powers of two below the
+    // one-CTA kernels' 64): Bluestein transforms of length blue_m
+    const int blue_m = !wall && (!pow2 || n < 64) ? qsg::blue_m_for(precision, n) : 0;
     qsg::FsGeom fsg{};
     const bool resident = wall ? !wall_ext : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
     if (wall_ext && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
@@ -1317,6 +1522,17 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (supported: powers of two, 64 .. 262144)");
+    // the plan: the one tuned for this shape (in this context or the plan cache),
+    // else the default (one CTA where it fits, else four-step, default split)
+    qsg_plan1d plan{resident ? 0 : 1, resident ? 0 : fsg.n1, 0, 0};
+    if (!resident && !wall_ext && ctx->fs_tma && qsg::fs_tma_supported(precision, fsg.n2)) plan.tma = 1;
+    if (!blue_m && !(wall && !wall_ext)) {
+        load_plans(ctx);
+        auto it = ctx->plans1d.find(std::make_tuple(precision, wall_ext ? 2 * n : n, wall_ext ? 1 : 0));
+        if (it != ctx->plans1d.end() && plan1d_valid(precision, n, boundary, it->second)) plan = it->second;
+    }
+    if (plan.kind == 1 && !qsg::fs_geom(precision, wall_ext ? 2 * n : n, &fsg, plan.n1))
+        return fail(QSG_ERR_STATE, "qsg_create_1d: plan cache entry does not fit n=" + std::to_string(n));
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();
     in->ctx = ctx;
@@ -1334,14 +1550,16 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     in->prec = precision;
     in->boundary = boundary;
     in->st = ctx->st;
-    in->fourstep = !resident;
-    in->fsg = fsg;
+    in->fourstep = plan.kind == 1;
+    in->fsg = in->fourstep ? fsg : qsg::FsGeom{};
+    in->plan1d = plan;
+    in->fs_tma = plan.tma != 0;
     in->blue = blue_m > 0;
     in->blue_m = blue_m;
     int rc = QSG_OK;
     if (in->blue) {
         rc = get_twiddles(ctx, precision, blue_m, qsg::blue_elems(precision), &in->tw);
-    } else if (resident) {
+    } else if (!in->fourstep) {
         // the wall transforms run on the 2n odd extension
         rc = get_twiddles(ctx, precision, (int)(wall ? 2 * n : n), qsg::elems_per_thread(precision), &in->tw);
     } else {
@@ -2143,6 +2361,103 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     return QSG_OK;
 }
 
+int qsg_candidate_plans_1d(int precision, uint64_t n, int boundary, qsg_plan1d *out, int cap)
+{
+    std::vector<qsg_plan1d> v;
+    plans_1d(precision, n, boundary, v);
+    for (int i = 0; out && i < (int)v.size() && i < cap; ++i) out[i] = v[i];
+    return (int)v.size();
+}
+
+int qsg_get_plan_1d(qsg_inst *in, qsg_plan1d *out)
+{
+    if (!in || !out) return fail(QSG_ERR_ARG, "qsg_get_plan_1d: null argument");
+    if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_get_plan_1d: 1D instances only");
+    *out = in->plan1d;
+    return QSG_OK;
+}
+
+int qsg_set_plan_1d(qsg_inst *in, const qsg_plan1d *p)
+{
+    if (!in || !p) return fail(QSG_ERR_ARG, "qsg_set_plan_1d: null argument");
+    if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_set_plan_1d: 1D instances only");
+    if (in->batch_member) return fail(QSG_ERR_STATE, "qsg_set_plan_1d: a batch member keeps its batch's plan");
+    std::lock_guard<std::mutex> lk(in->ctx->mu);
+    if (int rc = lost_state(in, "qsg_set_plan_1d")) return rc;
+    QSG_CUDA(cudaSetDevice(in->ctx->dev));
+    return apply_plan_1d(in, *p);
+}
+
+int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best, double *best_ms_per_step)
+{
+    if (!in) return fail(QSG_ERR_ARG, "qsg_autotune_1d: null instance");
+    if (in->dim != 1) return fail(QSG_ERR_ARG, "qsg_autotune_1d: 1D instances only");
+    if (in->batch_member) return fail(QSG_ERR_STATE, "qsg_autotune_1d: a batch member keeps its batch's plan");
+    if (trial_steps < 1) trial_steps = 4;
+    qsg_ctx *ctx = in->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (int rc = lost_state(in, "qsg_autotune_1d")) return rc;
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    std::vector<qsg_plan1d> cands;
+    plans_1d(in->prec, user_n(in), in->boundary, cands);
+    if (cands.empty()) return fail(QSG_ERR_UNSUPPORTED, "qsg_autotune_1d: no plan for this instance");
+    // each trial long enough to time: at least 2^22 site-steps
+    const uint64_t steps = std::max<uint64_t>((uint64_t)trial_steps, ((uint64_t)1 << 22) / in->n);
+    // the trials evolve a copy; psi is restored afterwards
+    const size_t bytes = in->n * csize(in->prec);
+    QSG_CUDA(cudaStreamSynchronize(in->st));
+    int rc = ensure_scratch(ctx, bytes);
+    if (rc) return rc;
+    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    const qsg_plan1d keep = in->plan1d;
+    const int prof = ctx->prof;
+    ctx->prof = 0;
+    cudaEvent_t e0, e1;
+    QSG_CUDA(cudaEventCreate(&e0));
+    QSG_CUDA(cudaEventCreate(&e1));
+    double best_ms = 1e30;
+    qsg_plan1d best_p = keep;
+    for (const qsg_plan1d &p : cands) {
+        if (apply_plan_1d(in, p)) {
+            if (in->lost) break;
+            continue;
+        }
+        if (step1d(in, 1, 0)) continue;  // warm-up (also loads the module)
+        cudaEventRecord(e0, in->st);
+        if (step1d(in, steps, 0)) continue;
+        cudaEventRecord(e1, in->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double per = ms / (double)steps;
+        if (per < best_ms) {
+            best_ms = per;
+            best_p = p;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->prof = prof;
+    cudaError_t err = cudaGetLastError();
+    if (in->lost) return fail(QSG_ERR_CUDA, "qsg_autotune_1d: a plan switch failed; the instance needs qsg_set_psi");
+    QSG_CUDA(cudaStreamSynchronize(in->st));
+    QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+    in->snorm_valid = false;
+    // a trial pass that ran out of time worked on the copy: acknowledge its count
+    if ((rc = queue_err_copy(in, ctx->st))) return rc;
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    std::memcpy(&in->err_seen, ctx->host_sums + 7, sizeof(unsigned));
+    if (err != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_autotune_1d: ") + cudaGetErrorString(err));
+    if ((rc = apply_plan_1d(in, best_p))) return rc;
+    const bool ext = in->wall_ext;
+    ctx->plans1d[std::make_tuple(in->prec, in->n, ext ? 1 : 0)] = best_p;
+    if (persist) save_plan_1d(ctx, in->prec, user_n(in), in->boundary, best_p, best_ms);
+    if (best) *best = best_p;
+    if (best_ms_per_step) *best_ms_per_step = best_ms;
+    return QSG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Batches of 1D instances: grouped by size; each size class is advanced by
 // launches over all its instances (resident: one launch per qsg_batch_step;
@@ -2290,6 +2605,7 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
             batch_free(b);
             return fail(rc, "qsg_batch_create_1d: instance " + std::to_string(i) + ": " + msg);
         }
+        in->batch_member = true;
         b->insts.push_back(in);
         b->sites += n[i];
         auto it = cls.find(n[i]);
@@ -2512,6 +2828,153 @@ void qsg_batch_destroy(qsg_batch *b)
     batch_free(b);
 }
 
+}  // extern "C"
+
+namespace {
+
+qsg_batch::Class *batch_class(qsg_batch *b, uint64_t n)
+{
+    for (auto &c : b->classes)
+        if (c.n == n) return &c;
+    return nullptr;
+}
+
+// Switch every member of a four-step class to plan p, then rebuild the class's
+// descriptors (the kinetic tables move with the split) and tensor maps; a
+// captured batch graph is dropped (it holds the old launches).
+int batch_class_plan(qsg_batch *b, qsg_batch::Class &c, const qsg_plan1d &p)
+{
+    qsg_ctx *ctx = b->ctx;
+    if (p.kind != 1 || !b->insts[c.members[0]]->fourstep)
+        return fail(QSG_ERR_UNSUPPORTED, "batch plans: four-step plans of four-step classes only");
+    QSG_CUDA(cudaStreamSynchronize(c.st));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    int rc;
+    for (int m : c.members)
+        if ((rc = apply_plan_1d(b->insts[m], p))) return rc;
+    std::vector<qsg::FsInst> h(c.members.size());
+    std::vector<qsg_inst *> mi(c.members.size());
+    for (size_t k = 0; k < c.members.size(); ++k) {
+        qsg_inst *in = b->insts[c.members[k]];
+        mi[k] = in;
+        h[k] = qsg::FsInst{};
+        h[k].psi = in->psi;
+        h[k].vtab[0] = in->vtab[0];
+        h[k].vtab[1] = in->vtab[1];
+        h[k].ktab[0] = in->ktab[0];
+        h[k].ktab[1] = in->ktab[1];
+    }
+    QSG_CUDA(cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice));
+    if (c.d_maps) cudaFreeAsync(c.d_maps, ctx->st);
+    size_t mb = 0;
+    c.d_maps = fs_make_maps(ctx, mi.data(), mi.size(), &mb);
+    if (b->gexec) {
+        cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+        b->gsteps = 0;
+    }
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    return QSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qsg_batch_get_plan_1d(qsg_batch *b, uint64_t n, qsg_plan1d *out)
+{
+    if (!b || !out) return fail(QSG_ERR_ARG, "qsg_batch_get_plan_1d: null argument");
+    qsg_batch::Class *c = batch_class(b, n);
+    if (!c) return fail(QSG_ERR_ARG, "qsg_batch_get_plan_1d: no member of length " + std::to_string(n));
+    *out = b->insts[c->members[0]]->plan1d;
+    return QSG_OK;
+}
+
+int qsg_batch_set_plan_1d(qsg_batch *b, uint64_t n, const qsg_plan1d *p)
+{
+    if (!b || !p) return fail(QSG_ERR_ARG, "qsg_batch_set_plan_1d: null argument");
+    std::lock_guard<std::mutex> lk(b->ctx->mu);
+    QSG_CUDA(cudaSetDevice(b->ctx->dev));
+    qsg_batch::Class *c = batch_class(b, n);
+    if (!c) return fail(QSG_ERR_ARG, "qsg_batch_set_plan_1d: no member of length " + std::to_string(n));
+    qsg_inst *proto = b->insts[c->members[0]];
+    if (same_plan1d(*p, proto->plan1d)) return QSG_OK;
+    if (!plan1d_valid(proto->prec, n, QSG_PERIOD, *p))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_batch_set_plan_1d: plan not available for length " + std::to_string(n));
+    return batch_class_plan(b, *c, *p);
+}
+
+int qsg_batch_autotune(qsg_batch *b, int trial_steps, double *ms_per_step)
+{
+    if (!b) return fail(QSG_ERR_ARG, "qsg_batch_autotune: null batch");
+    if (trial_steps < 1) trial_steps = 4;
+    qsg_ctx *ctx = b->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    QSG_CUDA(cudaSetDevice(ctx->dev));
+    QSG_CUDA(cudaStreamSynchronize(ctx->st));
+    const int prof = ctx->prof;
+    ctx->prof = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    QSG_CUDA(cudaEventCreate(&e0));
+    QSG_CUDA(cudaEventCreate(&e1));
+    double total = 0;
+    int rc = QSG_OK;
+    for (auto &c : b->classes) {
+        qsg_inst *proto = b->insts[c.members[0]];
+        if (!proto->fourstep) continue;
+        std::vector<qsg_plan1d> cands;
+        plans_1d(proto->prec, c.n, QSG_PERIOD, cands);
+        cands.erase(std::remove_if(cands.begin(), cands.end(), [](const qsg_plan1d &q) { return q.kind != 1; }),
+                    cands.end());
+        if (cands.size() < 2) continue;
+        const int ninst = (int)c.members.size();
+        const uint64_t steps =
+            std::max<uint64_t>((uint64_t)trial_steps, ((uint64_t)1 << 22) / (c.n * (uint64_t)ninst));
+        // the trials evolve the members' states: keep copies
+        const size_t bytes = proto->n * csize(proto->prec);
+        if ((rc = ensure_scratch(ctx, bytes * ninst))) break;
+        unsigned char *keep = static_cast<unsigned char *>(ctx->scratch);
+        for (int k = 0; k < ninst; ++k)
+            QSG_CUDA(cudaMemcpyAsync(keep + k * bytes, b->insts[c.members[k]]->psi, bytes, cudaMemcpyDeviceToDevice,
+                                     ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(ctx->st));
+        const qsg_plan1d start = proto->plan1d;
+        qsg_plan1d best_p = start;
+        double best_ms = 1e30;
+        for (const qsg_plan1d &p : cands) {
+            if (!same_plan1d(p, proto->plan1d) && (rc = batch_class_plan(b, c, p))) break;
+            if ((rc = step_fs(proto, c.d_desc, ninst, 1, c.st, c.d_maps))) break;  // warm-up
+            cudaEventRecord(e0, c.st);
+            if ((rc = step_fs(proto, c.d_desc, ninst, steps, c.st, c.d_maps))) break;
+            cudaEventRecord(e1, c.st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = fail(QSG_ERR_CUDA, "qsg_batch_autotune: trial failed");
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms / steps < best_ms) {
+                best_ms = ms / steps;
+                best_p = p;
+            }
+        }
+        if (!rc && !same_plan1d(best_p, proto->plan1d)) rc = batch_class_plan(b, c, best_p);
+        QSG_CUDA(cudaStreamSynchronize(c.st));
+        for (int k = 0; k < ninst; ++k)
+            QSG_CUDA(cudaMemcpyAsync(b->insts[c.members[k]]->psi, keep + k * bytes, bytes, cudaMemcpyDeviceToDevice,
+                                     ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(ctx->st));
+        if (rc) break;
+        total += best_ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->prof = prof;
+    if (rc) return rc;
+    if (ms_per_step) *ms_per_step = total;
+    return QSG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Serving: a scheduler thread with continuous batching.
 //
@@ -2698,7 +3161,36 @@ void srv_loop(qsg_server *S)
     std::deque<std::shared_ptr<SrvRequest>> pending;
     std::vector<std::shared_ptr<SrvRequest>> running;
     uint64_t rr = 0;
-    std::vector<cudaEvent_t> ring_events(S->ring_size, nullptr);
+    // Uses of the descriptor ring, in launch order: slots [pos, pos + cnt) (device
+    // ring and pinned staging) stay taken until the server-owned event `ev`,
+    // recorded after the launch that reads them, has completed.  (Requests' own
+    // events cannot mark the slots: a request that finishes destroys its event.)
+    struct RingUse {
+        int pos, cnt;
+        cudaEvent_t ev;
+    };
+    std::deque<RingUse> ring_uses;
+    std::vector<cudaEvent_t> ring_ev_pool;
+    // true when [pos, pos + cnt) is free; retires the completed uses it overlaps
+    auto ring_range_free = [&](int pos, int cnt) {
+        bool free = true;
+        for (auto it = ring_uses.begin(); it != ring_uses.end();) {
+            if (!(it->pos < pos + cnt && pos < it->pos + it->cnt)) {
+                ++it;
+                continue;
+            }
+            const cudaError_t q = cudaEventQuery(it->ev);
+            if (q == cudaErrorNotReady) {
+                free = false;
+                ++it;
+                continue;
+            }
+            if (q != cudaSuccess) cudaGetLastError();  // a failed context: nothing is running any more
+            ring_ev_pool.push_back(it->ev);
+            it = ring_uses.erase(it);
+        }
+        return free;
+    };
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(S->mu);
@@ -2787,12 +3279,15 @@ void srv_loop(qsg_server *S)
             if (cnt > S->ring_size) continue;
             if (S->ring_pos + cnt > S->ring_size) S->ring_pos = 0;
             // the slots must not be in use by a launch still running
-            bool busy = false;
-            for (int k = 0; k < cnt; ++k) {
-                cudaEvent_t e = ring_events[S->ring_pos + k];
-                if (e && cudaEventQuery(e) != cudaSuccess) busy = true;
+            if (!ring_range_free(S->ring_pos, cnt)) continue;
+            cudaEvent_t done = nullptr;
+            if (!ring_ev_pool.empty()) {
+                done = ring_ev_pool.back();
+                ring_ev_pool.pop_back();
+            } else if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                continue;  // retried on a later pass
             }
-            if (busy) continue;
             qsg::FsInst *h = S->ring_host + S->ring_pos;
             for (int k = 0; k < cnt; ++k) {
                 qsg_inst *in = g[k]->inst;
@@ -2829,10 +3324,13 @@ void srv_loop(qsg_server *S)
                 what = "resident 1D launch";
             }
             // ring slots (device and pinned staging) stay busy until this event
-            cudaEvent_t done = g[0]->ev;
             const cudaError_t er = cudaEventRecord(done, st);
-            if (er != cudaSuccess) cudaStreamSynchronize(st);  // no event to wait on: the slots are free after this
-            for (int k = 0; k < cnt; ++k) ring_events[S->ring_pos + k] = er == cudaSuccess ? done : nullptr;
+            if (er == cudaSuccess) {
+                ring_uses.push_back(RingUse{S->ring_pos, cnt, done});
+            } else {
+                cudaStreamSynchronize(st);  // no event to wait on: the slots are free after this
+                ring_ev_pool.push_back(done);
+            }
             S->ring_pos += cnt;
             progress = true;
             if (e != cudaSuccess || injected) {
@@ -2844,7 +3342,7 @@ void srv_loop(qsg_server *S)
                 continue;
             }
             for (int k = 0; k < cnt; ++k) {
-                if (k && cudaEventRecord(g[k]->ev, st) != cudaSuccess) {
+                if (cudaEventRecord(g[k]->ev, st) != cudaSuccess) {
                     srv_mark_failed(*g[k], st, QSG_ERR_CUDA, "cudaEventRecord failed after a resident 1D launch");
                     continue;
                 }
@@ -2892,6 +3390,8 @@ void srv_loop(qsg_server *S)
     cudaDeviceSynchronize();
     for (auto &q : running) srv_finish(S, *q, QSG_ERR_STATE, "server stopped");
     for (auto &q : pending) srv_finish(S, *q, QSG_ERR_STATE, "server stopped");
+    for (auto &u : ring_uses) cudaEventDestroy(u.ev);
+    for (cudaEvent_t e : ring_ev_pool) cudaEventDestroy(e);
 }
 
 }  // namespace
@@ -2908,6 +3408,12 @@ int qsg_server_create(int device_ordinal, size_t hbm_budget_bytes, int max_runni
     qsg_server *S = new qsg_server();
     S->ctx = ctx;
     if (max_running > 0) S->max_running = max_running;
+    if (const char *rs = std::getenv("QSG_SERVER_RING")) {
+        const long v = std::strtol(rs, nullptr, 10);
+        if (v >= 1 && v <= (1 << 20)) S->ring_size = (int)v;
+    }
+    // a resident group (at most max_running requests) must fit the ring
+    S->ring_size = std::max(S->ring_size, S->max_running);
     for (int i = 0; i < 8; ++i) {
         cudaStream_t st;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) break;

@@ -88,6 +88,8 @@ struct qsg_ctx {
     std::vector<std::string> prof_names;  // stable storage for returned names
     std::string device_name;
     std::map<std::tuple<int, int, int>, qsg::Plan2D> plans;  // tuned plans: (prec, nx, ny) -> plan
+    // tuned 1D plans: (prec, stepped length, wall extension) -> plan
+    std::map<std::tuple<int, uint64_t, int>, qsg_plan1d> plans1d;
     bool plans_loaded = false;
 };
 

@@ -195,6 +195,18 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+def candidate_plans_1d(precision, n, boundary=_lib.QSG_PERIOD, lib=None):
+    """qsg_candidate_plans_1d: the Plan1D list of a 1D instance shape (host
+    logic only; precision 0/1 or "fp64"/"mixed")."""
+    lib = lib or _lib.load()
+    prec = precision if isinstance(precision, int) else (1 if precision == "mixed" else 0)
+    b = getattr(boundary, "value", boundary)
+    k = lib.qsg_candidate_plans_1d(prec, n, b, None, 0)
+    arr = (_lib.Plan1D * max(k, 1))()
+    k = lib.qsg_candidate_plans_1d(prec, n, b, arr, k)
+    return [arr[i] for i in range(k)]
+
+
 class Instance:
     """One qsg_inst: a wavefunction resident on the device."""
 
@@ -204,6 +216,7 @@ class Instance:
         self.shape = shape
         self.dv = dv
         self._prec = prec
+        self._boundary = _lib.QSG_PERIOD
         ctx._adopt(self)
 
     @classmethod
@@ -219,7 +232,9 @@ class Instance:
                                     _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
                                     boundary.value, _dptr(psi0.view(np.float64)), _dptr(V),
                                     ctypes.byref(h)))
-        return cls(ctx, h, psi0.shape, dx, 1 if precision == "mixed" else 0)
+        inst = cls(ctx, h, psi0.shape, dx, 1 if precision == "mixed" else 0)
+        inst._boundary = boundary.value
+        return inst
 
     @classmethod
     def create_1d_spec(cls, ctx, spec, n, dx, dt, order=2, precision="fp64", mass=1.0, hbar=1.0,
@@ -230,7 +245,9 @@ class Instance:
         check(ctx.lib.qsg_create_1d_spec(ctx.h, n, dx, mass, hbar, dt.real, dt.imag, order,
                                          _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64,
                                          boundary.value, ctypes.byref(spec), ctypes.byref(h)))
-        return cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+        inst = cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+        inst._boundary = boundary.value
+        return inst
 
     @classmethod
     def create_2d_spec(cls, ctx, spec, nx, ny, dx, dy, dt, order=2, precision="fp64", mass=1.0, hbar=1.0):
@@ -252,7 +269,9 @@ class Instance:
         check(ctx.lib.qsg_create_1d_expr(ctx.h, n, x0, dx, mass, hbar, dt.real, dt.imag, order,
                                          _lib.QSG_MIXED if precision == "mixed" else _lib.QSG_FP64, boundary.value,
                                          psi_expr.encode(), v_expr.encode(), int(normalize), ctypes.byref(h)))
-        return cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+        inst = cls(ctx, h, (n,), dx, 1 if precision == "mixed" else 0)
+        inst._boundary = boundary.value
+        return inst
 
     @classmethod
     def create_2d_expr(cls, ctx, psi_expr, v_expr, nx, ny, x0, x1, y0, y1, dt, order=2, precision="fp64", mass=1.0,
@@ -351,11 +370,22 @@ class Instance:
         check(self.ctx.lib.qsg_set_psi(self.h, _dptr(psi.view(np.float64))))
 
     def plan(self):
+        """The execution plan in use: Plan2D for 2D instances, Plan1D for 1D."""
+        if len(self.shape) == 1:
+            p = _lib.Plan1D()
+            check(self.ctx.lib.qsg_get_plan_1d(self.h, ctypes.byref(p)))
+            return p
         p = _lib.Plan2D()
         check(self.ctx.lib.qsg_get_plan(self.h, ctypes.byref(p)))
         return p
 
     def set_plan(self, plan):
+        """Switch plans between steps (a Plan2D / Plan1D or its tuple)."""
+        if len(self.shape) == 1:
+            if not isinstance(plan, _lib.Plan1D):
+                plan = _lib.Plan1D(*plan)
+            check(self.ctx.lib.qsg_set_plan_1d(self.h, ctypes.byref(plan)))
+            return
         if not isinstance(plan, _lib.Plan2D):
             plan = _lib.Plan2D(*plan)
         check(self.ctx.lib.qsg_set_plan(self.h, ctypes.byref(plan)))
@@ -382,6 +412,8 @@ class Instance:
     def candidate_plans(self, precision=None):
         lib = self.ctx.lib
         prec = self._prec if precision is None else (1 if precision == "mixed" else 0)
+        if len(self.shape) == 1:
+            return candidate_plans_1d(prec, self.shape[0], self._boundary, lib)
         nx, ny = self.shape
         n = lib.qsg_candidate_plans(prec, nx, ny, None, 0)
         arr = (_lib.Plan2D * max(n, 1))()
@@ -390,8 +422,13 @@ class Instance:
 
     def autotune(self, trial_steps: int = 4, persist: bool = True):
         """Time every plan on a copy of the state, switch to the fastest; returns (plan, ms/step)."""
-        p = _lib.Plan2D()
         ms = ctypes.c_double()
+        if len(self.shape) == 1:
+            p = _lib.Plan1D()
+            check(self.ctx.lib.qsg_autotune_1d(self.h, trial_steps, int(persist), ctypes.byref(p),
+                                               ctypes.byref(ms)))
+            return p, ms.value
+        p = _lib.Plan2D()
         check(self.ctx.lib.qsg_autotune(self.h, trial_steps, int(persist), ctypes.byref(p), ctypes.byref(ms)))
         return p, ms.value
 
@@ -451,6 +488,26 @@ class Batch:
         c, s = ctypes.c_int(), ctypes.c_uint64()
         check(self.ctx.lib.qsg_batch_size(self.h, ctypes.byref(c), ctypes.byref(s)))
         return s.value
+
+    def plan(self, n: int):
+        """The Plan1D of the members of length n."""
+        p = _lib.Plan1D()
+        check(self.ctx.lib.qsg_batch_get_plan_1d(self.h, n, ctypes.byref(p)))
+        return p
+
+    def set_plan(self, n: int, plan):
+        """Switch the members of length n (a four-step class) to a four-step plan."""
+        if not isinstance(plan, _lib.Plan1D):
+            plan = _lib.Plan1D(*plan)
+        check(self.ctx.lib.qsg_batch_set_plan_1d(self.h, n, ctypes.byref(plan)))
+
+    def autotune(self, trial_steps: int = 8):
+        """qsg_batch_autotune: each four-step class timed alone on every four-step
+        plan, keeping its fastest; states unchanged.  Returns ({n: Plan1D}, ms/step
+        summed over the tuned classes)."""
+        ms = ctypes.c_double()
+        check(self.ctx.lib.qsg_batch_autotune(self.h, trial_steps, ctypes.byref(ms)))
+        return {n: self.plan(n) for n in sorted(set(self.sizes))}, ms.value
 
     def instance(self, i: int) -> "Instance":
         """A non-owning view of member i (get_psi, norm2, energies, ...)."""

@@ -551,13 +551,14 @@ def test_wall_extension_set_psi_round_trip(qsg, ctx, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("n", [3, 5, 100, 1000, 1234, 2047, 4095])
+@pytest.mark.parametrize("n", [3, 5, 8, 32, 100, 1000, 1234, 2047, 4095])
 @pytest.mark.parametrize("order", [2, 4])
 def test_lengths_not_powers_of_two_vs_oracle(qsg, ctx, oracle, n, order):
     """Periodic 1D grids of any length (the reference transforms them with KISS's
     mixed radix, src/kissfft.hh:26-45; 1234 is its FFT test's length,
     applications/QuSimTest/TestFFT.cpp:89-99): Bluestein transforms of a
-    power-of-two length.  Against the oracle (bit-exact with the reference's
+    power-of-two length (also for the powers of two 8 and 32, below the one-CTA
+    kernels' 64).  Against the oracle (bit-exact with the reference's
     KISS evolution): complex128 <= 1e-12 with Norm2, KinEn and PotEn to 1e-11,
     complex64 <= 1e-5 (complex128 is built up to n = 2048)."""
     L = max(10.0, 0.1 * n)

@@ -192,3 +192,38 @@ def test_served_length_not_power_of_two_equals_solo():
     for r, psi in zip(reqs, out):
         assert np.array_equal(psi, solo(q, ctx, r, "mixed"))
     ctx.close()
+
+
+def test_descriptor_ring_reused_many_times(monkeypatch):
+    """Batched resident launches take slots of a descriptor ring, free again
+    only once the launch that reads them has completed.  With an 8-slot ring
+    and 60 requests of 1 to 3 chunks each, submitted while earlier ones run,
+    the ring wraps dozens of times past requests that have already finished;
+    every request ends DONE, bitwise equal to its solo run."""
+    import qusim_gb300 as q
+    monkeypatch.setenv("QSG_SERVER_RING", "8")
+    rng = np.random.default_rng(11)
+    reqs = []
+    for k in range(60):
+        n = (1024, 2048, 4096)[k % 3]
+        box = 0.05 * n
+        p, v, dx = gauss_packet_1d(n, -box, box, rng.uniform(0.5, 3), -0.25 * box, rng.uniform(2, 20), barrier=0.8)
+        reqs.append(dict(psi0=p, V=v, dx=dx, dt=0.01, nsteps=int(rng.integers(100, 3000)), order=2 + 2 * (k % 2)))
+    srv = q.Server(0, max_running=6)
+    ids = []
+    for k, r in enumerate(reqs):
+        ids.append(srv.submit(r["psi0"], r["V"], r["dx"], r["dt"], r["nsteps"], order=r["order"],
+                              precision="mixed"))
+        if k % 10 == 9:
+            srv.wait(ids[-8], 300)  # later submissions arrive while the ring is in use
+    results = []
+    for i in ids:
+        assert srv.wait(i, 300) == q.Server.DONE
+        results.append(srv.take(i)[0])
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    ctx = q.Context(0)
+    for r, psi in zip(reqs, results):
+        assert np.array_equal(psi, solo(q, ctx, r, "mixed"))
+    ctx.close()

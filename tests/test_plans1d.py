@@ -1,0 +1,62 @@
+"""1D execution plans: the candidate list (qsg_candidate_plans_1d) is host
+logic of libqsg.so, checked here without a GPU."""
+import pytest
+
+WALL = 1
+
+
+@pytest.fixture(scope="module")
+def q():
+    import qusim_gb300 as q
+    q.load()
+    return q
+
+
+def tuples(q, prec, n, boundary=0):
+    return [p.as_tuple() for p in q.candidate_plans_1d(prec, n, boundary)]
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_four_step_splits(q, prec):
+    for lg in range(13, 19):
+        n = 1 << lg
+        plans = tuples(q, prec, n)
+        fs = [p for p in plans if p[0] == 1]
+        assert fs, n
+        # the default split first among the four-step plans: n1 = n2 or 2 n2
+        n1 = fs[0][1]
+        assert n1 * n1 in (n, 2 * n) and fs[0][2] == 0
+        for kind, n1, tma in fs:
+            n2 = n // n1
+            assert n1 * n2 == n and 64 <= n1 <= 1024 and 64 <= n2 <= 1024
+            # tensor-copy column passes: complex64, columns of 128 .. 512
+            assert not tma or (prec == "mixed" and n2 in (128, 256, 512))
+        assert len(set(plans)) == len(plans)
+
+
+def test_resident_plans(q):
+    assert tuples(q, "mixed", 1024) == [(0, 0, 0)]
+    assert tuples(q, "mixed", 8192)[0] == (0, 0, 0)   # one CTA where it fits: the default
+    assert (0, 0, 0) not in tuples(q, "fp64", 8192)  # complex128 holds 4096 in one CTA
+    assert tuples(q, "fp64", 4096) == [(0, 0, 0)]
+
+
+def test_lengths_without_choices(q):
+    # Bluestein lengths: one plan; lengths beyond every plan: none
+    assert tuples(q, "mixed", 1000) == [(0, 0, 0)]
+    assert tuples(q, "mixed", 5000) == []
+    assert tuples(q, "mixed", 1 << 19) == []
+    assert tuples(q, "mixed", 32) == [(0, 0, 0)]   # powers of two below 64: Bluestein
+    assert tuples(q, "mixed", 1) == []
+    assert tuples(q, 7, 1024) == []                # unknown precision
+
+
+def test_wall_plans(q):
+    # one CTA holds the 2n extension up to n = 4096 (complex64); above, the
+    # four-step plans of the periodic 2n extension, without tensor copies
+    assert tuples(q, "mixed", 4096, WALL) == [(0, 0, 0)]
+    plans = tuples(q, "mixed", 65536, WALL)
+    assert plans and all(k == 1 and t == 0 for k, _, t in plans)
+    assert {n1 for _, n1, _ in plans} == {n1 for k, n1, _ in tuples(q, "mixed", 131072) if k == 1}
+    assert tuples(q, "mixed", 262144, WALL) == []
+    assert tuples(q, "mixed", 1000, WALL) == []
