@@ -30,6 +30,10 @@
  *                       2048-instance batch; qsg_autotune_1d picks per size)
  *   QSG_BATCH_GRAPHS=1  batch steps replayed from captured CUDA graphs (off by
  *                       default: measured no faster)
+ *   QSG_FAIL_PLAN_SWITCH=1  (read at each 1D plan switch) failure injection for
+ *                       tests: a switch fails on the host after building the new
+ *                       plan's tables, which are released again; the instance
+ *                       keeps its plan
  * Every setting computes the same result bit for bit.
  * Read when a server is created (qsg_server_create):
  *   QSG_SERVER_FAIL_REQUEST=<id>  fault injection for tests of the failure

@@ -1271,7 +1271,36 @@ int apply_plan_1d(qsg_inst *in, const qsg_plan1d &p)
     // launches already queued read the old tables
     QSG_CUDA(cudaStreamSynchronize(in->st));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    release_shared_k(in);
+    // The new kinetic tables and descriptor are made first; the old tables are
+    // released only once the descriptor points at the new ones, so a failure
+    // on the way puts the old plan back as it was.
+    struct Saved {
+        bool fourstep, fs_tma;
+        qsg::FsGeom fsg;
+        const void *tfc, *tfr, *tn, *tw;
+        qsg_plan1d plan;
+        double *parts;
+        void *ktab[2];
+        std::vector<std::tuple<int, int, int, double, double>> keys;
+    } old{in->fourstep, in->fs_tma, in->fsg, in->tw_fs_col, in->tw_fs_row, in->tw_n, in->tw, in->plan1d, in->parts,
+          {in->ktab[0], in->ktab[1]}, in->shared_k};
+    auto restore = [&](int code) {
+        release_shared_k(in);  // the new plan's tables, if any were made
+        in->fourstep = old.fourstep;
+        in->fs_tma = old.fs_tma;
+        in->fsg = old.fsg;
+        in->tw_fs_col = old.tfc;
+        in->tw_fs_row = old.tfr;
+        in->tw_n = old.tn;
+        in->tw = old.tw;
+        in->plan1d = old.plan;
+        in->parts = old.parts;
+        in->ktab[0] = old.ktab[0];
+        in->ktab[1] = old.ktab[1];
+        in->shared_k = old.keys;
+        return code;
+    };
+    in->shared_k.clear();
     in->ktab[0] = in->ktab[1] = nullptr;
     in->fourstep = fs;
     in->fsg = g;
@@ -1282,16 +1311,9 @@ int apply_plan_1d(qsg_inst *in, const qsg_plan1d &p)
     in->fs_tma = p.tma != 0;
     in->plan1d = p;
     in->parts = fs ? in->parts_buf : nullptr;
-    in->snorm_valid = false;
-    if (in->fs_maps) {
-        inst_release(in, in->fs_maps, in->fs_maps_bytes);
-        in->fs_maps = nullptr;
-        in->fs_maps_bytes = 0;
-    }
-    if ((rc = build_ktab_1d(in))) {
-        in->lost = true;  // no kinetic tables for the plan: the instance cannot step
-        return rc;
-    }
+    if ((rc = build_ktab_1d(in))) return restore(rc);
+    if (std::getenv("QSG_FAIL_PLAN_SWITCH"))  // host-side failure injection for the tests of this path
+        return restore(fail(QSG_ERR_CUDA, "injected plan-switch failure (QSG_FAIL_PLAN_SWITCH)"));
     qsg::FsInst h{};
     h.psi = in->psi;
     h.vtab[0] = in->vtab[0];
@@ -1299,10 +1321,28 @@ int apply_plan_1d(qsg_inst *in, const qsg_plan1d &p)
     h.ktab[0] = in->ktab[0];
     h.ktab[1] = in->ktab[1];
     h.partials = in->parts;
-    QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
+    cudaError_t e = cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return restore(fail(QSG_ERR_CUDA, std::string("1D plan switch: ") + cudaGetErrorString(e)));
+    }
+    // committed: the old tables go, the tensor maps follow the split
+    {
+        std::vector<std::tuple<int, int, int, double, double>> now = in->shared_k;
+        in->shared_k = old.keys;
+        release_shared_k(in);
+        in->shared_k = now;
+    }
+    in->snorm_valid = false;
+    if (in->fs_maps) {
+        inst_release(in, in->fs_maps, in->fs_maps_bytes);
+        in->fs_maps = nullptr;
+        in->fs_maps_bytes = 0;
+    }
     if (fs && in->fs_tma) {
         size_t mb = 0;
-        in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);
+        in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);  // none: the column pass loads with instructions
         if (in->fs_maps) {
             in->allocs.push_back(in->fs_maps);
             in->fs_maps_bytes = mb;
@@ -2419,10 +2459,7 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     double best_ms = 1e30;
     qsg_plan1d best_p = keep;
     for (const qsg_plan1d &p : cands) {
-        if (apply_plan_1d(in, p)) {
-            if (in->lost) break;
-            continue;
-        }
+        if (apply_plan_1d(in, p)) continue;  // the instance keeps its plan
         if (step1d(in, 1, 0)) continue;  // warm-up (also loads the module)
         cudaEventRecord(e0, in->st);
         if (step1d(in, steps, 0)) continue;
@@ -2440,7 +2477,6 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     cudaEventDestroy(e1);
     ctx->prof = prof;
     cudaError_t err = cudaGetLastError();
-    if (in->lost) return fail(QSG_ERR_CUDA, "qsg_autotune_1d: a plan switch failed; the instance needs qsg_set_psi");
     QSG_CUDA(cudaStreamSynchronize(in->st));
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     in->snorm_valid = false;
@@ -2497,6 +2533,7 @@ struct qsg_batch {
     cudaGraphExec_t gexec = nullptr;
     uint64_t gsteps = 0;
     std::map<std::string, uint64_t> glaunches;  // launches per kernel name in the graph
+    bool broken = false;  // a plan switch failed half-way: the descriptors cannot be trusted
 };
 
 static void batch_free(qsg_batch *b)
@@ -2778,6 +2815,7 @@ extern "C" {
 int qsg_batch_step(qsg_batch *b, uint64_t nsteps)
 {
     if (!b) return fail(QSG_ERR_ARG, "qsg_batch_step: null batch");
+    if (b->broken) return fail(QSG_ERR_STATE, "qsg_batch_step: a failed plan switch left the batch unusable");
     if (nsteps == 0) return QSG_OK;
     qsg_ctx *ctx = b->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -2850,8 +2888,15 @@ int batch_class_plan(qsg_batch *b, qsg_batch::Class &c, const qsg_plan1d &p)
     QSG_CUDA(cudaStreamSynchronize(c.st));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     int rc;
-    for (int m : c.members)
-        if ((rc = apply_plan_1d(b->insts[m], p))) return rc;
+    const qsg_plan1d was = b->insts[c.members[0]]->plan1d;
+    for (size_t k = 0; k < c.members.size(); ++k) {
+        if ((rc = apply_plan_1d(b->insts[c.members[k]], p))) {
+            // put the members switched so far back, so that the class's descriptors stay right
+            const std::string msg = g_last_error;
+            for (size_t j = 0; j < k; ++j) apply_plan_1d(b->insts[c.members[j]], was);
+            return fail(rc, msg);
+        }
+    }
     std::vector<qsg::FsInst> h(c.members.size());
     std::vector<qsg_inst *> mi(c.members.size());
     for (size_t k = 0; k < c.members.size(); ++k) {
@@ -2864,7 +2909,13 @@ int batch_class_plan(qsg_batch *b, qsg_batch::Class &c, const qsg_plan1d &p)
         h[k].ktab[0] = in->ktab[0];
         h[k].ktab[1] = in->ktab[1];
     }
-    QSG_CUDA(cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice));
+    const cudaError_t e = cudaMemcpy(c.d_desc, h.data(), sizeof(qsg::FsInst) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        // the class's descriptors may name released tables: the batch cannot step any more
+        cudaGetLastError();
+        b->broken = true;
+        return fail(QSG_ERR_CUDA, std::string("batch plan switch: ") + cudaGetErrorString(e));
+    }
     if (c.d_maps) cudaFreeAsync(c.d_maps, ctx->st);
     size_t mb = 0;
     c.d_maps = fs_make_maps(ctx, mi.data(), mi.size(), &mb);
@@ -2893,6 +2944,7 @@ int qsg_batch_get_plan_1d(qsg_batch *b, uint64_t n, qsg_plan1d *out)
 int qsg_batch_set_plan_1d(qsg_batch *b, uint64_t n, const qsg_plan1d *p)
 {
     if (!b || !p) return fail(QSG_ERR_ARG, "qsg_batch_set_plan_1d: null argument");
+    if (b->broken) return fail(QSG_ERR_STATE, "qsg_batch_set_plan_1d: a failed plan switch left the batch unusable");
     std::lock_guard<std::mutex> lk(b->ctx->mu);
     QSG_CUDA(cudaSetDevice(b->ctx->dev));
     qsg_batch::Class *c = batch_class(b, n);
@@ -2907,6 +2959,7 @@ int qsg_batch_set_plan_1d(qsg_batch *b, uint64_t n, const qsg_plan1d *p)
 int qsg_batch_autotune(qsg_batch *b, int trial_steps, double *ms_per_step)
 {
     if (!b) return fail(QSG_ERR_ARG, "qsg_batch_autotune: null batch");
+    if (b->broken) return fail(QSG_ERR_STATE, "qsg_batch_autotune: a failed plan switch left the batch unusable");
     if (trial_steps < 1) trial_steps = 4;
     qsg_ctx *ctx = b->ctx;
     std::lock_guard<std::mutex> lk(ctx->mu);

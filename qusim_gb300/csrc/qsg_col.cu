@@ -114,7 +114,7 @@ bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
     g->kin_threads = g->kin_w * (g->m / g->kin_e);
     g->kin_smem = (size_t)csz * col_tile_elems(csz, g->m, g->kin_w);
     const size_t smem_max = 227 * 1024 - 1024;
-    return g->row_threads <= 512 && g->col_threads <= 512 && g->kin_threads <= 512 &&
+    return g->row_threads <= 1024 && g->col_threads <= 512 && g->kin_threads <= 512 &&
            g->row_smem <= smem_max && g->col_smem <= smem_max && g->kin_smem <= smem_max &&
            g->m >= 128 && g->m <= 2048;
 }
@@ -125,7 +125,7 @@ int candidate_plans(int prec, int nx, int ny, Plan2D *out, int cap)
     const int es[2] = {16, 8};
     const int ces[3] = {16, 8, 32};
     const int ws[5] = {4, 8, 16, 32, 2};
-    const int nts[2] = {512, 256};
+    const int nts[3] = {512, 256, 1024};
     for (int g = 1; g <= 4; g *= 2)
         for (int re : es)
             for (int nt : nts)

@@ -197,7 +197,8 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
     constexpr bool via_smem_in = in_split && G > 1;
     const bool via_smem_out = out_split && G > 1;
     constexpr int XV = B * NY / NT;                       // x-split columns per thread
-    constexpr bool XPF = via_smem_in && XV * G <= 32;     // split-k input held in registers
+    // split-k input held in registers (not with 1024 threads: 64 registers per thread)
+    constexpr bool XPF = via_smem_in && XV * G <= 32 && NT <= 512;
     C pf[XPF ? XV : 1][G];
     // issue the loads of unit uu's split-k input (consumed by the next x-split
     // stage).  Every path defines pf (zeros when !live), so the consumed values
@@ -301,19 +302,25 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
                 if (vt) {
                     const C *vr = opaque(vt) + (size_t)row * NY + t;
                     // all loads first, then the multiplies: interleaved, the
-                    // schedule exposed the load latency (152 vs 168 us at 4096^2)
-                    C mv[E];
+                    // schedule exposed the load latency (152 vs 168 us at 4096^2);
+                    // with 1024 threads in chunks of 8 (registers)
+                    constexpr int VC = NT > 512 && E > 8 ? 8 : E;
 #pragma unroll
-                    for (int e = 0; e < E; ++e) mv[e] = ld_stream(vr + e * TL);
-                    if (sizeof(C) == 8 && a.vdiff) {
+                    for (int e0 = 0; e0 < E; e0 += VC) {
+                        C mv[VC];
 #pragma unroll
-                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::increment(x[e], mv[e], a.vtwice);
-                    } else if (a.vtwice) {
+                        for (int e = 0; e < VC; ++e) mv[e] = ld_stream(vr + (e0 + e) * TL);
+                        if (sizeof(C) == 8 && a.vdiff) {
 #pragma unroll
-                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(PhaseOps<C>::apply(x[e], mv[e]), mv[e]);
-                    } else {
+                            for (int e = 0; e < VC; ++e) x[e0 + e] = PhaseOps<C>::increment(x[e0 + e], mv[e], a.vtwice);
+                        } else if (a.vtwice) {
 #pragma unroll
-                        for (int e = 0; e < E; ++e) x[e] = PhaseOps<C>::apply(x[e], mv[e]);
+                            for (int e = 0; e < VC; ++e)
+                                x[e0 + e] = PhaseOps<C>::apply(PhaseOps<C>::apply(x[e0 + e], mv[e]), mv[e]);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < VC; ++e) x[e0 + e] = PhaseOps<C>::apply(x[e0 + e], mv[e]);
+                        }
                     }
                 }
             }
@@ -340,6 +347,13 @@ __device__ __forceinline__ void row_pass_units(const RowPassArgs &a, unsigned ch
     // the next unit's split-k input is in flight while this unit's results go out
     if (via_smem_out) cbar();
     if constexpr (XPF) xs_load(unext, unext < a.units);
+    if constexpr (via_smem_in && !XPF && NT > 512) {
+        // 1024 threads hold no next-unit input in registers: its rows go to L2 instead
+        if (tid < G && unext < a.units) {
+            for (int bb = 0; bb < B; ++bb)
+                prefetch_l2_bulk(in + (size_t)(tid * a.m + unext * B + bb) * NY, NY * (unsigned)sizeof(C));
+        }
+    }
     if (via_smem_out) {
         if constexpr (G > 1) {
 #pragma unroll 2

@@ -210,7 +210,7 @@ def test_evolver_api_mirror(qsg):
                          BoundaryCondition.Period, SolverMethod.SplittingMethodO2, 1, 1, Options())
 
 
-@pytest.mark.parametrize("nx,ny", [(4096, 128), (2048, 256), (256, 1024), (512, 2048)])
+@pytest.mark.parametrize("nx,ny", [(4096, 128), (2048, 256), (256, 1024), (512, 2048), (1024, 4096)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_every_plan_matches_oracle(qsg, ctx, oracle, nx, ny, precision):
     hx, hy = 0.05 * nx, 0.05 * ny

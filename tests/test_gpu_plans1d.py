@@ -179,3 +179,40 @@ def test_batch_autotune_keeps_states_and_matches_solo(qsg, ctx):
         b.plan(4096)
     assert e.value.code == 1
     b.close()
+
+
+def test_failed_plan_switch_keeps_the_old_plan(qsg, ctx, monkeypatch):
+    """A 1D plan switch that fails after making the new plan's tables (failure
+    injected on the host, QSG_FAIL_PLAN_SWITCH) leaves the instance on its old
+    plan and state: it then steps bit for bit as an instance never switched.
+    In a batch, the failing class stays whole."""
+    n = 65536
+    psi0, V, dx = packet(n)
+    a = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01, order=4, precision="mixed")
+    ref = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01, order=4, precision="mixed")
+    a.step(2)
+    ref.step(2)
+    keep = a.plan().as_tuple()
+    other = next(p for p in qsg.candidate_plans_1d("mixed", n) if p.as_tuple() != keep)
+    bytes_before = ctx.bytes_in_use()
+    monkeypatch.setenv("QSG_FAIL_PLAN_SWITCH", "1")
+    with pytest.raises(qsg.QsgError) as e:
+        a.set_plan(other)
+    assert e.value.code == 3 and "injected" in str(e.value)
+    b = qsg.Batch(ctx, [psi0, psi0], [V, V], [dx, dx], [0.01, 0.01], order=4, precision="mixed")
+    with pytest.raises(qsg.QsgError):
+        b.set_plan(n, other)
+    monkeypatch.delenv("QSG_FAIL_PLAN_SWITCH")
+    assert a.plan().as_tuple() == keep and b.plan(n).as_tuple() == keep
+    a.step(3)
+    ref.step(3)
+    assert np.array_equal(a.get_psi(), ref.get_psi())
+    b.step(5)
+    ref5 = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01, order=4, precision="mixed")
+    ref5.step(5)  # one call of 5 steps, as the batch's
+    assert np.array_equal(b.instance(0).get_psi(), ref5.get_psi())
+    ref5.close()
+    b.close()
+    assert ctx.bytes_in_use() <= bytes_before
+    a.set_plan(other)  # and the switch itself still works
+    assert a.plan().as_tuple() == other.as_tuple()
