@@ -306,6 +306,10 @@ int compile(const char *src, const std::map<std::string, int> &vars, Program &p,
 
 template <class Cx> __host__ __device__ inline Cx cx_of(double2 v) { return Cx(v.x, v.y); }
 
+// One body for both sides: instantiated with std::complex and HostMath on the
+// host, with cuda::std::complex and DevMath in the sampling kernel; the check of
+// host calls from a host-device function does not apply to the host instance.
+#pragma nv_exec_check_disable
 template <class Cx, class M>
 __host__ __device__ inline Cx run(const Program &p, const Cx *vars)
 {
