@@ -809,6 +809,23 @@ int upload_factors(qsg_inst *in, const std::vector<std::complex<long double>> &s
 
 // --- 1D plans ----------------------------------------------------------------
 
+// The timing resources of a tuner, given back on every path out: its two
+// events, and the context's profiling mode (off while it times).
+struct TuneGuard {
+    qsg_ctx *ctx;
+    int prof;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    explicit TuneGuard(qsg_ctx *c) : ctx(c), prof(c->prof) { c->prof = 0; }
+    ~TuneGuard()
+    {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        ctx->prof = prof;
+    }
+    TuneGuard(const TuneGuard &) = delete;
+    TuneGuard &operator=(const TuneGuard &) = delete;
+};
+
 // four-step plans of a stepped length n: the default split first, then the
 // others from the longest rows down, each with and without tensor-copy columns
 void add_fs_plans(int prec, uint64_t n, bool tma_ok, std::vector<qsg_plan1d> &out)
@@ -2360,11 +2377,10 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
     if ((rc = ensure_scratch(ctx, bytes))) return rc;
     QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     const Plan2D keep = in->plan;
-    const int prof = ctx->prof;
-    ctx->prof = 0;
-    cudaEvent_t e0, e1;
-    QSG_CUDA(cudaEventCreate(&e0));
-    QSG_CUDA(cudaEventCreate(&e1));
+    TuneGuard g(ctx);
+    QSG_CUDA(cudaEventCreate(&g.e0));
+    QSG_CUDA(cudaEventCreate(&g.e1));
+    cudaEvent_t e0 = g.e0, e1 = g.e1;
     double best_ms = 1e30;
     Plan2D best_p = keep;
     for (const Plan2D &p : cands) {
@@ -2382,9 +2398,6 @@ int qsg_autotune(qsg_inst *in, int trial_steps, int persist, qsg_plan2d *best, d
             best_p = p;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ctx->prof = prof;
     cudaError_t err = cudaGetLastError();
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     in->pending = false;  // the restored copy is the settled state
@@ -2451,11 +2464,10 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     const qsg_plan1d keep = in->plan1d;
-    const int prof = ctx->prof;
-    ctx->prof = 0;
-    cudaEvent_t e0, e1;
-    QSG_CUDA(cudaEventCreate(&e0));
-    QSG_CUDA(cudaEventCreate(&e1));
+    TuneGuard g(ctx);
+    QSG_CUDA(cudaEventCreate(&g.e0));
+    QSG_CUDA(cudaEventCreate(&g.e1));
+    cudaEvent_t e0 = g.e0, e1 = g.e1;
     double best_ms = 1e30;
     qsg_plan1d best_p = keep;
     for (const qsg_plan1d &p : cands) {
@@ -2473,9 +2485,6 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
             best_p = p;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ctx->prof = prof;
     cudaError_t err = cudaGetLastError();
     QSG_CUDA(cudaStreamSynchronize(in->st));
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
@@ -2965,13 +2974,15 @@ int qsg_batch_autotune(qsg_batch *b, int trial_steps, double *ms_per_step)
     std::lock_guard<std::mutex> lk(ctx->mu);
     QSG_CUDA(cudaSetDevice(ctx->dev));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
-    const int prof = ctx->prof;
-    ctx->prof = 0;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    QSG_CUDA(cudaEventCreate(&e0));
-    QSG_CUDA(cudaEventCreate(&e1));
+    TuneGuard g(ctx);
+    QSG_CUDA(cudaEventCreate(&g.e0));
+    QSG_CUDA(cudaEventCreate(&g.e1));
+    auto check = [](cudaError_t e, const char *what) -> int {
+        if (e == cudaSuccess) return QSG_OK;
+        cudaGetLastError();
+        return fail(QSG_ERR_CUDA, std::string("qsg_batch_autotune: ") + what + ": " + cudaGetErrorString(e));
+    };
     double total = 0;
-    int rc = QSG_OK;
     for (auto &c : b->classes) {
         qsg_inst *proto = b->insts[c.members[0]];
         if (!proto->fourstep) continue;
@@ -2985,45 +2996,42 @@ int qsg_batch_autotune(qsg_batch *b, int trial_steps, double *ms_per_step)
             std::max<uint64_t>((uint64_t)trial_steps, ((uint64_t)1 << 22) / (c.n * (uint64_t)ninst));
         // the trials evolve the members' states: keep copies
         const size_t bytes = proto->n * csize(proto->prec);
-        if ((rc = ensure_scratch(ctx, bytes * ninst))) break;
+        int rc = ensure_scratch(ctx, bytes * ninst);
+        if (rc) return rc;
         unsigned char *keep = static_cast<unsigned char *>(ctx->scratch);
-        for (int k = 0; k < ninst; ++k)
-            QSG_CUDA(cudaMemcpyAsync(keep + k * bytes, b->insts[c.members[k]]->psi, bytes, cudaMemcpyDeviceToDevice,
-                                     ctx->st));
-        QSG_CUDA(cudaStreamSynchronize(ctx->st));
-        const qsg_plan1d start = proto->plan1d;
-        qsg_plan1d best_p = start;
+        for (int k = 0; k < ninst && !rc; ++k)
+            rc = check(cudaMemcpyAsync(keep + k * bytes, b->insts[c.members[k]]->psi, bytes, cudaMemcpyDeviceToDevice,
+                                       ctx->st), "copy of a state");
+        if (!rc) rc = check(cudaStreamSynchronize(ctx->st), "copy of the states");
+        if (rc) return rc;
+        qsg_plan1d best_p = proto->plan1d;
         double best_ms = 1e30;
         for (const qsg_plan1d &p : cands) {
             if (!same_plan1d(p, proto->plan1d) && (rc = batch_class_plan(b, c, p))) break;
             if ((rc = step_fs(proto, c.d_desc, ninst, 1, c.st, c.d_maps))) break;  // warm-up
-            cudaEventRecord(e0, c.st);
+            cudaEventRecord(g.e0, c.st);
             if ((rc = step_fs(proto, c.d_desc, ninst, steps, c.st, c.d_maps))) break;
-            cudaEventRecord(e1, c.st);
-            if (cudaEventSynchronize(e1) != cudaSuccess) {
-                rc = fail(QSG_ERR_CUDA, "qsg_batch_autotune: trial failed");
-                break;
-            }
+            cudaEventRecord(g.e1, c.st);
+            if ((rc = check(cudaEventSynchronize(g.e1), "trial"))) break;
             float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventElapsedTime(&ms, g.e0, g.e1);
             if (ms / steps < best_ms) {
                 best_ms = ms / steps;
                 best_p = p;
             }
         }
         if (!rc && !same_plan1d(best_p, proto->plan1d)) rc = batch_class_plan(b, c, best_p);
-        QSG_CUDA(cudaStreamSynchronize(c.st));
-        for (int k = 0; k < ninst; ++k)
-            QSG_CUDA(cudaMemcpyAsync(b->insts[c.members[k]]->psi, keep + k * bytes, bytes, cudaMemcpyDeviceToDevice,
-                                     ctx->st));
-        QSG_CUDA(cudaStreamSynchronize(ctx->st));
-        if (rc) break;
+        // the states go back whatever happened above
+        const std::string msg = rc ? g_last_error : std::string();
+        int rc2 = check(cudaStreamSynchronize(c.st), "trial stream");
+        for (int k = 0; k < ninst && !rc2; ++k)
+            rc2 = check(cudaMemcpyAsync(b->insts[c.members[k]]->psi, keep + k * bytes, bytes, cudaMemcpyDeviceToDevice,
+                                        ctx->st), "restore of a state");
+        if (!rc2) rc2 = check(cudaStreamSynchronize(ctx->st), "restore of the states");
+        if (rc) return fail(rc, msg);
+        if (rc2) return rc2;
         total += best_ms;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    ctx->prof = prof;
-    if (rc) return rc;
     if (ms_per_step) *ms_per_step = total;
     return QSG_OK;
 }
