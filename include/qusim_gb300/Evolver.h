@@ -151,7 +151,7 @@ inline int device_precision(Options const &o)
 {
     const std::string dev = o.GetString("device", "CPU_SEQ");
     if (dev != "GPU_GB300")
-        throw std::invalid_argument("invalid device: " + dev + " (this build serves GPU_GB300; use Options().Gb300())");
+        throw std::invalid_argument("invalid device: " + dev + " (this library serves GPU_GB300; use Options().Gb300())");
     const std::string p = o.GetString("precision", "fp64");
     if (p == "fp64") return QSG_FP64;
     if (p == "mixed") return QSG_MIXED;
