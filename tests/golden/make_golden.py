@@ -97,6 +97,10 @@ def main():
         ("evolve2d_256x128_o4_20", 256, 128, 30.0, 30.0, 4, 0.02, 20, 1, False),
         ("evolve2d_128x128_o4_b5x2_fnes", 128, 128, 10.0, 20.0, 4, 0.01 - 0.002j, 5, 2, True),
         ("evolve2d_128x256_o4_hbar07_m2", 128, 256, 20.0, 40.0, 4, 0.02, 20, 1, False, 2.0, 0.7),
+        # sides that are not powers of two: KISS radices 3, 5 (45) and 2, 5, 7 (70, a generic
+        # radix-7 butterfly); 96 x 50 mixes a power-of-two-free side with radix 3 and 2
+        ("evolve2d_45x70_o2_30", 45, 70, 9.0, 14.0, 2, 0.02, 30, 1, False),
+        ("evolve2d_96x50_o4_10", 96, 50, 12.0, 10.0, 4, 0.02, 10, 1, False),
     ]
     for case in cases_2d:
         name, nx, ny, hx, hy, order, dt, batch, calls, fnes = case[:10]
