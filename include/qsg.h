@@ -98,11 +98,13 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
  * boundary: QSG_PERIOD, or QSG_INFINITE_WALL (psi_0 = psi_n = 0, kinetic step
- * through the 2n odd extension, src/SplittingMethod1D.cpp:61-81) for
- * n = 64 .. 131072: one CTA holds the 2n extension up to n = 4096 (QSG_MIXED)
- * / 2048 (QSG_FP64); above that the instance keeps the 2n odd extension in
- * HBM and steps it with the four-step passes of a periodic 2n grid (reads and
- * writes of psi still cover its n sites).
+ * through the 2n odd extension, src/SplittingMethod1D.cpp:61-81): for powers
+ * of two from 64, one CTA holds the 2n extension up to n = 4096 (QSG_MIXED) /
+ * 2048 (QSG_FP64); above that, up to n = 131072, the instance keeps the 2n odd
+ * extension in HBM and steps it with the four-step passes of a periodic 2n
+ * grid; any other n from 2 to 2048 (QSG_MIXED) / 1024 (QSG_FP64) keeps the 2n
+ * extension in one CTA stepped by Bluestein transforms.  Reads and writes of
+ * psi cover its n sites.
  * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
  * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,

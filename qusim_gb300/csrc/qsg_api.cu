@@ -319,6 +319,8 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         a.n = (int)in->n;
         a.order = in->order;
         a.renormalize = renorm;
+        a.wall_n = in->wall_ext ? (int)in->n_out : 0;
+        a.norm_n = (int)user_n(in);
         ProfScope ps(ctx, "evolve1d_blue", in->st);
         QSG_CUDA(qsg::launch_evolve1d_blue(in->prec, in->blue_m, a, in->st));
         return QSG_OK;
@@ -849,7 +851,12 @@ void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
     if (prec != QSG_FP64 && prec != QSG_MIXED) return;
     const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
     if (boundary == QSG_INFINITE_WALL) {
-        if (!pow2 || n < 64 || n > 131072) return;
+        if (!pow2 || n < 64) {
+            // any other length: one Bluestein kernel on the 2n odd extension
+            if (n >= 2 && qsg::blue_m_for(prec, 2 * n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+            return;
+        }
+        if (n > 131072) return;
         if (qsg::wall1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
         else add_fs_plans(prec, 2 * n, false, out);  // the periodic 2n odd extension
         return;
@@ -1560,19 +1567,23 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
         return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
     const bool wall = boundary == QSG_INFINITE_WALL;
     const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
-    if (wall && !pow2)
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) +
-                                             " (supported: powers of two, 64 .. 131072)");
+    // walls of any other length (and powers of two below 64): the 2n odd
+    // extension stepped by one Bluestein kernel
+    const bool wall_blue = wall && (!pow2 || n < 64);
+    const std::string wall_limits = std::string(" (supported: any n from 2 to ") +
+                                    (precision == QSG_MIXED ? "2048" : "1024") + ", and powers of two up to 131072)";
+    if (wall_blue && (n < 2 || !qsg::blue_m_for(precision, 2 * n)))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     // walls above one CTA: a four-step periodic instance of the 2n odd extension
-    const bool wall_ext = wall && !qsg::wall1d_supported(precision, n);
+    const bool wall_ext = wall && (wall_blue || !qsg::wall1d_supported(precision, n));
     // periodic lengths that are not powers of two (and powers of two below the
     // one-CTA kernels' 64): Bluestein transforms of length blue_m
-    const int blue_m = !wall && (!pow2 || n < 64) ? qsg::blue_m_for(precision, n) : 0;
+    const int blue_m = wall_blue ? qsg::blue_m_for(precision, 2 * n)
+                                 : (!wall && (!pow2 || n < 64) ? qsg::blue_m_for(precision, n) : 0);
     qsg::FsGeom fsg{};
-    const bool resident = wall ? !wall_ext : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
-    if (wall_ext && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) +
-                                             " (supported: powers of two, 64 .. 131072)");
+    const bool resident = wall ? (wall_blue || !wall_ext) : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
+    if (wall_ext && !wall_blue && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     if (!wall && !pow2 && !blue_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) + " (lengths that are not powers of "
                                              "two: 2 .. " + (precision == QSG_MIXED ? "4096" : "2048") + ")");
@@ -2105,6 +2116,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
                 ba.w = in->bw;
                 ba.hs = in->bhs;
                 ba.n = (int)in->n;
+                ba.wall_n = in->wall_ext ? (int)in->n_out : 0;
                 QSG_CUDA(qsg::launch_kinetic1d_blue(in->prec, in->blue_m, ba, DT, ctx->sums, ctx->st));
             } else if (in->boundary == QSG_INFINITE_WALL && !in->wall_ext) {
                 // wall branch: Dk = pi/(dx N), DT = (Dk hbar)^2/(2m) (src/SplittingMethod1D.cpp:117-119)

@@ -41,6 +41,11 @@ struct BlueArgs {
     uint64_t nsteps;
     int n;                  // line length
     int order, renormalize;
+    int wall_n;             // InfiniteWall as the 2 wall_n odd extension (n = 2 wall_n): sites 0 and
+                            // wall_n are zeroed before each forward transform, as the reference's
+                            // wall ExpT and KinEn discard them (src/SplittingMethod1D.cpp:63-65,
+                            // 112-114); 0 for a periodic line
+    int norm_n;             // sites the norm sums (the wall's n), 0: all n
 };
 
 // 1D resident evolution of one instance of any length n (2n - 1 <= M)
@@ -89,6 +94,13 @@ __global__ void __launch_bounds__(M / E) k_evolve1d_blue(BlueArgs a)
     // (conj(FFT(conj z)) is the unnormalised inverse; the conjugations around the
     // kinetic product cancel into one conjugated factor)
     auto apply_t = [&](const C *kt) {
+        if (a.wall_n) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int j = t + e * TL;
+                if (j == 0 || j == a.wall_n) x[e] = cmk<C>(0, 0);
+            }
+        }
 #pragma unroll 1
         for (int ph = 0; ph < 4; ++ph) {
             if (ph == 0) {
@@ -119,10 +131,11 @@ __global__ void __launch_bounds__(M / E) k_evolve1d_blue(BlueArgs a)
         }
     }
     double nsum = 0;
+    const int nn = a.norm_n ? a.norm_n : n;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int j = t + e * TL;
-        if (j < n) nsum += abs2d(x[e]);
+        if (j < nn) nsum += abs2d(x[e]);
     }
     if (a.norm_out || a.renormalize) {
         __shared__ double red[32];
@@ -161,7 +174,8 @@ __global__ void __launch_bounds__(M / E) k_kinetic1d_blue(BlueArgs a, double dtk
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const int j = t + e * TL;
-        x[e] = j < n ? cmul(psi[j], ld_c(w + j)) : cmk<C>(0, 0);
+        const bool zero = j >= n || (a.wall_n && (j == 0 || j == a.wall_n));
+        x[e] = zero ? cmk<C>(0, 0) : cmul(psi[j], ld_c(w + j));
     }
     // FFT -> conj(. hs) -> FFT: X_k = w_k conj(result_k), |X_k| = |result_k|
     const tw_t<C> *tw = static_cast<const tw_t<C> *>(a.tw);

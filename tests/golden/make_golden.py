@@ -77,6 +77,8 @@ def main():
          2.0, 0.7),
         ("evolve1d_n512_o4_wall_hbar07_m2", 512, -40.0, 40.0, 1.0, -10.0, 3.0, 4, True, 0.02, 60, 1, False,
          2.0, 0.7),
+        # a wall of a length that is not a power of two: KISS transforms of 2n = 1200
+        ("evolve1d_n600_o4_wall", 600, -40.0, 40.0, 1.0, -10.0, 3.0, 4, True, 0.02, 40, 1, False),
     ]
     for case in cases_1d:
         name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes = case[:13]

@@ -57,7 +57,7 @@ def run_1d(qsg, ctx, g, precision):
 # src/SplittingMethod1D.cpp:101-102; the wall and 2D ones use (Dk hbar)^2 / 2m)
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1024_o2_hbar07_m2",
-             "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2"]
+             "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2", "evolve1d_n600_o4_wall"]
 GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
              "evolve2d_128x256_o4_hbar07_m2", "evolve2d_45x70_o2_30",
              "evolve2d_96x50_o4_10"]
@@ -169,8 +169,8 @@ def test_unsupported_sizes_are_reported(qsg, ctx):
         qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, precision="fp64")
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:1000], V[:1000], dx, 0.02,
-                               boundary=qsg.BoundaryCondition.InfiniteWall)
+        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02,
+                               boundary=qsg.BoundaryCondition.InfiniteWall, precision="mixed")
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:512], V[:512], dx, 0.02, order=3)
@@ -350,16 +350,69 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 
 def test_wall_limits_are_reported(qsg, ctx):
-    """InfiniteWall: powers of two 64 .. 131072 (the 2n extension of the largest
-    fits the four-step passes' 262144 sites)."""
+    """InfiniteWall: powers of two up to 131072 (the 2n extension of the largest
+    fits the four-step passes' 262144 sites) and any other length up to 2048
+    (complex64) / 1024 (complex128), whose 2n extension one Bluestein kernel holds."""
     wall = qsg.BoundaryCondition.InfiniteWall
     psi0, V, dx = gauss_packet_1d(262144, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:32], V[:32], dx, 0.02, boundary=wall)
+        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, boundary=wall, precision="mixed")
     assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:1500], V[:1500], dx, 0.02, boundary=wall, precision="fp64")
+    assert e.value.code == 5
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
+    assert e.value.code == 5
+
+
+@pytest.mark.parametrize("n", [2, 3, 10, 32, 100, 600, 1000, 2047])
+@pytest.mark.parametrize("order", [2, 4])
+def test_wall_any_length_vs_oracle(qsg, ctx, oracle, n, order):
+    """InfiniteWall at lengths that are not powers of two (and powers of two below
+    64): the reference's wall ExpT (src/SplittingMethod1D.cpp:61-81) on its KISS
+    transforms of length 2n, here the 2n odd extension in one Bluestein kernel.
+    Against the oracle: complex128 <= 1e-12 with the wall KinEn and PotEn at 1e-11
+    (complex128 up to n = 1024), complex64 <= 1e-5; hbar = 0.7, m = 2."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    L = max(6.0, 0.1 * n)
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.2, -0.2 * L, max(0.1 * L, 2 * 2 * L / n), barrier=0.6)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02, 12, order=order, mass=2.0, hbar=0.7, wall=True)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        if precision == "fp64" and n > 1024:
+            continue
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision, boundary=wall,
+                                      mass=2.0, hbar=0.7)
+        assert inst.plan().as_tuple() == (0, 0, 0)
+        inst.step(5)
+        inst.step(7)
+        got = inst.get_psi()
+        assert got.shape == (n,)
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        if precision == "fp64":
+            kin, pot = inst.energies()
+            kr = oracle.kinen1d(ref, dx, mass=2.0, hbar=0.7, wall=True)
+            assert abs(kin - kr) <= 1e-11 * abs(kr)
+            assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-11 * max(1.0, abs(pot))
+            assert abs(inst.norm2() - oracle.norm2(ref, dx)) <= 1e-12
+        inst.close()
+
+
+def test_wall_any_length_renormalising_and_set_psi(qsg, ctx, oracle):
+    """A renormalising wall of odd length and its set_psi (the extension rebuilt)."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    n = 777
+    psi0, V, dx = gauss_packet_1d(n, -40, 40, 1.0, -8.0, 3.0, barrier=0.5)
+    ref = oracle.evolve1d(psi0 * 1.3, V, dx, 0.01 - 0.002j, 9, order=2, wall=True, renormalize=True)
+    inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=2, precision="fp64", boundary=wall)
+    inst.step(3)
+    inst.set_psi(psi0 * 1.3)
+    inst.step(9, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1.0) <= 1e-13
 
 
 @pytest.mark.parametrize("nx,ny", [(512, 4096), (1024, 2048)])

@@ -59,4 +59,10 @@ def test_wall_plans(q):
     assert plans and all(k == 1 and t == 0 for k, _, t in plans)
     assert {n1 for _, n1, _ in plans} == {n1 for k, n1, _ in tuples(q, "mixed", 131072) if k == 1}
     assert tuples(q, "mixed", 262144, WALL) == []
-    assert tuples(q, "mixed", 1000, WALL) == []
+    # any other length: one Bluestein kernel on the 2n extension (2n - 1 <= 8192 / 4096)
+    assert tuples(q, "mixed", 1000, WALL) == [(0, 0, 0)]
+    assert tuples(q, "mixed", 32, WALL) == [(0, 0, 0)]
+    assert tuples(q, "mixed", 2048, WALL) == [(0, 0, 0)]
+    assert tuples(q, "mixed", 3000, WALL) == []
+    assert tuples(q, "fp64", 1500, WALL) == []
+    assert tuples(q, "mixed", 1, WALL) == []
