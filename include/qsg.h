@@ -92,8 +92,8 @@ void *qsg_ctx_stream(qsg_ctx *ctx);
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
 
 /* Create a 1D instance: n a power of two, 64 .. 262144, or any other length
- * from 2 to 4096 (QSG_MIXED) / 2048 (QSG_FP64), stepped through Bluestein
- * transforms (as are the powers of two below 64).  psi0: n complex (re,im); V: n real (the reference keeps
+ * from 2 to 4096, stepped through Bluestein transforms (as are the powers
+ * of two below 64).  psi0: n complex (re,im); V: n real (the reference keeps
  * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
@@ -102,8 +102,8 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * of two from 64, one CTA holds the 2n extension up to n = 4096 (QSG_MIXED) /
  * 2048 (QSG_FP64); above that, up to n = 131072, the instance keeps the 2n odd
  * extension in HBM and steps it with the four-step passes of a periodic 2n
- * grid; any other n from 2 to 2048 (QSG_MIXED) / 1024 (QSG_FP64) keeps the 2n
- * extension in one CTA stepped by Bluestein transforms.  Reads and writes of
+ * grid; any other n from 2 to 2048 keeps the 2n extension in one CTA stepped
+ * by Bluestein transforms.  Reads and writes of
  * psi cover its n sites.
  * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
  * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
@@ -114,8 +114,8 @@ int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
 /* Create a 2D instance, nx*ny sites, index iy + ix*ny.  Periodic only, as in
  * the reference (src/SplittingMethod2D.cpp:21-29).  Sides that are powers of
  * two (128 .. 4096) run the split-k passes with plans; a grid with a
- * side that is not a power of two (each side 2 .. 4096 for QSG_MIXED, 2 ..
- * 2048 for QSG_FP64) runs row and column passes of Bluestein transforms.
+ * side that is not a power of two (each side 2 .. 4096) runs row and column
+ * passes of Bluestein transforms.
  * Replaces SplittingMethod2D::InitSystem2D (src/SplittingMethod2D.cpp:5-31). */
 int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
                   double hbar, double dt_re, double dt_im, int order, int precision,

@@ -1570,8 +1570,7 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     // walls of any other length (and powers of two below 64): the 2n odd
     // extension stepped by one Bluestein kernel
     const bool wall_blue = wall && (!pow2 || n < 64);
-    const std::string wall_limits = std::string(" (supported: any n from 2 to ") +
-                                    (precision == QSG_MIXED ? "2048" : "1024") + ", and powers of two up to 131072)";
+    const std::string wall_limits = " (supported: any n from 2 to 2048, and powers of two up to 131072)";
     if (wall_blue && (n < 2 || !qsg::blue_m_for(precision, 2 * n)))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     // walls above one CTA: a four-step periodic instance of the 2n odd extension
@@ -1585,8 +1584,8 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     if (wall_ext && !wall_blue && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     if (!wall && !pow2 && !blue_m)
-        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) + " (lengths that are not powers of "
-                                             "two: 2 .. " + (precision == QSG_MIXED ? "4096" : "2048") + ")");
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
+                                             " (lengths that are not powers of two: 2 .. 4096)");
     if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (supported: powers of two, 64 .. 262144)");
@@ -1854,13 +1853,12 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
         !std::isfinite(dt_re) || !std::isfinite(dt_im))
         return fail(QSG_ERR_ARG, "qsg_create_2d: dx, dy, mass, hbar must be finite and > 0, dt finite");
     Plan2D plan{};
-    // grids without a power-of-two plan: Bluestein passes on sides up to 4096 (complex64) / 2048 (complex128)
+    // grids without a power-of-two plan: Bluestein passes on sides up to 4096
     const bool pow2_plan = nx <= 8192 && ny <= 8192 && qsg::default_plan(precision, (int)nx, (int)ny, &plan);
     const int bmx = pow2_plan ? 0 : qsg::blue_m_for(precision, nx), bmy = pow2_plan ? 0 : qsg::blue_m_for(precision, ny);
     if (!pow2_plan && (!bmx || !bmy))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" + std::to_string(ny) +
-                                             " (supported: sides 2 .. " + (precision == QSG_MIXED ? "4096" : "2048") +
-                                             ", and powers of two 128 .. 4096)");
+                                             " (supported: sides 2 .. 4096, and powers of two 128 .. 4096)");
     std::lock_guard<std::mutex> lk(ctx->mu);
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();

@@ -72,7 +72,7 @@ int blue_m_for(int prec, uint64_t n)
     if (n < 2) return 0;
     uint64_t m = 256;
     while (m < 2 * n - 1) m <<= 1;
-    return m <= (uint64_t)(prec == 1 ? 8192 : 4096) ? (int)m : 0;
+    return m <= 8192 ? (int)m : 0;
 }
 
 void blue_tables(uint64_t n, int m, std::vector<std::complex<long double>> &w,
@@ -100,7 +100,7 @@ cudaError_t launch_evolve1d_blue(int prec, int m, const BlueArgs &a, cudaStream_
     if (prec == 1) {
         switch (m) { X(float, 256) X(float, 512) X(float, 1024) X(float, 2048) X(float, 4096) X(float, 8192) default: break; }
     } else {
-        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) default: break; }
+        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) X(double, 8192) default: break; }
     }
 #undef X
     return cudaErrorNotSupported;
@@ -112,7 +112,7 @@ cudaError_t launch_kinetic1d_blue(int prec, int m, const BlueArgs &a, double dtk
     if (prec == 1) {
         switch (m) { X(float, 256) X(float, 512) X(float, 1024) X(float, 2048) X(float, 4096) X(float, 8192) default: break; }
     } else {
-        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) default: break; }
+        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) X(double, 8192) default: break; }
     }
 #undef X
     return cudaErrorNotSupported;
@@ -176,7 +176,7 @@ cudaError_t launch_row_blue(int prec, int m, const Blue2DArgs &a, cudaStream_t s
     if (prec == 1) {
         switch (m) { X(float, 256) X(float, 512) X(float, 1024) X(float, 2048) X(float, 4096) X(float, 8192) default: break; }
     } else {
-        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) default: break; }
+        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) X(double, 8192) default: break; }
     }
 #undef X
     return cudaErrorNotSupported;
@@ -189,7 +189,7 @@ cudaError_t launch_col_blue(int prec, int m, const Blue2DArgs &a, bool kinetic, 
     if (prec == 1) {
         switch (m) { X(float, 256) X(float, 512) X(float, 1024) X(float, 2048) X(float, 4096) X(float, 8192) default: break; }
     } else {
-        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) default: break; }
+        switch (m) { X(double, 256) X(double, 512) X(double, 1024) X(double, 2048) X(double, 4096) X(double, 8192) default: break; }
     }
 #undef X
     return cudaErrorNotSupported;

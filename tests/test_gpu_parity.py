@@ -160,14 +160,12 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    # lengths that are not powers of two: up to 4096 (complex64) / 2048 (complex128)
+    # lengths that are not powers of two: up to 4096
     psi0, V, dx = gauss_packet_1d(5000, -50, 50, 1.0, -10, 3.0)
-    with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision="mixed")
-    assert e.value.code == 5
-    with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, precision="fp64")
-    assert e.value.code == 5
+    for precision in ("mixed", "fp64"):
+        with pytest.raises(qsg.QsgError) as e:
+            qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision=precision)
+        assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02,
                                boundary=qsg.BoundaryCondition.InfiniteWall, precision="mixed")
@@ -175,7 +173,7 @@ def test_unsupported_sizes_are_reported(qsg, ctx):
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:512], V[:512], dx, 0.02, order=3)
     assert e.value.code == 1
-    # 2D sides that are not powers of two: up to 4096 (complex64) / 2048 (complex128)
+    # 2D sides that are not powers of two: up to 4096
     z = np.zeros((5000, 128), np.complex128)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_2d(ctx, z, z.real, 0.1, 0.1, 0.02, precision="mixed")
@@ -351,8 +349,8 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 def test_wall_limits_are_reported(qsg, ctx):
     """InfiniteWall: powers of two up to 131072 (the 2n extension of the largest
-    fits the four-step passes' 262144 sites) and any other length up to 2048
-    (complex64) / 1024 (complex128), whose 2n extension one Bluestein kernel holds."""
+    fits the four-step passes' 262144 sites) and any other length up to 2048,
+    whose 2n extension one Bluestein kernel holds."""
     wall = qsg.BoundaryCondition.InfiniteWall
     psi0, V, dx = gauss_packet_1d(262144, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
@@ -362,7 +360,7 @@ def test_wall_limits_are_reported(qsg, ctx):
         qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, boundary=wall, precision="mixed")
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:1500], V[:1500], dx, 0.02, boundary=wall, precision="fp64")
+        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, boundary=wall, precision="fp64")
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
@@ -375,15 +373,13 @@ def test_wall_any_length_vs_oracle(qsg, ctx, oracle, n, order):
     """InfiniteWall at lengths that are not powers of two (and powers of two below
     64): the reference's wall ExpT (src/SplittingMethod1D.cpp:61-81) on its KISS
     transforms of length 2n, here the 2n odd extension in one Bluestein kernel.
-    Against the oracle: complex128 <= 1e-12 with the wall KinEn and PotEn at 1e-11
-    (complex128 up to n = 1024), complex64 <= 1e-5; hbar = 0.7, m = 2."""
+    Against the oracle: complex128 <= 1e-12 with the wall KinEn and PotEn at 1e-11,
+    complex64 <= 1e-5; hbar = 0.7, m = 2."""
     wall = qsg.BoundaryCondition.InfiniteWall
     L = max(6.0, 0.1 * n)
     psi0, V, dx = gauss_packet_1d(n, -L, L, 1.2, -0.2 * L, max(0.1 * L, 2 * 2 * L / n), barrier=0.6)
     ref = oracle.evolve1d(psi0, V, dx, 0.02, 12, order=order, mass=2.0, hbar=0.7, wall=True)
     for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
-        if precision == "fp64" and n > 1024:
-            continue
         inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision, boundary=wall,
                                       mass=2.0, hbar=0.7)
         assert inst.plan().as_tuple() == (0, 0, 0)
@@ -614,13 +610,11 @@ def test_lengths_not_powers_of_two_vs_oracle(qsg, ctx, oracle, n, order):
     power-of-two length (also for the powers of two 8 and 32, below the one-CTA
     kernels' 64).  Against the oracle (bit-exact with the reference's
     KISS evolution): complex128 <= 1e-12 with Norm2, KinEn and PotEn to 1e-11,
-    complex64 <= 1e-5 (complex128 is built up to n = 2048)."""
+    complex64 <= 1e-5."""
     L = max(10.0, 0.1 * n)
     psi0, V, dx = gauss_packet_1d(n, -L, L, 1.5, -0.2 * L, max(0.08 * L, 2 * 2 * L / n), barrier=0.7)
     ref = oracle.evolve1d(psi0, V, dx, 0.02, 25, order=order)
     for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
-        if precision == "fp64" and n > 2048:
-            continue
         inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision)
         inst.step(20)
         inst.step(5)
@@ -659,15 +653,13 @@ def test_2d_grids_not_powers_of_two_vs_oracle(qsg, ctx, oracle, nx, ny, order):
     89-99) and on power-of-two sides without a compiled plan (64): Bluestein
     row and column passes in natural layout.  Against the oracle: complex128
     <= 1e-12 with Norm2, KinEn and PotEn to 1e-11; complex64 <= 1e-5 (sides up
-    to 2048 in complex128, 4096 in complex64)."""
+    to 4096)."""
     hx, hy = 0.1 * max(nx, 20), 0.1 * max(ny, 20)
     psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
                                    s=max(0.1 * min(hx, hy), 2 * max(2 * hx / nx, 2 * hy / ny)))
     V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=6, seed=4, spread=0.5 * min(hx, hy))
     ref = oracle.evolve2d(psi0, V, dx, dy, 0.02, 6, order=order)
     for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
-        if precision == "fp64" and max(nx, ny) > 2048:
-            continue
         inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.02, order=order, precision=precision)
         inst.step(4)
         inst.step(2)

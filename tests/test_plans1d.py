@@ -64,5 +64,6 @@ def test_wall_plans(q):
     assert tuples(q, "mixed", 32, WALL) == [(0, 0, 0)]
     assert tuples(q, "mixed", 2048, WALL) == [(0, 0, 0)]
     assert tuples(q, "mixed", 3000, WALL) == []
-    assert tuples(q, "fp64", 1500, WALL) == []
+    assert tuples(q, "fp64", 1500, WALL) == [(0, 0, 0)]
+    assert tuples(q, "fp64", 3000, WALL) == []
     assert tuples(q, "mixed", 1, WALL) == []
