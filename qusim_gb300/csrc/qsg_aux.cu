@@ -15,6 +15,35 @@ inline unsigned blocks_for(size_t n, int per_block = kThreads)
     return (unsigned)(b > 1048576 ? 1048576 : (b ? b : 1));
 }
 
+// sin and cos in fp64.  The phase arguments of the potential tables are small
+// (|V dt c / hbar| is 0.07 on the 4096^2 benchmark), where the Taylor series of
+// sin and cos, summed in Horner form to the y^13 / y^14 terms, is within an ulp
+// or two for |y| <= 1/4 (the first dropped terms are below 2^-56 relative) at
+// about a third of the general routine's cost; larger arguments take sincos.
+__device__ __forceinline__ void sincos_d(double y, double *s, double *c)
+{
+    if (fabs(y) > 0.25) {
+        sincos(y, s, c);
+        return;
+    }
+    const double z = y * y;
+    double ps = -1.0 / 6227020800.0;                     // -1/13!
+    ps = fma(ps, z, 1.0 / 39916800.0);                   //  1/11!
+    ps = fma(ps, z, -1.0 / 362880.0);                    // -1/9!
+    ps = fma(ps, z, 1.0 / 5040.0);                       //  1/7!
+    ps = fma(ps, z, -1.0 / 120.0);                       // -1/5!
+    ps = fma(ps, z, 1.0 / 6.0);                          //  1/3!
+    *s = fma(-y * z, ps, y);                             // y - y^3/3! + y^5/5! - ...
+    double pc = 1.0 / 87178291200.0;                     //  1/14!
+    pc = fma(pc, z, -1.0 / 479001600.0);                 // -1/12!
+    pc = fma(pc, z, 1.0 / 3628800.0);                    //  1/10!
+    pc = fma(pc, z, -1.0 / 40320.0);                     // -1/8!
+    pc = fma(pc, z, 1.0 / 720.0);                        //  1/6!
+    pc = fma(pc, z, -1.0 / 24.0);                        // -1/4!
+    pc = fma(pc, z, 0.5);                                //  1/2!
+    *c = fma(-z, pc, 1.0);                               // 1 - y^2/2! + y^4/4! - ...
+}
+
 // exp(z) and exp(z) - 1 in fp64.  The "-1" form keeps relative accuracy for
 // small |z|: re = expm1(x) - 2 e^x sin^2(y/2), im = e^x sin y.
 // A real time step (x == 0, the usual case) needs no exp / expm1, and the
@@ -23,17 +52,17 @@ inline unsigned blocks_for(size_t n, int per_block = kThreads)
 __device__ __forceinline__ double2 cexp_d(double x, double y)
 {
     double s, c;
-    sincos(y, &s, &c);
+    sincos_d(y, &s, &c);
     const double ex = x == 0.0 ? 1.0 : exp(x);
     return make_double2(ex * c, ex * s);
 }
 __device__ __forceinline__ float2 cexpm1_f(double x, double y)
 {
     double sh, ch;
-    sincos(0.5 * y, &sh, &ch);
+    sincos_d(0.5 * y, &sh, &ch);
     if (x == 0.0) return make_float2(float(-2.0 * sh * sh), float(2.0 * sh * ch));
     double s, c;
-    sincos(y, &s, &c);
+    sincos_d(y, &s, &c);
     const double ex = exp(x);
     return make_float2(float(expm1(x) - 2.0 * ex * sh * sh), float(ex * s));
 }
