@@ -92,8 +92,11 @@ void *qsg_ctx_stream(qsg_ctx *ctx);
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
 
 /* Create a 1D instance: n a power of two, 64 .. 262144, or any other length
- * from 2 to 4096, stepped through Bluestein transforms (as are the powers
- * of two below 64).  psi0: n complex (re,im); V: n real (the reference keeps
+ * from 2 to 131072, stepped through Bluestein transforms (as are the powers
+ * of two below 64): in one CTA up to n = 4096, above that as two circular
+ * convolutions of length M (the smallest power of two >= 2n - 1) on the
+ * four-step passes over a buffer of M sites whose sites from n on stay zero.
+ * psi0: n complex (re,im); V: n real (the reference keeps
  * only the real part of the potential, src/EvolverImpl1D.cpp:46).  dt is
  * complex (imaginary-time propagation allowed, include/QuSim.h:558-563).
  * order: 2 (SplittingMethodO2) or 4 (SplittingMethodO4).
@@ -322,7 +325,8 @@ int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
  *           its tiles with tensor copies instead of load instructions.
  * A wall above one CTA is stepped as its periodic 2n odd extension, so its
  * plans are the four-step plans of 2n (without tma).  Lengths that are not
- * powers of two (Bluestein) have one plan, kind 0.  Every plan computes the
+ * powers of two (Bluestein) have one plan: kind 0 up to n = 4096, else kind
+ * 1 with the default split of M.  Every plan computes the
  * same result to rounding; they differ in speed.  New instances of a size
  * take the plan qsg_autotune_1d last chose for that size and precision in
  * this context or in the plan cache file, else the default (resident where

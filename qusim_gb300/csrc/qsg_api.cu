@@ -103,6 +103,15 @@ struct qsg_inst {
     bool blue = false;
     int blue_m = 0;
     void *bw = nullptr, *bhs = nullptr;
+    // 1D periodic n above the one-CTA Bluestein lengths: Bluestein's convolutions
+    // on the four-step passes over a buffer of n = M sites (M >= 2 n_out - 1), the
+    // user's n_out sites first and zeros above; bdesc: the passes' descriptors
+    // ([0] open V / V c1, [1] K d1 / K d2, [2] V c2 / close, [3] chirp; ktab the
+    // two convolution kernels in row layout), bkw: KinEn weights fold(k)^2 DT
+    bool bfs = false;
+    qsg::FsInst *bdesc = nullptr;
+    double *bkw = nullptr;
+    const void *bchirp = nullptr, *bh1 = nullptr;  // chirp (column form) and first kernel, for KinEn
     // 2D grids with a side that is not a power of two: natural-layout Bluestein row
     // and column passes (qsg_blue.cuh); per side the transform length, chirp,
     // FFT_M(conj chirp) / M and twiddles, and per kinetic coefficient the factors
@@ -204,7 +213,7 @@ void prof_drain(qsg_ctx *ctx)
 }
 
 // sites of the state a caller sees (the first n_out of a wall extension)
-uint64_t user_n(const qsg_inst *in) { return in->wall_ext ? in->n_out : in->n; }
+uint64_t user_n(const qsg_inst *in) { return (in->wall_ext || in->bfs) ? in->n_out : in->n; }
 
 // --- steps -----------------------------------------------------------------
 
@@ -299,6 +308,40 @@ int step_fs(qsg_inst *in, const qsg::FsInst *desc, int ninst, uint64_t nsteps, c
     return QSG_OK;
 }
 
+// Bluestein four-step schedule (tables in build_bfs_tables): per kinetic
+// substep the column pass with the diagonal before it (open / V / V c2), the
+// row pass with the first kernel, the column pass with K_d, the row pass with
+// the second kernel; the call ends with the column pass of the closing factor
+// to natural order (its norm partials serve a renormalising call).
+int step_bfs(qsg_inst *in, uint64_t nsteps, cudaStream_t st)
+{
+    auto row = [&](int ksel) -> int {
+        qsg::FsRowArgs a{};
+        a.inst = in->bdesc;
+        a.tw_row = in->tw_fs_row;
+        a.ksel = ksel;
+        a.plain = 1;
+        ProfScope ps(in->ctx, "fs_row_pass", st);
+        QSG_CUDA(qsg::launch_fs_row(in->prec, in->fsg, a, 1, st));
+        return QSG_OK;
+    };
+    const int nsub = in->order == 2 ? 1 : 3;
+    int rc;
+    for (uint64_t s = 0; s < nsteps; ++s) {
+        for (int u = 0; u < nsub; ++u) {
+            // O2: V1/2 T V1/2;  O4: VC1 TD1 VC2 TD2 VC2 TD1 VC1 (V factors at step joins merged, twice)
+            if (u == 0) rc = s == 0 ? fs_col(in, in->bdesc + 0, 1, false, true, 0, false, st)
+                                    : fs_col(in, in->bdesc + 0, 1, true, true, 1, true, st);
+            else rc = fs_col(in, in->bdesc + 2, 1, true, true, 0, false, st);
+            if (rc || (rc = row(0))) return rc;
+            if ((rc = fs_col(in, in->bdesc + 1, 1, true, true, (in->order == 4 && u == 1) ? 1 : 0, false, st)))
+                return rc;
+            if ((rc = row(1))) return rc;
+        }
+    }
+    return fs_col(in, in->bdesc + 2, 1, true, false, 1, false, st);
+}
+
 int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
     qsg_ctx *ctx = in->ctx;
@@ -349,7 +392,7 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         return QSG_OK;
     }
     in->snorm_valid = false;
-    int rc = step_fs(in, in->desc, 1, nsteps, in->st, in->fs_maps);
+    int rc = in->bfs ? step_bfs(in, nsteps, in->st) : step_fs(in, in->desc, 1, nsteps, in->st, in->fs_maps);
     if (rc) return rc;
     if (renorm && in->wall_ext) {
         // Norm2 over the first n_out sites, then the whole extension scaled
@@ -863,7 +906,15 @@ void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
     }
     if (boundary != QSG_PERIOD) return;
     if (!pow2 || n < 64) {
-        if (qsg::blue_m_for(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+        if (qsg::blue_m_for(prec, n)) {
+            out.push_back(qsg_plan1d{0, 0, 0, 0});
+        } else if (n >= 2) {
+            // Bluestein on the four-step passes of the smallest power of two >= 2n - 1
+            uint64_t m = 1;
+            while (m < 2 * n - 1) m <<= 1;
+            qsg::FsGeom g;
+            if (qsg::fs_geom(prec, m, &g)) out.push_back(qsg_plan1d{1, g.n1, 0, 0});
+        }
         return;
     }
     if (qsg::evolve1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
@@ -944,6 +995,139 @@ int build_ktab_1d(qsg_inst *in)
     return QSG_OK;
 }
 
+// Tables of a Bluestein four-step instance (n_out sites in a buffer of M = in->n).
+// A kinetic substep x -> (1/n) IDFT(K DFT x) is, with the chirp w_j =
+// exp(-i pi j^2 / n) and circular convolutions C_h, C_h* by h = conj(w) and by
+// w (length M), the product W* C_h* K C_h W (the chirps between the two DFTs
+// cancel, 1/n goes into the second kernel).  A convolution is a forward
+// transform, a product in frequency, an inverse: the column pass, the row pass
+// with the kernel FFT_M(h) / M (or FFT_M(h*) / (M n)) as a plain product, the
+// next column pass.  The diagonal factors meet in the column passes in natural
+// layout: V w before the first convolution of a call ("open"), K_d between the
+// two, V merged with w* and w between substeps (plain V), w* V at the end of a
+// call ("close"); each is zero above n_out, which truncates the convolutions'
+// outputs and keeps the buffer zero there.  Values are formed in long double
+// on the host: plain complex (complex128) or factor - 1 (complex64 columns);
+// the kernels are plain complex in both.
+int build_bfs_tables(qsg_inst *in)
+{
+    const SplitConsts sc;
+    const int ntab = in->order == 2 ? 1 : 2;
+    const long double vc[2] = {in->order == 2 ? 0.5L : (long double)sc.c1, (long double)sc.c2};
+    const long double tc[2] = {in->order == 2 ? 1.0L : (long double)sc.d1, (long double)sc.d2};
+    using cl = std::complex<long double>;
+    const uint64_t n = in->n_out, M = in->n;
+    const size_t cs = csize(in->prec);
+    int rc;
+    std::vector<cl> w, hs;
+    qsg::blue_tables(n, (int)M, w, hs);  // chirp (zero above n), FFT_M(h) / M
+    std::vector<double> Vh(n);
+    QSG_CUDA(cudaMemcpyAsync(Vh.data(), in->V, n * 8, cudaMemcpyDeviceToHost, in->ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    // exp(f x) for f = a (-i dt / hbar) (ExpV: a = c, x = V; ExpT: a = d, x = fold(k)^2 DT)
+    const cl dt((long double)in->dt.real(), (long double)in->dt.imag());
+    const cl mi_dt_h = cl(0, -1) * dt / (long double)in->hbar;
+    auto phase = [&](long double a, long double x) { return std::exp(mi_dt_h * (a * x)); };
+    // upload M natural values: complex64 as factor - 1, complex128 plain
+    auto put = [&](const std::vector<cl> &v, void **dst, bool minus_one) -> int {
+        if (int r = inst_alloc(in, M * cs, dst)) return r;
+        std::vector<unsigned char> h(M * cs);
+        for (uint64_t i = 0; i < M; ++i) {
+            const cl z = (minus_one && in->prec == 1) ? v[i] - 1.0L : v[i];
+            if (in->prec == 0) {
+                const double d[2] = {(double)z.real(), (double)z.imag()};
+                std::memcpy(&h[i * cs], d, cs);
+            } else {
+                const float f[2] = {(float)z.real(), (float)z.imag()};
+                std::memcpy(&h[i * cs], f, cs);
+            }
+        }
+        QSG_CUDA(cudaMemcpyAsync(*dst, h.data(), h.size(), cudaMemcpyHostToDevice, in->ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(in->ctx->st));  // h is pageable and goes out of scope
+        return QSG_OK;
+    };
+    std::vector<cl> t(M);
+    auto fill = [&](auto f) {
+        for (uint64_t j = 0; j < M; ++j) t[j] = j < n ? f(j) : cl(0);
+    };
+    void *open = nullptr, *vc1 = nullptr, *vc2 = nullptr, *close = nullptr, *k1 = nullptr, *k2 = nullptr;
+    void *chirp = nullptr, *h1 = nullptr, *h2 = nullptr;
+    fill([&](uint64_t j) { return w[j] * phase(vc[0], Vh[j]); });
+    if ((rc = put(t, &open, true))) return rc;
+    fill([&](uint64_t j) { return phase(vc[0], Vh[j]); });
+    if ((rc = put(t, &vc1, true))) return rc;
+    fill([&](uint64_t j) { return std::conj(w[j]) * phase(vc[0], Vh[j]); });
+    if ((rc = put(t, &close, true))) return rc;
+    if (ntab == 2) {
+        fill([&](uint64_t j) { return phase(vc[1], Vh[j]); });
+        if ((rc = put(t, &vc2, true))) return rc;
+    }
+    // ExpT periodic (SplittingMethod1D.cpp:51-53): DT = (Dk hbar)^2 / (2m), Dk = 2 pi / (dx n)
+    const long double dk = 2 * (long double)kPi / ((long double)in->dx * n);
+    const long double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * (long double)in->mass);
+    auto fold2 = [&](uint64_t k) {
+        const long double f = (long double)(k > n / 2 ? n - k : k);
+        return f * f * DT;
+    };
+    fill([&](uint64_t k) { return phase(tc[0], fold2(k)); });
+    if ((rc = put(t, &k1, true))) return rc;
+    if (ntab == 2) {
+        fill([&](uint64_t k) { return phase(tc[1], fold2(k)); });
+        if ((rc = put(t, &k2, true))) return rc;
+    }
+    fill([&](uint64_t j) { return w[j]; });
+    if ((rc = put(t, &chirp, true))) return rc;
+    // the kernels in the row pass's layout: position k2 n1 + k1 holds frequency k2 + n2 k1
+    const uint64_t n1 = (uint64_t)in->fsg.n1, n2 = (uint64_t)in->fsg.n2;
+    for (uint64_t k2 = 0; k2 < n2; ++k2)
+        for (uint64_t k1 = 0; k1 < n1; ++k1) t[k2 * n1 + k1] = hs[k2 + n2 * k1];
+    if ((rc = put(t, &h1, false))) return rc;
+    // FFT_M(h*)_k = conj(FFT_M(h)_{-k}), with the 1/n of the inverse DFT
+    for (uint64_t k2 = 0; k2 < n2; ++k2)
+        for (uint64_t k1 = 0; k1 < n1; ++k1) {
+            const uint64_t k = k2 + n2 * k1;
+            t[k2 * n1 + k1] = std::conj(hs[(M - k) % M]) / (long double)n;
+        }
+    if ((rc = put(t, &h2, false))) return rc;
+    // KinEn weights of the n frequencies: fold(k)^2 DT with the periodic branch's DT
+    // (it omits hbar^2, src/SplittingMethod1D.cpp:101-102)
+    {
+        const long double DTk = dk * dk / (2 * (long double)in->mass);
+        std::vector<double> kw(n);
+        for (uint64_t k = 0; k < n; ++k) {
+            const long double f = (long double)(k > n / 2 ? n - k : k);
+            kw[k] = (double)(f * f * DTk);
+        }
+        void *p = nullptr;
+        if ((rc = inst_alloc(in, n * 8, &p))) return rc;
+        in->bkw = static_cast<double *>(p);
+        QSG_CUDA(cudaMemcpyAsync(in->bkw, kw.data(), n * 8, cudaMemcpyHostToDevice, in->ctx->st));
+        QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    }
+    // descriptors (the closing pass's norm partials are set in common_create)
+    qsg::FsInst h[4] = {};
+    for (auto &d : h) {
+        d.psi = in->psi;
+        d.ktab[0] = h1;
+        d.ktab[1] = h2;
+    }
+    h[0].vtab[0] = open;
+    h[0].vtab[1] = vc1;
+    h[1].vtab[0] = k1;
+    h[1].vtab[1] = k2;
+    h[2].vtab[0] = vc2;
+    h[2].vtab[1] = close;
+    h[3].vtab[0] = chirp;
+    in->bchirp = chirp;
+    in->bh1 = h1;
+    void *bd = nullptr;
+    if ((rc = inst_alloc(in, sizeof(h), &bd))) return rc;
+    in->bdesc = static_cast<qsg::FsInst *>(bd);
+    QSG_CUDA(cudaMemcpyAsync(in->bdesc, h, sizeof(h), cudaMemcpyHostToDevice, in->ctx->st));
+    QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
+    return QSG_OK;
+}
+
 int build_tables(qsg_inst *in)
 {
     qsg_ctx *ctx = in->ctx;
@@ -954,6 +1138,7 @@ int build_tables(qsg_inst *in)
     const size_t cs = csize(in->prec);
     const cd I(0, 1);
     int rc;
+    if (in->bfs) return build_bfs_tables(in);
     for (int k = 0; k < ntab; ++k) {
         // ExpV coefficient -i/hbar * dt * c (SplittingMethod1D.cpp:87, SplittingMethod2D.cpp:43-50)
         const cd f = (-I / in->hbar) * in->dt * vc[k];
@@ -1068,13 +1253,17 @@ int build_tables(qsg_inst *in)
 int upload_psi(qsg_inst *in, const double *psi)
 {
     qsg_ctx *ctx = in->ctx;
+    // the source holds the user's sites; a Bluestein buffer is zero above them
+    const size_t src = (in->bfs ? in->n_out : in->n) * 16;
     if (in->prec == 0) {
-        QSG_CUDA(cudaMemcpyAsync(in->psi, psi, in->n * 16, cudaMemcpyDefault, ctx->st));  // host or device source
+        if (in->bfs) QSG_CUDA(cudaMemsetAsync(in->psi, 0, in->n * 16, ctx->st));
+        QSG_CUDA(cudaMemcpyAsync(in->psi, psi, src, cudaMemcpyDefault, ctx->st));  // host or device source
         return QSG_OK;
     }
     int rc = ensure_scratch(ctx, in->n * 16);
     if (rc) return rc;
-    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, psi, in->n * 16, cudaMemcpyDefault, ctx->st));
+    if (in->bfs) QSG_CUDA(cudaMemsetAsync(ctx->scratch, 0, in->n * 16, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(ctx->scratch, psi, src, cudaMemcpyDefault, ctx->st));
     QSG_CUDA(qsg::launch_c128_to_c64(in->psi, ctx->scratch, in->n, ctx->st));
     return QSG_OK;
 }
@@ -1120,7 +1309,10 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     QSG_CUDA(cudaMemsetAsync(in->err, 0, sizeof(unsigned), ctx->st));
     if ((rc = inst_alloc(in, in->n * 8, &v))) return rc;
     in->V = (double *)v;
-    QSG_CUDA(cudaMemcpyAsync(in->V, V, in->n * 8, cudaMemcpyDefault, ctx->st));  // host or device source
+    // (a wall extension's V comes extended to all n sites; a Bluestein buffer's is zero above n_out)
+    if (in->bfs) QSG_CUDA(cudaMemsetAsync(in->V, 0, in->n * 8, ctx->st));
+    QSG_CUDA(cudaMemcpyAsync(in->V, V, (in->bfs ? in->n_out : in->n) * 8, cudaMemcpyDefault,
+                             ctx->st));  // host or device source
     if ((rc = upload_psi(in, psi0))) return rc;
     if ((rc = build_tables(in))) return rc;
     if (in->dim == 1) {
@@ -1143,6 +1335,9 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
         h.partials = in->parts;
         QSG_CUDA(cudaMemcpyAsync(in->desc, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->d_dv, &in->dv, sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+        if (in->bfs)  // the Bluestein closing pass (descriptor 2) sums the norm partials
+            QSG_CUDA(cudaMemcpyAsync(&in->bdesc[2].partials, &in->parts, sizeof(double *), cudaMemcpyHostToDevice,
+                                     ctx->st));
         if (in->fourstep && in->fs_tma) {
             size_t mb = 0;
             in->fs_maps = fs_make_maps(ctx, &in, 1, &mb);
@@ -1583,29 +1778,38 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     const bool resident = wall ? (wall_blue || !wall_ext) : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
     if (wall_ext && !wall_blue && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
-    if (!wall && !pow2 && !blue_m)
+    // longer periodic lengths that are not powers of two: Bluestein's convolutions on
+    // the four-step passes over a buffer of bfs_m >= 2n - 1 sites
+    uint64_t bfs_m = 0;
+    if (!wall && !pow2 && !blue_m && n >= 2) {
+        uint64_t m = 1;
+        while (m < 2 * n - 1) m <<= 1;
+        if (qsg::fs_geom(precision, m, &fsg)) bfs_m = m;
+    }
+    if (!wall && !pow2 && !blue_m && !bfs_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
-                                             " (lengths that are not powers of two: 2 .. 4096)");
+                                             " (lengths that are not powers of two: 2 .. 131072)");
     if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (supported: powers of two, 64 .. 262144)");
     // the plan: the one tuned for this shape (in this context or the plan cache),
     // else the default (one CTA where it fits, else four-step, default split)
     qsg_plan1d plan{resident ? 0 : 1, resident ? 0 : fsg.n1, 0, 0};
-    if (!resident && !wall_ext && ctx->fs_tma && qsg::fs_tma_supported(precision, fsg.n2)) plan.tma = 1;
-    if (!blue_m && !(wall && !wall_ext)) {
+    if (!resident && !wall_ext && !bfs_m && ctx->fs_tma && qsg::fs_tma_supported(precision, fsg.n2)) plan.tma = 1;
+    if (!blue_m && !bfs_m && !(wall && !wall_ext)) {
         load_plans(ctx);
         auto it = ctx->plans1d.find(std::make_tuple(precision, wall_ext ? 2 * n : n, wall_ext ? 1 : 0));
         if (it != ctx->plans1d.end() && plan1d_valid(precision, n, boundary, it->second)) plan = it->second;
     }
-    if (plan.kind == 1 && !qsg::fs_geom(precision, wall_ext ? 2 * n : n, &fsg, plan.n1))
+    if (plan.kind == 1 && !qsg::fs_geom(precision, bfs_m ? bfs_m : (wall_ext ? 2 * n : n), &fsg, plan.n1))
         return fail(QSG_ERR_STATE, "qsg_create_1d: plan cache entry does not fit n=" + std::to_string(n));
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();
     in->ctx = ctx;
     in->dim = 1;
-    in->n = wall_ext ? 2 * n : n;
+    in->n = bfs_m ? bfs_m : (wall_ext ? 2 * n : n);
     in->n_out = n;
+    in->bfs = bfs_m > 0;
     in->wall_ext = wall_ext;
     in->nx = (int)n;
     in->dx = dx;
@@ -2123,6 +2327,51 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
                 QSG_CUDA(qsg::launch_kinetic1d_wall(in->prec, (int)in->n, in->psi, in->tw, DTw, ctx->sums, ctx->st));
             } else if (!in->fourstep) {
                 QSG_CUDA(qsg::launch_kinetic1d(in->prec, (int)in->n, in->psi, in->tw, DT, ctx->sums, ctx->st));
+            } else if (in->bfs) {
+                // |DFT_n(psi)_k| = |C_h(w psi)_k| for k < n: on a copy, the column pass
+                // with the chirp, the row pass with FFT_M(h) / M, the column pass back
+                // to natural order; then sum |.|^2 fold(k)^2 DT / sum |.|^2 over k < n
+                const size_t bytes = in->n * csize(in->prec);
+                if ((rc = ensure_scratch(ctx, bytes + sizeof(qsg::FsInst)))) return rc;
+                qsg::FsInst h{};
+                h.psi = ctx->scratch;
+                h.vtab[0] = in->bchirp;
+                h.ktab[0] = in->bh1;
+                qsg::FsInst *dd = reinterpret_cast<qsg::FsInst *>(static_cast<char *>(ctx->scratch) + bytes);
+                QSG_CUDA(cudaMemcpyAsync(dd, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->st));
+                QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+                qsg::FsColArgs ca{};
+                ca.inst = dd;
+                ca.tw_col = in->tw_fs_col;
+                ca.tw_n = in->tw_n;
+                ca.n1 = in->fsg.n1;
+                ca.vsel = 0;
+                ca.in_k = 0;
+                ca.out_k = 1;
+                QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, ca, 1, ctx->st));
+                qsg::FsRowArgs ra{};
+                ra.inst = dd;
+                ra.tw_row = in->tw_fs_row;
+                ra.ksel = 0;
+                ra.plain = 1;
+                QSG_CUDA(qsg::launch_fs_row(in->prec, in->fsg, ra, 1, ctx->st));
+                ca.vsel = 1;  // no table: the descriptor's second V entry is null
+                ca.in_k = 1;
+                ca.out_k = 0;
+                QSG_CUDA(qsg::launch_fs_col(in->prec, in->fsg, ca, 1, ctx->st));
+                double sk[2];
+                for (int mode = 1; mode >= 0; --mode) {
+                    int np = 0;
+                    QSG_CUDA(qsg::launch_reduce(in->prec, ctx->scratch, in->bkw, 0, in->n_out, mode, ctx->partials,
+                                                ctx->max_partials, &np, ctx->st));
+                    QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
+                    QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost,
+                                             ctx->st));
+                    if ((rc = sync_checked(in, ctx->st, "qsg_energies"))) return rc;
+                    sk[mode] = ctx->host_sums[0];
+                }
+                *kin = sk[1] / sk[0];
+                return QSG_OK;
             } else {
                 // forward transform of a copy: column pass (natural -> k layout), then row
                 // FFTs with the reductions
@@ -2505,9 +2754,10 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     std::memcpy(&in->err_seen, ctx->host_sums + 7, sizeof(unsigned));
     if (err != cudaSuccess) return fail(QSG_ERR_CUDA, std::string("qsg_autotune_1d: ") + cudaGetErrorString(err));
     if ((rc = apply_plan_1d(in, best_p))) return rc;
+    // a Bluestein four-step length has its one plan: nothing to remember
     const bool ext = in->wall_ext;
-    ctx->plans1d[std::make_tuple(in->prec, in->n, ext ? 1 : 0)] = best_p;
-    if (persist) save_plan_1d(ctx, in->prec, user_n(in), in->boundary, best_p, best_ms);
+    if (!in->bfs) ctx->plans1d[std::make_tuple(in->prec, in->n, ext ? 1 : 0)] = best_p;
+    if (persist && !in->bfs) save_plan_1d(ctx, in->prec, user_n(in), in->boundary, best_p, best_ms);
     if (best) *best = best_p;
     if (best_ms_per_step) *best_ms_per_step = best_ms;
     return QSG_OK;
@@ -2652,7 +2902,7 @@ int qsg_batch_create_1d(qsg_ctx *ctx, int count, const uint64_t *n, const double
         qsg_inst *in = nullptr;
         int rc = create_1d_locked(ctx, n[i], dx[i], mass, hbar, dt_re[i], dt_im ? dt_im[i] : 0.0, order, precision,
                                   QSG_PERIOD, psi0[i], V[i], &in);
-        if (!rc && in->blue) {
+        if (!rc && (in->blue || in->bfs)) {
             free_inst(in);
             rc = fail(QSG_ERR_UNSUPPORTED, "n=" + std::to_string(n[i]) + ": batches take powers of two");
         }

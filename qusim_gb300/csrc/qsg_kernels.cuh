@@ -763,6 +763,8 @@ struct FsRowArgs {
     const void *tw_row;     // stage twiddles for (N1, E)
     int ksel;
     float inv_n;            // 1/N (complex64 path; complex128 tables carry it)
+    int plain;              // the table holds plain complex factors (any modulus, scale included):
+                            // a plain product, no 1/N (Bluestein's convolution kernels)
 };
 
 // B rows of N1 per CTA (B * N1/E threads)
@@ -794,11 +796,16 @@ __global__ void __launch_bounds__(B *(N1 / E)) k_fs_row(FsRowArgs a)
         line_fft<C, N1, E, false>(x, sm, lay, lbar, t, tw);
         if (p == 1) continue;
         const C *kt = opaque(static_cast<const C *>(in.ktab[a.ksel])) + base;
+        if (a.plain) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            C v = x[e];
-            if constexpr (sizeof(C) == 8) v = cscale(v, a.inv_n);
-            x[e] = cconj(PhaseOps<C>::apply(v, ld_stream(kt + e * TL)));
+            for (int e = 0; e < E; ++e) x[e] = cconj(cmul(x[e], ld_stream(kt + e * TL)));
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                C v = x[e];
+                if constexpr (sizeof(C) == 8) v = cscale(v, a.inv_n);
+                x[e] = cconj(PhaseOps<C>::apply(v, ld_stream(kt + e * TL)));
+            }
         }
     }
     C *p = const_cast<C *>(opaque(psi)) + base;

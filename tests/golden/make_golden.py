@@ -79,6 +79,10 @@ def main():
          2.0, 0.7),
         # a wall of a length that is not a power of two: KISS transforms of 2n = 1200
         ("evolve1d_n600_o4_wall", 600, -40.0, 40.0, 1.0, -10.0, 3.0, 4, True, 0.02, 40, 1, False),
+        # periodic lengths above 4096 that are not powers of two: 5000 = 2^3 5^4 and the
+        # prime 4099 (a generic-radix KISS transform), renormalising calls
+        ("evolve1d_n5000_o4", 5000, -100.0, 100.0, 1.0, -20.0, 5.0, 4, False, 0.02, 20, 1, False),
+        ("evolve1d_n4099_o2_b5x2_fnes", 4099, -80.0, 80.0, 1.0, -15.0, 4.0, 2, False, 0.02, 5, 2, True),
     ]
     for case in cases_1d:
         name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes = case[:13]

@@ -57,7 +57,8 @@ def run_1d(qsg, ctx, g, precision):
 # src/SplittingMethod1D.cpp:101-102; the wall and 2D ones use (Dk hbar)^2 / 2m)
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1024_o2_hbar07_m2",
-             "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2", "evolve1d_n600_o4_wall"]
+             "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2", "evolve1d_n600_o4_wall",
+             "evolve1d_n5000_o4", "evolve1d_n4099_o2_b5x2_fnes"]
 GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
              "evolve2d_128x256_o4_hbar07_m2", "evolve2d_45x70_o2_30",
              "evolve2d_96x50_o4_10"]
@@ -160,12 +161,16 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    # lengths that are not powers of two: up to 4096
-    psi0, V, dx = gauss_packet_1d(5000, -50, 50, 1.0, -10, 3.0)
+    # periodic lengths that are not powers of two: up to 131072 (2n - 1 <= 262144)
+    psi0, V, dx = gauss_packet_1d(131073, -5000, 5000, 1.0, -10, 3.0)
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
             qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision=precision)
         assert e.value.code == 5
+    # batches take powers of two
+    with pytest.raises(qsg.QsgError) as e:
+        qsg.Batch(ctx, [psi0[:5000]], [V[:5000]], [dx], [0.01], order=2, precision="mixed")
+    assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02,
                                boundary=qsg.BoundaryCondition.InfiniteWall, precision="mixed")
@@ -406,6 +411,55 @@ def test_wall_any_length_renormalising_and_set_psi(qsg, ctx, oracle):
     inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=2, precision="fp64", boundary=wall)
     inst.step(3)
     inst.set_psi(psi0 * 1.3)
+    inst.step(9, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1.0) <= 1e-13
+
+
+@pytest.mark.parametrize("n,order", [(4097, 4), (4099, 2), (6000, 4), (10007, 2), (100000, 4), (131070, 2)])
+def test_periodic_long_any_length_vs_oracle(qsg, ctx, oracle, n, order):
+    """Periodic lengths above 4096 that are not powers of two: the reference's
+    ExpT/ExpV (src/SplittingMethod1D.cpp:48-57, 83-90) on its KISS transforms of
+    length n; here Bluestein's two circular convolutions of length M (the
+    smallest power of two >= 2n - 1) per kinetic factor, on the four-step passes.
+    Against the oracle: complex128 <= 1e-12 with KinEn and PotEn at 1e-11,
+    complex64 <= 1e-5; hbar = 0.7, m = 2, a complex time step."""
+    L = 0.02 * n
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.3, -0.2 * L, 0.05 * L, barrier=0.6)
+    dt = 0.02 - 0.001j
+    ref = oracle.evolve1d(psi0, V, dx, dt, 6, order=order, mass=2.0, hbar=0.7)
+    m = 1 << (2 * n - 2).bit_length()
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, dt, order=order, precision=precision, mass=2.0, hbar=0.7)
+        plan = inst.plan().as_tuple()
+        assert plan[0] == 1 and plan[2] == 0 and m % plan[1] == 0
+        inst.step(2)
+        inst.step(4)
+        got = inst.get_psi()
+        assert got.shape == (n,)
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        kin, pot = inst.energies()
+        kr = oracle.kinen1d(ref, dx, mass=2.0, hbar=0.7)
+        etol = 1e-11 if precision == "fp64" else 1e-4
+        assert abs(kin - kr) <= etol * abs(kr), (precision, kin, kr)
+        assert abs(pot - oracle.poten(ref, V, dx)) <= etol * max(1.0, abs(pot))
+        assert abs(inst.norm2() - oracle.norm2(ref, dx)) <= (1e-12 if precision == "fp64" else 1e-5)
+        inst.close()
+
+
+def test_periodic_long_any_length_renormalising_set_psi_and_tune(qsg, ctx, oracle):
+    """A renormalising Bluestein four-step instance, its set_psi (the buffer above
+    n stays zero) and its tuner (one plan: the state is kept and the plan too)."""
+    n = 7777
+    psi0, V, dx = gauss_packet_1d(n, -150, 150, 1.0, -30.0, 6.0, barrier=0.5)
+    ref = oracle.evolve1d(psi0 * 1.3, V, dx, 0.01 - 0.002j, 9, order=4, renormalize=True)
+    inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=4, precision="fp64")
+    inst.step(3)
+    inst.set_psi(psi0 * 1.3)
+    plan = inst.plan().as_tuple()
+    best, ms = inst.autotune(trial_steps=2)
+    assert best.as_tuple() == plan and ms > 0
+    assert np.array_equal(inst.get_psi(), psi0 * 1.3)
     inst.step(9, renormalize=True)
     assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
     assert abs(inst.norm2() - 1.0) <= 1e-13

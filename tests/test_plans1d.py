@@ -44,7 +44,14 @@ def test_resident_plans(q):
 def test_lengths_without_choices(q):
     # Bluestein lengths: one plan; lengths beyond every plan: none
     assert tuples(q, "mixed", 1000) == [(0, 0, 0)]
-    assert tuples(q, "mixed", 5000) == []
+    assert tuples(q, "fp64", 4095) == [(0, 0, 0)]
+    # longer lengths that are not powers of two: Bluestein on the four-step passes
+    # of the smallest power of two M >= 2n - 1, its default split
+    assert tuples(q, "mixed", 5000) == [(1, 128, 0)]      # M = 16384
+    assert tuples(q, "fp64", 4097) == [(1, 128, 0)]
+    assert tuples(q, "mixed", 100000) == [(1, 512, 0)]    # M = 262144
+    assert tuples(q, "fp64", 131071) == [(1, 512, 0)]
+    assert tuples(q, "mixed", 131073) == []               # M = 524288: beyond the passes
     assert tuples(q, "mixed", 1 << 19) == []
     assert tuples(q, "mixed", 32) == [(0, 0, 0)]   # powers of two below 64: Bluestein
     assert tuples(q, "mixed", 1) == []
