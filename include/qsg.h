@@ -106,8 +106,10 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * 2048 (QSG_FP64); above that, up to n = 131072, the instance keeps the 2n odd
  * extension in HBM and steps it with the four-step passes of a periodic 2n
  * grid; any other n from 2 to 2048 keeps the 2n extension in one CTA stepped
- * by Bluestein transforms.  Reads and writes of
- * psi cover its n sites.
+ * by Bluestein transforms, and from 2049 to 65536 steps it by Bluestein's
+ * convolutions on the four-step passes (M >= 4n - 1).  Kept in HBM or in one
+ * CTA, the extension's sites 0 and n are zeroed before the first transform of
+ * each call.  Reads and writes of psi cover its n sites.
  * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
  * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
@@ -325,8 +327,8 @@ int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
  *           its tiles with tensor copies instead of load instructions.
  * A wall above one CTA is stepped as its periodic 2n odd extension, so its
  * plans are the four-step plans of 2n (without tma).  Lengths that are not
- * powers of two (Bluestein) have one plan: kind 0 up to n = 4096, else kind
- * 1 with the default split of M.  Every plan computes the
+ * powers of two (Bluestein) have one plan: kind 0 up to n = 4096 (a wall's
+ * up to 2048), else kind 1 with the default split of M.  Every plan computes the
  * same result to rounding; they differ in speed.  New instances of a size
  * take the plan qsg_autotune_1d last chose for that size and precision in
  * this context or in the plan cache file, else the default (resident where

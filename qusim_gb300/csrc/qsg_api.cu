@@ -109,6 +109,7 @@ struct qsg_inst {
     // ([0] open V / V c1, [1] K d1 / K d2, [2] V c2 / close, [3] chirp; ktab the
     // two convolution kernels in row layout), bkw: KinEn weights fold(k)^2 DT
     bool bfs = false;
+    uint64_t bfs_n = 0;  // Bluestein four-step: the transform length (n, or a wall's 2n)
     qsg::FsInst *bdesc = nullptr;
     double *bkw = nullptr;
     const void *bchirp = nullptr, *bh1 = nullptr;  // chirp (column form) and first kernel, for KinEn
@@ -230,7 +231,12 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     a.vtwice = vtwice ? 1 : 0;
     a.in_k = in_k ? 1 : 0;
     a.out_k = out_k ? 1 : 0;
-    a.wall = in->wall_ext ? 1 : 0;
+    // a wall's extension: sites 0 and n zeroed before the first forward transform of a
+    // call (the pass that reads natural order); later transforms keep the extension
+    // as it evolves, since zeroing them again feeds rounding noise back (amplified by
+    // an O4 substep of negative coefficient under a complex dt).  A Bluestein wall
+    // zeroes through its opening table.
+    a.wall = in->wall_ext && !in->bfs && !in_k ? 1 : 0;
     ProfScope ps(in->ctx, "fs_col_pass", st);
     if (maps && !in->wall_ext && in->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
         a.maps = maps;
@@ -888,6 +894,16 @@ void add_fs_plans(int prec, uint64_t n, bool tma_ok, std::vector<qsg_plan1d> &ou
 }
 
 // every plan of a 1D instance of n sites (the default first)
+// Bluestein on the four-step passes: the buffer length M (the smallest power of
+// two >= 2 len - 1) for a transform of len sites, 0 where the passes do not reach
+uint64_t bfs_len_m(int prec, uint64_t len, qsg::FsGeom *g)
+{
+    if (len < 2) return 0;
+    uint64_t m = 1;
+    while (m < 2 * len - 1) m <<= 1;
+    return qsg::fs_geom(prec, m, g) ? m : 0;
+}
+
 void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
 {
     out.clear();
@@ -895,8 +911,11 @@ void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
     const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
     if (boundary == QSG_INFINITE_WALL) {
         if (!pow2 || n < 64) {
-            // any other length: one Bluestein kernel on the 2n odd extension
+            // any other length: Bluestein transforms of the 2n odd extension, in one
+            // kernel or (longer) on the four-step passes
+            qsg::FsGeom g;
             if (n >= 2 && qsg::blue_m_for(prec, 2 * n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+            else if (bfs_len_m(prec, 2 * n, &g)) out.push_back(qsg_plan1d{1, g.n1, 0, 0});
             return;
         }
         if (n > 131072) return;
@@ -906,15 +925,9 @@ void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
     }
     if (boundary != QSG_PERIOD) return;
     if (!pow2 || n < 64) {
-        if (qsg::blue_m_for(prec, n)) {
-            out.push_back(qsg_plan1d{0, 0, 0, 0});
-        } else if (n >= 2) {
-            // Bluestein on the four-step passes of the smallest power of two >= 2n - 1
-            uint64_t m = 1;
-            while (m < 2 * n - 1) m <<= 1;
-            qsg::FsGeom g;
-            if (qsg::fs_geom(prec, m, &g)) out.push_back(qsg_plan1d{1, g.n1, 0, 0});
-        }
+        qsg::FsGeom g;
+        if (qsg::blue_m_for(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
+        else if (bfs_len_m(prec, n, &g)) out.push_back(qsg_plan1d{1, g.n1, 0, 0});
         return;
     }
     if (qsg::evolve1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
@@ -995,8 +1008,9 @@ int build_ktab_1d(qsg_inst *in)
     return QSG_OK;
 }
 
-// Tables of a Bluestein four-step instance (n_out sites in a buffer of M = in->n).
-// A kinetic substep x -> (1/n) IDFT(K DFT x) is, with the chirp w_j =
+// Tables of a Bluestein four-step instance: transforms of n = bfs_n sites (the
+// user's n, or a wall's 2n odd extension) in a buffer of M = in->n sites.
+// A kinetic substep x -> IDFT(K DFT x) is, with the chirp w_j =
 // exp(-i pi j^2 / n) and circular convolutions C_h, C_h* by h = conj(w) and by
 // w (length M), the product W* C_h* K C_h W (the chirps between the two DFTs
 // cancel, 1/n goes into the second kernel).  A convolution is a forward
@@ -1005,7 +1019,7 @@ int build_ktab_1d(qsg_inst *in)
 // next column pass.  The diagonal factors meet in the column passes in natural
 // layout: V w before the first convolution of a call ("open"), K_d between the
 // two, V merged with w* and w between substeps (plain V), w* V at the end of a
-// call ("close"); each is zero above n_out, which truncates the convolutions'
+// call ("close"); each is zero from n on, which truncates the convolutions'
 // outputs and keeps the buffer zero there.  Values are formed in long double
 // on the host: plain complex (complex128) or factor - 1 (complex64 columns);
 // the kernels are plain complex in both.
@@ -1016,7 +1030,7 @@ int build_bfs_tables(qsg_inst *in)
     const long double vc[2] = {in->order == 2 ? 0.5L : (long double)sc.c1, (long double)sc.c2};
     const long double tc[2] = {in->order == 2 ? 1.0L : (long double)sc.d1, (long double)sc.d2};
     using cl = std::complex<long double>;
-    const uint64_t n = in->n_out, M = in->n;
+    const uint64_t n = in->bfs_n, M = in->n;
     const size_t cs = csize(in->prec);
     int rc;
     std::vector<cl> w, hs;
@@ -1050,11 +1064,17 @@ int build_bfs_tables(qsg_inst *in)
     auto fill = [&](auto f) {
         for (uint64_t j = 0; j < M; ++j) t[j] = j < n ? f(j) : cl(0);
     };
+    // a wall's 2n odd extension: sites 0 and n / 2 are zeroed before the first forward
+    // transform of a call (the reference's wall ExpT discards them, src/SplittingMethod1D.cpp:
+    // 63-65), in the opening factor; later transforms keep the extension as it evolves
+    // (zeroing again feeds rounding noise back, amplified under a complex dt)
+    const bool wall = in->wall_ext;
+    auto mask = [&](uint64_t j) { return wall && (j == 0 || j == n / 2) ? 0.0L : 1.0L; };
     void *open = nullptr, *vc1 = nullptr, *vc2 = nullptr, *close = nullptr, *k1 = nullptr, *k2 = nullptr;
     void *chirp = nullptr, *h1 = nullptr, *h2 = nullptr;
-    fill([&](uint64_t j) { return w[j] * phase(vc[0], Vh[j]); });
+    fill([&](uint64_t j) { return mask(j) * w[j] * phase(vc[0], Vh[j]); });
     if ((rc = put(t, &open, true))) return rc;
-    fill([&](uint64_t j) { return phase(vc[0], Vh[j]); });
+    fill([&](uint64_t j) { return phase(vc[0], Vh[j]); });  // applied twice at step joins
     if ((rc = put(t, &vc1, true))) return rc;
     fill([&](uint64_t j) { return std::conj(w[j]) * phase(vc[0], Vh[j]); });
     if ((rc = put(t, &close, true))) return rc;
@@ -1062,7 +1082,8 @@ int build_bfs_tables(qsg_inst *in)
         fill([&](uint64_t j) { return phase(vc[1], Vh[j]); });
         if ((rc = put(t, &vc2, true))) return rc;
     }
-    // ExpT periodic (SplittingMethod1D.cpp:51-53): DT = (Dk hbar)^2 / (2m), Dk = 2 pi / (dx n)
+    // ExpT periodic (SplittingMethod1D.cpp:51-53): DT = (Dk hbar)^2 / (2m), Dk = 2 pi / (dx n);
+    // on a wall's 2n extension Dk = pi / (dx n_wall), the wall ExpT's (:72-74)
     const long double dk = 2 * (long double)kPi / ((long double)in->dx * n);
     const long double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * (long double)in->mass);
     auto fold2 = [&](uint64_t k) {
@@ -1075,7 +1096,7 @@ int build_bfs_tables(qsg_inst *in)
         fill([&](uint64_t k) { return phase(tc[1], fold2(k)); });
         if ((rc = put(t, &k2, true))) return rc;
     }
-    fill([&](uint64_t j) { return w[j]; });
+    fill([&](uint64_t j) { return mask(j) * w[j]; });
     if ((rc = put(t, &chirp, true))) return rc;
     // the kernels in the row pass's layout: position k2 n1 + k1 holds frequency k2 + n2 k1
     const uint64_t n1 = (uint64_t)in->fsg.n1, n2 = (uint64_t)in->fsg.n2;
@@ -1090,9 +1111,11 @@ int build_bfs_tables(qsg_inst *in)
         }
     if ((rc = put(t, &h2, false))) return rc;
     // KinEn weights of the n frequencies: fold(k)^2 DT with the periodic branch's DT
-    // (it omits hbar^2, src/SplittingMethod1D.cpp:101-102)
+    // (it omits hbar^2, src/SplittingMethod1D.cpp:101-102), the wall's with it (:117-119;
+    // |F|^2 of the odd extension is even, so the ratio over the 2n frequencies is the
+    // wall's over k < n)
     {
-        const long double DTk = dk * dk / (2 * (long double)in->mass);
+        const long double DTk = wall ? DT : dk * dk / (2 * (long double)in->mass);
         std::vector<double> kw(n);
         for (uint64_t k = 0; k < n; ++k) {
             const long double f = (long double)(k > n / 2 ? n - k : k);
@@ -1254,7 +1277,7 @@ int upload_psi(qsg_inst *in, const double *psi)
 {
     qsg_ctx *ctx = in->ctx;
     // the source holds the user's sites; a Bluestein buffer is zero above them
-    const size_t src = (in->bfs ? in->n_out : in->n) * 16;
+    const size_t src = (in->bfs ? in->bfs_n : in->n) * 16;
     if (in->prec == 0) {
         if (in->bfs) QSG_CUDA(cudaMemsetAsync(in->psi, 0, in->n * 16, ctx->st));
         QSG_CUDA(cudaMemcpyAsync(in->psi, psi, src, cudaMemcpyDefault, ctx->st));  // host or device source
@@ -1311,7 +1334,7 @@ int common_create(qsg_inst *in, const double *psi0, const double *V)
     in->V = (double *)v;
     // (a wall extension's V comes extended to all n sites; a Bluestein buffer's is zero above n_out)
     if (in->bfs) QSG_CUDA(cudaMemsetAsync(in->V, 0, in->n * 8, ctx->st));
-    QSG_CUDA(cudaMemcpyAsync(in->V, V, (in->bfs ? in->n_out : in->n) * 8, cudaMemcpyDefault,
+    QSG_CUDA(cudaMemcpyAsync(in->V, V, (in->bfs ? in->bfs_n : in->n) * 8, cudaMemcpyDefault,
                              ctx->st));  // host or device source
     if ((rc = upload_psi(in, psi0))) return rc;
     if ((rc = build_tables(in))) return rc;
@@ -1762,31 +1785,26 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
         return fail(QSG_ERR_ARG, "qsg_create_1d: unknown boundary");
     const bool wall = boundary == QSG_INFINITE_WALL;
     const bool pow2 = n >= 1 && (n & (n - 1)) == 0;
-    // walls of any other length (and powers of two below 64): the 2n odd
-    // extension stepped by one Bluestein kernel
-    const bool wall_blue = wall && (!pow2 || n < 64);
-    const std::string wall_limits = " (supported: any n from 2 to 2048, and powers of two up to 131072)";
-    if (wall_blue && (n < 2 || !qsg::blue_m_for(precision, 2 * n)))
+    qsg::FsGeom fsg{};
+    // lengths that are not powers of two (and powers of two below 64): Bluestein
+    // transforms of n sites (a wall: of its 2n odd extension), in one kernel where
+    // M >= 2 len - 1 fits one CTA, else two convolutions on the four-step passes
+    // over a buffer of bfs_m >= 2 len - 1 sites
+    const bool any_len = !pow2 || n < 64;
+    const uint64_t blue_len = wall ? 2 * n : n;
+    const int one_cta_m = any_len && n >= 2 ? qsg::blue_m_for(precision, blue_len) : 0;
+    const uint64_t bfs_m = any_len && !one_cta_m ? bfs_len_m(precision, blue_len, &fsg) : 0;
+    const bool wall_blue = wall && one_cta_m > 0;
+    const std::string wall_limits = " (supported: any n from 2 to 65536, and powers of two up to 131072)";
+    if (wall && any_len && !one_cta_m && !bfs_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     // walls above one CTA: a four-step periodic instance of the 2n odd extension
-    const bool wall_ext = wall && (wall_blue || !qsg::wall1d_supported(precision, n));
-    // periodic lengths that are not powers of two (and powers of two below the
-    // one-CTA kernels' 64): Bluestein transforms of length blue_m
-    const int blue_m = wall_blue ? qsg::blue_m_for(precision, 2 * n)
-                                 : (!wall && (!pow2 || n < 64) ? qsg::blue_m_for(precision, n) : 0);
-    qsg::FsGeom fsg{};
+    const bool wall_ext = wall && (any_len || !qsg::wall1d_supported(precision, n));
+    const int blue_m = one_cta_m;
     const bool resident = wall ? (wall_blue || !wall_ext) : (blue_m > 0 || qsg::evolve1d_supported(precision, n));
-    if (wall_ext && !wall_blue && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
+    if (wall_ext && !any_len && (n < 64 || !qsg::fs_geom(precision, 2 * n, &fsg)))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
-    // longer periodic lengths that are not powers of two: Bluestein's convolutions on
-    // the four-step passes over a buffer of bfs_m >= 2n - 1 sites
-    uint64_t bfs_m = 0;
-    if (!wall && !pow2 && !blue_m && n >= 2) {
-        uint64_t m = 1;
-        while (m < 2 * n - 1) m <<= 1;
-        if (qsg::fs_geom(precision, m, &fsg)) bfs_m = m;
-    }
-    if (!wall && !pow2 && !blue_m && !bfs_m)
+    if (!wall && any_len && !blue_m && !bfs_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
                                              " (lengths that are not powers of two: 2 .. 131072)");
     if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
@@ -1810,6 +1828,7 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     in->n = bfs_m ? bfs_m : (wall_ext ? 2 * n : n);
     in->n_out = n;
     in->bfs = bfs_m > 0;
+    in->bfs_n = bfs_m ? blue_len : 0;
     in->wall_ext = wall_ext;
     in->nx = (int)n;
     in->dx = dx;
@@ -2362,7 +2381,7 @@ int qsg_energies(qsg_inst *in, double *kin, double *pot)
                 double sk[2];
                 for (int mode = 1; mode >= 0; --mode) {
                     int np = 0;
-                    QSG_CUDA(qsg::launch_reduce(in->prec, ctx->scratch, in->bkw, 0, in->n_out, mode, ctx->partials,
+                    QSG_CUDA(qsg::launch_reduce(in->prec, ctx->scratch, in->bkw, 0, in->bfs_n, mode, ctx->partials,
                                                 ctx->max_partials, &np, ctx->st));
                     QSG_CUDA(qsg::launch_finalize(ctx->partials, np, 1, ctx->sums, ctx->st));
                     QSG_CUDA(cudaMemcpyAsync(ctx->host_sums, ctx->sums, sizeof(double), cudaMemcpyDeviceToHost,

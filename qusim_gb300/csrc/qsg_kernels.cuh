@@ -667,8 +667,9 @@ struct FsColArgs {
     int tiles;              // tensor-copy pass: column blocks x instances
     int *err;               // tensor-copy pass: counter it adds 1 to when a bounded wait ran out
     int wall;               // the state is a wall's 2n odd extension: sites 0 and n (rows 0 and
-                            // n2 / 2 of column 0) are zeroed before each forward transform, as the
-                            // reference's wall ExpT discards them (src/SplittingMethod1D.cpp:63-65)
+                            // n2 / 2 of column 0) are zeroed before this pass's forward transform,
+                            // as the reference's wall ExpT discards them (src/SplittingMethod1D.cpp:
+                            // 63-65); set on the first pass of a call only (see qsg_blue.cuh, wall_n)
 };
 
 // three 256-thread CTAs per SM (registers capped at 85) for the strided

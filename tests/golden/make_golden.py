@@ -83,6 +83,8 @@ def main():
         # prime 4099 (a generic-radix KISS transform), renormalising calls
         ("evolve1d_n5000_o4", 5000, -100.0, 100.0, 1.0, -20.0, 5.0, 4, False, 0.02, 20, 1, False),
         ("evolve1d_n4099_o2_b5x2_fnes", 4099, -80.0, 80.0, 1.0, -15.0, 4.0, 2, False, 0.02, 5, 2, True),
+        # a wall whose 2n = 6000 extension is too long for one CTA's Bluestein transform
+        ("evolve1d_n3000_o4_wall", 3000, -60.0, 60.0, 1.0, -15.0, 4.0, 4, True, 0.02, 20, 1, False),
     ]
     for case in cases_1d:
         name, n, x0, x1, k0, xc, s, order, wall, dt, batch, calls, fnes = case[:13]

@@ -58,7 +58,7 @@ def run_1d(qsg, ctx, g, precision):
 GOLDEN_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1024_o2_hbar07_m2",
              "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n1000_o2", "evolve1d_n600_o4_wall",
-             "evolve1d_n5000_o4", "evolve1d_n4099_o2_b5x2_fnes"]
+             "evolve1d_n5000_o4", "evolve1d_n4099_o2_b5x2_fnes", "evolve1d_n3000_o4_wall"]
 GOLDEN_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
              "evolve2d_128x256_o4_hbar07_m2", "evolve2d_45x70_o2_30",
              "evolve2d_96x50_o4_10"]
@@ -170,10 +170,6 @@ def test_unsupported_sizes_are_reported(qsg, ctx):
     # batches take powers of two
     with pytest.raises(qsg.QsgError) as e:
         qsg.Batch(ctx, [psi0[:5000]], [V[:5000]], [dx], [0.01], order=2, precision="mixed")
-    assert e.value.code == 5
-    with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02,
-                               boundary=qsg.BoundaryCondition.InfiniteWall, precision="mixed")
     assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:512], V[:512], dx, 0.02, order=3)
@@ -354,19 +350,17 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 def test_wall_limits_are_reported(qsg, ctx):
     """InfiniteWall: powers of two up to 131072 (the 2n extension of the largest
-    fits the four-step passes' 262144 sites) and any other length up to 2048,
-    whose 2n extension one Bluestein kernel holds."""
+    fits the four-step passes' 262144 sites) and any other length up to 65536,
+    whose Bluestein transforms of the 2n extension take 4n - 1 <= 262144 sites."""
     wall = qsg.BoundaryCondition.InfiniteWall
     psi0, V, dx = gauss_packet_1d(262144, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
-    with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, boundary=wall, precision="mixed")
-    assert e.value.code == 5
-    with pytest.raises(qsg.QsgError) as e:
-        qsg.Instance.create_1d(ctx, psi0[:3000], V[:3000], dx, 0.02, boundary=wall, precision="fp64")
-    assert e.value.code == 5
+    for precision in ("mixed", "fp64"):
+        with pytest.raises(qsg.QsgError) as e:
+            qsg.Instance.create_1d(ctx, psi0[:65537], V[:65537], dx, 0.02, boundary=wall, precision=precision)
+        assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
     assert e.value.code == 5
@@ -400,6 +394,75 @@ def test_wall_any_length_vs_oracle(qsg, ctx, oracle, n, order):
             assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-11 * max(1.0, abs(pot))
             assert abs(inst.norm2() - oracle.norm2(ref, dx)) <= 1e-12
         inst.close()
+
+
+@pytest.mark.parametrize("n,order", [(2049, 4), (3000, 2), (20000, 4), (65535, 2)])
+def test_wall_long_any_length_vs_oracle(qsg, ctx, oracle, n, order):
+    """InfiniteWall at lengths above 2048 that are not powers of two: Bluestein
+    transforms of the 2n odd extension on the four-step passes (the two sites the
+    reference's wall ExpT discards, src/SplittingMethod1D.cpp:63-65, zeroed by the
+    factors that open each transform).  Against the oracle (KISS transforms of
+    length 2n): complex128 <= 1e-12 with the wall KinEn and PotEn at 1e-11,
+    complex64 <= 1e-5; hbar = 0.7, m = 2."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    L = 0.02 * n
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.2, -0.2 * L, 0.05 * L, barrier=0.6)
+    ref = oracle.evolve1d(psi0, V, dx, 0.02, 6, order=order, mass=2.0, hbar=0.7, wall=True)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, order=order, precision=precision, boundary=wall,
+                                      mass=2.0, hbar=0.7)
+        assert inst.plan().as_tuple()[0] == 1
+        inst.step(4)
+        inst.step(2)
+        got = inst.get_psi()
+        assert got.shape == (n,)
+        assert rel_l2(got, ref) <= tol, (precision, rel_l2(got, ref))
+        kin, pot = inst.energies()
+        kr = oracle.kinen1d(ref, dx, mass=2.0, hbar=0.7, wall=True)
+        etol = 1e-11 if precision == "fp64" else 1e-4
+        assert abs(kin - kr) <= etol * abs(kr), (precision, kin, kr)
+        assert abs(pot - oracle.poten(ref, V, dx)) <= etol * max(1.0, abs(pot))
+        inst.close()
+
+
+@pytest.mark.parametrize("n", [1000, 2048, 5000, 8192])
+def test_wall_imaginary_time_o4_fine_grid_vs_oracle(qsg, ctx, oracle, n):
+    """A wall under a complex dt with O4 on a fine grid (dx = 0.04): the middle
+    kinetic substep's negative coefficient d2 amplifies the highest modes by
+    exp(|d2| Im(dt) k^2 DT) ~ 3.6e4, so rounding noise fed back at the wall sites
+    each transform would grow step after step.  Every wall path (one CTA on the
+    2n extension for 2048; Bluestein on it for 1000, in one CTA, and 5000, on the
+    four-step passes; the four-step 2n extension for 8192) matches the oracle's
+    transforms of the odd extension (src/SplittingMethod1D.cpp:61-81) after 9
+    steps in two calls: complex128 <= 1e-12, complex64 <= 1e-5 (zeroing the two
+    sites before every transform instead left 4e-3 .. 2e-2 here)."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    L = 0.02 * n
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.0, -0.2 * L, 0.05 * L, barrier=0.5)
+    dt = 0.01 - 0.002j
+    ref = oracle.evolve1d(psi0, V, dx, dt, 9, order=4, wall=True)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, dt, order=4, precision=precision, boundary=wall)
+        inst.step(4)
+        inst.step(5)
+        err = rel_l2(inst.get_psi(), ref)
+        assert err <= tol, (precision, err)
+        inst.close()
+
+
+def test_wall_long_renormalising_and_set_psi(qsg, ctx, oracle):
+    """A renormalising Bluestein four-step wall and its set_psi (the odd
+    extension rebuilt, zero above it)."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    n = 5001
+    psi0, V, dx = gauss_packet_1d(n, -100, 100, 1.0, -20.0, 5.0, barrier=0.5)
+    ref = oracle.evolve1d(psi0 * 1.3, V, dx, 0.01 - 0.002j, 9, order=4, wall=True, renormalize=True)
+    inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=4, precision="fp64", boundary=wall)
+    inst.step(3)
+    inst.set_psi(psi0 * 1.3)
+    inst.step(9, renormalize=True)
+    assert rel_l2(inst.get_psi(), ref) <= PLAIN_TOL
+    assert abs(inst.norm2() - 1.0) <= 1e-13
 
 
 def test_wall_any_length_renormalising_and_set_psi(qsg, ctx, oracle):

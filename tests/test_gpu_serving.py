@@ -80,7 +80,7 @@ def test_bad_requests_are_refused():
     with pytest.raises(q.QsgError) as e:
         srv.submit(big, big.real, 0.1, 0.01, 10, dy=0.1)
     assert e.value.code == 2
-    odd = np.ones(5000, np.complex128)  # not a power of two and above 4096: no transform for it
+    odd = np.ones(131073, np.complex128)  # not a power of two and above 131072: no transform for it
     rid = srv.submit(odd, odd.real, 0.1, 0.01, 10)
     assert srv.wait(rid, 60) == q.Server.FAILED
     with pytest.raises(q.QsgError) as e:

@@ -13,7 +13,7 @@ from tests.conftest import load_golden
 EVOLVE_1D = ["evolve1d_n4096_o2_2000", "evolve1d_n4096_o4_200", "evolve1d_n256_o2_b7x3_fnes",
              "evolve1d_n1024_o4_imag", "evolve1d_n512_o2_wall", "evolve1d_n1000_o2",
              "evolve1d_n1024_o2_hbar07_m2", "evolve1d_n512_o4_wall_hbar07_m2", "evolve1d_n600_o4_wall",
-             "evolve1d_n5000_o4", "evolve1d_n4099_o2_b5x2_fnes"]
+             "evolve1d_n5000_o4", "evolve1d_n4099_o2_b5x2_fnes", "evolve1d_n3000_o4_wall"]
 EVOLVE_2D = ["evolve2d_128x256_o2_50", "evolve2d_256x128_o4_20", "evolve2d_128x128_o4_b5x2_fnes",
              "evolve2d_128x256_o4_hbar07_m2", "evolve2d_45x70_o2_30",
              "evolve2d_96x50_o4_10"]

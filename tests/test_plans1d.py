@@ -70,7 +70,10 @@ def test_wall_plans(q):
     assert tuples(q, "mixed", 1000, WALL) == [(0, 0, 0)]
     assert tuples(q, "mixed", 32, WALL) == [(0, 0, 0)]
     assert tuples(q, "mixed", 2048, WALL) == [(0, 0, 0)]
-    assert tuples(q, "mixed", 3000, WALL) == []
     assert tuples(q, "fp64", 1500, WALL) == [(0, 0, 0)]
-    assert tuples(q, "fp64", 3000, WALL) == []
+    # longer: Bluestein on the four-step passes of M >= 4n - 1 (the extension's 2 (2n) - 1)
+    assert tuples(q, "mixed", 3000, WALL) == [(1, 128, 0)]     # M = 16384
+    assert tuples(q, "fp64", 3000, WALL) == [(1, 128, 0)]
+    assert tuples(q, "mixed", 65535, WALL) == [(1, 512, 0)]    # M = 262144
+    assert tuples(q, "mixed", 65537, WALL) == []
     assert tuples(q, "mixed", 1, WALL) == []
