@@ -109,6 +109,8 @@ struct qsg_inst {
     // ([0] open V / V c1, [1] K d1 / K d2, [2] V c2 / close, [3] chirp; ktab the
     // two convolution kernels in row layout), bkw: KinEn weights fold(k)^2 DT
     bool bfs = false;
+    bool wall_zero = false;  // a wall extension's site 0 still holds the caller's value: zeroed
+                             // before the next step (the reference's wall ExpT discards it)
     uint64_t bfs_n = 0;  // Bluestein four-step: the transform length (n, or a wall's 2n)
     qsg::FsInst *bdesc = nullptr;
     double *bkw = nullptr;
@@ -231,12 +233,7 @@ int fs_col(qsg_inst *in, const qsg::FsInst *desc, int ninst, bool in_k, bool out
     a.vtwice = vtwice ? 1 : 0;
     a.in_k = in_k ? 1 : 0;
     a.out_k = out_k ? 1 : 0;
-    // a wall's extension: sites 0 and n zeroed before the first forward transform of a
-    // call (the pass that reads natural order); later transforms keep the extension
-    // as it evolves, since zeroing them again feeds rounding noise back (amplified by
-    // an O4 substep of negative coefficient under a complex dt).  A Bluestein wall
-    // zeroes through its opening table.
-    a.wall = in->wall_ext && !in->bfs && !in_k ? 1 : 0;
+    a.wall = 0;  // a wall extension's site 0 is zeroed once per uploaded state (step1d)
     ProfScope ps(in->ctx, "fs_col_pass", st);
     if (maps && !in->wall_ext && in->fs_tma && qsg::fs_tma_supported(in->prec, in->fsg.n2)) {
         a.maps = maps;
@@ -351,6 +348,18 @@ int step_bfs(qsg_inst *in, uint64_t nsteps, cudaStream_t st)
 int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
 {
     qsg_ctx *ctx = in->ctx;
+    if (in->wall_zero) {
+        // A wall's 2n odd extension: the reference's wall ExpT discards sites 0 and n
+        // before each transform (src/SplittingMethod1D.cpp:63-65) and rebuilds the odd
+        // half.  Site n is 0 from the upload and the steps keep the extension odd to
+        // rounding, so the caller's psi_0 is the one value to discard, once.  Zeroing
+        // the two sites again before every transform feeds the rounding noise there
+        // back into every mode; under a complex dt the O4 middle substep (d2 < 0)
+        // multiplies the highest modes by exp(|d2| Im(dt) k^2 DT), and that loop grew
+        // the error about 30x per step on fine grids.
+        QSG_CUDA(cudaMemsetAsync(in->psi, 0, csize(in->prec), in->st));
+        in->wall_zero = false;
+    }
     if (in->blue) {
         qsg::BlueArgs a{};
         a.psi = in->psi;
@@ -368,7 +377,6 @@ int step1d(qsg_inst *in, uint64_t nsteps, int renorm)
         a.n = (int)in->n;
         a.order = in->order;
         a.renormalize = renorm;
-        a.wall_n = in->wall_ext ? (int)in->n_out : 0;
         a.norm_n = (int)user_n(in);
         ProfScope ps(ctx, "evolve1d_blue", in->st);
         QSG_CUDA(qsg::launch_evolve1d_blue(in->prec, in->blue_m, a, in->st));
@@ -1064,15 +1072,13 @@ int build_bfs_tables(qsg_inst *in)
     auto fill = [&](auto f) {
         for (uint64_t j = 0; j < M; ++j) t[j] = j < n ? f(j) : cl(0);
     };
-    // a wall's 2n odd extension: sites 0 and n / 2 are zeroed before the first forward
-    // transform of a call (the reference's wall ExpT discards them, src/SplittingMethod1D.cpp:
-    // 63-65), in the opening factor; later transforms keep the extension as it evolves
-    // (zeroing again feeds rounding noise back, amplified under a complex dt)
+    // a wall's 2n odd extension: KinEn transforms it with sites 0 and n / 2 zeroed
+    // (src/SplittingMethod1D.cpp:112-114); the steps zero site 0 once per uploaded state
     const bool wall = in->wall_ext;
     auto mask = [&](uint64_t j) { return wall && (j == 0 || j == n / 2) ? 0.0L : 1.0L; };
     void *open = nullptr, *vc1 = nullptr, *vc2 = nullptr, *close = nullptr, *k1 = nullptr, *k2 = nullptr;
     void *chirp = nullptr, *h1 = nullptr, *h2 = nullptr;
-    fill([&](uint64_t j) { return mask(j) * w[j] * phase(vc[0], Vh[j]); });
+    fill([&](uint64_t j) { return w[j] * phase(vc[0], Vh[j]); });
     if ((rc = put(t, &open, true))) return rc;
     fill([&](uint64_t j) { return phase(vc[0], Vh[j]); });  // applied twice at step joins
     if ((rc = put(t, &vc1, true))) return rc;
@@ -1276,6 +1282,7 @@ int build_tables(qsg_inst *in)
 int upload_psi(qsg_inst *in, const double *psi)
 {
     qsg_ctx *ctx = in->ctx;
+    in->wall_zero = in->wall_ext;
     // the source holds the user's sites; a Bluestein buffer is zero above them
     const size_t src = (in->bfs ? in->bfs_n : in->n) * 16;
     if (in->prec == 0) {
@@ -1733,7 +1740,7 @@ namespace {
 // The 2n-site odd extension of a wall state (host or device source, n
 // complex): ext_j = psi_j (j < n), 0 at j = n, ext_{2n-j} = -psi_j (0 < j < n).
 // Site 0 keeps psi_0 as given: the reference discards it (and site n) only when
-// a kinetic factor is applied, which the four-step column pass mirrors.
+// a kinetic factor is applied; step1d zeroes it before the first step.
 int wall_odd_extension(const double *psi, uint64_t n, std::vector<double> &ext)
 {
     std::vector<double> h(2 * n);
@@ -2742,6 +2749,7 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     QSG_CUDA(cudaMemcpyAsync(ctx->scratch, in->psi, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     QSG_CUDA(cudaStreamSynchronize(ctx->st));
     const qsg_plan1d keep = in->plan1d;
+    const bool wall_zero = in->wall_zero;  // the trials step a copy: the state's zeroing is still due
     TuneGuard g(ctx);
     QSG_CUDA(cudaEventCreate(&g.e0));
     QSG_CUDA(cudaEventCreate(&g.e1));
@@ -2767,6 +2775,7 @@ int qsg_autotune_1d(qsg_inst *in, int trial_steps, int persist, qsg_plan1d *best
     QSG_CUDA(cudaStreamSynchronize(in->st));
     QSG_CUDA(cudaMemcpyAsync(in->psi, ctx->scratch, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     in->snorm_valid = false;
+    in->wall_zero = wall_zero;
     // a trial pass that ran out of time worked on the copy: acknowledge its count
     if ((rc = queue_err_copy(in, ctx->st))) return rc;
     QSG_CUDA(cudaStreamSynchronize(ctx->st));

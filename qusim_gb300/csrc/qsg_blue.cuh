@@ -41,14 +41,11 @@ struct BlueArgs {
     uint64_t nsteps;
     int n;                  // line length
     int order, renormalize;
-    int wall_n;             // InfiniteWall as the 2 wall_n odd extension (n = 2 wall_n): sites 0 and
-                            // wall_n are zeroed before the first forward transform of a call (and
-                            // of KinEn), as the reference's wall ExpT and KinEn discard them
-                            // (src/SplittingMethod1D.cpp:63-65, 112-114); 0 for a periodic line.
-                            // Later transforms keep the extension as it evolves: zeroing the two
-                            // sites again would feed the rounding noise there back, and with a
-                            // complex dt an O4 substep with a negative coefficient amplifies it
-                            // (exp(|d2| Im(dt) k^2 DT)) step after step
+    int wall_n;             // InfiniteWall as the 2 wall_n odd extension (n = 2 wall_n), 0 for a
+                            // periodic line: KinEn zeroes sites 0 and wall_n as the reference's
+                            // wall KinEn discards them (src/SplittingMethod1D.cpp:112-114).  The
+                            // steps keep the extension as it evolves (odd to rounding; the host
+                            // zeroes the caller's site 0 once per uploaded state)
     int norm_n;             // sites the norm sums (the wall's n), 0: all n
 };
 
@@ -97,16 +94,7 @@ __global__ void __launch_bounds__(M / E) k_evolve1d_blue(BlueArgs a)
     //   x w -> FFT -> conj(. hs) -> FFT -> . conj(K / n) -> FFT -> conj(. hs) -> FFT -> . conj(w)
     // (conj(FFT(conj z)) is the unnormalised inverse; the conjugations around the
     // kinetic product cancel into one conjugated factor)
-    bool first_t = true;
     auto apply_t = [&](const C *kt) {
-        if (a.wall_n && first_t) {
-#pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const int j = t + e * TL;
-                if (j == 0 || j == a.wall_n) x[e] = cmk<C>(0, 0);
-            }
-        }
-        first_t = false;
 #pragma unroll 1
         for (int ph = 0; ph < 4; ++ph) {
             if (ph == 0) {

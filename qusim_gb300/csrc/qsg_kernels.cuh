@@ -32,9 +32,16 @@ namespace qsg {
 
 template <class C> struct PhaseOps;
 // complex128: tables hold the factor itself (the reference's own exp(f V)),
-// multiplied in as a plain complex product.
+// multiplied in as a plain complex product with explicit roundings (one product
+// rounded, one fused): the same bits in every pass that applies a factor, once
+// or twice in a row, so a step split across calls equals the step in one call
+// (left to the compiler, the contraction of a.x m.x - a.y m.y can differ
+// between two inlined copies).
 template <> struct PhaseOps<double2> {
-    static __device__ __forceinline__ double2 apply(double2 a, double2 m) { return cmul(a, m); }
+    static __device__ __forceinline__ double2 apply(double2 a, double2 m)
+    {
+        return double2{__fma_rn(a.x, m.x, -__dmul_rn(a.y, m.y)), __fma_rn(a.x, m.y, __dmul_rn(a.y, m.x))};
+    }
     static __device__ __forceinline__ double2 increment(double2 a, double2, int) { return a; }  // unused
 };
 // complex64: tables hold factor - 1 (see cmul1p).
@@ -667,9 +674,9 @@ struct FsColArgs {
     int tiles;              // tensor-copy pass: column blocks x instances
     int *err;               // tensor-copy pass: counter it adds 1 to when a bounded wait ran out
     int wall;               // the state is a wall's 2n odd extension: sites 0 and n (rows 0 and
-                            // n2 / 2 of column 0) are zeroed before this pass's forward transform,
-                            // as the reference's wall ExpT discards them (src/SplittingMethod1D.cpp:
-                            // 63-65); set on the first pass of a call only (see qsg_blue.cuh, wall_n)
+                            // n2 / 2 of column 0) are zeroed before the forward transform, as the
+                            // reference's wall KinEn discards them (src/SplittingMethod1D.cpp:
+                            // 112-114); set by KinEn's transform only
 };
 
 // three 256-thread CTAs per SM (registers capped at 85) for the strided

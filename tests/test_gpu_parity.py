@@ -450,6 +450,32 @@ def test_wall_imaginary_time_o4_fine_grid_vs_oracle(qsg, ctx, oracle, n):
         inst.close()
 
 
+@pytest.mark.parametrize("n", [1000, 2048, 8192])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_wall_split_calls_equal_one_call(qsg, ctx, oracle, n, precision):
+    """A wall keeps the caller's psi_0 until the first step discards it (as the
+    reference's first wall ExpT does, src/SplittingMethod1D.cpp:63-65); the state
+    then stays odd to rounding, so 9 steps in one call equal 4 + 5 in two, bit for
+    bit, on the one-CTA Bluestein, one-CTA and four-step wall paths."""
+    wall = qsg.BoundaryCondition.InfiniteWall
+    L = 0.02 * n
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.0, -0.2 * L, 0.05 * L, barrier=0.5)
+    psi0 = psi0.copy()
+    psi0[0] = 0.3
+    a = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=4, precision=precision, boundary=wall)
+    b = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01 - 0.002j, order=4, precision=precision, boundary=wall)
+    assert abs(a.get_psi()[0] - 0.3) <= 1e-7
+    a.step(9)
+    b.step(4)
+    b.step(5)
+    got = a.get_psi()
+    assert np.array_equal(got, b.get_psi())
+    ref = oracle.evolve1d(psi0, V, dx, 0.01 - 0.002j, 9, order=4, wall=True)
+    assert rel_l2(got, ref) <= (PLAIN_TOL if precision == "fp64" else MIXED_TOL)
+    a.close()
+    b.close()
+
+
 def test_wall_long_renormalising_and_set_psi(qsg, ctx, oracle):
     """A renormalising Bluestein four-step wall and its set_psi (the odd
     extension rebuilt, zero above it)."""
