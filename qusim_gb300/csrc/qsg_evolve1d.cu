@@ -155,7 +155,7 @@ cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *
 }
 
 // ---------------------------------------------------------------------------
-// four-step geometry: n = n1 * n2 (8192 .. 262144), n1 (row, contiguous) and n2
+// four-step geometry: n = n1 * n2 (8192 .. 1048576), n1 (row, contiguous) and n2
 // (column) each 64 .. 1024; by default n1 = n2 or 2*n2
 // ---------------------------------------------------------------------------
 
@@ -171,7 +171,7 @@ int fs_default_n1(uint64_t n)
 
 bool fs_geom(int prec, uint64_t n, FsGeom *g, int n1)
 {
-    if ((n & (n - 1)) || n < 8192 || n > 262144) return false;
+    if ((n & (n - 1)) || n < 8192 || n > 1048576) return false;
     if (n1 == 0) n1 = fs_default_n1(n);
     if (n1 < 64 || n1 > 1024 || (n1 & (n1 - 1)) || n % (uint64_t)n1) return false;
     const uint64_t n2 = n / (uint64_t)n1;

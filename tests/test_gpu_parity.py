@@ -161,8 +161,8 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    # periodic lengths that are not powers of two: up to 131072 (2n - 1 <= 262144)
-    psi0, V, dx = gauss_packet_1d(131073, -5000, 5000, 1.0, -10, 3.0)
+    # periodic lengths that are not powers of two: up to 524288 (2n - 1 <= 1048576)
+    psi0, V, dx = gauss_packet_1d(524289, -5000, 5000, 1.0, -10, 3.0)
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
             qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision=precision)
@@ -245,7 +245,7 @@ def test_autotune_keeps_state(qsg, ctx):
     assert inst.steps_taken() == 3
 
 
-@pytest.mark.parametrize("n", [8192, 16384, 32768, 65536, 131072, 262144])
+@pytest.mark.parametrize("n", [8192, 16384, 32768, 65536, 131072, 262144, 524288, 1048576])
 @pytest.mark.parametrize("order", [2, 4])
 def test_evolve1d_fourstep_vs_oracle(qsg, ctx, oracle, n, order):
     """Sizes above one CTA run as four-step column / row passes."""
@@ -349,17 +349,17 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 
 def test_wall_limits_are_reported(qsg, ctx):
-    """InfiniteWall: powers of two up to 131072 (the 2n extension of the largest
-    fits the four-step passes' 262144 sites) and any other length up to 65536,
-    whose Bluestein transforms of the 2n extension take 4n - 1 <= 262144 sites."""
+    """InfiniteWall: powers of two up to 524288 (the 2n extension of the largest
+    fits the four-step passes' 1048576 sites) and any other length up to 262144,
+    whose Bluestein transforms of the 2n extension take 4n - 1 <= 1048576 sites."""
     wall = qsg.BoundaryCondition.InfiniteWall
-    psi0, V, dx = gauss_packet_1d(262144, -5000, 5000, 1.0, -10, 3.0)
+    psi0, V, dx = gauss_packet_1d(1 << 20, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
-            qsg.Instance.create_1d(ctx, psi0[:65537], V[:65537], dx, 0.02, boundary=wall, precision=precision)
+            qsg.Instance.create_1d(ctx, psi0[:262145], V[:262145], dx, 0.02, boundary=wall, precision=precision)
         assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
@@ -396,7 +396,7 @@ def test_wall_any_length_vs_oracle(qsg, ctx, oracle, n, order):
         inst.close()
 
 
-@pytest.mark.parametrize("n,order", [(2049, 4), (3000, 2), (20000, 4), (65535, 2)])
+@pytest.mark.parametrize("n,order", [(2049, 4), (3000, 2), (20000, 4), (65535, 2), (250000, 4)])
 def test_wall_long_any_length_vs_oracle(qsg, ctx, oracle, n, order):
     """InfiniteWall at lengths above 2048 that are not powers of two: Bluestein
     transforms of the 2n odd extension on the four-step passes (the two sites the
@@ -505,7 +505,8 @@ def test_wall_any_length_renormalising_and_set_psi(qsg, ctx, oracle):
     assert abs(inst.norm2() - 1.0) <= 1e-13
 
 
-@pytest.mark.parametrize("n,order", [(4097, 4), (4099, 2), (6000, 4), (10007, 2), (100000, 4), (131070, 2)])
+@pytest.mark.parametrize("n,order", [(4097, 4), (4099, 2), (6000, 4), (10007, 2), (100000, 4), (131070, 2),
+                                     (200000, 4), (500000, 2)])
 def test_periodic_long_any_length_vs_oracle(qsg, ctx, oracle, n, order):
     """Periodic lengths above 4096 that are not powers of two: the reference's
     ExpT/ExpV (src/SplittingMethod1D.cpp:48-57, 83-90) on its KISS transforms of
@@ -691,7 +692,7 @@ def wall_packet(n):
     return psi.astype(np.complex128), 0.7 * np.exp(-xs * xs / 2), 0.1
 
 
-@pytest.mark.parametrize("n", [4096, 8192, 32768, 131072])
+@pytest.mark.parametrize("n", [4096, 8192, 32768, 131072, 524288])
 @pytest.mark.parametrize("order", [2, 4])
 def test_wall_beyond_one_cta_vs_oracle(qsg, ctx, oracle, n, order):
     """InfiniteWall above the one-CTA sizes (n > 4096 complex64, > 2048

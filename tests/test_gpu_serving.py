@@ -80,8 +80,8 @@ def test_bad_requests_are_refused():
     with pytest.raises(q.QsgError) as e:
         srv.submit(big, big.real, 0.1, 0.01, 10, dy=0.1)
     assert e.value.code == 2
-    odd = np.ones(131073, np.complex128)  # not a power of two and above 131072: no transform for it
-    rid = srv.submit(odd, odd.real, 0.1, 0.01, 10)
+    odd = np.ones((4097, 2), np.complex128)  # a 2D side above 4096 that is not a power of two
+    rid = srv.submit(odd, odd.real, 0.1, 0.01, 10, dy=0.1)
     assert srv.wait(rid, 60) == q.Server.FAILED
     with pytest.raises(q.QsgError) as e:
         srv.take(rid)

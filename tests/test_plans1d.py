@@ -18,7 +18,7 @@ def tuples(q, prec, n, boundary=0):
 
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
 def test_four_step_splits(q, prec):
-    for lg in range(13, 19):
+    for lg in range(13, 21):
         n = 1 << lg
         plans = tuples(q, prec, n)
         fs = [p for p in plans if p[0] == 1]
@@ -51,8 +51,10 @@ def test_lengths_without_choices(q):
     assert tuples(q, "fp64", 4097) == [(1, 128, 0)]
     assert tuples(q, "mixed", 100000) == [(1, 512, 0)]    # M = 262144
     assert tuples(q, "fp64", 131071) == [(1, 512, 0)]
-    assert tuples(q, "mixed", 131073) == []               # M = 524288: beyond the passes
-    assert tuples(q, "mixed", 1 << 19) == []
+    assert tuples(q, "mixed", 131073) == [(1, 1024, 0)]   # M = 524288
+    assert tuples(q, "fp64", 524287) == [(1, 1024, 0)]    # M = 1048576
+    assert tuples(q, "mixed", 524289) == []               # M = 2097152: beyond the passes
+    assert tuples(q, "mixed", 1 << 21) == []
     assert tuples(q, "mixed", 32) == [(0, 0, 0)]   # powers of two below 64: Bluestein
     assert tuples(q, "mixed", 1) == []
     assert tuples(q, 7, 1024) == []                # unknown precision
@@ -65,7 +67,8 @@ def test_wall_plans(q):
     plans = tuples(q, "mixed", 65536, WALL)
     assert plans and all(k == 1 and t == 0 for k, _, t in plans)
     assert {n1 for _, n1, _ in plans} == {n1 for k, n1, _ in tuples(q, "mixed", 131072) if k == 1}
-    assert tuples(q, "mixed", 262144, WALL) == []
+    assert tuples(q, "mixed", 524288, WALL)[0] == (1, 1024, 0)   # the 2^20 extension
+    assert tuples(q, "mixed", 1 << 20, WALL) == []
     # any other length: one Bluestein kernel on the 2n extension (2n - 1 <= 8192 / 4096)
     assert tuples(q, "mixed", 1000, WALL) == [(0, 0, 0)]
     assert tuples(q, "mixed", 32, WALL) == [(0, 0, 0)]
@@ -75,5 +78,6 @@ def test_wall_plans(q):
     assert tuples(q, "mixed", 3000, WALL) == [(1, 128, 0)]     # M = 16384
     assert tuples(q, "fp64", 3000, WALL) == [(1, 128, 0)]
     assert tuples(q, "mixed", 65535, WALL) == [(1, 512, 0)]    # M = 262144
-    assert tuples(q, "mixed", 65537, WALL) == []
+    assert tuples(q, "fp64", 262143, WALL) == [(1, 1024, 0)]   # M = 1048576
+    assert tuples(q, "mixed", 262145, WALL) == []
     assert tuples(q, "mixed", 1, WALL) == []
