@@ -155,8 +155,8 @@ cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *
 }
 
 // ---------------------------------------------------------------------------
-// four-step geometry: n = n1 * n2 (8192 .. 1048576), n1 (row, contiguous) and n2
-// (column) each 64 .. 1024; by default n1 = n2 or 2*n2
+// four-step geometry: n = n1 * n2 (8192 .. 4194304), n1 (row, contiguous) and n2
+// (column) each 64 .. 2048; by default n1 = n2 or 2*n2
 // ---------------------------------------------------------------------------
 
 constexpr int fs_col_w(int prec, int n2) { return prec == 1 ? 4096 / n2 : 2048 / n2; }   // W*n2/E = 256
@@ -171,11 +171,11 @@ int fs_default_n1(uint64_t n)
 
 bool fs_geom(int prec, uint64_t n, FsGeom *g, int n1)
 {
-    if ((n & (n - 1)) || n < 8192 || n > 1048576) return false;
+    if ((n & (n - 1)) || n < 8192 || n > 4194304) return false;
     if (n1 == 0) n1 = fs_default_n1(n);
-    if (n1 < 64 || n1 > 1024 || (n1 & (n1 - 1)) || n % (uint64_t)n1) return false;
+    if (n1 < 64 || n1 > 2048 || (n1 & (n1 - 1)) || n % (uint64_t)n1) return false;
     const uint64_t n2 = n / (uint64_t)n1;
-    if (n2 < 64 || n2 > 1024) return false;
+    if (n2 < 64 || n2 > 2048) return false;
     g->n = (int)n;
     g->n2 = (int)n2;
     g->n1 = n1;
@@ -235,8 +235,8 @@ static cudaError_t run_fs_rowkin(const FsGeom &g, const FsRowArgs &a, double dtk
     return cudaGetLastError();
 }
 
-#define QSG_FS_N(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024)
-#define QSG_FS_N2(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024)
+#define QSG_FS_N(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
+#define QSG_FS_N2(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
 
 cudaError_t launch_fs_col(int prec, const FsGeom &g, const FsColArgs &a, int ninst, cudaStream_t st)
 {

@@ -161,8 +161,8 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    # periodic lengths that are not powers of two: up to 524288 (2n - 1 <= 1048576)
-    psi0, V, dx = gauss_packet_1d(524289, -5000, 5000, 1.0, -10, 3.0)
+    # periodic lengths that are not powers of two: up to 2097152 (2n - 1 <= 4194304)
+    psi0, V, dx = gauss_packet_1d(2097153, -5000, 5000, 1.0, -10, 3.0)
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
             qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision=precision)
@@ -262,6 +262,30 @@ def test_evolve1d_fourstep_vs_oracle(qsg, ctx, oracle, n, order):
             assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-10 * max(1, abs(pot))
 
 
+@pytest.mark.parametrize("n,wall", [(1 << 22, False), (2000000, False), (1 << 21, True), (1000000, True)])
+def test_largest_1d_lengths_vs_oracle(qsg, ctx, oracle, n, wall):
+    """The largest 1D lengths: 2^22 sites on the 2048 x 2048 four-step passes, a
+    periodic 2,000,000 through Bluestein (M = 2^22), a 2^21 wall (its 2^22
+    extension) and a 1,000,000 wall (Bluestein of its extension, M = 2^22).
+    Three O2 steps in two calls against the oracle: complex128 <= 1e-12 with
+    KinEn and PotEn at 1e-10, complex64 <= 1e-5."""
+    bc = qsg.BoundaryCondition.InfiniteWall if wall else qsg.BoundaryCondition.Period
+    L = 0.01 * n
+    psi0, V, dx = gauss_packet_1d(n, -L, L, 1.5, -0.2 * L, 0.02 * L, barrier=0.7)
+    ref = oracle.evolve1d(psi0, V, dx, 0.01, 3, order=2, wall=wall)
+    for precision, tol in (("fp64", PLAIN_TOL), ("mixed", MIXED_TOL)):
+        inst = qsg.Instance.create_1d(ctx, psi0, V, dx, 0.01, order=2, precision=precision, boundary=bc)
+        assert inst.plan().as_tuple()[0] == 1
+        inst.step(1)
+        inst.step(2)
+        assert rel_l2(inst.get_psi(), ref) <= tol, (precision, rel_l2(inst.get_psi(), ref))
+        if precision == "fp64":
+            kin, pot = inst.energies()
+            assert abs(kin - oracle.kinen1d(ref, dx, wall=wall)) <= 1e-10 * abs(kin)
+            assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-10 * max(1, abs(pot))
+        inst.close()
+
+
 def test_fourstep_renormalize(qsg, ctx, oracle):
     n = 65536
     psi0, V, dx = gauss_packet_1d(n, -0.05 * n, 0.05 * n, 1.0, -100.0, 40.0, barrier=0.5)
@@ -349,17 +373,17 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 
 def test_wall_limits_are_reported(qsg, ctx):
-    """InfiniteWall: powers of two up to 524288 (the 2n extension of the largest
-    fits the four-step passes' 1048576 sites) and any other length up to 262144,
-    whose Bluestein transforms of the 2n extension take 4n - 1 <= 1048576 sites."""
+    """InfiniteWall: powers of two up to 2097152 (the 2n extension of the largest
+    fits the four-step passes' 4194304 sites) and any other length up to 1048576,
+    whose Bluestein transforms of the 2n extension take 4n - 1 <= 4194304 sites."""
     wall = qsg.BoundaryCondition.InfiniteWall
-    psi0, V, dx = gauss_packet_1d(1 << 20, -5000, 5000, 1.0, -10, 3.0)
+    psi0, V, dx = gauss_packet_1d(1 << 22, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
-            qsg.Instance.create_1d(ctx, psi0[:262145], V[:262145], dx, 0.02, boundary=wall, precision=precision)
+            qsg.Instance.create_1d(ctx, psi0[:1048577], V[:1048577], dx, 0.02, boundary=wall, precision=precision)
         assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
