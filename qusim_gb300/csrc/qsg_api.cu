@@ -1028,34 +1028,35 @@ int build_ktab_1d(qsg_inst *in)
 // layout: V w before the first convolution of a call ("open"), K_d between the
 // two, V merged with w* and w between substeps (plain V), w* V at the end of a
 // call ("close"); each is zero from n on, which truncates the convolutions'
-// outputs and keeps the buffer zero there.  Values are formed in long double
-// on the host: plain complex (complex128) or factor - 1 (complex64 columns);
-// the kernels are plain complex in both.
+// outputs and keeps the buffer zero there.  The chirp and FFT_M(h) / M come
+// from double-double arithmetic; the phase factors are formed in double as the
+// reference forms its own (exp(f V) and exp(f K), src/SplittingMethod1D.cpp:
+// 51-53, 87), and uploaded as plain complex (complex128) or factor - 1 (complex64
+// columns); the kernels are plain complex in both.
 int build_bfs_tables(qsg_inst *in)
 {
     const SplitConsts sc;
     const int ntab = in->order == 2 ? 1 : 2;
-    const long double vc[2] = {in->order == 2 ? 0.5L : (long double)sc.c1, (long double)sc.c2};
-    const long double tc[2] = {in->order == 2 ? 1.0L : (long double)sc.d1, (long double)sc.d2};
-    using cl = std::complex<long double>;
+    const double vc[2] = {in->order == 2 ? 0.5 : sc.c1, sc.c2};
+    const double tc[2] = {in->order == 2 ? 1.0 : sc.d1, sc.d2};
+    using cl = std::complex<double>;
     const uint64_t n = in->bfs_n, M = in->n;
     const size_t cs = csize(in->prec);
     int rc;
     std::vector<cl> w, hs;
-    qsg::blue_tables(n, (int)M, w, hs);  // chirp (zero above n), FFT_M(h) / M
+    qsg::blue_tables_dd(n, M, w, hs);  // chirp (zero above n), FFT_M(h) / M
     std::vector<double> Vh(n);
     QSG_CUDA(cudaMemcpyAsync(Vh.data(), in->V, n * 8, cudaMemcpyDeviceToHost, in->ctx->st));
     QSG_CUDA(cudaStreamSynchronize(in->ctx->st));
     // exp(f x) for f = a (-i dt / hbar) (ExpV: a = c, x = V; ExpT: a = d, x = fold(k)^2 DT)
-    const cl dt((long double)in->dt.real(), (long double)in->dt.imag());
-    const cl mi_dt_h = cl(0, -1) * dt / (long double)in->hbar;
-    auto phase = [&](long double a, long double x) { return std::exp(mi_dt_h * (a * x)); };
+    const cl mi_dt_h = cl(0, -1) * in->dt / in->hbar;
+    auto phase = [&](double a, double x) { return std::exp(mi_dt_h * (a * x)); };
     // upload M natural values: complex64 as factor - 1, complex128 plain
     auto put = [&](const std::vector<cl> &v, void **dst, bool minus_one) -> int {
         if (int r = inst_alloc(in, M * cs, dst)) return r;
         std::vector<unsigned char> h(M * cs);
         for (uint64_t i = 0; i < M; ++i) {
-            const cl z = (minus_one && in->prec == 1) ? v[i] - 1.0L : v[i];
+            const cl z = (minus_one && in->prec == 1) ? v[i] - 1.0 : v[i];
             if (in->prec == 0) {
                 const double d[2] = {(double)z.real(), (double)z.imag()};
                 std::memcpy(&h[i * cs], d, cs);
@@ -1075,7 +1076,7 @@ int build_bfs_tables(qsg_inst *in)
     // a wall's 2n odd extension: KinEn transforms it with sites 0 and n / 2 zeroed
     // (src/SplittingMethod1D.cpp:112-114); the steps zero site 0 once per uploaded state
     const bool wall = in->wall_ext;
-    auto mask = [&](uint64_t j) { return wall && (j == 0 || j == n / 2) ? 0.0L : 1.0L; };
+    auto mask = [&](uint64_t j) { return wall && (j == 0 || j == n / 2) ? 0.0 : 1.0; };
     void *open = nullptr, *vc1 = nullptr, *vc2 = nullptr, *close = nullptr, *k1 = nullptr, *k2 = nullptr;
     void *chirp = nullptr, *h1 = nullptr, *h2 = nullptr;
     fill([&](uint64_t j) { return w[j] * phase(vc[0], Vh[j]); });
@@ -1090,10 +1091,10 @@ int build_bfs_tables(qsg_inst *in)
     }
     // ExpT periodic (SplittingMethod1D.cpp:51-53): DT = (Dk hbar)^2 / (2m), Dk = 2 pi / (dx n);
     // on a wall's 2n extension Dk = pi / (dx n_wall), the wall ExpT's (:72-74)
-    const long double dk = 2 * (long double)kPi / ((long double)in->dx * n);
-    const long double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * (long double)in->mass);
+    const double dk = 2 * kPi / (in->dx * (double)n);
+    const double DT = (dk * in->hbar) * (dk * in->hbar) / (2 * in->mass);
     auto fold2 = [&](uint64_t k) {
-        const long double f = (long double)(k > n / 2 ? n - k : k);
+        const double f = (double)(k > n / 2 ? n - k : k);
         return f * f * DT;
     };
     fill([&](uint64_t k) { return phase(tc[0], fold2(k)); });
@@ -1113,7 +1114,7 @@ int build_bfs_tables(qsg_inst *in)
     for (uint64_t k2 = 0; k2 < n2; ++k2)
         for (uint64_t k1 = 0; k1 < n1; ++k1) {
             const uint64_t k = k2 + n2 * k1;
-            t[k2 * n1 + k1] = std::conj(hs[(M - k) % M]) / (long double)n;
+            t[k2 * n1 + k1] = std::conj(hs[(M - k) % M]) / (double)n;
         }
     if ((rc = put(t, &h2, false))) return rc;
     // KinEn weights of the n frequencies: fold(k)^2 DT with the periodic branch's DT
@@ -1121,11 +1122,11 @@ int build_bfs_tables(qsg_inst *in)
     // |F|^2 of the odd extension is even, so the ratio over the 2n frequencies is the
     // wall's over k < n)
     {
-        const long double DTk = wall ? DT : dk * dk / (2 * (long double)in->mass);
+        const double DTk = wall ? DT : dk * dk / (2 * in->mass);
         std::vector<double> kw(n);
         for (uint64_t k = 0; k < n; ++k) {
-            const long double f = (long double)(k > n / 2 ? n - k : k);
-            kw[k] = (double)(f * f * DTk);
+            const double f = (double)(k > n / 2 ? n - k : k);
+            kw[k] = f * f * DTk;
         }
         void *p = nullptr;
         if ((rc = inst_alloc(in, n * 8, &p))) return rc;
@@ -3412,6 +3413,13 @@ size_t request_bytes(const qsg_request &r)
     const size_t n = (size_t)r.nx * (r.dim == 2 ? r.ny : 1);
     const size_t cs = r.precision == QSG_MIXED ? 8 : 16;
     const int ntab = r.order == 2 ? 1 : 2;
+    if (r.dim == 1 && (n & (n - 1)) && n > 4096) {
+        // Bluestein on the four-step passes: a buffer of M >= 2n - 1 sites with its
+        // state, V, 7 (O2) or 9 (O4) tables and the upload staging, KinEn weights of n
+        size_t m = 1;
+        while (m < 2 * n - 1) m <<= 1;
+        return m * (cs + 8 + (r.order == 2 ? 7 : 9) * cs + 16) + n * 8 + (r.spec ? n * 24 : 0);
+    }
     const size_t work = r.dim == 2 && r.precision == QSG_MIXED ? n * cs : 0;  // momentum form
     return n * (cs + 8 + ntab * cs * 2) + n * 16 + work + (r.spec ? n * 24 : 0);  // psi, V, tables, staging, spec buffer
 }
@@ -3457,7 +3465,7 @@ void srv_finish(qsg_server *S, SrvRequest &q, int err, const std::string &msg)
             }
         }
         if (!err) {
-            q.result.resize(2 * (size_t)q.inst->n);
+            q.result.resize(2 * (size_t)user_n(q.inst));  // the caller's sites (a Bluestein buffer holds more)
             q.inst->st = S->ctx->st;
             S->ctx->mu.unlock();
             int rc = qsg_get_psi(q.inst, q.result.data());

@@ -32,6 +32,10 @@ int blue_m_for(int prec, uint64_t n);
 int blue_elems(int prec);
 void blue_tables(uint64_t n, int m, std::vector<std::complex<long double>> &w,
                  std::vector<std::complex<long double>> &hs);
+// the same tables for the long buffers of the four-step passes (m up to 2^22),
+// computed in double-double arithmetic on host threads and rounded to double
+void blue_tables_dd(uint64_t n, uint64_t m, std::vector<std::complex<double>> &w,
+                    std::vector<std::complex<double>> &hs);
 cudaError_t launch_evolve1d_blue(int prec, int m, const BlueArgs &a, cudaStream_t st);
 cudaError_t launch_kinetic1d_blue(int prec, int m, const BlueArgs &a, double dtk, double *sums, cudaStream_t st);
 // 2D grids with a side that is not a power of two: row pass (rows of ny), column pass

@@ -175,11 +175,14 @@ def test_requests_admitted_while_others_run():
 
 
 def test_served_length_not_power_of_two_equals_solo():
-    """A request on a 1000-site grid (Bluestein transforms) beside power-of-two
-    ones: served in chunks, bitwise its solo run."""
+    """Requests on a 1000-site grid (Bluestein transforms in one CTA) and a
+    5000-site grid (Bluestein on the four-step passes) beside power-of-two ones:
+    served in chunks, bitwise their solo runs."""
     import qusim_gb300 as q
     p, v, dx = gauss_packet_1d(1000, -50, 50, 1.0, -10, 3.0, barrier=0.8)
-    reqs = make_requests()[:3] + [dict(psi0=p, V=v, dx=dx, dt=0.01, nsteps=333, order=4)]
+    p5, v5, dx5 = gauss_packet_1d(5000, -100, 100, 1.0, -20, 5.0, barrier=0.8)
+    reqs = make_requests()[:3] + [dict(psi0=p, V=v, dx=dx, dt=0.01, nsteps=333, order=4),
+                                  dict(psi0=p5, V=v5, dx=dx5, dt=0.01, nsteps=40, order=4)]
     srv = q.Server(0)
     ids = [srv.submit(r["psi0"], r["V"], r["dx"], r["dt"], r["nsteps"], order=r["order"], precision="mixed",
                       dy=r.get("dy")) for r in reqs]
