@@ -65,6 +65,26 @@ def test_double_slit_expression_equals_arrays(q, ctx, precision):
     b.close()
 
 
+@pytest.mark.parametrize("n,wall", [(5000, False), (3000, True), (1 << 20, True)])
+def test_expression_inputs_on_long_lines_equal_arrays(q, ctx, n, wall):
+    """Device-sampled inputs on the long 1D paths (a Bluestein four-step buffer,
+    a wall's odd extension rebuilt from a device source): the instance evolves
+    exactly as one created from its own sampled psi0 and the same V."""
+    bc = q.BoundaryCondition.InfiniteWall if wall else q.BoundaryCondition.Period
+    h = 0.01 * n
+    a = q.Instance.create_1d_expr(ctx, "exp(I*x)*exp(-(x+0.2*%g)^2/%g)" % (h, 0.002 * h * h), "0.5*exp(-x*x/2)",
+                                  n, -h, h, 0.01, order=4, precision="fp64", boundary=bc)
+    xs, dx = grid(n, -h, h)
+    psi0 = a.get_psi()
+    b = q.Instance.create_1d(ctx, psi0, 0.5 * np.exp(-xs * xs / 2), dx, 0.01, order=4, precision="fp64", boundary=bc)
+    a.step(3)
+    b.step(3)
+    pa, pb = a.get_psi(), b.get_psi()
+    assert np.linalg.norm(pa - pb) <= 1e-13 * np.linalg.norm(pb)
+    a.close()
+    b.close()
+
+
 def test_expression_errors_are_reported(q, ctx):
     with pytest.raises(q.QsgError) as e:
         q.Instance.create_1d_expr(ctx, "gauss(x,-20,5", "exp(-x*x)", 1024, -50.0, 50.0, 0.02)
