@@ -108,8 +108,9 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * grid; any other n from 2 to 2048 keeps the 2n extension in one CTA stepped
  * by Bluestein transforms, and from 2049 to 1048576 steps it by Bluestein's
  * convolutions on the four-step passes (M >= 4n - 1).  Kept in HBM or in one
- * CTA, the extension's sites 0 and n are zeroed before the first transform of
- * each call.  Reads and writes of psi cover its n sites.
+ * CTA, the extension's site 0 (the caller's psi_0) is zeroed before the first
+ * step after each upload of the state (create, qsg_set_psi), site n is zero
+ * from the upload on.  Reads and writes of psi cover its n sites.
  * Replaces SplittingMethod1D::InitSystem1D (src/SplittingMethod1D.cpp:5-31)
  * after the host has sampled psi0 / V (src/EvolverImpl1D.cpp:33-81). */
 int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
