@@ -170,6 +170,46 @@ inline int get_twiddles(qsg_ctx *ctx, int prec, int L, int E, const void **out)
     return QSG_OK;
 }
 
+// exp(-2 pi i m / n) for m < n in long double: cosl / sinl of angles of at most
+// pi / 4 only, from a table of n / 8 + 1 entries and the quarter-turn symmetries
+// (exact sign changes and swaps) where 8 divides n, directly otherwise.  Long
+// circles (2^22 entries for the longest four-step lines) cost an eighth of the
+// trigonometric calls, which some hosts run in software for long double.
+struct CircleLD {
+    long n, n8;
+    std::vector<long double> c, s;
+    explicit CircleLD(long n_) : n(n_), n8(n_ % 8 == 0 ? n_ / 8 : 0)
+    {
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (long j = 0; n8 && j <= n8; ++j) {
+            const long double ang = two_pi * (long double)j / (long double)n;
+            c.push_back(cosl(ang));
+            s.push_back(sinl(ang));
+        }
+    }
+    void at(long m, long double *re, long double *im) const
+    {
+        if (!n8) {
+            const long double ang = 6.283185307179586476925286766559005768L * (long double)m / (long double)n;
+            *re = cosl(ang);
+            *im = -sinl(ang);
+            return;
+        }
+        // theta = 2 pi m / n = k pi / 2 + alpha, alpha = 2 pi a / n with a in [-n/8, n/8)
+        const long n4 = 2 * n8, k = (m + n8) / n4, a = m - k * n4;
+        const long double ca = c[a < 0 ? -a : a], sa = a < 0 ? -s[-a] : s[a];
+        long double cs, sn;
+        switch (k & 3) {
+        case 0: cs = ca; sn = sa; break;
+        case 1: cs = -sa; sn = ca; break;
+        case 2: cs = -ca; sn = -sa; break;
+        default: cs = sa; sn = -ca; break;
+        }
+        *re = cs;
+        *im = -sn;
+    }
+};
+
 // exp(-2 pi i m / n), m < n
 inline int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
 {
@@ -180,10 +220,11 @@ inline int get_circle(qsg_ctx *ctx, int prec, int n, const void **out)
         return QSG_OK;
     }
     std::vector<unsigned char> host((size_t)n * twsize(prec));
-    const long double two_pi = 6.283185307179586476925286766559005768L;
+    const CircleLD circle(n);
     for (int m = 0; m < n; ++m) {
-        const long double ang = two_pi * (long double)m / (long double)n;
-        put_twiddle(prec, &host[(size_t)m * twsize(prec)], cosl(ang), -sinl(ang));
+        long double re, im;
+        circle.at(m, &re, &im);
+        put_twiddle(prec, &host[(size_t)m * twsize(prec)], re, im);
     }
     void *d = nullptr;
     int rc = dev_alloc(ctx, host.size(), &d, nullptr);
@@ -208,11 +249,12 @@ inline int get_fs_grid(qsg_ctx *ctx, int prec, int n1, int n2, const void **out)
     }
     const long n = (long)n1 * n2;
     std::vector<unsigned char> host((size_t)n * twsize(prec));
-    const long double two_pi = 6.283185307179586476925286766559005768L;
+    const CircleLD circle(n);
     for (long r = 0; r < n2; ++r)
         for (long c = 0; c < n1; ++c) {
-            const long double ang = two_pi * (long double)(r * c) / (long double)n;
-            put_twiddle(prec, &host[(size_t)(r * n1 + c) * twsize(prec)], cosl(ang), -sinl(ang));
+            long double re, im;
+            circle.at(r * c, &re, &im);
+            put_twiddle(prec, &host[(size_t)(r * n1 + c) * twsize(prec)], re, im);
         }
     void *d = nullptr;
     int rc = dev_alloc(ctx, host.size(), &d, nullptr);
