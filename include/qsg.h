@@ -91,8 +91,8 @@ void *qsg_ctx_stream(qsg_ctx *ctx);
 /* Device bytes currently held by the context's instances and scratch. */
 size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
 
-/* Create a 1D instance: n a power of two, 64 .. 4194304, or any other length
- * from 2 to 2097152, stepped through Bluestein transforms (as are the powers
+/* Create a 1D instance: n a power of two, 64 .. 8388608, or any other length
+ * from 2 to 4194304, stepped through Bluestein transforms (as are the powers
  * of two below 64): in one CTA up to n = 4096, above that as two circular
  * convolutions of length M (the smallest power of two >= 2n - 1) on the
  * four-step passes over a buffer of M sites whose sites from n on stay zero.
@@ -103,10 +103,10 @@ size_t qsg_ctx_bytes_in_use(qsg_ctx *ctx);
  * boundary: QSG_PERIOD, or QSG_INFINITE_WALL (psi_0 = psi_n = 0, kinetic step
  * through the 2n odd extension, src/SplittingMethod1D.cpp:61-81): for powers
  * of two from 64, one CTA holds the 2n extension up to n = 4096 (QSG_MIXED) /
- * 2048 (QSG_FP64); above that, up to n = 2097152, the instance keeps the 2n odd
+ * 2048 (QSG_FP64); above that, up to n = 4194304, the instance keeps the 2n odd
  * extension in HBM and steps it with the four-step passes of a periodic 2n
  * grid; any other n from 2 to 2048 keeps the 2n extension in one CTA stepped
- * by Bluestein transforms, and from 2049 to 1048576 steps it by Bluestein's
+ * by Bluestein transforms, and from 2049 to 2097152 steps it by Bluestein's
  * convolutions on the four-step passes (M >= 4n - 1).  Kept in HBM or in one
  * CTA, the extension's site 0 (the caller's psi_0) is zeroed before the first
  * step after each upload of the state (create, qsg_set_psi), site n is zero
@@ -321,8 +321,8 @@ int qsg_autotune(qsg_inst *inst, int trial_steps, int persist, qsg_plan2d *best,
  *   kind 0: resident -- one CTA holds the whole line for the whole call
  *           (periodic n <= 8192 complex64 / 4096 complex128, one-CTA walls);
  *   kind 1: four-step -- two passes per substep over the n2 x n1 view of the
- *           line (n = n1 * n2, n from 8192 to 4194304, n1 and n2 powers of two
- *           from 64 to 2048): column transforms of length n2, row transforms
+ *           line (n = n1 * n2, n from 8192 to 8388608, n1 a power of two from
+ *           64 to 4096, n2 from 64 to 2048): column transforms of length n2, row transforms
  *           of length n1;
  *   tma:    four-step complex64 with n2 = 128 .. 512: the column pass stages
  *           its tiles with tensor copies instead of load instructions.

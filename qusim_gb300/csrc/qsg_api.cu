@@ -891,7 +891,7 @@ void add_fs_plans(int prec, uint64_t n, bool tma_ok, std::vector<qsg_plan1d> &ou
 {
     const int d = qsg::fs_default_n1(n);
     std::vector<int> n1s{d};
-    for (int n1 = 2048; n1 >= 64; n1 >>= 1)
+    for (int n1 = 4096; n1 >= 64; n1 >>= 1)
         if (n1 != d) n1s.push_back(n1);
     for (int n1 : n1s) {
         qsg::FsGeom g;
@@ -926,7 +926,7 @@ void plans_1d(int prec, uint64_t n, int boundary, std::vector<qsg_plan1d> &out)
             else if (bfs_len_m(prec, 2 * n, &g)) out.push_back(qsg_plan1d{1, g.n1, 0, 0});
             return;
         }
-        if (n > 2097152) return;
+        if (n > 4194304) return;
         if (qsg::wall1d_supported(prec, n)) out.push_back(qsg_plan1d{0, 0, 0, 0});
         else add_fs_plans(prec, 2 * n, false, out);  // the periodic 2n odd extension
         return;
@@ -1803,7 +1803,7 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
     const int one_cta_m = any_len && n >= 2 ? qsg::blue_m_for(precision, blue_len) : 0;
     const uint64_t bfs_m = any_len && !one_cta_m ? bfs_len_m(precision, blue_len, &fsg) : 0;
     const bool wall_blue = wall && one_cta_m > 0;
-    const std::string wall_limits = " (supported: any n from 2 to 1048576, and powers of two up to 2097152)";
+    const std::string wall_limits = " (supported: any n from 2 to 2097152, and powers of two up to 4194304)";
     if (wall && any_len && !one_cta_m && !bfs_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     // walls above one CTA: a four-step periodic instance of the 2n odd extension
@@ -1814,10 +1814,10 @@ static int create_1d_locked(qsg_ctx *ctx, uint64_t n, double dx, double mass, do
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: InfiniteWall n=" + std::to_string(n) + wall_limits);
     if (!wall && any_len && !blue_m && !bfs_m)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
-                                             " (lengths that are not powers of two: 2 .. 2097152)");
+                                             " (lengths that are not powers of two: 2 .. 4194304)");
     if (!wall && pow2 && !resident && !qsg::fs_geom(precision, n, &fsg))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_1d: n=" + std::to_string(n) +
-                                             " (supported: powers of two, 64 .. 4194304)");
+                                             " (supported: powers of two, 64 .. 8388608)");
     // the plan: the one tuned for this shape (in this context or the plan cache),
     // else the default (one CTA where it fits, else four-step, default split)
     qsg_plan1d plan{resident ? 0 : 1, resident ? 0 : fsg.n1, 0, 0};
@@ -1998,7 +1998,7 @@ int qsg_create_1d_expr(qsg_ctx *ctx, uint64_t n, double x0, double dx, double ma
                        int normalize, qsg_inst **out)
 {
     if (!ctx || !out || !psi_expr || !v_expr) return fail(QSG_ERR_ARG, "qsg_create_1d_expr: null argument");
-    if (n == 0 || n > 4194304 || !(dx > 0) || !std::isfinite(x0))
+    if (n == 0 || n > 8388608 || !(dx > 0) || !std::isfinite(x0))
         return fail(QSG_ERR_ARG, "qsg_create_1d_expr: bad n, x0 or dx");
     void *buf = nullptr;
     int rc = sample_expr_buf(ctx, 1, n, 1, x0, 0.0, dx, 0.0, psi_expr, v_expr, normalize, &buf);
@@ -2036,7 +2036,7 @@ int qsg_create_1d_spec(qsg_ctx *ctx, uint64_t n, double dx, double mass, double 
     if (!ctx || !out) return fail(QSG_ERR_ARG, "qsg_create_1d_spec: null argument");
     int rc = check_spec(spec, "qsg_create_1d_spec");
     if (rc) return rc;
-    if (n == 0 || n > 4194304 || !(dx > 0)) return fail(QSG_ERR_ARG, "qsg_create_1d_spec: bad n or dx");
+    if (n == 0 || n > 8388608 || !(dx > 0)) return fail(QSG_ERR_ARG, "qsg_create_1d_spec: bad n or dx");
     void *buf = nullptr;
     {
         std::lock_guard<std::mutex> lk(ctx->mu);

@@ -155,25 +155,31 @@ cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *
 }
 
 // ---------------------------------------------------------------------------
-// four-step geometry: n = n1 * n2 (8192 .. 4194304), n1 (row, contiguous) and n2
-// (column) each 64 .. 2048; by default n1 = n2 or 2*n2
+// four-step geometry: n = n1 * n2 (8192 .. 8388608), n1 (row, contiguous) 64 ..
+// 4096 and n2 (column) 64 .. 2048; by default n1 = n2 or 2*n2, or n2 = 1024
+// where that would make n2 2048 (a column pass of 2048-point columns takes two
+// columns per CTA: 16-byte row segments, half a memory sector)
 // ---------------------------------------------------------------------------
 
 constexpr int fs_col_w(int prec, int n2) { return prec == 1 ? 4096 / n2 : 2048 / n2; }   // W*n2/E = 256
-constexpr int fs_row_b(int prec, int n1) { return prec == 1 ? 4096 / n1 : 2048 / n1; }   // B*n1/E = 256
+constexpr int fs_row_b(int prec, int n1)   // B*n1/E = 256 (512 for complex128 rows of 4096)
+{
+    return prec == 1 ? 4096 / n1 : (n1 >= 2048 ? 1 : 2048 / n1);
+}
 
 int fs_default_n1(uint64_t n)
 {
     int lg = 0;
     while ((1ull << lg) < n) ++lg;
-    return (int)(n >> (lg / 2));
+    const uint64_t n1 = n >> (lg / 2);
+    return (int)(n / n1 > 1024 && n / 1024 <= 4096 ? n / 1024 : n1);
 }
 
 bool fs_geom(int prec, uint64_t n, FsGeom *g, int n1)
 {
-    if ((n & (n - 1)) || n < 8192 || n > 4194304) return false;
+    if ((n & (n - 1)) || n < 8192 || n > 8388608) return false;
     if (n1 == 0) n1 = fs_default_n1(n);
-    if (n1 < 64 || n1 > 2048 || (n1 & (n1 - 1)) || n % (uint64_t)n1) return false;
+    if (n1 < 64 || n1 > 4096 || (n1 & (n1 - 1)) || n % (uint64_t)n1) return false;
     const uint64_t n2 = n / (uint64_t)n1;
     if (n2 < 64 || n2 > 2048) return false;
     g->n = (int)n;
@@ -235,7 +241,7 @@ static cudaError_t run_fs_rowkin(const FsGeom &g, const FsRowArgs &a, double dtk
     return cudaGetLastError();
 }
 
-#define QSG_FS_N(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
+#define QSG_FS_N(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048) X(T, 4096)
 #define QSG_FS_N2(X, T) X(T, 64) X(T, 128) X(T, 256) X(T, 512) X(T, 1024) X(T, 2048)
 
 cudaError_t launch_fs_col(int prec, const FsGeom &g, const FsColArgs &a, int ninst, cudaStream_t st)

@@ -161,8 +161,8 @@ def test_tunnelling_known_answer_gpu(qsg, ctx):
 
 
 def test_unsupported_sizes_are_reported(qsg, ctx):
-    # periodic lengths that are not powers of two: up to 2097152 (2n - 1 <= 4194304)
-    psi0, V, dx = gauss_packet_1d(2097153, -5000, 5000, 1.0, -10, 3.0)
+    # periodic lengths that are not powers of two: up to 4194304 (2n - 1 <= 8388608)
+    psi0, V, dx = gauss_packet_1d(4194305, -5000, 5000, 1.0, -10, 3.0)
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
             qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, precision=precision)
@@ -262,11 +262,13 @@ def test_evolve1d_fourstep_vs_oracle(qsg, ctx, oracle, n, order):
             assert abs(pot - oracle.poten(ref, V, dx)) <= 1e-10 * max(1, abs(pot))
 
 
-@pytest.mark.parametrize("n,wall", [(1 << 22, False), (2000000, False), (1 << 21, True), (1000000, True)])
+@pytest.mark.parametrize("n,wall", [(1 << 22, False), (1 << 23, False), (2000000, False), (4000000, False),
+                                    (1 << 21, True), (1 << 22, True), (1000000, True), (2000000, True)])
 def test_largest_1d_lengths_vs_oracle(qsg, ctx, oracle, n, wall):
-    """The largest 1D lengths: 2^22 sites on the 2048 x 2048 four-step passes, a
-    periodic 2,000,000 through Bluestein (M = 2^22), a 2^21 wall (its 2^22
-    extension) and a 1,000,000 wall (Bluestein of its extension, M = 2^22).
+    """The largest 1D lengths: 2^22 sites (4096 x 1024 four-step passes) and 2^23
+    (4096 x 2048), periodic 2,000,000 and 4,000,000 through Bluestein (M = 2^22,
+    2^23), walls of 2^21 and 2^22 (their 2^22 and 2^23 extensions) and of
+    1,000,000 and 2,000,000 (Bluestein of the extension, M = 2^22, 2^23).
     Three O2 steps in two calls against the oracle: complex128 <= 1e-12 with
     KinEn and PotEn at 1e-10, complex64 <= 1e-5."""
     bc = qsg.BoundaryCondition.InfiniteWall if wall else qsg.BoundaryCondition.Period
@@ -373,17 +375,17 @@ def test_wall_box_eigenstate(qsg, ctx, precision):
 
 
 def test_wall_limits_are_reported(qsg, ctx):
-    """InfiniteWall: powers of two up to 2097152 (the 2n extension of the largest
-    fits the four-step passes' 4194304 sites) and any other length up to 1048576,
-    whose Bluestein transforms of the 2n extension take 4n - 1 <= 4194304 sites."""
+    """InfiniteWall: powers of two up to 4194304 (the 2n extension of the largest
+    fits the four-step passes' 8388608 sites) and any other length up to 2097152,
+    whose Bluestein transforms of the 2n extension take 4n - 1 <= 8388608 sites."""
     wall = qsg.BoundaryCondition.InfiniteWall
-    psi0, V, dx = gauss_packet_1d(1 << 22, -5000, 5000, 1.0, -10, 3.0)
+    psi0, V, dx = gauss_packet_1d(1 << 23, -5000, 5000, 1.0, -10, 3.0)
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0, V, dx, 0.02, boundary=wall)
     assert e.value.code == 5
     for precision in ("mixed", "fp64"):
         with pytest.raises(qsg.QsgError) as e:
-            qsg.Instance.create_1d(ctx, psi0[:1048577], V[:1048577], dx, 0.02, boundary=wall, precision=precision)
+            qsg.Instance.create_1d(ctx, psi0[:2097153], V[:2097153], dx, 0.02, boundary=wall, precision=precision)
         assert e.value.code == 5
     with pytest.raises(qsg.QsgError) as e:
         qsg.Instance.create_1d(ctx, psi0[:1], V[:1], dx, 0.02, boundary=wall)
