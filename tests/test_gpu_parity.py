@@ -124,6 +124,31 @@ def test_evolve2d_shapes_vs_oracle(qsg, ctx, oracle, nx, ny, order, precision):
     assert rel_l2(inst.get_psi(), ref) <= tol
 
 
+@pytest.mark.parametrize("nx,ny,precision", [(8192, 128, "fp64"), (8192, 128, "mixed"), (8192, 2048, "fp64"),
+                                             (8192, 4096, "mixed")])
+def test_evolve2d_8192_columns_vs_oracle(qsg, ctx, oracle, nx, ny, precision):
+    """Grids with 8192 sites along x (the columns): the x split (G = 4) leaves
+    2048-point column transforms.  Two O2 steps in two calls against the oracle,
+    with Norm2, KinEn and PotEn."""
+    hx, hy = 0.0125 * nx, 0.05 * ny
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=0.08 * min(hx, hy))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=8, seed=2, spread=0.5 * min(hx, hy))
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.01, 2, order=2)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=2, precision=precision)
+    inst.step(1)
+    inst.step(1)
+    tol = PLAIN_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_l2(inst.get_psi(), ref) <= tol
+    etol = 1e-10 if precision == "fp64" else 1e-4
+    kin, pot = inst.energies()
+    assert abs(kin - oracle.kinen2d(ref, dx, dy)) <= etol * abs(kin)
+    assert abs(pot - oracle.poten(ref, V, dx * dy)) <= etol * max(1.0, abs(pot))
+    # sums of up to 33.5 M terms in another order than the reference's: 1e-11 for complex128
+    assert abs(inst.norm2() - oracle.norm2(ref, dx * dy)) <= (1e-11 if precision == "fp64" else 1e-5)
+    inst.close()
+
+
 @pytest.mark.parametrize("n", [64, 128, 512, 2048, 4096])
 @pytest.mark.parametrize("order", [2, 4])
 def test_evolve1d_sizes_vs_oracle(qsg, ctx, oracle, n, order):
