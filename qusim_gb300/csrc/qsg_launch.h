@@ -58,8 +58,8 @@ cudaError_t launch_wall1d(int prec, int n, const Evolve1DBatchArgs &a, cudaStrea
 cudaError_t launch_kinetic1d_wall(int prec, int n, const void *psi, const void *tw, double dtk, double *sums,
                                   cudaStream_t st);
 
-// 1D four-step geometry (n = n1 * n2, 2^13 .. 2^18; n1, n2 in 64 .. 1024) and
-// passes over ninst instances
+// 1D four-step geometry (n = n1 * n2, 2^13 .. 2^23; n1 in 64 .. 4096, n2 in
+// 64 .. 2048) and passes over ninst instances
 struct FsGeom {
     int n, n1, n2;
     int col_e, col_w, col_threads, col_blocks;
@@ -67,7 +67,7 @@ struct FsGeom {
     int row_e, row_b, row_threads, row_blocks;
     size_t row_smem;
 };
-// n1 = 0: the default split (n1 = n2 or 2 n2)
+// n1 = 0: the default split (n1 = n2 or 2 n2; 4096 x 1024 for 2^22)
 bool fs_geom(int prec, uint64_t n, FsGeom *g, int n1 = 0);
 int fs_default_n1(uint64_t n);
 cudaError_t launch_fs_col(int prec, const FsGeom &g, const FsColArgs &a, int ninst, cudaStream_t st);
