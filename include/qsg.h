@@ -119,10 +119,10 @@ int qsg_create_1d(qsg_ctx *ctx, uint64_t n, double dx, double mass, double hbar,
 
 /* Create a 2D instance, nx*ny sites, index iy + ix*ny.  Periodic only, as in
  * the reference (src/SplittingMethod2D.cpp:21-29).  Sides that are powers of
- * two (128 .. 4096, and nx = 8192: complex64 with any such ny, complex128 with
- * ny <= 2048) run the split-k passes with plans; a grid with a side that is
- * not a power of two (each side 2 .. 4096) runs row and column passes of
- * Bluestein transforms.
+ * two (128 .. 4096; nx = 8192 with ny up to 4096 in complex64, up to 2048 in
+ * complex128; ny = 8192 with nx up to 4096 in complex64) run the split-k
+ * passes with plans; a grid with a side that is not a power of two (each side
+ * 2 .. 4096) runs row and column passes of Bluestein transforms.
  * Replaces SplittingMethod2D::InitSystem2D (src/SplittingMethod2D.cpp:5-31). */
 int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, double mass,
                   double hbar, double dt_re, double dt_im, int order, int precision,

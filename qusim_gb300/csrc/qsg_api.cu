@@ -2089,7 +2089,7 @@ int qsg_create_2d(qsg_ctx *ctx, uint64_t nx, uint64_t ny, double dx, double dy, 
     const int bmx = pow2_plan ? 0 : qsg::blue_m_for(precision, nx), bmy = pow2_plan ? 0 : qsg::blue_m_for(precision, ny);
     if (!pow2_plan && (!bmx || !bmy))
         return fail(QSG_ERR_UNSUPPORTED, "qsg_create_2d: grid " + std::to_string(nx) + "x" + std::to_string(ny) +
-                                             " (supported: sides 2 .. 4096, and powers of two 128 .. 4096 with nx up to 8192)");
+                                             " (supported: sides 2 .. 4096, and powers of two 128 .. 4096 with one side up to 8192)");
     std::lock_guard<std::mutex> lk(ctx->mu);
     QSG_CUDA(cudaSetDevice(ctx->dev));
     qsg_inst *in = new qsg_inst();

@@ -79,7 +79,7 @@ cudaError_t launch_row_pass(int prec, const Geom2D &g, const RowPassArgs &a, cud
 bool geom2d(int prec, int nx, int ny, const Plan2D &p, Geom2D *g)
 {
     auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
-    if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 4096 || nx < 128 || nx > 8192) return false;
+    if (!pow2(nx) || !pow2(ny) || ny < 128 || ny > 8192 || nx < 128 || nx > 8192) return false;
     if (!pow2(p.g) || p.g > 4 || nx % p.g) return false;
     const int csz = prec == 1 ? 8 : 16;
     if (p.row_kind != 0 && p.row_kind != 1) return false;

@@ -67,7 +67,8 @@ constexpr size_t row_smem_for(int csz, int ny, int e, int g)
     QSG_ROW_SMALL(X, float, 16) \
     X(float, 2048, 16, 1, 256) X(float, 2048, 16, 2, 256) X(float, 2048, 16, 4, 256) X(float, 2048, 16, 4, 512) \
     X(float, 4096, 16, 1, 256) X(float, 4096, 16, 2, 256) X(float, 4096, 16, 2, 512) \
-    X(float, 4096, 16, 4, 256) X(float, 4096, 16, 4, 512) X(float, 4096, 16, 4, 1024)
+    X(float, 4096, 16, 4, 256) X(float, 4096, 16, 4, 512) X(float, 4096, 16, 4, 1024) \
+    X(float, 8192, 16, 1, 512) X(float, 8192, 16, 2, 512) X(float, 8192, 16, 2, 1024)
 #define QSG_ROW_VARIANTS_F32B(X) \
     X(float, 128, 8, 1, 256) X(float, 128, 8, 2, 256) X(float, 128, 8, 4, 256) \
     X(float, 256, 8, 1, 256) X(float, 256, 8, 2, 256) X(float, 256, 8, 4, 256) \

@@ -149,6 +149,32 @@ def test_evolve2d_8192_columns_vs_oracle(qsg, ctx, oracle, nx, ny, precision):
     inst.close()
 
 
+@pytest.mark.parametrize("nx,form", [(128, "momentum"), (1024, "direct"), (4096, "momentum")])
+def test_evolve2d_8192_rows_vs_oracle(qsg, ctx, oracle, nx, form):
+    """complex64 grids with rows of 8192 sites (y), one or two rows per unit of
+    the row pass.  Two O2 steps in two calls against the oracle, with the
+    energies; complex128 has no row pass of that length and refuses the grid."""
+    ny = 8192
+    hx, hy = 0.05 * nx, 0.0125 * ny
+    psi0, dx, dy = gauss_packet_2d(nx, ny, -hx, hx, -hy, hy, kx=1.0, ky=0.5, xc=-0.2 * hx, yc=0.1 * hy,
+                                   s=0.08 * min(hx, hy))
+    V = gaussian_bumps_2d(nx, ny, -hx, hx, -hy, hy, nbumps=8, seed=3, spread=0.5 * min(hx, hy))
+    ref = oracle.evolve2d(psi0, V, dx, dy, 0.01, 2, order=2)
+    inst = qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=2, precision="mixed")
+    inst.form = form
+    inst.step(1)
+    inst.step(1)
+    assert rel_l2(inst.get_psi(), ref) <= MIXED_TOL
+    kin, pot = inst.energies()
+    assert abs(kin - oracle.kinen2d(ref, dx, dy)) <= 1e-4 * abs(kin)
+    assert abs(pot - oracle.poten(ref, V, dx * dy)) <= 1e-4 * max(1.0, abs(pot))
+    inst.close()
+    if nx == 128:
+        with pytest.raises(qsg.QsgError) as e:
+            qsg.Instance.create_2d(ctx, psi0, V, dx, dy, 0.01, order=2, precision="fp64")
+        assert e.value.code == 5
+
+
 @pytest.mark.parametrize("n", [64, 128, 512, 2048, 4096])
 @pytest.mark.parametrize("order", [2, 4])
 def test_evolve1d_sizes_vs_oracle(qsg, ctx, oracle, n, order):
