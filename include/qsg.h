@@ -274,7 +274,7 @@ typedef struct {
 } qsg_plan2d;
 
 /* Plans compiled for an nx x ny grid at `precision`; fills up to cap, returns
- * the count. */
+ * the count (0 for an unknown precision or a grid without split-k plans). */
 int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out, int cap);
 int qsg_get_plan(qsg_inst *inst, qsg_plan2d *out);
 int qsg_set_plan(qsg_inst *inst, const qsg_plan2d *plan);

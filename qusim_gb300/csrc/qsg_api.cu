@@ -2577,7 +2577,7 @@ void qsg_destroy(qsg_inst *in)
 
 int qsg_candidate_plans(int precision, uint64_t nx, uint64_t ny, qsg_plan2d *out, int cap)
 {
-    if (nx > 8192 || ny > 8192) return 0;
+    if ((precision != QSG_FP64 && precision != QSG_MIXED) || nx > 8192 || ny > 8192) return 0;
     std::vector<Plan2D> v(256);
     const int n = qsg::candidate_plans(precision, (int)nx, (int)ny, v.data(), (int)v.size());
     for (int i = 0; i < n && i < cap && out; ++i)
